@@ -1,0 +1,412 @@
+#!/usr/bin/env python3
+"""Benchmark of the SDPD step: particle-steps/s on the 3D 1M workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (configs.c3_poiseuille_3d): 100^3 = 1,000,000 fluid particles on a
+unit lattice between two solid walls in y (4 layers of 100x100 wall
+particles per side, 80,000 in total), quintic kernel rc = 3dx, Hu-Adams
+force, Morris EOS c = 20, eta = 0.5, g_x = 0.1, kT = 1e-4 with the Philox
+Wiener increments, dt = 5e-5.  Synthetic inputs, generated with the
+reference's lattice rule.  A step is one velocity-Verlet step (kick, drift,
+wrap, cell list, density, pressure, pair force, body force, kick); the
+metric counts fluid particles.
+
+`value` is the FP32-mixed path with the state resident in HBM (device time,
+CUDA events on the library's stream).  `fp64` is the plain FP64 path on the
+same workload.  `e2e` is the same metric through the C-ABI with host
+buffers: every step uploads x, v, f, m, id from pinned host memory, runs
+mcfg_step_vv and downloads x, v, f.  `cpu_baseline` is the CPU restatement
+of MCF's path (the oracle; MCF itself cannot be built here) on the host
+cores.  With --impl reference only that CPU path is timed.
+
+With torchrun (N > 1) every rank runs an independent replica on its own GPU
+("replicas only": this workload is not decomposed across GPUs); value sums
+the ranks' particle-steps over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s, 3D SDPD 1M: FP32-mixed vs FP64 at stated error; adjoint/fwd"
+UNIT = "particle-steps/s"
+
+# algorithmic bytes per particle and pass (minimum HBM traffic with every
+# per-particle array read or written once), FP32-mixed / FP64
+ALGO_BYTES = {
+    "list": (128, 184),
+    "density": (20, 32),
+    "force": (64, 92),
+    "update": (80, 120),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n-side", type=int, default=100)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--cpu-sample-steps", type=int, default=2)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- dist
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        backend = "nccl"
+        try:
+            import torch
+
+            if not torch.cuda.is_available():
+                backend = "gloo"
+            else:
+                torch.cuda.set_device(local)
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(val: float, ws: int) -> float:
+    if ws == 1:
+        return val
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([val], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_throughput(per_rank_units: float, max_seconds: float, ws: int) -> float:
+    """Whole-job particle-steps/s: all ranks' work over the slowest rank."""
+    return per_rank_units * ws / max_seconds
+
+
+# -------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 8:
+                    continue
+                try:
+                    sm.append(float(parts[0]))
+                    smax.append(float(parts[1]))
+                except ValueError:
+                    continue
+                for nm, val in zip(names, parts[4:8]):
+                    if val.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------- CPU baseline
+def cpu_baseline(w, steps: int, threads: int | None = None) -> dict:
+    from oracle.oracle import Oracle
+
+    threads = threads or os.cpu_count() or 1
+    p = w.params.copy()
+    p.symmetry = 0 if threads > 1 else 1  # full stencil parallelises race-free
+    o = Oracle(p, threads=threads)
+    o.upload(w.x, w.v, w.m, w.id)
+    o.marching_init_force(0)
+    t0 = time.perf_counter()
+    o.run_vv(0, steps, w.dt)
+    dt = time.perf_counter() - t0
+    return {"value": w.n_fluid * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{w.name}: {steps} full VV steps of all {w.n} particles "
+                      f"({w.n_fluid} fluid), OpenMP full-stencil loops, {dt:.1f} s",
+            "seconds_per_step": dt / steps}
+
+
+def run_reference(args, ws, rank):
+    """Reference arm: the CPU path on all host cores.  A step is one full VV
+    step of a sub-box of the same workload, sized from a one-step
+    calibration so that warm-up plus timed steps take about two minutes."""
+    from mcf_gb300 import configs
+    from oracle.oracle import Oracle
+
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+
+    def make(n_side):
+        w = configs.c3_poiseuille_3d(n_side=n_side)
+        p = w.params.copy()
+        p.symmetry = 0  # full-stencil loops: race-free over cells
+        o = Oracle(p, threads=threads)
+        o.upload(w.x, w.v, w.m, w.id)
+        o.marching_init_force(0)
+        return w, o
+
+    n_side = min(args.n_side, 40)
+    w, o = make(n_side)
+    t0 = time.perf_counter()
+    o.run_vv(0, 1, w.dt)
+    t1 = time.perf_counter() - t0
+    budget = 120.0
+    nsteps = args.warmup + args.steps
+    scale = (budget / max(nsteps * t1, 1e-9)) ** (1.0 / 3.0)
+    n_new = int(max(12, min(args.n_side, n_side * scale)))
+    if n_new != n_side:
+        w, o = make(n_new)
+        o.run_vv(0, 1, w.dt)
+    o.run_vv(1, args.warmup, w.dt)
+    t0 = time.perf_counter()
+    o.run_vv(1 + args.warmup, args.steps, w.dt)
+    dt = time.perf_counter() - t0
+    value = w.n_fluid * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": w.name + " with y-walls (CPU sample of the 100^3 workload)",
+                   "n_fluid": w.n_fluid, "n_wall": w.n - w.n_fluid,
+                   "note": "CPU restatement of MCF's FP64 SDPD step (MCF is Fortran+MPI and "
+                           "cannot be built here), OpenMP over all host cores"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} timed full VV steps of a {w.n_fluid}-fluid "
+                                   f"sub-box of the 1M workload ({w.n} particles)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------- GPU arm
+def timed_run(sd, torch, nsteps, step0, dt, ws):
+    stream = torch.cuda.ExternalStream(sd.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier(ws)
+    torch.cuda.synchronize()
+    l0 = sd.info()["kernel_launches"]
+    e0.record(stream)
+    sd.run_vv(step0, nsteps, dt)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches = sd.info()["kernel_launches"] - l0
+    return e0.elapsed_time(e1) / 1e3, launches
+
+
+def roofline_for(sd, torch, w, prec_idx, peaks, step0):
+    sd.set_profiling(2)
+    sd.set_profiling(1)
+    sd.run_vv(step0, 5, w.dt)
+    sd.set_profiling(0)
+    ph = sd.phase_times()
+    phases = {k: v for k, v in ph.items() if k in ALGO_BYTES and v[1] > 0}
+    top = max(phases, key=lambda k: phases[k][0])
+    avg_ms = phases[top][0] / phases[top][1]
+    algo = ALGO_BYTES[top][prec_idx] * w.n
+    achieved = algo / (avg_ms / 1e3) / 1e9
+    peak = peaks.get("hbm_gbs")
+    share = {k: round(v[0] / sum(x[0] for x in phases.values()), 4) for k, v in phases.items()}
+    return {"kernel_phase": top, "bound": "hbm", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": (achieved / peak) if peak else None, "traffic": None,
+            "avg_ms": avg_ms, "algo_bytes_per_launch": algo,
+            "peak_source": peaks.get("source"), "phase_share": share}
+
+
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    import torch
+
+    from mcf_gb300 import SDPD, configs
+    from mcf_gb300.params import PRECISION_FP32_MIXED, PRECISION_FP64
+
+    torch.cuda.set_device(local)
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+        peaks["source"] = "measured (MEASURED_PEAKS.json)"
+    else:
+        peaks = {"hbm_gbs": 6800.0, "source": "fallback 6.8 TB/s"}
+
+    w = configs.c3_poiseuille_3d(n_side=args.n_side, precision=PRECISION_FP32_MIXED)
+    w.params.device = local
+    sd = SDPD(w.params)
+    sd.upload(w.x, w.v, w.m, w.id)
+    sd.marching_init_force(0)
+    sd.run_vv(0, args.warmup, w.dt)
+    clk = ClockSampler(local)
+    clk.start()
+    t, launches = timed_run(sd, torch, args.steps, args.warmup, w.dt, ws)
+    clocks = clk.stop()
+    tmax = max_over_ranks(t, ws)
+    value = aggregate_throughput(w.n_fluid * args.steps, tmax, ws)
+    info = sd.info()
+    roof = roofline_for(sd, torch, w, 0, peaks, args.warmup + args.steps)
+    # FP32-mixed error against the FP64 path on the same state
+    err = None
+    fp64 = None
+    if not args.no_fp64:
+        w64 = configs.c3_poiseuille_3d(n_side=args.n_side, precision=PRECISION_FP64)
+        w64.params.device = local
+        sd64 = SDPD(w64.params)
+        sd64.upload(w.x, w.v, w.m, w.id)
+        sd64.marching_init_force(0)
+        sd32 = SDPD(w.params)
+        sd32.upload(w.x, w.v, w.m, w.id)
+        sd32.marching_init_force(0)
+        a = sd32.download("rho", "f")
+        b = sd64.download("rho", "f")
+        fl = w.id[:, 1] == 0
+        err = {"density_max_rel": float(np.max(np.abs(a["rho"] - b["rho"]) / b["rho"])),
+               "accel_rms_rel": float(np.sqrt(np.mean((a["f"][fl] - b["f"][fl]) ** 2)) /
+                                      np.sqrt(np.mean(b["f"][fl] ** 2)))}
+        del sd32
+        k64 = max(3, args.steps // 20)
+        sd64.run_vv(0, 2, w.dt)
+        t64, _ = timed_run(sd64, torch, k64, 2, w.dt, ws)
+        t64 = max_over_ranks(t64, ws)
+        v64 = aggregate_throughput(w.n_fluid * k64, t64, ws)
+        roof64 = roofline_for(sd64, torch, w64, 1, peaks, 2 + k64)
+        fp64 = {"value": v64, "unit": UNIT, "steps": k64, "ms_per_step": 1e3 * t64 / k64,
+                "fp32_mixed_speedup": value / v64, "roofline": roof64}
+        del sd64
+    # end to end through the C-ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        n, d = w.n, 3
+        pin = lambda shape, dt_: torch.empty(shape, dtype=dt_, pin_memory=True).numpy()  # noqa
+        hx, hv, hf = pin((n, d), torch.float64), pin((n, d), torch.float64), pin((n, d), torch.float64)
+        hm, hid = pin((n,), torch.float64), pin((n, 2), torch.int32)
+        st = sd.download("x", "v", "f")
+        hx[:], hv[:], hf[:] = st["x"], st["v"], st["f"]
+        hm[:], hid[:] = w.m, w.id
+        ke = max(3, min(args.steps, 20))
+        step = args.warmup + args.steps + 10
+
+        import ctypes as C
+        dp = C.POINTER(C.c_double)
+
+        def step_e2e(s):
+            sd.upload(hx, hv, hm, hid)
+            sd.upload_force(hf)
+            sd.marching_integrate_VV(s, w.dt)
+            rc = sd.lib.mcfg_download(sd._h, hx.ctypes.data_as(dp), hv.ctypes.data_as(dp), None,
+                                      None, hf.ctypes.data_as(dp), None, None)
+            if rc != 0:
+                raise RuntimeError(sd.lib.mcfg_last_error(sd._h).decode())
+
+        for q in range(2):
+            step_e2e(step + q)
+        barrier(ws)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for q in range(ke):
+            step_e2e(step + 2 + q)
+        torch.cuda.synchronize()
+        te = max_over_ranks(time.perf_counter() - t0, ws)
+        e2e = {"value": aggregate_throughput(w.n_fluid * ke, te, ws), "unit": UNIT,
+               "h2d_bytes_per_step": int(n * (3 * 8 * 3 + 8 + 8)),
+               "d2h_bytes_per_step": int(n * 3 * 8 * 3), "steps": ke,
+               "path": "mcfg_upload + mcfg_upload_force + mcfg_step_vv + mcfg_download per step"}
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(w, args.cpu_sample_steps)
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP32-mixed; f64 state)",
+        "data": "synthetic",
+        "config": {"workload": w.name + " with y-walls", "n_fluid": w.n_fluid,
+                   "n_wall": w.n - w.n_fluid, "precision": "FP32-mixed",
+                   "kernel": "quintic rc=3dx", "force": "Hu-Adams + Philox Wiener",
+                   "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2 "
+                   f"({info['device_bytes'] / 1e6:.0f} MB device state)",
+                   "neighbour_capacity": info["neigh_capacity"], "max_neigh": info["max_neigh"],
+                   "pairs_per_step": info["num_pairs"]},
+        "roofline": roof, "fp64": fp64, "fp32_error_vs_fp64": err, "e2e": e2e,
+        "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
+        "pair_interactions_per_s": info["num_pairs"] * args.steps * ws / tmax,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

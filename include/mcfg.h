@@ -1,0 +1,232 @@
+/*
+ * mcfg.h -- C-ABI of the GB300-native SDPD right-hand side and time step.
+ *
+ * This library replaces the per-step particle routines of MCF (Fortran 90 on
+ * the PPM library) with CUDA kernels for sm_103a.  MCF's driver keeps its
+ * configuration files, its Physics/Control objects and its particle arrays;
+ * a thin iso_c_binding module fills `mcfg_params` from MCF's getters and
+ * calls the entry points below.  Every entry point:
+ *   - returns an int status: MCFG_OK (0) or a negative MCFG_E* code.  It never
+ *     aborts the process (MCF's convention is `stat_info = 0 / -1`,
+ *     e.g. mcf/src/particles_compute_interaction.F90:896-953);
+ *   - takes caller-owned host buffers that it never frees; device memory is
+ *     owned by the handle and released by mcfg_destroy;
+ *   - uses MCF's array layout on the host side: x(d,N) column-major REAL(8),
+ *     i.e. interleaved [x0 y0 (z0) x1 y1 (z1) ...], id(2,N) INTEGER(4) with
+ *     id(1)=pid, id(2)=sid (sid 0 fluid, <0 wall, >0 colloid number),
+ *     mcf/src/Class_Particles.F90:132-141, mcf/src/mcf_header.F90:118-120.
+ * A handle is used by one host thread at a time and drives one GPU.
+ */
+#ifndef MCFG_H
+#define MCFG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MCFG_OK 0
+#define MCFG_EINVAL -1     /* bad argument or parameter combination          */
+#define MCFG_ECUDA -2      /* CUDA runtime error (message in mcfg_last_error) */
+#define MCFG_ENOMEM -3     /* device allocation failed                        */
+#define MCFG_ESTATE -4     /* call out of order (e.g. force before density)   */
+#define MCFG_EOVERFLOW -5  /* a fixed-capacity list overflowed (neighbours)   */
+#define MCFG_EPHYS -6      /* physics check failed (zero mass/density, NaN)   */
+#define MCFG_ENODEV -7     /* no CUDA device / kernels not loadable           */
+#define MCFG_ETIMEOUT -8   /* a bounded device wait gave up                   */
+#define MCFG_ENOTSUP -9    /* option not supported by this build              */
+
+/* ---- enumerations (values are MCF's own) -------------------------------- */
+/* boundary types, PPM ppm_param.h: periodic 1, symmetry 3, wall_sym 7,
+ * wall_solid 9, Lees-Edwards 10 */
+#define MCFG_BC_PERIODIC 1
+#define MCFG_BC_WALL_SOLID 9
+
+#define MCFG_PRECISION_FP64 0       /* pair arithmetic in FP64              */
+#define MCFG_PRECISION_FP32_MIXED 1 /* FP32 pair arithmetic, FP64 state     */
+
+/* Flat parameter block, filled from MCF's Control/Physics/Boundary/Colloid
+ * getters.  Field names follow the keys of mcf_config/ctrl.mcf and
+ * mcf_config/physics_config.mcf. */
+typedef struct mcfg_params {
+  int32_t num_dim;            /* 2 or 3                                      */
+  int32_t bcdef[6];           /* per face x-,x+,y-,y+,z-,z+: 1 or 9          */
+  double min_phys[3];         /* fluid domain                                */
+  double max_phys[3];
+  double min_phys_t[3];       /* total domain incl. wall layers              */
+  double max_phys_t[3];
+  double cut_off;             /* kernel support rc                           */
+  double cell_factor;         /* cell side = cell_factor*rc (MCF: 1.0001)    */
+  int32_t kernel_type;        /* 1 quintic spline (h=rc/3), 2 Lucy (h=rc)    */
+  int32_t rhs_density_type;   /* 1 mass density, 2 number density            */
+  int32_t rhs_force_type;     /* 1 Morris, 2 Espanol-Revenga, 3 Hu-Adams,
+                                 4 Hu-Adams angular                          */
+  int32_t stateEquation_type; /* 1 Morris p=c^2(rho^gamma-rho_ref),
+                                 2 Batchelor p=p0((rho/rho_ref)^gamma-1)     */
+  double c;                   /* sound speed                                 */
+  double rho;                 /* initial density (Batchelor p0)              */
+  double rho_ref;
+  double gamma;
+  double eta;                 /* shear viscosity (solvent eta_s if not
+                                 Newtonian)                                  */
+  double eta_coef;            /* angular Hu-Adams viscosity coefficient      */
+  double kt;                  /* thermal energy kT                           */
+  double dt;                  /* time step used by the random force when the
+                                 interaction is called outside a VV step     */
+  int32_t Brownian;           /* 1: Wiener-increment random force            */
+  int32_t symmetry;           /* MCF symmetry flag (pair evaluation mode of
+                                 the CPU path; the GPU result is the same)   */
+  int32_t body_force_type;    /* 0 none, 1 constant, 2 reverse Poiseuille,
+                                 3 g_x*sin(2 pi y / L_y)                     */
+  int32_t wall_rho_type;      /* 0 constant, 1 dynamic                       */
+  double body_force[3];
+  int32_t wall_noslip_type;   /* 1 frozen, 2 Morris extrapolation            */
+  int32_t stress_tensor;      /* 1: accumulate per-particle stress s(d^2,N) */
+  double wall_v[6][3];        /* velocity of each solid wall face (shear_v)  */
+  double init_density;        /* constant density of boundary particles      */
+  int32_t Newtonian;          /* 1 Newtonian; 0 Oldroyd-B conformation model */
+  int32_t precision;          /* MCFG_PRECISION_*                            */
+  double tau;                 /* Oldroyd-B relaxation time                   */
+  double n_p;                 /* polymer number density                      */
+  double kt_p;                /* polymer kT (G = n_p*kt_p)                   */
+  uint64_t seed;              /* Philox key for the Wiener increments        */
+  int32_t device;             /* CUDA device ordinal                         */
+  int32_t reserved[7];
+} mcfg_params;
+
+typedef struct mcfg_handle mcfg_handle;
+
+/* sizeof(mcfg_params) as compiled into the library, so that bindings
+ * (iso_c_binding, ctypes) can verify their copy of the layout. */
+int64_t mcfg_sizeof_params(void);
+
+/* Per-handle counters, readable at any time. */
+typedef struct mcfg_info {
+  int64_t num_part;       /* particles uploaded                              */
+  int32_t num_cell_dim[3];/* real cells per dimension of the cell list       */
+  int32_t num_cell;       /* product of num_cell_dim                         */
+  int64_t num_outside;    /* particles outside the cell mesh at the last
+                             list build (PPM gives them no box; they do not
+                             interact)                                       */
+  int64_t num_pairs;      /* directed pairs inside the cut-off, last build   */
+  int32_t max_neigh;      /* largest per-particle neighbour count           */
+  int32_t neigh_capacity; /* per-particle neighbour list capacity           */
+  int64_t kernel_launches;/* kernels launched by this handle so far          */
+  int64_t device_bytes;   /* device memory held by the handle               */
+} mcfg_info;
+
+/* Create a handle on params->device.  Replaces the construction of MCF's
+ * Technique/Kernel/Rhs/StateEquation objects, mcf/src/mcf.F90:335-659
+ * (kernel_new.F90:41-93, stateEquation_new.F90:65-110). */
+int mcfg_create(const mcfg_params* params, mcfg_handle** out);
+
+/* Release all device memory of the handle. */
+int mcfg_destroy(mcfg_handle* h);
+
+/* Message of the last failing call on this handle (never NULL). */
+const char* mcfg_last_error(const mcfg_handle* h);
+
+/* Message of the last mcfg_create failure (no handle exists yet). */
+const char* mcfg_create_error(void);
+
+int mcfg_get_info(const mcfg_handle* h, mcfg_info* info);
+
+/* Copy the real particles to the device (host order is kept as the
+ * particle index of every output).  x, v: [n*d]; m: [n]; id: [n*2];
+ * ct: [n*d*d] conformation tensor or NULL (Newtonian).  Replaces the
+ * particle arrays of Class_Particles (mcf/src/Class_Particles.F90:132-141)
+ * as produced by particles_init_* / io_read_particles. */
+int mcfg_upload(mcfg_handle* h, int64_t n, const double* x, const double* v,
+                const double* m, const int32_t* id, const double* ct);
+
+/* Load accelerations f(d,N) in host order (e.g. MCF's this%f of the last
+ * step) so that mcfg_step_vv can follow mcfg_upload directly, as when MCF
+ * keeps its particle arrays on the host between steps. */
+int mcfg_upload_force(mcfg_handle* h, const double* f);
+
+/* Periodic wrap of the real particles, particles_adjust_particles.F90:137-389
+ * (periodic faces only; solid-wall faces clamp wall particles). */
+int mcfg_adjust_particles(mcfg_handle* h);
+
+/* Build the cell list of the current positions.  Replaces
+ * technique_build_list (mcf/src/technique_build_list.F90:94-109) ->
+ * ppm_neighlist_clist -> ppm_util_rank3d/2d.  Cells are the real cells of
+ * PPM's mesh, numbered i + j*Nx + k*Nx*Ny (0-based).  Optional outputs:
+ * num_cell_dim[3]; cell_start[num_cell+1] (0-based CSR, like PPM lhbx minus
+ * one and restricted to real cells); lpdx[n] (0-based host particle indices
+ * sorted by cell, stable in host index order, like PPM lpdx). */
+int mcfg_build_list(mcfg_handle* h, int32_t* num_cell_dim,
+                    int32_t* cell_start, int32_t* lpdx);
+
+/* Density summation, particles_compute_density.F90:369-867 with
+ * rhs_density.F90:95-96 (includes the self term W(0) and the half-shell
+ * pair fold-back of particles_map_ghost_put).  Needs mcfg_build_list. */
+int mcfg_compute_density(mcfg_handle* h);
+
+/* Equation of state for all particles, particles_compute_pressure.F90:66-95
+ * -> stateEquation_compute_pressure.F90:147-180. */
+int mcfg_compute_pressure(mcfg_handle* h);
+
+/* Pair accelerations f(d,N) (and stress s(d^2,N) if params.stress_tensor),
+ * particles_compute_interaction.F90:609-900 with pp_interaction.inc:37-223,
+ * rhs_force_ff_Newtonian*.F90; the random term is keyed by
+ * (seed, step, min pid, max pid) so dW_ij = dW_ji. */
+int mcfg_compute_interaction(mcfg_handle* h, int64_t step);
+
+/* f += body force, particles_apply_body_force.F90:96-353 (types 1-3). */
+int mcfg_apply_body_force(mcfg_handle* h);
+
+/* v += lambda*f*dt for fluid particles, particles_integrate_velocity.F90:84-94 */
+int mcfg_integrate_velocity(mcfg_handle* h, double dt, double lambda);
+
+/* x += v*dt for fluid particles, particles_integrate_position.F90:82-111
+ * (accuracy order 1). */
+int mcfg_integrate_position(mcfg_handle* h, double dt);
+
+/* Right-hand side before the first step: list, density, pressure, force,
+ * body force, as marching_marching.F90:528-911. */
+int mcfg_init_force(mcfg_handle* h, int64_t step);
+
+/* One velocity-Verlet step, marching_integrate_VV.F90:303-1620: half kick,
+ * drift, wrap, list, density, pressure, force, body force, half kick. */
+int mcfg_step_vv(mcfg_handle* h, int64_t step, double dt);
+
+/* nsteps consecutive VV steps starting at step0 (step numbers step0+1 ...),
+ * the loop of marching_marching.F90:1329-1531 without I/O. */
+int mcfg_run_vv(mcfg_handle* h, int64_t step0, int32_t nsteps, double dt);
+
+/* Copy state back in host particle order; any pointer may be NULL.
+ * x,v,f: [n*d]; rho,p: [n]; ct: [n*d*d]; s: [n*d*d] (stress_tensor). */
+int mcfg_download(mcfg_handle* h, double* x, double* v, double* rho,
+                  double* p, double* f, double* ct, double* s);
+
+/* Global FP64 sums of statistic_compute_statistic.F90:230-303: kinetic
+ * energy and momentum over fluid particles, stress sum over sid >= 0.
+ * mom: [3], stress: [9] (column-major d x d); either may be NULL. */
+int mcfg_statistics(mcfg_handle* h, double* k_energy, double* momentum,
+                    double* stress);
+
+/* Wait for all work of the handle to finish (error check point). */
+int mcfg_synchronize(mcfg_handle* h);
+
+/* The CUDA stream (cudaStream_t) all kernels of the handle run on, for
+ * callers that time or order work around them; NULL on error. */
+void* mcfg_get_stream(mcfg_handle* h);
+
+/* Per-phase device timers (CUDA events on the handle's stream), the
+ * GPU counterpart of MCF's __DEBUG_INTEGRATE_VV phase times
+ * (marching_integrate_VV.F90:131-143,1679-1709).  Phases: 0 cell list,
+ * 1 density (+ neighbour list, pressure), 2 pair force (+ body force, kick),
+ * 3 kick-drift-wrap, 4 other.  ms[5] total milliseconds, counts[5] launches
+ * timed; mcfg_set_profiling(h, 0) stops recording, (h, 1) starts, (h, 2)
+ * clears the totals. */
+int mcfg_set_profiling(mcfg_handle* h, int mode);
+int mcfg_get_phase_times(mcfg_handle* h, double* ms, int64_t* counts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MCFG_H */

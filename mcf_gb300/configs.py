@@ -1,0 +1,164 @@
+"""Synthetic SDPD workloads (MCF input decks restated as parameter blocks
+and seeded initial particles).
+
+Particles are placed like particles_init_global_inter_cubic/_square
+(lattice at min + dx/2 + k*dx over the total domain, repeated addition),
+solid-wall particles are the lattice sites outside the fluid domain along a
+wall axis (boundary_check_wall_solid_particle.F90: sid = 1-2i below, -2i
+above), masses are rho0 * prod(dx) (particles_compute_mass.F90:363-450) and
+pids run 1..N.  Perturbations MCF itself does not generate (jitter, initial
+velocity noise) are seeded numpy draws, fed the way MCF's read_external
+input would feed them.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .params import BC_PERIODIC, BC_WALL_SOLID, PRECISION_FP64, SDPDParams, make_params
+
+BASE_SEED = 20261203
+
+
+@dataclass
+class Workload:
+    name: str
+    params: SDPDParams
+    x: np.ndarray
+    v: np.ndarray
+    m: np.ndarray
+    id: np.ndarray
+    dt: float
+    steps: int
+
+    @property
+    def n(self) -> int:
+        return int(self.m.shape[0])
+
+    @property
+    def n_fluid(self) -> int:
+        return int((self.id[:, 1] == 0).sum())
+
+
+def lattice(dim: int, min_t, max_t, dx) -> np.ndarray:
+    """particles_init_global_inter_cubic/_square: sx = min + dx/2, sx += dx
+    while sx < max (x fastest), exactly as the repeated addition rounds."""
+    axes = []
+    for a in range(dim):
+        vals = []
+        s = min_t[a] + 0.5 * dx[a]
+        while s < max_t[a]:
+            vals.append(s)
+            s = s + dx[a]
+        axes.append(np.array(vals))
+    if dim == 2:
+        yy, xx = np.meshgrid(axes[1], axes[0], indexing="ij")
+        return np.stack([xx.ravel(), yy.ravel()], axis=1)
+    zz, yy, xx = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    return np.stack([xx.ravel(), yy.ravel(), zz.ravel()], axis=1)
+
+
+def wall_sid(x: np.ndarray, params: SDPDParams) -> np.ndarray:
+    dim = params.num_dim
+    sid = np.zeros(x.shape[0], np.int32)
+    for i in range(dim):
+        if params.bcdef[2 * i] == BC_WALL_SOLID:
+            lo = (x[:, i] <= params.min_phys[i]) & (x[:, i] >= params.min_phys_t[i]) & (sid == 0)
+            sid[lo] = 1 - 2 * (i + 1)
+        if params.bcdef[2 * i + 1] == BC_WALL_SOLID:
+            hi = (x[:, i] >= params.max_phys[i]) & (x[:, i] < params.max_phys_t[i]) & (sid == 0)
+            sid[hi] = -2 * (i + 1)
+    return sid
+
+
+def _finish(name, p, dx, jitter, vstd, seed, dt, steps, rho0=1.0) -> Workload:
+    dim = p.num_dim
+    x = lattice(dim, list(p.min_phys_t)[:dim], list(p.max_phys_t)[:dim], dx)
+    sid = wall_sid(x, p)
+    rng = np.random.default_rng(seed)
+    if jitter:
+        fl = sid == 0
+        x[fl] += rng.uniform(-jitter, jitter, size=(int(fl.sum()), dim)) * np.asarray(dx)
+    n = x.shape[0]
+    v = np.zeros((n, dim))
+    if vstd:
+        fl = sid == 0
+        v[fl] = rng.normal(0.0, vstd, size=(int(fl.sum()), dim))
+    m = np.full(n, rho0 * float(np.prod(dx)))
+    ids = np.stack([np.arange(1, n + 1, dtype=np.int32), sid], axis=1).astype(np.int32)
+    return Workload(name, p, x, v, m, ids, dt, steps)
+
+
+def _box(dim, lo, hi, walls_axis=None, nwall_layers=0, dx=1.0):
+    mn = [0.0] * 3
+    mx = [0.0] * 3
+    mn_t = [0.0] * 3
+    mx_t = [0.0] * 3
+    bc = [BC_PERIODIC] * 6
+    for a in range(dim):
+        mn[a], mx[a] = lo, hi
+        mn_t[a], mx_t[a] = lo, hi
+    if walls_axis is not None:
+        a = walls_axis
+        bc[2 * a] = bc[2 * a + 1] = BC_WALL_SOLID
+        # physics_adjust_parameters.F90:229-273
+        mn_t[a] = lo - nwall_layers * dx
+        mx_t[a] = hi + nwall_layers * dx
+    return dict(num_dim=dim, bcdef=bc, min_phys=mn, max_phys=mx, min_phys_t=mn_t, max_phys_t=mx_t)
+
+
+def wall_layers(cut_off: float, dx: float, dynamic: bool = False) -> int:
+    """CEILING((1 + 0.05) * cut_off [* 2 if dynamic] / dx),
+    physics_adjust_parameters.F90:229-273 with mcf_wall_in_layer_coeff."""
+    w = (1.0 + 0.05) * cut_off
+    if dynamic:
+        w *= 2.0
+    return int(np.ceil(w / dx - 1e-12))
+
+
+def c1_poiseuille_2d(n_side: int = 64, precision: int = PRECISION_FP64, seed: int = BASE_SEED + 1,
+                     body_force_type: int = 2) -> Workload:
+    """2D 64x64 periodic unit box, dx=1/64, rc=3dx, c=10, eta=1, g_x=1,
+    kT=0, v0 ~ N(0, (1e-4)^2), dt=1e-4, 1000 steps.  Fully periodic with a
+    constant g is uniform acceleration, so the profile uses MCF's periodic
+    reverse-Poiseuille body force (body_force_type 2)."""
+    dx = 1.0 / n_side
+    p = make_params(**_box(2, 0.0, 1.0), cut_off=3 * dx, c=10.0, eta=1.0, kt=0.0, Brownian=0,
+                    body_force_type=body_force_type, body_force=[1.0, 0.0, 0.0], dt=1e-4,
+                    precision=precision, seed=seed)
+    return _finish("C1 2D 64^2 Poiseuille FP64", p, [dx, dx], 0.0, 1e-4, seed, 1e-4, 1000)
+
+
+def c2_fluctuating_3d(n_side: int = 64, precision: int = PRECISION_FP64,
+                      seed: int = BASE_SEED + 2) -> Workload:
+    """3D 64^3 periodic cube, dx=1, jitter U(-0.05,0.05)dx, rc=3, c=10,
+    eta=1, kT=1e-3 (Brownian), no body force, dt=1e-4, 2000 steps."""
+    L = float(n_side)
+    p = make_params(**_box(3, 0.0, L), cut_off=3.0, c=10.0, eta=1.0, kt=1e-3, Brownian=1,
+                    body_force_type=0, dt=1e-4, precision=precision, seed=seed)
+    return _finish(f"C2 3D {n_side}^3 fluctuating", p, [1.0] * 3, 0.05, 0.0, seed, 1e-4, 2000)
+
+
+def c3_poiseuille_3d(n_side: int = 100, precision: int = PRECISION_FP64, walls: bool = True,
+                     seed: int = BASE_SEED + 3) -> Workload:
+    """3D 100^3, dx=1, rc=3, c=20, eta=0.5, g_x=0.1, kT=1e-4, dt=5e-5,
+    5000 steps.  Poiseuille in y with solid walls in y (4 layers of
+    constant-density wall particles per side, Morris no-slip) or, with
+    walls=False, MCF's periodic reverse-Poiseuille force."""
+    L = float(n_side)
+    if walls:
+        nl = wall_layers(3.0, 1.0)
+        box = _box(3, 0.0, L, walls_axis=1, nwall_layers=nl, dx=1.0)
+        p = make_params(**box, cut_off=3.0, c=20.0, eta=0.5, kt=1e-4, Brownian=1,
+                        body_force_type=1, body_force=[0.1, 0.0, 0.0], dt=5e-5,
+                        wall_noslip_type=2, wall_rho_type=0, init_density=1.0,
+                        precision=precision, seed=seed)
+    else:
+        p = make_params(**_box(3, 0.0, L), cut_off=3.0, c=20.0, eta=0.5, kt=1e-4, Brownian=1,
+                        body_force_type=2, body_force=[0.1, 0.0, 0.0], dt=5e-5,
+                        precision=precision, seed=seed)
+    return _finish(f"C3 3D {n_side}^3 Poiseuille", p, [1.0] * 3, 0.0, 0.0, seed, 5e-5, 5000)
+
+
+WORKLOADS = {"c1": c1_poiseuille_2d, "c2": c2_fluctuating_3d, "c3": c3_poiseuille_3d}

@@ -1,0 +1,726 @@
+// mcfg_api.cu -- the extern "C" boundary (include/mcfg.h): parameter checks,
+// device memory, host<->device layout conversion and the orchestration of
+// the per-step kernels.  Every entry point returns a status; none aborts.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "mcfg_internal.cuh"
+#include "sph.cuh"
+
+using namespace mcfg;
+
+struct mcfg_handle : public Handle {};
+
+namespace mcfg {
+
+int set_error(Handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int cuda_check(Handle* h, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return 0;
+  char buf[256];
+  snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+  h->err = buf;
+  return MCFG_ECUDA;
+}
+
+void resolve_phases(Handle* h) {
+  for (int ph = 0; ph < 5; ++ph) {
+    for (auto& ev : h->ev_pending[ph]) {
+      float ms = 0.0f;
+      if (cudaEventElapsedTime(&ms, ev.first, ev.second) == cudaSuccess) {
+        h->phase_ms[ph] += ms;
+        h->phase_cnt[ph] += 1;
+      }
+      h->ev_pool.push_back(ev);
+    }
+    h->ev_pending[ph].clear();
+  }
+}
+
+int check_device_errors(Handle* h) {
+  unsigned e = 0;
+  int st[4] = {0, 0, 0, 0};
+  unsigned long long pairs = 0;
+  if (cuda_check(h, cudaMemcpyAsync(&e, h->d_err, sizeof e, cudaMemcpyDeviceToHost, h->stream),
+                 "error flag copy"))
+    return MCFG_ECUDA;
+  if (cuda_check(h, cudaMemcpyAsync(st, h->d_stats, sizeof st, cudaMemcpyDeviceToHost, h->stream),
+                 "stats copy"))
+    return MCFG_ECUDA;
+  if (cuda_check(h, cudaMemcpyAsync(&pairs, h->d_pairs, sizeof pairs, cudaMemcpyDeviceToHost,
+                                    h->stream),
+                 "pairs copy"))
+    return MCFG_ECUDA;
+  if (cuda_check(h, cudaStreamSynchronize(h->stream), "synchronize")) return MCFG_ECUDA;
+  resolve_phases(h);
+  h->max_neigh = st[1];
+  h->num_pairs = (int64_t)pairs;
+  if (e) {
+    cudaMemsetAsync(h->d_err, 0, sizeof(unsigned), h->stream);
+    if (e & kErrNeighOverflow) {
+      char buf[200];
+      snprintf(buf, sizeof buf,
+               "neighbour list overflow: a particle has %d candidates, capacity %d "
+               "(raise mcfg_params.reserved[0])",
+               st[1], h->neigh_cap);
+      return set_error(h, MCFG_EOVERFLOW, buf);
+    }
+    if (e & kErrCellOverflow)
+      return set_error(h, MCFG_EOVERFLOW, "a cell holds more than 2048 particles");
+    if (e & kErrZeroDensity) return set_error(h, MCFG_EPHYS, "non-positive density");
+    if (e & kErrNonFinite) return set_error(h, MCFG_EPHYS, "non-finite acceleration");
+  }
+  return MCFG_OK;
+}
+
+}  // namespace mcfg
+
+namespace {
+
+std::mutex g_create_mu;
+std::string g_create_err = "no error";
+
+template <typename T>
+int dalloc(Handle* h, T** p, size_t count) {
+  if (*p) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  if (count == 0) count = 1;
+  const size_t bytes = sizeof(T) * count;
+  cudaError_t e = cudaMalloc((void**)p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    char buf[160];
+    snprintf(buf, sizeof buf, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    h->err = buf;
+    return MCFG_ENOMEM;
+  }
+  h->device_bytes += (int64_t)bytes;
+  return MCFG_OK;
+}
+
+void free_all(Handle* h) {
+  void* ptrs[] = {h->x, h->v, h->f, h->m, h->pid, h->sid, h->hidx, h->rho, h->pr, h->st,
+                  h->x2, h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->key, h->rank,
+                  h->cnt, h->cell_start, h->scan_part, h->order, h->off, h->cell_of, h->nl,
+                  h->ncount, h->pc, h->pcf, h->vf, h->red, h->d_err, h->d_stats, h->d_pairs,
+                  h->up_x, h->up_v, h->up_m, h->up_id};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  h->x = h->v = h->f = h->x2 = h->v2 = h->f2 = nullptr;
+  h->m = h->m2 = h->rho = h->pr = h->st = h->red = h->up_x = h->up_v = h->up_m = nullptr;
+  h->pid = h->sid = h->hidx = h->pid2 = h->sid2 = h->hidx2 = nullptr;
+  h->key = h->rank = h->cnt = h->cell_start = h->scan_part = h->order = h->cell_of = nullptr;
+  h->ncount = h->d_stats = h->up_id = nullptr;
+  h->off = h->pcf = h->vf = nullptr;
+  h->pc = nullptr;
+  h->nl = nullptr;
+  h->d_err = nullptr;
+  h->d_pairs = nullptr;
+  h->device_bytes = 0;
+}
+
+const char* validate(const mcfg_params* p) {
+  if (!p) return "params is NULL";
+  if (p->num_dim != 2 && p->num_dim != 3) return "num_dim must be 2 or 3";
+  if (!(p->cut_off > 0.0)) return "cut_off must be positive";
+  if (p->kernel_type != 1 && p->kernel_type != 2) return "kernel_type must be 1 or 2";
+  if (p->rhs_density_type != 1 && p->rhs_density_type != 2)
+    return "rhs_density_type must be 1 or 2";
+  if (p->rhs_force_type < 1 || p->rhs_force_type > 4) return "rhs_force_type must be 1..4";
+  if (p->stateEquation_type != 1 && p->stateEquation_type != 2)
+    return "stateEquation_type must be 1 or 2";
+  if (p->body_force_type < 0 || p->body_force_type > 3) return "body_force_type must be 0..3";
+  if (p->precision != MCFG_PRECISION_FP64 && p->precision != MCFG_PRECISION_FP32_MIXED)
+    return "precision must be MCFG_PRECISION_FP64 or MCFG_PRECISION_FP32_MIXED";
+  if (!p->Newtonian) return "non-Newtonian (Oldroyd-B) model is not in this build";
+  for (int a = 0; a < p->num_dim; ++a) {
+    const int lo = p->bcdef[2 * a], hi = p->bcdef[2 * a + 1];
+    if ((lo != MCFG_BC_PERIODIC && lo != MCFG_BC_WALL_SOLID) ||
+        (hi != MCFG_BC_PERIODIC && hi != MCFG_BC_WALL_SOLID))
+      return "bcdef: only periodic (1) and solid wall (9) faces are supported";
+    if ((lo == MCFG_BC_PERIODIC) != (hi == MCFG_BC_PERIODIC))
+      return "bcdef: a periodic face needs a periodic opposite face";
+    if (!(p->max_phys_t[a] > p->min_phys_t[a])) return "max_phys_t must exceed min_phys_t";
+    if (!(p->max_phys[a] > p->min_phys[a])) return "max_phys must exceed min_phys";
+  }
+  if (p->rhs_force_type == 1 && p->rhs_density_type != 1)
+    return "rhs_force_type 1 (Morris) needs rhs_density_type 1 (mass density)";
+  if (p->stateEquation_type == 2 && (p->rho_ref == 0.0 || p->gamma == 0.0))
+    return "Batchelor EOS needs non-zero rho_ref and gamma";
+  return nullptr;
+}
+
+void fill_consts(Handle* h) {
+  const mcfg_params& p = h->p;
+  Consts& k = h->k;
+  memset(&k, 0, sizeof k);
+  k.d = p.num_dim;
+  const double cf = p.cell_factor > 0.0 ? p.cell_factor : 1.0001;
+  const double gs = p.cut_off * cf;  // mcf.F90:617
+  k.ncell = 1;
+  for (int a = 0; a < 3; ++a) {
+    k.nm[a] = 1;
+    k.csf[a] = 0.0f;
+  }
+  for (int a = 0; a < k.d; ++a) {
+    k.xmin[a] = p.min_phys_t[a];
+    k.xmax[a] = p.max_phys_t[a];
+    int nm = (int)((k.xmax[a] - k.xmin[a]) / gs);  // ppm_neighlist_clist.F90:370-376
+    if (nm < 1) nm = 1;
+    k.nm[a] = nm;
+    k.ncell *= nm;
+    k.rdx[a] = (double)nm / (k.xmax[a] - k.xmin[a]);
+    k.cs[a] = (k.xmax[a] - k.xmin[a]) / (double)nm;
+    k.csf[a] = (float)k.cs[a];
+    k.len[a] = p.max_phys_t[a] - p.min_phys_t[a];
+    k.bc_lo[a] = p.bcdef[2 * a];
+    k.bc_hi[a] = p.bcdef[2 * a + 1];
+    k.periodic[a] = (p.bcdef[2 * a] == MCFG_BC_PERIODIC) ? 1 : 0;
+    k.min_phys[a] = p.min_phys[a];
+    k.max_phys[a] = p.max_phys[a];
+  }
+  k.rc2 = p.cut_off * p.cut_off;
+  k.rc2f = (float)k.rc2;
+  // FP32 prefilter of the FP64 path: relative slack far above the FP32
+  // rounding of cell offsets (|offset| <= cell side)
+  k.rc2f_hi = (float)(k.rc2 * (1.0 + 1e-4));
+  // kernel_new.F90:41-93
+  k.kernel_type = p.kernel_type;
+  if (p.kernel_type == 1) {
+    k.h = p.cut_off / 3.0;
+    k.coef = (k.d == 2) ? 7.0 / (478.0 * kPi * k.h * k.h) : 3.0 / (359.0 * kPi * k.h * k.h * k.h);
+  } else {
+    k.h = p.cut_off;
+    k.coef = (k.d == 2) ? 5.0 / (kPi * k.h * k.h) : 105.0 / (16.0 * kPi * k.h * k.h * k.h);
+  }
+  k.coef_grad = -k.coef / k.h;
+  k.inv_h = 1.0 / k.h;
+  k.w0 = (p.kernel_type == 1) ? k.coef * (243.0 - 6.0 * 32.0 + 15.0) : k.coef;
+  k.hf = (float)k.h;
+  k.inv_hf = (float)k.inv_h;
+  k.coeff = (float)k.coef;
+  k.coef_gradf = (float)k.coef_grad;
+  k.w0f = (float)k.w0;
+  k.rhs_density_type = p.rhs_density_type;
+  k.rhs_force_type = p.rhs_force_type;
+  k.eos_type = p.stateEquation_type;
+  k.c2 = p.c * p.c;
+  k.rho_ref = p.rho_ref;
+  k.gamma = p.gamma;
+  if (p.stateEquation_type == 2)  // stateEquation_new.F90:102-103
+    k.p0 = p.c * p.c * p.rho * std::pow(p.rho_ref / p.rho, p.gamma) / p.gamma;
+  k.eta = p.eta;
+  k.eta_coef = p.eta_coef;
+  k.kt = p.kt;
+  k.machine_zero = 1e-14;  // technique_new.F90:361-363
+  k.noise = (p.Brownian && p.kt > k.machine_zero) ? 1 : 0;
+  k.wall_rho_type = p.wall_rho_type;
+  k.wall_noslip_type = p.wall_noslip_type;
+  k.init_density = p.init_density;
+  for (int f = 0; f < 6; ++f)
+    for (int a = 0; a < 3; ++a) k.wall_v[f][a] = p.wall_v[f][a];
+  k.stress = p.stress_tensor ? 1 : 0;
+  k.key0 = (uint32_t)p.seed;
+  k.key1 = (uint32_t)(p.seed >> 32);
+  k.body_force_type = p.body_force_type;
+  for (int a = 0; a < 3; ++a) k.body_force[a] = p.body_force[a];
+}
+
+__global__ void k_upload(int n, int d, const double* __restrict__ hx, const double* __restrict__ hv,
+                         const double* __restrict__ hm, const int* __restrict__ hid,
+                         double4_32a* __restrict__ x, double4_32a* __restrict__ v,
+                         double4_32a* __restrict__ f, double* __restrict__ m, int* __restrict__ pid,
+                         int* __restrict__ sid, int* __restrict__ hidx) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* xp = hx + (size_t)i * d;
+  const double* vp = hv + (size_t)i * d;
+  x[i] = make_double4_32a(xp[0], xp[1], d == 3 ? xp[2] : 0.0, 0.0);
+  v[i] = make_double4_32a(vp[0], vp[1], d == 3 ? vp[2] : 0.0, 0.0);
+  f[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+  m[i] = hm[i];
+  pid[i] = hid[2 * i];
+  sid[i] = hid[2 * i + 1];
+  hidx[i] = i;
+}
+
+// scatter sorted state back to host order: interleaved (d, N) layout
+__global__ void k_download(int n, int d, const int* __restrict__ hidx, const double4_32a* __restrict__ a4,
+                           double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int hi = hidx[i];
+  const double4_32a v = a4[i];
+  double* o = out + (size_t)hi * d;
+  o[0] = v.x;
+  o[1] = v.y;
+  if (d == 3) o[2] = v.z;
+}
+
+__global__ void k_download_scalar(int n, const int* __restrict__ hidx, const double* __restrict__ a,
+                                  double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[hidx[i]] = a[i];
+}
+
+// stress: device [d2][n] component-major -> host (d2, N) interleaved
+__global__ void k_download_tensor(int n, int d2, const int* __restrict__ hidx,
+                                  const double* __restrict__ a, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int hi = hidx[i];
+  for (int c = 0; c < d2; ++c) out[(size_t)hi * d2 + c] = a[(size_t)c * n + i];
+}
+
+int ensure_capacity(Handle* h, int64_t n64) {
+  if (n64 > (int64_t)0x7fffffff / 4) return set_error(h, MCFG_EINVAL, "too many particles");
+  const int n = (int)n64;
+  const int d = h->p.num_dim;
+  int rc;
+  if (n > h->cap_n || !h->x) {
+    free_all(h);
+    const size_t cap = (size_t)(n > 0 ? n : 1);
+    int neigh = h->p.reserved[0] > 0 ? h->p.reserved[0] : (d == 3 ? 256 : 96);
+    h->neigh_cap = neigh;
+    const int nbins = h->k.ncell + 1;
+    const int ntiles = (nbins + 4095) / 4096 + 1;
+    if ((rc = dalloc(h, &h->x, cap)) || (rc = dalloc(h, &h->v, cap)) ||
+        (rc = dalloc(h, &h->f, cap)) || (rc = dalloc(h, &h->m, cap)) ||
+        (rc = dalloc(h, &h->pid, cap)) || (rc = dalloc(h, &h->sid, cap)) ||
+        (rc = dalloc(h, &h->hidx, cap)) || (rc = dalloc(h, &h->rho, cap)) ||
+        (rc = dalloc(h, &h->pr, cap)) || (rc = dalloc(h, &h->x2, cap)) ||
+        (rc = dalloc(h, &h->v2, cap)) || (rc = dalloc(h, &h->f2, cap)) ||
+        (rc = dalloc(h, &h->m2, cap)) || (rc = dalloc(h, &h->pid2, cap)) ||
+        (rc = dalloc(h, &h->sid2, cap)) || (rc = dalloc(h, &h->hidx2, cap)) ||
+        (rc = dalloc(h, &h->key, cap)) || (rc = dalloc(h, &h->rank, cap)) ||
+        (rc = dalloc(h, &h->order, cap)) || (rc = dalloc(h, &h->off, cap)) ||
+        (rc = dalloc(h, &h->cell_of, cap)) || (rc = dalloc(h, &h->ncount, cap)) ||
+        (rc = dalloc(h, &h->nl, cap * (size_t)neigh)) ||
+        (rc = dalloc(h, &h->cnt, (size_t)nbins + 1)) ||
+        (rc = dalloc(h, &h->cell_start, (size_t)nbins + 2)) ||
+        (rc = dalloc(h, &h->scan_part, (size_t)ntiles + 1)) ||
+        (rc = dalloc(h, &h->red, (size_t)1024 * 13 + 64)) ||
+        (rc = dalloc(h, &h->d_err, 1)) || (rc = dalloc(h, &h->d_stats, 4)) ||
+        (rc = dalloc(h, &h->d_pairs, 1)))
+      return rc;
+    if (h->p.precision == MCFG_PRECISION_FP64) {
+      if ((rc = dalloc(h, &h->pc, cap))) return rc;
+    } else {
+      if ((rc = dalloc(h, &h->pcf, cap)) || (rc = dalloc(h, &h->vf, cap))) return rc;
+    }
+    if (h->p.stress_tensor)
+      if ((rc = dalloc(h, &h->st, cap * (size_t)(d * d)))) return rc;
+    if ((rc = dalloc(h, &h->up_x, cap * 9)) || (rc = dalloc(h, &h->up_v, cap * 3)) ||
+        (rc = dalloc(h, &h->up_m, cap)) || (rc = dalloc(h, &h->up_id, cap * 2)))
+      return rc;
+    h->up_cap = cap;
+    h->cap_n = n;
+    if (cuda_check(h, cudaMemsetAsync(h->d_err, 0, sizeof(unsigned), h->stream), "memset err"))
+      return MCFG_ECUDA;
+  }
+  return MCFG_OK;
+}
+
+int set_device(Handle* h) {
+  return cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice") ? MCFG_ECUDA : MCFG_OK;
+}
+
+#define GUARD(h)                                                    \
+  do {                                                              \
+    if (!(h)) return MCFG_EINVAL;                                   \
+    int _rc = set_device(h);                                        \
+    if (_rc) return _rc;                                            \
+  } while (0)
+
+#define TRY(expr)          \
+  do {                     \
+    int _rc = (expr);      \
+    if (_rc) return _rc;   \
+  } while (0)
+
+int rhs(Handle* h, int64_t step, int fuse_mode, double dt) {
+  {
+    PhaseScope ps(h, kPhaseList);
+    TRY(build_cell_list(h));
+  }
+  h->have_list = true;
+  {
+    PhaseScope ps(h, kPhaseDensity);
+    TRY(compute_density(h, true));
+  }
+  h->have_density = h->have_pressure = true;
+  {
+    PhaseScope ps(h, kPhaseForce);
+    TRY(compute_force(h, step, fuse_mode, dt));
+  }
+  h->have_force = true;
+  return MCFG_OK;
+}
+
+int kdw(Handle* h, double dt) {
+  PhaseScope ps(h, kPhaseUpdate);
+  return kick_drift_wrap(h, dt);
+}
+
+__global__ void k_upload_force(int n, int d, const double* __restrict__ hf,
+                               const int* __restrict__ hidx, double4_32a* __restrict__ f) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* fp = hf + (size_t)hidx[i] * d;
+  f[i] = make_double4_32a(fp[0], fp[1], d == 3 ? fp[2] : 0.0, 0.0);
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t mcfg_sizeof_params(void) { return (int64_t)sizeof(mcfg_params); }
+
+const char* mcfg_create_error(void) {
+  std::lock_guard<std::mutex> lk(g_create_mu);
+  return g_create_err.c_str();
+}
+
+int mcfg_create(const mcfg_params* params, mcfg_handle** out) {
+  if (!out) return MCFG_EINVAL;
+  *out = nullptr;
+  const char* msg = validate(params);
+  if (msg) {
+    std::lock_guard<std::mutex> lk(g_create_mu);
+    g_create_err = msg;
+    return MCFG_EINVAL;
+  }
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev <= params->device || params->device < 0) {
+    std::lock_guard<std::mutex> lk(g_create_mu);
+    g_create_err = std::string("no usable CUDA device: ") +
+                   (e != cudaSuccess ? cudaGetErrorString(e) : "ordinal out of range");
+    return MCFG_ENODEV;
+  }
+  mcfg_handle* h = new mcfg_handle();
+  h->p = *params;
+  h->device = params->device;
+  h->dt = params->dt;
+  fill_consts(h);
+  for (int a = 0; a < h->k.d; ++a) {
+    if (h->k.periodic[a] && h->k.nm[a] < 3) {
+      std::lock_guard<std::mutex> lk(g_create_mu);
+      g_create_err = "a periodic axis needs at least 3 cells (box >= 3*1.0001*cut_off)";
+      delete h;
+      return MCFG_EINVAL;
+    }
+  }
+  if (cudaSetDevice(h->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    std::lock_guard<std::mutex> lk(g_create_mu);
+    g_create_err = "cannot create a CUDA stream";
+    delete h;
+    return MCFG_ECUDA;
+  }
+  *out = h;
+  return MCFG_OK;
+}
+
+int mcfg_destroy(mcfg_handle* h) {
+  if (!h) return MCFG_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  resolve_phases(h);
+  for (auto& ev : h->ev_pool) {
+    cudaEventDestroy(ev.first);
+    cudaEventDestroy(ev.second);
+  }
+  h->ev_pool.clear();
+  free_all(h);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return MCFG_OK;
+}
+
+const char* mcfg_last_error(const mcfg_handle* h) {
+  if (!h) return "null handle";
+  return h->err.empty() ? "no error" : h->err.c_str();
+}
+
+int mcfg_get_info(const mcfg_handle* h, mcfg_info* info) {
+  if (!h || !info) return MCFG_EINVAL;
+  memset(info, 0, sizeof *info);
+  info->num_part = h->n;
+  for (int a = 0; a < 3; ++a) info->num_cell_dim[a] = h->k.nm[a];
+  info->num_cell = h->k.ncell;
+  info->num_outside = h->num_outside;
+  info->num_pairs = h->num_pairs;
+  info->max_neigh = h->max_neigh;
+  info->neigh_capacity = h->neigh_cap;
+  info->kernel_launches = h->launches;
+  info->device_bytes = h->device_bytes;
+  return MCFG_OK;
+}
+
+int mcfg_upload(mcfg_handle* h, int64_t n, const double* x, const double* v, const double* m,
+                const int32_t* id, const double* ct) {
+  GUARD(h);
+  if (n < 0 || (n > 0 && (!x || !v || !m || !id)))
+    return set_error(h, MCFG_EINVAL, "mcfg_upload: NULL array");
+  if (ct && h->p.Newtonian == 0) return set_error(h, MCFG_ENOTSUP, "conformation tensor");
+  TRY(ensure_capacity(h, n));
+  const int d = h->p.num_dim;
+  h->n = n;
+  h->k.n = (int)n;
+  if (n > 0) {
+    cudaStream_t s = h->stream;
+    if (cuda_check(h, cudaMemcpyAsync(h->up_x, x, sizeof(double) * (size_t)(n * d),
+                                      cudaMemcpyHostToDevice, s), "upload x") ||
+        cuda_check(h, cudaMemcpyAsync(h->up_v, v, sizeof(double) * (size_t)(n * d),
+                                      cudaMemcpyHostToDevice, s), "upload v") ||
+        cuda_check(h, cudaMemcpyAsync(h->up_m, m, sizeof(double) * (size_t)n,
+                                      cudaMemcpyHostToDevice, s), "upload m") ||
+        cuda_check(h, cudaMemcpyAsync(h->up_id, id, sizeof(int32_t) * (size_t)(2 * n),
+                                      cudaMemcpyHostToDevice, s), "upload id"))
+      return MCFG_ECUDA;
+    const int tb = 256, gb = (int)((n + tb - 1) / tb);
+    k_upload<<<gb, tb, 0, s>>>((int)n, d, h->up_x, h->up_v, h->up_m, h->up_id, h->x, h->v, h->f,
+                               h->m, h->pid, h->sid, h->hidx);
+    h->launches++;
+    if (cuda_check(h, cudaGetLastError(), "upload kernel")) return MCFG_ECUDA;
+    if (h->p.stress_tensor)
+      if (cuda_check(h, cudaMemsetAsync(h->st, 0, sizeof(double) * (size_t)(n * d * d), s),
+                     "memset stress"))
+        return MCFG_ECUDA;
+    if (cuda_check(h, cudaMemsetAsync(h->rho, 0, sizeof(double) * (size_t)n, s), "memset rho") ||
+        cuda_check(h, cudaMemsetAsync(h->pr, 0, sizeof(double) * (size_t)n, s), "memset p"))
+      return MCFG_ECUDA;
+  }
+  // pageable host buffers: the copies above are complete only after a sync
+  if (cuda_check(h, cudaStreamSynchronize(h->stream), "upload sync")) return MCFG_ECUDA;
+  h->have_particles = true;
+  h->have_list = h->have_density = h->have_pressure = h->have_force = false;
+  return MCFG_OK;
+}
+
+int mcfg_upload_force(mcfg_handle* h, const double* f) {
+  GUARD(h);
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  if (!f) return set_error(h, MCFG_EINVAL, "mcfg_upload_force: NULL array");
+  const int n = (int)h->n, d = h->p.num_dim;
+  if (n == 0) return MCFG_OK;
+  cudaStream_t s = h->stream;
+  if (cuda_check(h, cudaMemcpyAsync(h->up_x, f, sizeof(double) * (size_t)n * d,
+                                    cudaMemcpyHostToDevice, s), "upload f"))
+    return MCFG_ECUDA;
+  const int tb = 256, gb = (n + tb - 1) / tb;
+  k_upload_force<<<gb, tb, 0, s>>>(n, d, h->up_x, h->hidx, h->f);
+  h->launches++;
+  if (cuda_check(h, cudaGetLastError(), "upload force kernel") ||
+      cuda_check(h, cudaStreamSynchronize(s), "upload force sync"))
+    return MCFG_ECUDA;
+  h->have_force = true;
+  return MCFG_OK;
+}
+
+int mcfg_adjust_particles(mcfg_handle* h) {
+  GUARD(h);
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  TRY(adjust_particles(h));
+  h->have_list = h->have_density = h->have_pressure = false;
+  return MCFG_OK;
+}
+
+int mcfg_build_list(mcfg_handle* h, int32_t* num_cell_dim, int32_t* cell_start, int32_t* lpdx) {
+  GUARD(h);
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  TRY(build_cell_list(h));
+  h->have_list = true;
+  h->have_density = h->have_pressure = false;
+  if (num_cell_dim)
+    for (int a = 0; a < 3; ++a) num_cell_dim[a] = h->k.nm[a];
+  cudaStream_t s = h->stream;
+  int outside_start = 0;
+  if (cuda_check(h, cudaMemcpyAsync(&outside_start, h->cell_start + h->k.ncell, sizeof(int),
+                                    cudaMemcpyDeviceToHost, s), "copy cell_start"))
+    return MCFG_ECUDA;
+  if (cell_start &&
+      cuda_check(h, cudaMemcpyAsync(cell_start, h->cell_start, sizeof(int) * (size_t)(h->k.ncell + 1),
+                                    cudaMemcpyDeviceToHost, s), "copy cell_start"))
+    return MCFG_ECUDA;
+  if (lpdx && h->n > 0 &&
+      cuda_check(h, cudaMemcpyAsync(lpdx, h->hidx, sizeof(int) * (size_t)h->n,
+                                    cudaMemcpyDeviceToHost, s), "copy lpdx"))
+    return MCFG_ECUDA;
+  if (cuda_check(h, cudaStreamSynchronize(s), "build_list sync")) return MCFG_ECUDA;
+  h->num_outside = h->n - outside_start;
+  return check_device_errors(h);
+}
+
+int mcfg_compute_density(mcfg_handle* h) {
+  GUARD(h);
+  if (!h->have_list) return set_error(h, MCFG_ESTATE, "mcfg_build_list must come first");
+  TRY(compute_density(h, false));
+  TRY(check_device_errors(h));
+  h->have_density = true;
+  h->have_pressure = false;
+  return MCFG_OK;
+}
+
+int mcfg_compute_pressure(mcfg_handle* h) {
+  GUARD(h);
+  if (!h->have_density) return set_error(h, MCFG_ESTATE, "mcfg_compute_density must come first");
+  TRY(compute_pressure(h));
+  h->have_pressure = true;
+  return MCFG_OK;
+}
+
+int mcfg_compute_interaction(mcfg_handle* h, int64_t step) {
+  GUARD(h);
+  if (!h->have_pressure) return set_error(h, MCFG_ESTATE, "mcfg_compute_pressure must come first");
+  TRY(compute_force(h, step, kForceOnly, h->dt));
+  TRY(check_device_errors(h));
+  h->have_force = true;
+  return MCFG_OK;
+}
+
+int mcfg_apply_body_force(mcfg_handle* h) {
+  GUARD(h);
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  return apply_body_force(h);
+}
+
+int mcfg_integrate_velocity(mcfg_handle* h, double dt, double lambda) {
+  GUARD(h);
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  return integrate_velocity(h, dt, lambda);
+}
+
+int mcfg_integrate_position(mcfg_handle* h, double dt) {
+  GUARD(h);
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  TRY(integrate_position(h, dt));
+  h->have_list = h->have_density = h->have_pressure = false;
+  return MCFG_OK;
+}
+
+int mcfg_init_force(mcfg_handle* h, int64_t step) {
+  GUARD(h);
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  TRY(adjust_particles(h));
+  TRY(rhs(h, step, kForceBody, h->dt));
+  return check_device_errors(h);
+}
+
+int mcfg_step_vv(mcfg_handle* h, int64_t step, double dt) {
+  GUARD(h);
+  if (!h->have_force) return set_error(h, MCFG_ESTATE, "mcfg_init_force must come first");
+  if (!(dt > 0.0)) return set_error(h, MCFG_EINVAL, "dt must be positive");
+  h->dt = dt;
+  TRY(kdw(h, dt));
+  TRY(rhs(h, step, kForceBodyKick, dt));
+  return check_device_errors(h);
+}
+
+int mcfg_run_vv(mcfg_handle* h, int64_t step0, int32_t nsteps, double dt) {
+  GUARD(h);
+  if (!h->have_force) return set_error(h, MCFG_ESTATE, "mcfg_init_force must come first");
+  if (!(dt > 0.0)) return set_error(h, MCFG_EINVAL, "dt must be positive");
+  h->dt = dt;
+  for (int32_t q = 1; q <= nsteps; ++q) {
+    TRY(kdw(h, dt));
+    TRY(rhs(h, step0 + q, kForceBodyKick, dt));
+  }
+  return check_device_errors(h);
+}
+
+int mcfg_download(mcfg_handle* h, double* x, double* v, double* rho, double* p, double* f,
+                  double* ct, double* s) {
+  GUARD(h);
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  if (ct) return set_error(h, MCFG_ENOTSUP, "conformation tensor not in this build");
+  if (s && !h->p.stress_tensor) return set_error(h, MCFG_EINVAL, "stress_tensor is off");
+  const int n = (int)h->n, d = h->p.num_dim;
+  if (n == 0) return MCFG_OK;
+  cudaStream_t st = h->stream;
+  const int tb = 256, gb = (n + tb - 1) / tb;
+  double* stage = h->up_x;  // n*9 doubles of staging
+  auto vec_out = [&](const double4_32a* a4, double* host) -> int {
+    k_download<<<gb, tb, 0, st>>>(n, d, h->hidx, a4, stage);
+    h->launches++;
+    if (cuda_check(h, cudaMemcpyAsync(host, stage, sizeof(double) * (size_t)n * d,
+                                      cudaMemcpyDeviceToHost, st), "download"))
+      return MCFG_ECUDA;
+    return cuda_check(h, cudaStreamSynchronize(st), "download sync") ? MCFG_ECUDA : MCFG_OK;
+  };
+  auto sca_out = [&](const double* a, double* host) -> int {
+    k_download_scalar<<<gb, tb, 0, st>>>(n, h->hidx, a, stage);
+    h->launches++;
+    if (cuda_check(h, cudaMemcpyAsync(host, stage, sizeof(double) * (size_t)n,
+                                      cudaMemcpyDeviceToHost, st), "download"))
+      return MCFG_ECUDA;
+    return cuda_check(h, cudaStreamSynchronize(st), "download sync") ? MCFG_ECUDA : MCFG_OK;
+  };
+  if (x) TRY(vec_out(h->x, x));
+  if (v) TRY(vec_out(h->v, v));
+  if (f) TRY(vec_out(h->f, f));
+  if (rho) TRY(sca_out(h->rho, rho));
+  if (p) TRY(sca_out(h->pr, p));
+  if (s) {
+    k_download_tensor<<<gb, tb, 0, st>>>(n, d * d, h->hidx, h->st, stage);
+    h->launches++;
+    if (cuda_check(h, cudaMemcpyAsync(s, stage, sizeof(double) * (size_t)n * d * d,
+                                      cudaMemcpyDeviceToHost, st), "download s") ||
+        cuda_check(h, cudaStreamSynchronize(st), "download sync"))
+      return MCFG_ECUDA;
+  }
+  return MCFG_OK;
+}
+
+int mcfg_statistics(mcfg_handle* h, double* k_energy, double* momentum, double* stress) {
+  GUARD(h);
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  return statistics(h, k_energy, momentum, stress);
+}
+
+void* mcfg_get_stream(mcfg_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int mcfg_set_profiling(mcfg_handle* h, int mode) {
+  GUARD(h);
+  if (mode == 2) {
+    if (cuda_check(h, cudaStreamSynchronize(h->stream), "synchronize")) return MCFG_ECUDA;
+    resolve_phases(h);
+    for (int ph = 0; ph < 5; ++ph) {
+      h->phase_ms[ph] = 0.0;
+      h->phase_cnt[ph] = 0;
+    }
+    return MCFG_OK;
+  }
+  if (mode != 0 && mode != 1) return set_error(h, MCFG_EINVAL, "profiling mode must be 0, 1 or 2");
+  h->profiling = mode == 1;
+  return MCFG_OK;
+}
+
+int mcfg_get_phase_times(mcfg_handle* h, double* ms, int64_t* counts) {
+  GUARD(h);
+  if (cuda_check(h, cudaStreamSynchronize(h->stream), "synchronize")) return MCFG_ECUDA;
+  resolve_phases(h);
+  for (int ph = 0; ph < 5; ++ph) {
+    if (ms) ms[ph] = h->phase_ms[ph];
+    if (counts) counts[ph] = h->phase_cnt[ph];
+  }
+  return MCFG_OK;
+}
+
+int mcfg_synchronize(mcfg_handle* h) {
+  GUARD(h);
+  if (cuda_check(h, cudaStreamSynchronize(h->stream), "synchronize")) return MCFG_ECUDA;
+  return check_device_errors(h);
+}
+
+}  // extern "C"

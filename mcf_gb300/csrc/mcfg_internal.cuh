@@ -1,0 +1,239 @@
+// mcfg_internal.cuh -- handle layout and device helpers shared by the
+// translation units of libmcfg (GB300-native SDPD step, sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/mcfg.h"
+
+namespace mcfg {
+
+constexpr int kWarp = 32;
+constexpr int kMaxStencil = 27;   // 3D full stencil (9 in 2D)
+constexpr int kLocalBits = 11;    // neighbour entry: slot<<11 | local index
+constexpr int kMaxCellCount = 1 << kLocalBits;  // particles per cell limit
+constexpr double kPi = 3.141592653589793238;    // mcf_header.F90:50
+
+// device-side error flags (bitmask in Handle::d_err)
+enum DevErr : unsigned {
+  kErrNeighOverflow = 1u,   // neighbour list capacity exceeded
+  kErrCellOverflow = 2u,    // a cell holds more than kMaxCellCount particles
+  kErrZeroDensity = 4u,     // non-positive density met in a pair
+  kErrNonFinite = 8u,       // NaN/Inf produced
+};
+
+// Constants of one configuration, passed by value to kernels.
+struct Consts {
+  int d;
+  int n;                 // particles
+  int ncell;             // real cells
+  int nm[3];             // cells per dimension
+  int periodic[3];
+  int bc_lo[3], bc_hi[3];   // bcdef of the lower / upper face per axis
+  double xmin[3], xmax[3];  // mesh extent (min_phys_t, max_phys_t)
+  double rdx[3];            // Nm/(xmax-xmin), ppm_util_rank3d.F90:352-354
+  double cs[3];             // cell side (xmax-xmin)/Nm
+  double len[3];            // period per dimension
+  float csf[3];
+  double rc2;               // cut_off**2
+  float rc2f, rc2f_hi;      // FP32 cut-off^2 and its prefilter bound
+  // kernel
+  int kernel_type;
+  double h, inv_h, coef, coef_grad, w0;
+  float hf, inv_hf, coeff, coef_gradf, w0f;
+  // physics
+  int rhs_density_type, rhs_force_type, eos_type;
+  double c2, rho_ref, gamma, p0;
+  double eta, eta_coef, kt;
+  int noise;             // Brownian && kt > machine_zero
+  int wall_rho_type, wall_noslip_type;
+  double init_density;
+  double min_phys[3], max_phys[3];
+  double wall_v[6][3];
+  int stress;
+  uint32_t key0, key1;   // Philox key (seed)
+  int body_force_type;
+  double body_force[3];
+  double machine_zero;
+};
+
+struct Handle {
+  mcfg_params p{};
+  Consts k{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  bool have_particles = false, have_list = false, have_density = false,
+       have_pressure = false, have_force = false;
+  int64_t n = 0;
+  int cap_n = 0;           // allocated particle capacity
+  int neigh_cap = 0;       // neighbour list capacity per particle
+  double dt = 0.0;
+  int64_t launches = 0;
+  int64_t device_bytes = 0;
+  int64_t num_outside = 0;
+  int64_t num_pairs = 0;
+  int max_neigh = 0;
+
+  // ---- state, sorted by cell (index = sorted slot) ----
+  double4_32a* x = nullptr;   // position (w unused)
+  double4_32a* v = nullptr;   // velocity
+  double4_32a* f = nullptr;   // acceleration
+  double* m = nullptr;
+  int* pid = nullptr;
+  int* sid = nullptr;
+  int* hidx = nullptr;    // host index of the particle in this slot
+  double* rho = nullptr;
+  double* pr = nullptr;
+  double* st = nullptr;   // stress, [d*d][cap] component-major
+  // double buffers for the permutation
+  double4_32a *x2 = nullptr, *v2 = nullptr, *f2 = nullptr;
+  double* m2 = nullptr;
+  int *pid2 = nullptr, *sid2 = nullptr, *hidx2 = nullptr;
+  // ---- cell list ----
+  int* key = nullptr;        // cell of each particle (pre-sort order)
+  int* rank = nullptr;       // arrival rank within the cell
+  int* cnt = nullptr;        // [ncell+1] counts (last bin: outside)
+  int* cell_start = nullptr; // [ncell+2]
+  int* scan_part = nullptr;  // scan partials
+  int* order = nullptr;      // pre-sort index per unsorted slot
+  float4* off = nullptr;     // FP32 offset to the cell origin, w = cell id
+  int* cell_of = nullptr;    // cell per sorted particle (ncell = outside)
+  // ---- neighbours ----
+  uint16_t* nl = nullptr;    // [neigh_cap][cap] entries slot<<11|local
+  int* ncount = nullptr;     // [cap]
+  // ---- pair records ----
+  double4_32a* pc = nullptr;     // FP64 path: (p/n^2 or p, 1/n^2, 1/m, rho)
+  float4* pcf = nullptr;     // FP32 path: same in float
+  float4* vf = nullptr;      // FP32 path: velocity (w = packed id bits)
+  // ---- reductions & errors ----
+  double* red = nullptr;     // block partials
+  unsigned* d_err = nullptr; // device error bitmask
+  int* d_stats = nullptr;    // [0] outside count, [1] max neigh, [2] pairs lo
+  unsigned long long* d_pairs = nullptr;
+  void* h_pinned = nullptr;  // small pinned staging
+  // upload staging (device copies of host-order arrays)
+  double* up_x = nullptr;
+  double* up_v = nullptr;
+  double* up_m = nullptr;
+  int* up_id = nullptr;
+  size_t up_cap = 0;
+  // ---- per-phase device timers ----
+  bool profiling = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pending[5];
+  double phase_ms[5] = {0, 0, 0, 0, 0};
+  int64_t phase_cnt[5] = {0, 0, 0, 0, 0};
+};
+
+enum Phase { kPhaseList = 0, kPhaseDensity = 1, kPhaseForce = 2, kPhaseUpdate = 3, kPhaseOther = 4 };
+
+// Records CUDA events around one phase when profiling is on.
+struct PhaseScope {
+  Handle* h;
+  int phase;
+  std::pair<cudaEvent_t, cudaEvent_t> ev{nullptr, nullptr};
+  PhaseScope(Handle* hh, int ph) : h(hh), phase(ph) {
+    if (!h->profiling) return;
+    if (h->ev_pool.empty()) {
+      cudaEvent_t a, b;
+      if (cudaEventCreate(&a) != cudaSuccess) return;
+      if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return;
+      }
+      h->ev_pool.push_back({a, b});
+    }
+    ev = h->ev_pool.back();
+    h->ev_pool.pop_back();
+    cudaEventRecord(ev.first, h->stream);
+  }
+  ~PhaseScope() {
+    if (!ev.first) return;
+    cudaEventRecord(ev.second, h->stream);
+    h->ev_pending[phase].push_back(ev);
+  }
+};
+
+// accumulate completed phase events (call after a stream synchronize)
+void resolve_phases(Handle* h);
+
+// set err and return code
+int set_error(Handle* h, int code, const std::string& msg);
+int cuda_check(Handle* h, cudaError_t e, const char* what);
+
+// launches (implemented in the .cu files)
+int build_cell_list(Handle* h);
+int compute_density(Handle* h, bool with_pressure);
+int compute_pressure(Handle* h);
+int compute_force(Handle* h, int64_t step, int fuse_mode, double dt);
+int apply_body_force(Handle* h);
+int integrate_velocity(Handle* h, double dt, double lambda);
+int integrate_position(Handle* h, double dt);
+int adjust_particles(Handle* h);
+int kick_drift_wrap(Handle* h, double dt);
+int statistics(Handle* h, double* ke, double* mom, double* stress);
+int check_device_errors(Handle* h);
+
+// fuse_mode of compute_force
+enum { kForceOnly = 0, kForceBody = 1, kForceBodyKick = 2 };
+
+// ------------------------------------------------------------------------
+// Device helpers
+// ------------------------------------------------------------------------
+
+// Philox4x32-10, Salmon et al., SC'11 ("Parallel random numbers: as easy as
+// 1, 2, 3"): multipliers and Weyl key increments of the published algorithm.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t lo0 = 0xD2511F53u * c.x;
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x);
+    const uint32_t lo1 = 0xCD9E8D57u * c.z;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z);
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// odd multiple of 2^-24 in (0,1), exact in FP32
+__device__ __forceinline__ float u01(uint32_t r) {
+  return (float)((r >> 9) * 2u + 1u) * (1.0f / 16777216.0f);
+}
+
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {
+  const float u1 = u01(a), u2 = u01(b);
+  const float rad = sqrtf(-2.0f * logf(u1));
+  float sn, cs;
+  sincospif(2.0f * u2, &sn, &cs);
+  z0 = rad * cs;
+  z1 = rad * sn;
+}
+
+// normals of a pair: 3D z[0..5] (diagonal 0..2, off-diagonal 3..5),
+// 2D z[0..2]; the counter is (min pid, max pid, step, call) so the draw is
+// the same from both particles of the pair.
+template <int D>
+__device__ __forceinline__ void pair_normals(uint32_t k0, uint32_t k1, uint32_t step,
+                                             int pa, int pb, float* z) {
+  const uint32_t a = (uint32_t)min(pa, pb), b = (uint32_t)max(pa, pb);
+  uint4 r = philox4x32_10(make_uint4(a, b, step, 0u), k0, k1);
+  float t0, t1;
+  box_muller(r.x, r.y, z[0], z[1]);
+  box_muller(r.z, r.w, t0, t1);
+  z[2] = t0;
+  if (D == 3) {
+    z[3] = t1;
+    r = philox4x32_10(make_uint4(a, b, step, 1u), k0, k1);
+    box_muller(r.x, r.y, z[4], z[5]);
+  }
+}
+
+}  // namespace mcfg

@@ -1,0 +1,289 @@
+// sph.cuh -- SPH kernel, equation of state and pair force forms, templated
+// on the arithmetic type (double: FP64 path, float: FP32-mixed path).
+#pragma once
+#include "mcfg_internal.cuh"
+
+namespace mcfg {
+
+template <typename T>
+struct KC;  // kernel constants in T
+template <>
+struct KC<double> {
+  __device__ static double inv_h(const Consts& k) { return k.inv_h; }
+  __device__ static double coef(const Consts& k) { return k.coef; }
+  __device__ static double coef_grad(const Consts& k) { return k.coef_grad; }
+};
+template <>
+struct KC<float> {
+  __device__ static float inv_h(const Consts& k) { return k.inv_hf; }
+  __device__ static float coef(const Consts& k) { return k.coeff; }
+  __device__ static float coef_grad(const Consts& k) { return k.coef_gradf; }
+};
+
+// W(r): kernel_kernel_quintic_spline.F90:69-99 (h = rc/3, W = coef*[(3-s)^5
+// - 6(2-s)^5 + 15(1-s)^5] piecewise) and kernel_kernel_Lucy.F90:68-78.
+template <typename T>
+__device__ __forceinline__ T kernel_w(const Consts& k, T r) {
+  const T s = r * KC<T>::inv_h(k);
+  if (k.kernel_type == 1) {
+    const T s3 = T(3) - s, s2 = T(2) - s, s1 = T(1) - s;
+    T a3 = s3 * s3;
+    a3 = a3 * a3 * s3;
+    T w = T(0);
+    if (s < T(3)) w = a3;
+    if (s < T(2)) {
+      T a2 = s2 * s2;
+      a2 = a2 * a2 * s2;
+      w = w - T(6) * a2;
+    }
+    if (s < T(1)) {
+      T a1 = s1 * s1;
+      a1 = a1 * a1 * s1;
+      w = w + T(15) * a1;
+    }
+    return KC<T>::coef(k) * w;
+  } else {
+    if (s > T(1)) return T(0);
+    const T om = T(1) - s;
+    return KC<T>::coef(k) * (T(1) + T(3) * s) * (om * om * om);
+  }
+}
+
+// dW/dr: kernel_kernel_quintic_spline.F90:177-215, kernel_kernel_Lucy.F90:155-168
+template <typename T>
+__device__ __forceinline__ T kernel_gradw(const Consts& k, T r) {
+  const T s = r * KC<T>::inv_h(k);
+  if (k.kernel_type == 1) {
+    const T s3 = T(3) - s, s2 = T(2) - s, s1 = T(1) - s;
+    T g = T(0);
+    if (s < T(3)) {
+      const T a = s3 * s3;
+      g = T(5) * (a * a);
+    }
+    if (s < T(2)) {
+      const T a = s2 * s2;
+      g = g - T(30) * (a * a);
+    }
+    if (s < T(1)) {
+      const T a = s1 * s1;
+      g = g + T(75) * (a * a);
+    }
+    return KC<T>::coef_grad(k) * g;
+  } else {
+    if (s > T(1)) return T(0);
+    const T om = T(1) - s;
+    return KC<T>::coef_grad(k) * T(12) * s * (om * om);
+  }
+}
+
+// Pressure, stateEquation_compute_pressure.F90:147-180 (vector forms):
+// Morris p = c^2 (rho^gamma - rho_ref), Batchelor p = p0((rho/rho_ref)^gamma - 1).
+__device__ __forceinline__ double eos_pressure(const Consts& k, double rho) {
+  if (k.eos_type == 1) {
+    const double rg = (k.gamma == 1.0) ? rho : pow(rho, k.gamma);
+    return k.c2 * (rg - k.rho_ref);
+  }
+  const double q = rho / k.rho_ref;
+  const double qg = (k.gamma == 1.0) ? q : pow(q, k.gamma);
+  return k.p0 * (qg - 1.0);
+}
+
+// Per-particle pair coefficients (A, B, C) of each force form so that the
+// pair loop does no division by per-particle quantities:
+//   type 1 Morris      : A = p/rho^2, B = 1/rho, C = m
+//   type 2 Espanol     : A = p/n^2,   B = 1/n,   C = 1/m
+//   type 3 Hu-Adams    : A = p/n^2,   B = 1/n^2, C = 1/m
+//   type 4 HA angular  : A = p,       B = 1/n^2, C = 1/m
+__device__ __forceinline__ double4_32a pair_coeffs(const Consts& k, double rho, double p, double m) {
+  const double inv = 1.0 / rho;
+  double4_32a r;
+  switch (k.rhs_force_type) {
+    case 1:
+      r = make_double4_32a(p * inv * inv, inv, m, p);
+      break;
+    case 2:
+      r = make_double4_32a(p * inv * inv, inv, 1.0 / m, p);
+      break;
+    case 3:
+      r = make_double4_32a(p * inv * inv, inv * inv, 1.0 / m, p);
+      break;
+    default:
+      r = make_double4_32a(p, inv * inv, 1.0 / m, p);
+      break;
+  }
+  return r;
+}
+
+// A coefficient of a boundary particle whose pressure is replaced by the
+// fluid partner's (pp_interaction_fw.inc: this%p(jp) = this%p(ip)).
+template <typename T>
+__device__ __forceinline__ T boundary_A(int type, T p_fluid, T B) {
+  switch (type) {
+    case 1:
+    case 2:
+      return p_fluid * B * B;
+    case 3:
+      return p_fluid * B;
+    default:
+      return p_fluid;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T my_sqrt(T a);
+template <>
+__device__ __forceinline__ double my_sqrt<double>(double a) { return sqrt(a); }
+template <>
+__device__ __forceinline__ float my_sqrt<float>(float a) { return sqrtf(a); }
+
+// Acceleration of particle i from partner j (i side of the symmetric pair
+// forces of rhs_force_ff_Newtonian_{Morris,Espanol,HuAdams,HuAdams_angular}
+// .F90).  r = x_i - x_j (image), d = |r|, vij = v_i - v_j.  Returns the pair
+// acceleration in acc[].
+template <typename T, int D>
+__device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T d, const T* vij,
+                                           T Ai, T Bi, T Ci, T Aj, T Bj, T Cj, T gw,
+                                           bool noise, const float* z, T inv_sqdt, T* acc) {
+  const T inv_d = T(1) / d;
+  T e[3];
+#pragma unroll
+  for (int a = 0; a < D; ++a) e[a] = r[a] * inv_d;
+  const T eta = (T)k.eta;
+  switch (k.rhs_force_type) {
+    case 1: {
+      const T f_c = (Ai + Aj) * gw;
+      const T f_d = T(2) * eta * gw * Bi * Bj * inv_d;
+#pragma unroll
+      for (int a = 0; a < D; ++a) acc[a] = Cj * (f_d * vij[a] - f_c * e[a]);
+      break;
+    }
+    case 2: {
+      T ev = T(0);
+#pragma unroll
+      for (int a = 0; a < D; ++a) ev += e[a] * vij[a];
+      const T f_c = (Ai + Aj) * gw;
+      const T bb = Bi * Bj * gw * inv_d * eta;
+      const T f_d1 = (T(2) - T(1) / T(D)) * bb;
+      const T f_d2 = (T(D + 2) / T(D)) * bb * ev;
+#pragma unroll
+      for (int a = 0; a < D; ++a) acc[a] = Ci * (f_d1 * vij[a] + (f_d2 - f_c) * e[a]);
+      if (noise) {
+        T dW[3][3];
+        T tr = T(0);
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          dW[a][a] = (T)z[a];
+          tr += dW[a][a];
+        }
+        tr = tr / T(D);
+        const T s2 = T(0.70710678118654752440);
+        if (D == 3) {
+          dW[0][1] = dW[1][0] = (T)z[3] * s2;
+          dW[0][2] = dW[2][0] = (T)z[4] * s2;
+          dW[1][2] = dW[2][1] = (T)z[5] * s2;
+        } else {
+          dW[0][1] = dW[1][0] = (T)z[2] * s2;
+        }
+#pragma unroll
+        for (int a = 0; a < D; ++a) dW[a][a] -= tr;
+        const T Zij = T(4) * (T)k.kt * gw * inv_d * Bi * Bj;
+        const T aa = T(5) * eta / T(3);
+        const T bq = (T(D) + T(2)) * eta / T(3);
+        const T Aij = my_sqrt<T>(-Zij * aa);
+        const T Bij = my_sqrt<T>(-Zij * T(D) / T(2) * (bq + aa * (T(2) / T(D) - T(1))));
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          T We = T(0);
+#pragma unroll
+          for (int b = 0; b < D; ++b) We += dW[a][b] * e[b];
+          acc[a] += Ci * (Aij * We + Bij * tr * e[a]) * inv_sqdt;
+        }
+      }
+      break;
+    }
+    case 3: {
+      const T f_c = (Ai + Aj) * gw;
+      const T f_d = eta * (Bi + Bj) * gw * inv_d;
+#pragma unroll
+      for (int a = 0; a < D; ++a) acc[a] = Ci * (f_d * vij[a] - f_c * e[a]);
+      if (noise) {
+        T dW[3][3];
+        T tr = T(0);
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          dW[a][a] = (T)z[a];
+          tr += dW[a][a];
+        }
+        tr = tr / T(D);
+        const T s2 = T(0.70710678118654752440);
+        if (D == 3) {
+          dW[0][1] = dW[1][0] = (T)z[3] * s2;
+          dW[0][2] = dW[2][0] = (T)z[4] * s2;
+          dW[1][2] = dW[2][1] = (T)z[5] * s2;
+        } else {
+          dW[0][1] = dW[1][0] = (T)z[2] * s2;
+        }
+#pragma unroll
+        for (int a = 0; a < D; ++a) dW[a][a] -= tr;
+        const T f_r = my_sqrt<T>(T(-4) * (T)k.kt * f_d) * inv_sqdt;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          T We = T(0);
+#pragma unroll
+          for (int b = 0; b < D; ++b) We += dW[a][b] * e[b];
+          acc[a] += Ci * f_r * We;
+        }
+      }
+      break;
+    }
+    default: {
+      T ev = T(0);
+#pragma unroll
+      for (int a = 0; a < D; ++a) ev += e[a] * vij[a];
+      const T pij = (Ai + Aj) * T(0.5);
+      const T Aij = (Bi + Bj) * gw;
+      const T f_c = Aij * pij;
+      const T f_d = (T)k.eta_coef * eta * Aij * ev * inv_d;
+      T fe = f_d - f_c;
+      if (noise) {
+        const T eps = (T)z[0];
+        fe += eps * my_sqrt<T>(T(2) * (T)k.kt * eta) * my_sqrt<T>(-(T)k.eta_coef * Aij * inv_d) *
+              inv_sqdt;
+      }
+#pragma unroll
+      for (int a = 0; a < D; ++a) acc[a] = Ci * fe * e[a];
+      break;
+    }
+  }
+}
+
+// Morris no-slip velocity of a solid-wall particle,
+// boundary_noslip_solid.F90:40-95 (frozen) and :137-240 (Morris): wall
+// particles carry sid = -face (1..2d); x_f, x_w are the coordinates along the
+// wall-normal axis.
+template <typename T, int D>
+__device__ __forceinline__ void wall_noslip(const Consts& k, double xf_n, double xw_n,
+                                            const T* vf, int sid_w, T* vw, int& axis) {
+  const int index_w = -sid_w;
+  axis = (index_w - 1) >> 1;
+  const double* sv = k.wall_v[index_w - 1];
+  if (k.wall_noslip_type <= 1) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) vw[a] = (T)sv[a];
+    return;
+  }
+  const double x_sur = (index_w & 1) ? k.min_phys[axis] : k.max_phys[axis];
+  double f_sur = xf_n - x_sur, w_sur = xw_n - x_sur;
+  if (f_sur * w_sur >= 0.0) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) vw[a] = (T)sv[a];
+  } else {
+    double corr = fabs(w_sur) / fabs(f_sur);
+    if (corr > 0.5) corr = 0.5;  // mcf_wall_dist_ratio, mcf_header.F90:282
+    const T c = (T)corr;
+#pragma unroll
+    for (int a = 0; a < D; ++a) vw[a] = -c * (vf[a] - (T)sv[a]) + (T)sv[a];
+  }
+}
+
+}  // namespace mcfg

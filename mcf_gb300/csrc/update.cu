@@ -1,0 +1,212 @@
+// update.cu -- per-particle O(N) kernels of the velocity-Verlet step and the
+// FP64 global reductions.
+//
+// Reference: particles_integrate_velocity.F90:84-94, particles_integrate_
+// position.F90:82-111, particles_adjust_particles.F90:137-389,
+// particles_apply_body_force.F90:96-353, marching_integrate_VV.F90:303-322,
+// statistic_compute_statistic.F90:230-303.
+#include "mcfg_internal.cuh"
+
+namespace mcfg {
+
+// Periodic wrap of one coordinate, particles_adjust_particles.F90:150-161,
+// 268-279: x < min -> x + length; then x >= max -> x - length.  Solid-wall
+// faces only clamp wall particles to the total domain.
+__device__ __forceinline__ void wrap_axis(const Consts& k, int a,
+                                          int sid, double& x, double& v) {
+  if (x < k.min_phys[a]) {
+    if (k.bc_lo[a] == MCFG_BC_PERIODIC) {
+      x = __dadd_rn(x, k.len[a]);
+    } else if (k.bc_lo[a] == MCFG_BC_WALL_SOLID) {
+      if (sid < 0 && x < k.xmin[a]) {
+        x = k.xmin[a];
+        v = 0.0;
+      }
+    }
+  }
+  if (x >= k.max_phys[a]) {
+    if (k.bc_hi[a] == MCFG_BC_PERIODIC) {
+      x = __dsub_rn(x, k.len[a]);
+    } else if (k.bc_hi[a] == MCFG_BC_WALL_SOLID) {
+      if (sid < 0 && x > k.xmax[a]) {
+        x = k.xmax[a] - k.machine_zero;
+        v = 0.0;
+      }
+    }
+  }
+}
+
+// flags: 1 half kick, 2 drift, 4 wrap.  The arithmetic is rounded exactly
+// like MCF's: v + (lambda*f)*dt, x + v*dt (no fused multiply-add).
+template <int D>
+__global__ void k_integrate(Consts k, int flags, double dt, double lambda,
+                            double4_32a* __restrict__ x, double4_32a* __restrict__ v,
+                            const double4_32a* __restrict__ f, const int* __restrict__ sid) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= k.n) return;
+  const int s = sid[i];
+  double4_32a xv = x[i], vv = v[i];
+  double xs[3] = {xv.x, xv.y, xv.z}, vs[3] = {vv.x, vv.y, vv.z};
+  if (s == 0) {
+    if (flags & 1) {
+      const double4_32a fv = f[i];
+      const double fs[3] = {fv.x, fv.y, fv.z};
+#pragma unroll
+      for (int a = 0; a < D; ++a) vs[a] = __dadd_rn(vs[a], __dmul_rn(__dmul_rn(lambda, fs[a]), dt));
+    }
+    if (flags & 2) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) xs[a] = __dadd_rn(xs[a], __dmul_rn(vs[a], dt));
+    }
+  }
+  if (flags & 4) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) wrap_axis(k, a, s, xs[a], vs[a]);
+  }
+  x[i] = make_double4_32a(xs[0], xs[1], D == 3 ? xs[2] : 0.0, 0.0);
+  v[i] = make_double4_32a(vs[0], vs[1], D == 3 ? vs[2] : 0.0, 0.0);
+}
+
+template <int D>
+__global__ void k_body_force(Consts k, const double4_32a* __restrict__ x, double4_32a* __restrict__ f,
+                             const int* __restrict__ sid) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= k.n || sid[i] != 0) return;
+  double4_32a fv = f[i];
+  const double4_32a xv = x[i];
+  const double* g = k.body_force;
+  if (k.body_force_type == 1) {
+    if (fabs(g[0]) > k.machine_zero) fv.x = fv.x + g[0];
+    if (fabs(g[1]) > k.machine_zero) fv.y = fv.y + g[1];
+    if (D == 3 && fabs(g[2]) > k.machine_zero) fv.z = fv.z + g[2];
+  } else if (k.body_force_type == 2) {
+    if (fabs(g[0]) > k.machine_zero) {
+      const double half = k.max_phys[D - 1] * 0.5;
+      const double xl = (D == 3) ? xv.z : xv.y;
+      if (xl < half)
+        fv.x = fv.x + g[0];
+      else if (xl > half)
+        fv.x = fv.x - g[0];
+    }
+  } else if (k.body_force_type == 3) {
+    if (fabs(g[0]) > k.machine_zero) {
+      const double kw = 2.0 * kPi / (k.max_phys[1] - k.min_phys[1]);
+      fv.x = fv.x + g[0] * sin(kw * xv.y);
+    }
+  }
+  f[i] = fv;
+}
+
+// ---- FP64 reductions: fixed-order two-pass block sums (deterministic) ----
+constexpr int kRedThreads = 256;
+constexpr int kRedVals = 13;  // ke, mom[3], stress[9]
+
+template <int D>
+__global__ void k_stats_partial(Consts k, const double4_32a* __restrict__ v,
+                                const double* __restrict__ m, const int* __restrict__ sid,
+                                const double* __restrict__ st, double* __restrict__ part) {
+  __shared__ double sm[kRedVals][kRedThreads];
+  double acc[kRedVals];
+#pragma unroll
+  for (int q = 0; q < kRedVals; ++q) acc[q] = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k.n; i += gridDim.x * blockDim.x) {
+    const int s = sid[i];
+    if (s == 0) {
+      const double4_32a vv = v[i];
+      const double mi = m[i];
+      double v2 = vv.x * vv.x + vv.y * vv.y;
+      if (D == 3) v2 += vv.z * vv.z;
+      acc[0] += 0.5 * mi * v2;
+      acc[1] += mi * vv.x;
+      acc[2] += mi * vv.y;
+      if (D == 3) acc[3] += mi * vv.z;
+    }
+    if (k.stress && s >= 0) {
+#pragma unroll
+      for (int a = 0; a < D * D; ++a) acc[4 + a] += st[(size_t)a * k.n + i];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kRedVals; ++q) sm[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+#pragma unroll
+      for (int q = 0; q < kRedVals; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int q = 0; q < kRedVals; ++q) part[(size_t)blockIdx.x * kRedVals + q] = sm[q][0];
+}
+
+__global__ void k_stats_final(const double* __restrict__ part, int nparts, double* __restrict__ out) {
+  const int q = threadIdx.x;
+  if (q >= kRedVals) return;
+  double s = 0.0;
+  for (int b = 0; b < nparts; ++b) s += part[(size_t)b * kRedVals + q];
+  out[q] = s;
+}
+
+static int launch_integrate(Handle* h, int flags, double dt, double lambda) {
+  const int n = (int)h->n;
+  if (n == 0) return MCFG_OK;
+  const int tb = 256, gb = (n + tb - 1) / tb;
+  if (h->k.d == 3)
+    k_integrate<3><<<gb, tb, 0, h->stream>>>(h->k, flags, dt, lambda, h->x, h->v, h->f,
+                                             h->sid);
+  else
+    k_integrate<2><<<gb, tb, 0, h->stream>>>(h->k, flags, dt, lambda, h->x, h->v, h->f,
+                                             h->sid);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "integrate launch") ? MCFG_ECUDA : MCFG_OK;
+}
+
+int integrate_velocity(Handle* h, double dt, double lambda) {
+  return launch_integrate(h, 1, dt, lambda);
+}
+int integrate_position(Handle* h, double dt) { return launch_integrate(h, 2, dt, 0.0); }
+int adjust_particles(Handle* h) { return launch_integrate(h, 4, 0.0, 0.0); }
+int kick_drift_wrap(Handle* h, double dt) { return launch_integrate(h, 7, dt, 0.5); }
+
+int apply_body_force(Handle* h) {
+  const int n = (int)h->n;
+  if (n == 0 || h->k.body_force_type == 0) return MCFG_OK;
+  const int tb = 256, gb = (n + tb - 1) / tb;
+  if (h->k.d == 3)
+    k_body_force<3><<<gb, tb, 0, h->stream>>>(h->k, h->x, h->f, h->sid);
+  else
+    k_body_force<2><<<gb, tb, 0, h->stream>>>(h->k, h->x, h->f, h->sid);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "body force launch") ? MCFG_ECUDA : MCFG_OK;
+}
+
+int statistics(Handle* h, double* ke, double* mom, double* stress) {
+  const int n = (int)h->n;
+  int nb = (n + kRedThreads - 1) / kRedThreads;
+  if (nb > 1024) nb = 1024;
+  if (nb < 1) nb = 1;
+  double* part = h->red;
+  double* out = h->red + (size_t)1024 * kRedVals;
+  if (h->k.d == 3)
+    k_stats_partial<3><<<nb, kRedThreads, 0, h->stream>>>(h->k, h->v, h->m, h->sid, h->st, part);
+  else
+    k_stats_partial<2><<<nb, kRedThreads, 0, h->stream>>>(h->k, h->v, h->m, h->sid, h->st, part);
+  k_stats_final<<<1, 32, 0, h->stream>>>(part, nb, out);
+  h->launches += 2;
+  double res[kRedVals];
+  if (cuda_check(h, cudaMemcpyAsync(res, out, sizeof res, cudaMemcpyDeviceToHost, h->stream),
+                 "stats copy"))
+    return MCFG_ECUDA;
+  if (cuda_check(h, cudaStreamSynchronize(h->stream), "stats sync")) return MCFG_ECUDA;
+  if (ke) *ke = res[0];
+  if (mom)
+    for (int a = 0; a < 3; ++a) mom[a] = res[1 + a];
+  if (stress) {
+    const int d = h->k.d;
+    for (int a = 0; a < 9; ++a) stress[a] = (a < d * d && h->k.stress) ? res[4 + a] : 0.0;
+  }
+  return MCFG_OK;
+}
+
+}  // namespace mcfg

@@ -1,0 +1,251 @@
+"""Host-side mirror of MCF's per-step particle interface over libmcfg.so.
+
+The methods carry the names of the Fortran routines they replace
+(technique_build_list, particles_compute_density, ...), take MCF's array
+layout (x(d,N) stored as an (N, d) C-contiguous array, id(2,N) as (N, 2)
+int32) and report failures the way MCF's `stat_info` does, as an exception
+naming the routine.  There is no CPU fallback: if libmcfg.so cannot be
+loaded or no GPU is present, construction fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from .params import STATUS_NAMES, SDPDInfo, SDPDParams
+
+_LIB = None
+LIB_PATH = Path(__file__).resolve().parent / "libmcfg.so"
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_h = C.c_void_p
+
+
+class MCFGError(RuntimeError):
+    """A libmcfg call returned a non-zero status."""
+
+    def __init__(self, routine: str, code: int, message: str):
+        self.routine = routine
+        self.code = code
+        super().__init__(f"{routine} : {message} ({STATUS_NAMES.get(code, code)})")
+
+
+def load_library(path: Path | str | None = None) -> C.CDLL:
+    """Load libmcfg.so and declare the C-ABI prototypes (include/mcfg.h)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(f"{p} not found: build it with `python -m mcf_gb300.build`")
+    lib = C.CDLL(str(p))
+    sig = {
+        "mcfg_sizeof_params": (C.c_int64, []),
+        "mcfg_create": (C.c_int, [C.POINTER(SDPDParams), C.POINTER(_h)]),
+        "mcfg_destroy": (C.c_int, [_h]),
+        "mcfg_last_error": (C.c_char_p, [_h]),
+        "mcfg_create_error": (C.c_char_p, []),
+        "mcfg_get_info": (C.c_int, [_h, C.POINTER(SDPDInfo)]),
+        "mcfg_upload": (C.c_int, [_h, C.c_int64, _dp, _dp, _dp, _ip, _dp]),
+        "mcfg_adjust_particles": (C.c_int, [_h]),
+        "mcfg_build_list": (C.c_int, [_h, _ip, _ip, _ip]),
+        "mcfg_compute_density": (C.c_int, [_h]),
+        "mcfg_compute_pressure": (C.c_int, [_h]),
+        "mcfg_compute_interaction": (C.c_int, [_h, C.c_int64]),
+        "mcfg_apply_body_force": (C.c_int, [_h]),
+        "mcfg_integrate_velocity": (C.c_int, [_h, C.c_double, C.c_double]),
+        "mcfg_integrate_position": (C.c_int, [_h, C.c_double]),
+        "mcfg_init_force": (C.c_int, [_h, C.c_int64]),
+        "mcfg_step_vv": (C.c_int, [_h, C.c_int64, C.c_double]),
+        "mcfg_run_vv": (C.c_int, [_h, C.c_int64, C.c_int32, C.c_double]),
+        "mcfg_download": (C.c_int, [_h, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+        "mcfg_statistics": (C.c_int, [_h, _dp, _dp, _dp]),
+        "mcfg_synchronize": (C.c_int, [_h]),
+        "mcfg_upload_force": (C.c_int, [_h, _dp]),
+        "mcfg_get_stream": (C.c_void_p, [_h]),
+        "mcfg_set_profiling": (C.c_int, [_h, C.c_int]),
+        "mcfg_get_phase_times": (C.c_int, [_h, _dp, C.POINTER(C.c_int64)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.mcfg_sizeof_params() != C.sizeof(SDPDParams):
+        raise ImportError("mcfg_params layout mismatch between libmcfg.so and params.py")
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def _ptr(a: np.ndarray | None, ctype):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def _as(a, dtype, shape=None) -> np.ndarray:
+    out = np.ascontiguousarray(a, dtype=dtype)
+    if shape is not None and out.shape != shape:
+        out = out.reshape(shape)
+    return out
+
+
+class SDPD:
+    """One GPU-resident particle system (an MCF Particles object's hot path)."""
+
+    def __init__(self, params: SDPDParams, lib: C.CDLL | None = None):
+        self.lib = lib or load_library()
+        self.params = params.copy()
+        self.dim = int(params.num_dim)
+        h = _h()
+        rc = self.lib.mcfg_create(C.byref(self.params), C.byref(h))
+        if rc != 0:
+            raise MCFGError("mcfg_create", rc, self.lib.mcfg_create_error().decode())
+        self._h = h
+        self.n = 0
+
+    # -- bookkeeping -------------------------------------------------------
+    def _check(self, routine: str, rc: int) -> None:
+        if rc != 0:
+            raise MCFGError(routine, rc, self.lib.mcfg_last_error(self._h).decode())
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self.lib.mcfg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def info(self) -> dict:
+        inf = SDPDInfo()
+        self._check("mcfg_get_info", self.lib.mcfg_get_info(self._h, C.byref(inf)))
+        return {
+            "num_part": inf.num_part,
+            "num_cell_dim": tuple(inf.num_cell_dim),
+            "num_cell": inf.num_cell,
+            "num_outside": inf.num_outside,
+            "num_pairs": inf.num_pairs,
+            "max_neigh": inf.max_neigh,
+            "neigh_capacity": inf.neigh_capacity,
+            "kernel_launches": inf.kernel_launches,
+            "device_bytes": inf.device_bytes,
+        }
+
+    # -- data --------------------------------------------------------------
+    def upload(self, x, v, m, id_, ct=None) -> None:
+        n = int(np.asarray(m).shape[0])
+        d = self.dim
+        self._x = _as(x, np.float64, (n, d))
+        self._v = _as(v, np.float64, (n, d))
+        self._m = _as(m, np.float64, (n,))
+        self._id = _as(id_, np.int32, (n, 2))
+        ctp = None if ct is None else _as(ct, np.float64, (n, d * d))
+        rc = self.lib.mcfg_upload(self._h, n, _ptr(self._x, C.c_double), _ptr(self._v, C.c_double),
+                                  _ptr(self._m, C.c_double), _ptr(self._id, C.c_int32),
+                                  _ptr(ctp, C.c_double))
+        self._check("mcfg_upload", rc)
+        self.n = n
+
+    def download(self, *fields: str) -> dict:
+        """fields among x, v, rho, p, f, s; arrays in host particle order."""
+        n, d = self.n, self.dim
+        shapes = {"x": (n, d), "v": (n, d), "rho": (n,), "p": (n,), "f": (n, d), "s": (n, d * d)}
+        out = {k: np.empty(shapes[k], np.float64) for k in fields}
+        g = lambda k: _ptr(out.get(k), C.c_double)  # noqa: E731
+        rc = self.lib.mcfg_download(self._h, g("x"), g("v"), g("rho"), g("p"), g("f"), None, g("s"))
+        self._check("mcfg_download", rc)
+        return out
+
+    # -- MCF routines ------------------------------------------------------
+    def particles_adjust_particles(self) -> None:
+        self._check("particles_adjust_particles", self.lib.mcfg_adjust_particles(self._h))
+
+    def technique_build_list(self, want_lists: bool = True):
+        """Cell list of the current positions.  Returns (num_cell_dim,
+        cell_start[num_cell+1], lpdx[n]) with 0-based host indices, or None."""
+        if not want_lists:
+            self._check("technique_build_list", self.lib.mcfg_build_list(self._h, None, None, None))
+            return None
+        ncell = self.info()["num_cell"]
+        ncd = np.zeros(3, np.int32)
+        cs = np.empty(ncell + 1, np.int32)
+        lp = np.empty(max(self.n, 1), np.int32)
+        self._check("technique_build_list",
+                    self.lib.mcfg_build_list(self._h, _ptr(ncd, C.c_int32), _ptr(cs, C.c_int32),
+                                             _ptr(lp, C.c_int32)))
+        return ncd, cs, lp[: self.n]
+
+    def particles_compute_density(self) -> None:
+        self._check("particles_compute_density", self.lib.mcfg_compute_density(self._h))
+
+    def particles_compute_pressure(self) -> None:
+        self._check("particles_compute_pressure", self.lib.mcfg_compute_pressure(self._h))
+
+    def particles_compute_interaction(self, step: int = 0) -> None:
+        self._check("particles_compute_interaction",
+                    self.lib.mcfg_compute_interaction(self._h, int(step)))
+
+    def particles_apply_body_force(self) -> None:
+        self._check("particles_apply_body_force", self.lib.mcfg_apply_body_force(self._h))
+
+    def particles_integrate_velocity(self, dt: float, lam: float) -> None:
+        self._check("particles_integrate_velocity",
+                    self.lib.mcfg_integrate_velocity(self._h, float(dt), float(lam)))
+
+    def particles_integrate_position(self, dt: float) -> None:
+        self._check("particles_integrate_position",
+                    self.lib.mcfg_integrate_position(self._h, float(dt)))
+
+    def marching_init_force(self, step: int = 0) -> None:
+        self._check("marching_init_force", self.lib.mcfg_init_force(self._h, int(step)))
+
+    def marching_integrate_VV(self, step: int, dt: float) -> None:
+        self._check("marching_integrate_VV", self.lib.mcfg_step_vv(self._h, int(step), float(dt)))
+
+    def run_vv(self, step0: int, nsteps: int, dt: float) -> None:
+        self._check("marching_marching", self.lib.mcfg_run_vv(self._h, int(step0), int(nsteps), float(dt)))
+
+    def statistic_compute_statistic(self):
+        ke = C.c_double()
+        mom = np.zeros(3)
+        st = np.zeros(9)
+        self._check("statistic_compute_statistic",
+                    self.lib.mcfg_statistics(self._h, C.byref(ke), _ptr(mom, C.c_double),
+                                             _ptr(st, C.c_double)))
+        return ke.value, mom, st
+
+    def upload_force(self, f) -> None:
+        self._f = _as(f, np.float64, (self.n, self.dim))
+        self._check("mcfg_upload_force", self.lib.mcfg_upload_force(self._h, _ptr(self._f, C.c_double)))
+
+    def stream(self) -> int:
+        """cudaStream_t of the handle as an integer (for torch.cuda.ExternalStream)."""
+        return int(self.lib.mcfg_get_stream(self._h) or 0)
+
+    def set_profiling(self, mode: int) -> None:
+        self._check("mcfg_set_profiling", self.lib.mcfg_set_profiling(self._h, int(mode)))
+
+    def phase_times(self) -> dict:
+        ms = np.zeros(5)
+        cnt = np.zeros(5, np.int64)
+        self._check("mcfg_get_phase_times",
+                    self.lib.mcfg_get_phase_times(self._h, _ptr(ms, C.c_double),
+                                                  cnt.ctypes.data_as(C.POINTER(C.c_int64))))
+        names = ("list", "density", "force", "update", "other")
+        return {n: (float(ms[i]), int(cnt[i])) for i, n in enumerate(names)}
+
+    def synchronize(self) -> None:
+        self._check("mcfg_synchronize", self.lib.mcfg_synchronize(self._h))

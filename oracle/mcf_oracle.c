@@ -1,0 +1,1208 @@
+/*
+ * mcf_oracle.c -- CPU FP64 restatement of MCF's SDPD right-hand side and
+ * velocity-Verlet step.  TEST INFRASTRUCTURE ONLY: it is the parity checker
+ * of the CUDA path and the timed CPU baseline; the product never links it.
+ *
+ * Parity unpinned (see mcf_oracle.h): MCF cannot be built here and ships no
+ * golden vectors.  Each routine cites the Fortran it restates
+ * (paths relative to the MCF project; "ppm:" = libppm-1.1.1/src inside
+ * ppm/distfiles/libppm-1.1.1.tar.gz).
+ *
+ * Build with -ffp-contract=off so that every FP64 expression is rounded as
+ * the gfortran -O2 x86-64 build of MCF rounds it (no fused multiply-add).
+ */
+#include "mcf_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define MK_PI 3.141592653589793238 /* mcf_header.F90:50 */
+#define MAX_NNP 27
+
+struct orc_state {
+  mcfg_params p;
+  int d;
+  /* kernel (kernel_new.F90:41-93) */
+  double h, coef, coef_grad, cut_off2;
+  /* Batchelor p0 (stateEquation_new.F90:102-103) */
+  double p0;
+  double gs;           /* ghost size = cut_off * 1.0001 (mcf.F90:617) */
+  double len[3];       /* max_phys_t - min_phys_t                      */
+  double machine_zero; /* technique_new.F90:361-363 -> 1e-14           */
+  int periodic[3];
+  /* particles: reals [0,nreal), ghosts [nreal,nall) */
+  int64_t nreal, nall, cap;
+  double *x, *v, *f, *rho, *pr, *m, *s, *ct;
+  double* fabs_sum; /* per particle sum of |pair acceleration| (test scale) */
+  int32_t *pid, *sid;
+  int64_t* owner;
+  /* cell list (ppm_util_rank3d.F90 / rank2d) */
+  int Nm[3], Ngl[6], Nmtot[3];
+  int64_t nbox;
+  int32_t* lhbx; /* nbox+1, 0-based CSR                                  */
+  int32_t* lpdx; /* particle indices (0-based) sorted by box             */
+  int64_t nlpdx;
+  int32_t* pbox; /* box per particle, -1 = no box                        */
+  int inp[MAX_NNP][3], jnp[MAX_NNP][3], nnp;
+  int have_list, have_density, have_pressure;
+  int64_t npairs;
+  int nthreads;
+  double timers[4];
+  char err[256];
+};
+
+static double now_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+static int fail(orc_state* s, const char* msg) {
+  snprintf(s->err, sizeof s->err, "%s", msg);
+  return MCFG_EINVAL;
+}
+
+const char* orc_last_error(const orc_state* s) { return s ? s->err : "null"; }
+
+/* ------------------------------------------------------------------------
+ * Kernel: kernel_new.F90:41-93, kernel_kernel_quintic_spline.F90:69-99,
+ * 177-215, kernel_kernel_Lucy.F90:68-78,155-168.
+ * ---------------------------------------------------------------------- */
+static void kernel_init(orc_state* s) {
+  const double rc = s->p.cut_off;
+  const int d = s->d;
+  if (s->p.kernel_type == 1) {
+    s->h = rc / 3.0;
+    if (d == 2)
+      s->coef = 7.0 / (478.0 * MK_PI * (s->h * s->h));
+    else
+      s->coef = 3.0 / (359.0 * MK_PI * (s->h * s->h * s->h));
+  } else {
+    s->h = rc;
+    if (d == 2)
+      s->coef = 5.0 / (MK_PI * (s->h * s->h));
+    else
+      s->coef = 105.0 / (16.0 * MK_PI * (s->h * s->h * s->h));
+  }
+  s->coef_grad = -s->coef / s->h;
+}
+
+static inline double pow4(double a) {
+  double a2 = a * a;
+  return a2 * a2;
+}
+
+/* returns W; *gw (if non-NULL) = dW/dr */
+static inline double kernel_eval(const orc_state* s, double rij, double* gw) {
+  const double sv = rij / s->h;
+  if (s->p.kernel_type == 1) {
+    const double s1 = 1.0 - sv, s2 = 2.0 - sv, s3 = 3.0 - sv;
+    double s1_4 = pow4(s1), s2_4 = pow4(s2), s3_4 = pow4(s3);
+    const double s1_5 = 15.0 * s1_4 * s1;
+    const double s2_5 = -6.0 * s2_4 * s2;
+    const double s3_5 = s3_4 * s3;
+    s1_4 = 75.0 * s1_4;
+    s2_4 = -30.0 * s2_4;
+    s3_4 = 5.0 * s3_4;
+    double w, g;
+    if (sv < 1.0) {
+      w = s->coef * (s3_5 + s2_5 + s1_5);
+      g = s->coef_grad * (s3_4 + s2_4 + s1_4);
+    } else if (sv < 2.0) {
+      w = s->coef * (s3_5 + s2_5);
+      g = s->coef_grad * (s3_4 + s2_4);
+    } else if (sv < 3.0) {
+      w = s->coef * s3_5;
+      g = s->coef_grad * s3_4;
+    } else {
+      w = 0.0;
+      g = 0.0;
+    }
+    if (gw) *gw = g;
+    return w;
+  } else {
+    double w = 0.0, g = 0.0;
+    if (sv <= 1.0) {
+      const double om = 1.0 - sv;
+      w = s->coef * (1.0 + 3.0 * sv) * (om * om * om);
+      g = s->coef_grad * 12.0 * sv * (om * om);
+    }
+    if (gw) *gw = g;
+    return w;
+  }
+}
+
+int orc_kernel(const orc_state* s, double r, double* w, double* gradw) {
+  double g;
+  double wv = kernel_eval(s, r, &g);
+  if (w) *w = wv;
+  if (gradw) *gradw = g;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------
+ * Counter-based stream (replaces random_random.F90:48-73 /
+ * random_random_Gaussian.F90:79-175): Philox4x32-10 of Salmon, Moraes,
+ * Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3" (SC'11),
+ * Box-Muller normals.  Key = seed, counter = (min pid, max pid, step, call).
+ * ---------------------------------------------------------------------- */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
+                       uint32_t out[4]) {
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+  uint32_t k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * (uint64_t)c0;
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * (uint64_t)c2;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    c0 = hi1 ^ c1 ^ k0;
+    c1 = lo1;
+    c2 = hi0 ^ c3 ^ k1;
+    c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
+/* odd multiple of 2^-24 in (0,1): exact in FP32 */
+static inline float u01(uint32_t r) {
+  return (float)((r >> 9) * 2u + 1u) * (1.0f / 16777216.0f);
+}
+
+/* Box-Muller pair; the device code calls CUDA's logf / sincospif, here the
+ * same quantities are formed in double and rounded to float. */
+static inline void box_muller(uint32_t a, uint32_t b, float* z0, float* z1) {
+  const float u1 = u01(a), u2 = u01(b);
+  const float lg = (float)log((double)u1);
+  const float rad = sqrtf(-2.0f * lg);
+  const double th = 2.0 * MK_PI * (double)u2;
+  const float cs = (float)cos(th), sn = (float)sin(th);
+  *z0 = rad * cs;
+  *z1 = rad * sn;
+}
+
+/* Normals for one pair: 3D -> z[0..5] (diag 0..2, off-diagonal 3..5),
+ * 2D -> z[0..2] (diag 0..1, off-diagonal 2).  Independent of pair order. */
+void orc_pair_normals(uint64_t seed, int64_t step, int32_t pid_a, int32_t pid_b,
+                      int dim, float* z) {
+  const uint32_t a = (uint32_t)(pid_a < pid_b ? pid_a : pid_b);
+  const uint32_t b = (uint32_t)(pid_a < pid_b ? pid_b : pid_a);
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t ctr[4] = {a, b, (uint32_t)step, 0u};
+  uint32_t r[4];
+  orc_philox4x32_10(ctr, key, r);
+  box_muller(r[0], r[1], &z[0], &z[1]);
+  float t0, t1;
+  box_muller(r[2], r[3], &t0, &t1);
+  z[2] = t0;
+  if (dim == 3) {
+    z[3] = t1;
+    ctr[3] = 1u;
+    orc_philox4x32_10(ctr, key, r);
+    box_muller(r[0], r[1], &z[4], &z[5]);
+  }
+}
+
+/* ------------------------------------------------------------------------
+ * Create / destroy
+ * ---------------------------------------------------------------------- */
+orc_state* orc_create(const mcfg_params* p, char* err, int errlen) {
+  const char* msg = NULL;
+  if (!p)
+    msg = "params NULL";
+  else if (p->num_dim != 2 && p->num_dim != 3)
+    msg = "num_dim must be 2 or 3";
+  else if (!(p->cut_off > 0.0))
+    msg = "cut_off must be positive";
+  else if (p->kernel_type != 1 && p->kernel_type != 2)
+    msg = "kernel_type must be 1 or 2";
+  else if (p->rhs_density_type != 1 && p->rhs_density_type != 2)
+    msg = "rhs_density_type must be 1 or 2";
+  else if (p->rhs_force_type < 1 || p->rhs_force_type > 4)
+    msg = "rhs_force_type must be 1..4";
+  else if (p->stateEquation_type != 1 && p->stateEquation_type != 2)
+    msg = "stateEquation_type must be 1 or 2";
+  if (msg) {
+    if (err) snprintf(err, (size_t)errlen, "%s", msg);
+    return NULL;
+  }
+  orc_state* s = (orc_state*)calloc(1, sizeof(orc_state));
+  s->p = *p;
+  s->d = p->num_dim;
+  if (!(s->p.cell_factor > 0.0)) s->p.cell_factor = 1.0001;
+  kernel_init(s);
+  s->cut_off2 = p->cut_off * p->cut_off;
+  s->gs = p->cut_off * s->p.cell_factor;
+  /* stateEquation_new.F90:102-103 */
+  if (p->stateEquation_type == 2)
+    s->p0 = p->c * p->c * p->rho * pow(p->rho_ref / p->rho, p->gamma) / p->gamma;
+  s->machine_zero = 1e-14; /* 10**(INT(LOG10(EPSILON(1d0)))+1) */
+  for (int i = 0; i < s->d; ++i) {
+    s->len[i] = p->max_phys_t[i] - p->min_phys_t[i];
+    s->periodic[i] = (p->bcdef[2 * i] == MCFG_BC_PERIODIC);
+  }
+  s->nthreads = 1;
+  return s;
+}
+
+static void free_arrays(orc_state* s) {
+  free(s->x); free(s->v); free(s->f); free(s->rho); free(s->pr); free(s->m);
+  free(s->s); free(s->ct); free(s->pid); free(s->sid); free(s->owner); free(s->fabs_sum);
+  s->x = s->v = s->f = s->rho = s->pr = s->m = s->s = s->ct = s->fabs_sum = NULL;
+  s->pid = s->sid = NULL;
+  s->owner = NULL;
+}
+
+void orc_destroy(orc_state* s) {
+  if (!s) return;
+  free_arrays(s);
+  free(s->lhbx); free(s->lpdx); free(s->pbox);
+  free(s);
+}
+
+int orc_set_threads(orc_state* s, int nthreads) {
+  s->nthreads = nthreads < 1 ? 1 : nthreads;
+  return 0;
+}
+
+static void ensure_cap(orc_state* s, int64_t need) {
+  if (need <= s->cap) return;
+  int64_t cap = need + need / 2 + 16;
+  const int d = s->d, d2 = s->d * s->d;
+  s->x = (double*)realloc(s->x, sizeof(double) * (size_t)(cap * d));
+  s->v = (double*)realloc(s->v, sizeof(double) * (size_t)(cap * d));
+  s->f = (double*)realloc(s->f, sizeof(double) * (size_t)(cap * d));
+  s->rho = (double*)realloc(s->rho, sizeof(double) * (size_t)cap);
+  s->pr = (double*)realloc(s->pr, sizeof(double) * (size_t)cap);
+  s->m = (double*)realloc(s->m, sizeof(double) * (size_t)cap);
+  s->s = (double*)realloc(s->s, sizeof(double) * (size_t)(cap * d2));
+  s->ct = (double*)realloc(s->ct, sizeof(double) * (size_t)(cap * d2));
+  s->pid = (int32_t*)realloc(s->pid, sizeof(int32_t) * (size_t)cap);
+  s->sid = (int32_t*)realloc(s->sid, sizeof(int32_t) * (size_t)cap);
+  s->owner = (int64_t*)realloc(s->owner, sizeof(int64_t) * (size_t)cap);
+  s->fabs_sum = (double*)realloc(s->fabs_sum, sizeof(double) * (size_t)cap);
+  s->cap = cap;
+}
+
+int orc_upload(orc_state* s, int64_t n, const double* x, const double* v,
+               const double* m, const int32_t* id, const double* ct) {
+  if (n < 0 || (n > 0 && (!x || !v || !m || !id))) return fail(s, "orc_upload: bad arguments");
+  const int d = s->d, d2 = d * d;
+  ensure_cap(s, n + 1);
+  memcpy(s->x, x, sizeof(double) * (size_t)(n * d));
+  memcpy(s->v, v, sizeof(double) * (size_t)(n * d));
+  memcpy(s->m, m, sizeof(double) * (size_t)n);
+  for (int64_t j = 0; j < n; ++j) {
+    s->pid[j] = id[2 * j];
+    s->sid[j] = id[2 * j + 1];
+    s->owner[j] = j;
+  }
+  if (ct)
+    memcpy(s->ct, ct, sizeof(double) * (size_t)(n * d2));
+  else
+    for (int64_t j = 0; j < n; ++j)
+      for (int a = 0; a < d2; ++a) s->ct[j * d2 + a] = (a % (d + 1) == 0) ? 1.0 : 0.0;
+  memset(s->f, 0, sizeof(double) * (size_t)(n * d));
+  memset(s->rho, 0, sizeof(double) * (size_t)n);
+  memset(s->pr, 0, sizeof(double) * (size_t)n);
+  memset(s->s, 0, sizeof(double) * (size_t)(n * d2));
+  s->nreal = s->nall = n;
+  s->have_list = s->have_density = s->have_pressure = 0;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------
+ * Periodic wrap, particles_adjust_particles.F90:137-389 (periodic faces;
+ * solid walls clamp wall particles to the total domain).
+ * ---------------------------------------------------------------------- */
+int orc_adjust_particles(orc_state* s) {
+  const int d = s->d;
+  const double* mn = s->p.min_phys;
+  const double* mx = s->p.max_phys;
+  for (int64_t j = 0; j < s->nreal; ++j) {
+    for (int i = 0; i < d; ++i) {
+      double* xi = &s->x[j * d + i];
+      if (*xi < mn[i]) {
+        if (s->p.bcdef[2 * i] == MCFG_BC_PERIODIC) {
+          *xi = *xi + s->len[i];
+        } else if (s->p.bcdef[2 * i] == MCFG_BC_WALL_SOLID) {
+          if (s->sid[j] < 0 && *xi < s->p.min_phys_t[i]) {
+            *xi = s->p.min_phys_t[i];
+            s->v[j * d + i] = 0.0;
+          }
+        }
+      }
+      if (*xi >= mx[i]) {
+        if (s->p.bcdef[2 * i + 1] == MCFG_BC_PERIODIC) {
+          *xi = *xi - s->len[i];
+        } else if (s->p.bcdef[2 * i + 1] == MCFG_BC_WALL_SOLID) {
+          if (s->sid[j] < 0 && *xi > s->p.max_phys_t[i]) {
+            *xi = s->p.max_phys_t[i] - s->machine_zero;
+            s->v[j * d + i] = 0.0;
+          }
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------
+ * Periodic ghosts, ppm:src/ppm_map_part_ghost_get.F90:441-525 with
+ * ppm_bcdef_periodic_{x,y,z}.inc: images x + len for x < min + ghostsize
+ * (and, without symmetry, x - len for x > max - ghostsize), x first, then y
+ * over reals and x-images, then z.  Ghost fields are copies of the owner.
+ * ---------------------------------------------------------------------- */
+static void copy_particle(orc_state* s, int64_t to, int64_t from) {
+  const int d = s->d, d2 = d * d;
+  memcpy(&s->x[to * d], &s->x[from * d], sizeof(double) * (size_t)d);
+  memcpy(&s->v[to * d], &s->v[from * d], sizeof(double) * (size_t)d);
+  memcpy(&s->ct[to * d2], &s->ct[from * d2], sizeof(double) * (size_t)d2);
+  s->m[to] = s->m[from];
+  s->rho[to] = s->rho[from];
+  s->pr[to] = s->pr[from];
+  s->pid[to] = s->pid[from];
+  s->sid[to] = s->sid[from];
+  s->owner[to] = s->owner[from];
+}
+
+static void ghost_get(orc_state* s) {
+  const int d = s->d;
+  s->nall = s->nreal;
+  for (int dim = 0; dim < d; ++dim) {
+    if (!s->periodic[dim]) continue;
+    const double xminf = s->p.min_phys_t[dim], xmini = xminf + s->gs;
+    const double xmaxf = s->p.max_phys_t[dim], xmaxi = xmaxf - s->gs;
+    const int64_t nnow = s->nall;
+    for (int64_t i = 0; i < nnow; ++i) {
+      const double xv = s->x[i * d + dim];
+      if (xv >= xminf && xv < xmini) {
+        ensure_cap(s, s->nall + 1);
+        copy_particle(s, s->nall, i);
+        s->x[s->nall * d + dim] = xv + s->len[dim];
+        s->nall++;
+      }
+    }
+    if (!s->p.symmetry) {
+      for (int64_t i = 0; i < nnow; ++i) {
+        const double xv = s->x[i * d + dim];
+        if (xv > xmaxi && xv <= xmaxf) {
+          ensure_cap(s, s->nall + 1);
+          copy_particle(s, s->nall, i);
+          s->x[s->nall * d + dim] = xv - s->len[dim];
+          s->nall++;
+        }
+      }
+    }
+  }
+}
+
+/* refresh ghost copies of rho, v, p (second ghost get,
+ * marching_integrate_VV.F90:1128) */
+static void ghost_refresh(orc_state* s) {
+  const int d = s->d, d2 = d * d;
+  for (int64_t g = s->nreal; g < s->nall; ++g) {
+    const int64_t o = s->owner[g];
+    s->rho[g] = s->rho[o];
+    s->pr[g] = s->pr[o];
+    memcpy(&s->v[g * d], &s->v[o * d], sizeof(double) * (size_t)d);
+    memcpy(&s->ct[g * d2], &s->ct[o * d2], sizeof(double) * (size_t)d2);
+  }
+}
+
+/* ------------------------------------------------------------------------
+ * Cell list: ppm:src/ppm_neighlist_clist.F90:318-438 ->
+ * ppm:src/ppm_util_rank3d.F90:308-531 (rank2d alike) and
+ * ppm:src/ppm_neighlist_MkNeighIdx.F90:146-269.
+ * ---------------------------------------------------------------------- */
+static void make_neigh_idx(orc_state* s) {
+  memset(s->inp, 0, sizeof s->inp);
+  memset(s->jnp, 0, sizeof s->jnp);
+  if (s->p.symmetry) {
+    if (s->d == 2) {
+      s->nnp = 5;
+      s->jnp[1][0] = 1;                    /* 0 -- 1 */
+      s->inp[2][1] = 1;                    /* 0 -- 3 */
+      s->jnp[3][0] = 1; s->jnp[3][1] = 1;  /* 0 -- 4 */
+      s->inp[4][0] = 1; s->jnp[4][1] = 1;  /* 1 -- 3 */
+    } else {
+      s->nnp = 14;
+      s->jnp[1][0] = 1;
+      s->inp[2][1] = 1;
+      s->jnp[3][0] = 1; s->jnp[3][1] = 1;
+      s->jnp[4][2] = 1;
+      s->jnp[5][0] = 1; s->jnp[5][2] = 1;
+      s->jnp[6][1] = 1; s->jnp[6][2] = 1;
+      s->jnp[7][0] = 1; s->jnp[7][1] = 1; s->jnp[7][2] = 1;
+      s->inp[8][0] = 1; s->jnp[8][1] = 1;
+      s->inp[9][0] = 1; s->jnp[9][2] = 1;
+      s->inp[10][0] = 1; s->jnp[10][1] = 1; s->jnp[10][2] = 1;
+      s->inp[11][1] = 1; s->jnp[11][2] = 1;
+      s->inp[12][1] = 1; s->jnp[12][0] = 1; s->jnp[12][2] = 1;
+      s->inp[13][0] = 1; s->inp[13][1] = 1; s->jnp[13][2] = 1;
+    }
+  } else {
+    const int nz = (s->d == 3) ? 1 : 0;
+    int l = 0;
+    for (int k = -nz; k <= nz; ++k)
+      for (int j = -1; j <= 1; ++j)
+        for (int i = -1; i <= 1; ++i) {
+          s->jnp[l][0] = i;
+          s->jnp[l][1] = j;
+          s->jnp[l][2] = k;
+          ++l;
+        }
+    s->nnp = l;
+  }
+}
+
+static int rank_particles(orc_state* s) {
+  const int d = s->d;
+  double xmin[3], xmax[3], rdx[3];
+  for (int i = 0; i < d; ++i) {
+    xmin[i] = s->p.min_phys_t[i];
+    xmax[i] = s->p.max_phys_t[i];
+    int nm = (int)((xmax[i] - xmin[i]) / s->gs); /* clist.F90:370-376 */
+    if (nm < 1) nm = 1;
+    s->Nm[i] = nm;
+  }
+  for (int i = 0; i < 6; ++i) s->Ngl[i] = 0;
+  for (int i = 0; i < d; ++i) {
+    if (s->p.symmetry) {
+      s->Ngl[d + i] = 1;
+    } else {
+      s->Ngl[i] = 1;
+      s->Ngl[d + i] = 1;
+    }
+  }
+  s->nbox = 1;
+  for (int i = 0; i < 3; ++i) s->Nmtot[i] = 1;
+  for (int i = 0; i < d; ++i) {
+    s->Nmtot[i] = s->Nm[i] + s->Ngl[i] + s->Ngl[d + i];
+    s->nbox *= s->Nmtot[i];
+    rdx[i] = (double)s->Nm[i] / (xmax[i] - xmin[i]); /* rank3d.F90:352-354 */
+  }
+  free(s->lhbx);
+  free(s->pbox);
+  free(s->lpdx);
+  s->lhbx = (int32_t*)calloc((size_t)s->nbox + 1, sizeof(int32_t));
+  s->pbox = (int32_t*)malloc(sizeof(int32_t) * (size_t)(s->nall + 1));
+  int32_t* npbx = (int32_t*)calloc((size_t)s->nbox + 1, sizeof(int32_t));
+  const int64_t n2 = (int64_t)s->Nmtot[0] * s->Nmtot[1];
+  int64_t icount = 0;
+  for (int64_t ip = 0; ip < s->nall; ++ip) {
+    int c[3] = {0, 0, 0};
+    for (int a = 0; a < d; ++a) {
+      const double xa = s->x[ip * d + a];
+      /* rank3d.F90:422-424: subtraction before multiplication */
+      int ia = (int)floor((xa - xmin[a]) * rdx[a]) + s->Ngl[a];
+      const int top = s->Nm[a] + s->Ngl[a];
+      if (xa >= xmax[a] && ia < top) ia = top;      /* :433-445 */
+      if (xa < xmax[a] && ia >= top) ia = top - 1;  /* :447-459 */
+      c[a] = ia;
+    }
+    int inside = 1;
+    for (int a = 0; a < d; ++a)
+      if (c[a] < 0 || c[a] >= s->Nmtot[a]) inside = 0;
+    if (inside) {
+      const int64_t ibox = c[0] + (int64_t)c[1] * s->Nmtot[0] + (int64_t)c[2] * n2;
+      s->pbox[ip] = (int32_t)ibox;
+      npbx[ibox]++;
+      icount++;
+    } else {
+      s->pbox[ip] = -1;
+    }
+  }
+  /* stable counting sort, rank3d.F90:504-531 */
+  s->lhbx[0] = 0;
+  for (int64_t b = 0; b < s->nbox; ++b) s->lhbx[b + 1] = s->lhbx[b] + npbx[b];
+  s->lpdx = (int32_t*)malloc(sizeof(int32_t) * (size_t)(icount + 1));
+  s->nlpdx = icount;
+  for (int64_t b = 0; b < s->nbox; ++b) npbx[b] = s->lhbx[b];
+  for (int64_t ip = 0; ip < s->nall; ++ip) {
+    const int32_t b = s->pbox[ip];
+    if (b >= 0) s->lpdx[npbx[b]++] = (int32_t)ip;
+  }
+  free(npbx);
+  make_neigh_idx(s);
+  return 0;
+}
+
+int orc_build_list(orc_state* s) {
+  const double t0 = now_s();
+  ghost_get(s);
+  rank_particles(s);
+  s->have_list = 1;
+  s->have_density = s->have_pressure = 0;
+  s->timers[0] += now_s() - t0;
+  return 0;
+}
+
+/* Real-cell lists in the layout of mcfg_build_list: cells i+j*Nx+k*Nx*Ny
+ * over the real cells only; entries are real particle indices. */
+int orc_export_lists(orc_state* s, int32_t* num_cell_dim, int32_t* cell_start,
+                     int32_t* lpdx) {
+  if (!s->have_list) return fail(s, "orc_export_lists: no list");
+  const int d = s->d;
+  int nm[3] = {1, 1, 1};
+  for (int a = 0; a < d; ++a) nm[a] = s->Nm[a];
+  if (num_cell_dim)
+    for (int a = 0; a < 3; ++a) num_cell_dim[a] = nm[a];
+  const int64_t n2 = (int64_t)s->Nmtot[0] * s->Nmtot[1];
+  int64_t pos = 0, cell = 0;
+  for (int k = 0; k < nm[2]; ++k)
+    for (int j = 0; j < nm[1]; ++j)
+      for (int i = 0; i < nm[0]; ++i) {
+        const int64_t ibox = (i + s->Ngl[0]) + (int64_t)(j + s->Ngl[1]) * s->Nmtot[0] +
+                             (d == 3 ? (int64_t)(k + s->Ngl[2]) * n2 : 0);
+        if (cell_start) cell_start[cell] = (int32_t)pos;
+        for (int32_t q = s->lhbx[ibox]; q < s->lhbx[ibox + 1]; ++q) {
+          const int32_t ip = s->lpdx[q];
+          if (ip < s->nreal) {
+            if (lpdx) lpdx[pos] = ip;
+            pos++;
+          }
+        }
+        cell++;
+      }
+  if (cell_start) cell_start[cell] = (int32_t)pos;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------
+ * Cell-pair iteration shared by density and force:
+ * particles_compute_density.F90:578-867, particles_compute_interaction.F90:
+ * 609-900.  Symmetric: real cells 0..Nm-1, 14/5 cell pairs, j>i inside one
+ * cell; full: real cells with 27/9 neighbours, self excluded.
+ * ---------------------------------------------------------------------- */
+typedef void (*pair_fn)(orc_state* s, int64_t ip, int64_t jp, void* ctx);
+
+static void cell_range(const orc_state* s, int* st, int* en) {
+  const int d = s->d;
+  for (int a = 0; a < 3; ++a) {
+    st[a] = 0;
+    en[a] = 0;
+  }
+  for (int a = 0; a < d; ++a) {
+    if (s->p.symmetry) {
+      st[a] = 0;
+      en[a] = s->Nmtot[a] - 2;
+    } else {
+      st[a] = 1;
+      en[a] = s->Nmtot[a] - 2;
+    }
+  }
+}
+
+/* one centre cell: all its (icell,jcell) interactions */
+static void loop_centre_cell(orc_state* s, int ci, int cj, int ck, pair_fn fn,
+                             void* ctx, int64_t* npairs_out) {
+  const int d = s->d;
+  const int64_t n1 = s->Nmtot[0];
+  const int64_t n2 = (d == 2) ? 0 : (int64_t)s->Nmtot[0] * s->Nmtot[1];
+  const int64_t ccell = ci + n1 * cj + n2 * ck;
+  int64_t np = 0;
+  for (int it = 0; it < s->nnp; ++it) {
+    const int64_t icell = ccell + s->inp[it][0] + n1 * s->inp[it][1] + n2 * s->inp[it][2];
+    const int64_t jcell = ccell + s->jnp[it][0] + n1 * s->jnp[it][1] + n2 * s->jnp[it][2];
+    if (icell < 0 || jcell < 0 || icell >= s->nbox || jcell >= s->nbox) continue;
+    const int32_t istart = s->lhbx[icell], iend = s->lhbx[icell + 1];
+    int32_t jstart = s->lhbx[jcell];
+    const int32_t jend = s->lhbx[jcell + 1];
+    for (int32_t ipart = istart; ipart < iend; ++ipart) {
+      const int64_t ip = s->lpdx[ipart];
+      if (jcell == icell && s->p.symmetry) jstart = ipart + 1;
+      for (int32_t jpart = jstart; jpart < jend; ++jpart) {
+        if (jcell == icell && jpart == ipart) continue;
+        const int64_t jp = s->lpdx[jpart];
+        fn(s, ip, jp, ctx);
+        ++np;
+      }
+    }
+  }
+  *npairs_out += np;
+}
+
+static void for_all_pairs(orc_state* s, pair_fn fn, void* ctx) {
+  int st[3], en[3];
+  cell_range(s, st, en);
+  const int d = s->d;
+  const int kst = (d == 2) ? 0 : st[2], ken = (d == 2) ? 0 : en[2];
+  int64_t npairs = 0;
+  if (s->nthreads > 1 && !s->p.symmetry) {
+    /* full stencil writes only to particles of the centre cell: cells are
+     * independent and the loop parallelises without races */
+    const int nx = en[0] - st[0] + 1, ny = en[1] - st[1] + 1, nz = ken - kst + 1;
+    const int64_t ncell = (int64_t)nx * ny * nz;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64) num_threads(s->nthreads) reduction(+ : npairs)
+#endif
+    for (int64_t c = 0; c < ncell; ++c) {
+      const int i = st[0] + (int)(c % nx);
+      const int j = st[1] + (int)((c / nx) % ny);
+      const int k = kst + (int)(c / ((int64_t)nx * ny));
+      loop_centre_cell(s, i, j, k, fn, ctx, &npairs);
+    }
+  } else {
+    for (int k = kst; k <= ken; ++k)
+      for (int j = st[1]; j <= en[1]; ++j)
+        for (int i = st[0]; i <= en[0]; ++i) loop_centre_cell(s, i, j, k, fn, ctx, &npairs);
+  }
+  s->npairs = npairs;
+}
+
+/* ------------------------------------------------------------------------
+ * Density: particles_compute_density.F90:369-558 (self terms) and
+ * :700-855 (pairs), rhs_density.F90:95-96; ghost put particles_map_ghost_put.
+ * ---------------------------------------------------------------------- */
+static int dyn_rho(const orc_state* s, int32_t sid) {
+  if (sid == 0) return 1;
+  if (sid < 0) return s->p.wall_rho_type == 1;
+  return 0; /* colloid boundary particles: constant density in this build */
+}
+
+static void density_pair(orc_state* s, int64_t ip, int64_t jp, void* ctx) {
+  (void)ctx;
+  const int d = s->d;
+  const int32_t si = s->sid[ip], sj = s->sid[jp];
+  if (!s->p.symmetry && !dyn_rho(s, si)) return;
+  if (si != 0 && sj != 0 && !dyn_rho(s, si) && !dyn_rho(s, sj)) return;
+  double dij = 0.0;
+  for (int a = 0; a < d; ++a) {
+    const double r = s->x[ip * d + a] - s->x[jp * d + a];
+    dij = dij + r * r;
+  }
+  if (dij >= s->cut_off2) return;
+  dij = sqrt(dij);
+  const double w = kernel_eval(s, dij, NULL);
+  double rhoi, rhoj;
+  if (s->p.rhs_density_type == 1) {
+    rhoi = w * s->m[jp];
+    rhoj = w * s->m[ip];
+  } else {
+    rhoi = w;
+    rhoj = w;
+  }
+  if (dyn_rho(s, si)) s->rho[ip] = s->rho[ip] + rhoi;
+  if (s->p.symmetry && dyn_rho(s, sj)) s->rho[jp] = s->rho[jp] + rhoj;
+}
+
+int orc_compute_density(orc_state* s) {
+  if (!s->have_list) return fail(s, "orc_compute_density: build the list first");
+  const double t0 = now_s();
+  const double w0 = kernel_eval(s, 0.0, NULL);
+  for (int64_t j = 0; j < s->nall; ++j) s->rho[j] = 0.0;
+  for (int64_t j = 0; j < s->nreal; ++j) {
+    const int32_t sid = s->sid[j];
+    if (sid == 0 || dyn_rho(s, sid)) {
+      s->rho[j] = (s->p.rhs_density_type == 1) ? w0 * s->m[j] : w0;
+    } else {
+      if (s->m[j] < s->machine_zero) return fail(s, "orc_compute_density: zero mass");
+      s->rho[j] = (s->p.rhs_density_type == 1) ? s->p.init_density
+                                                 : s->p.init_density / s->m[j];
+    }
+  }
+  for_all_pairs(s, density_pair, NULL);
+  if (s->p.symmetry)
+    for (int64_t g = s->nreal; g < s->nall; ++g) {
+      const int64_t o = s->owner[g];
+      if (dyn_rho(s, s->sid[o])) s->rho[o] = s->rho[o] + s->rho[g];
+    }
+  ghost_refresh(s);
+  s->have_density = 1;
+  s->timers[1] += now_s() - t0;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------
+ * Pressure: particles_compute_pressure.F90:66-95 ->
+ * stateEquation_compute_pressure.F90:147-180 (vector forms).
+ * ---------------------------------------------------------------------- */
+int orc_compute_pressure(orc_state* s) {
+  if (!s->have_density) return fail(s, "orc_compute_pressure: no density");
+  const double t0 = now_s();
+  for (int64_t j = 0; j < s->nall; ++j) {
+    const double r = (s->p.rhs_density_type == 1) ? s->rho[j] : s->rho[j] * s->m[j];
+    if (s->p.stateEquation_type == 1)
+      s->pr[j] = (s->p.c * s->p.c) * (pow(r, s->p.gamma) - s->p.rho_ref);
+    else
+      s->pr[j] = s->p0 * (pow(r / s->p.rho_ref, s->p.gamma) - 1.0);
+  }
+  s->have_pressure = 1;
+  s->timers[2] += now_s() - t0;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------
+ * Pair forces: rhs_force_ff_Newtonian_{Morris,Espanol,HuAdams,
+ * HuAdams_angular}.F90; accelerations (force per unit mass).
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int64_t step;
+  int noise;
+  double sqdt;
+} force_ctx;
+
+static void noise_matrix(const orc_state* s, const float* z, double dW[3][3],
+                         double* trace_out) {
+  const int d = s->d;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) dW[a][b] = 0.0;
+  double trace = 0.0;
+  for (int a = 0; a < d; ++a) {
+    dW[a][a] = (double)z[a];
+    trace = trace + dW[a][a];
+  }
+  trace = trace / d;
+  if (d == 3) {
+    dW[0][1] = dW[1][0] = (double)z[3] * 0.70710678118654752440;
+    dW[0][2] = dW[2][0] = (double)z[4] * 0.70710678118654752440;
+    dW[1][2] = dW[2][1] = (double)z[5] * 0.70710678118654752440;
+  } else {
+    dW[0][1] = dW[1][0] = (double)z[2] * 0.70710678118654752440;
+  }
+  *trace_out = trace;
+  for (int a = 0; a < d; ++a) dW[a][a] = dW[a][a] - trace;
+}
+
+static void rhs_force_ff(orc_state* s, const force_ctx* fc, const double* xi,
+                         const double* xj, double dij, const double* vi,
+                         const double* vj, double numi, double numj, double pi,
+                         double pj, double mi, double mj, double gradw,
+                         int32_t pidi, int32_t pidj, double* fi, double* fj) {
+  const int d = s->d;
+  double eij[3], vij[3];
+  for (int a = 0; a < d; ++a) {
+    fi[a] = 0.0;
+    fj[a] = 0.0;
+    eij[a] = (xi[a] - xj[a]) / dij;
+    vij[a] = vi[a] - vj[a];
+  }
+  const double eta = s->p.eta, kt = s->p.kt;
+  const int brown = fc->noise;
+  switch (s->p.rhs_force_type) {
+    case 1: { /* Morris, rhs_force_ff_Newtonian_Morris.F90:89-133 */
+      const double f_c = (pi / (numi * numi) + pj / (numj * numj)) * gradw;
+      for (int a = 0; a < d; ++a) {
+        fi[a] = fi[a] - mj * f_c * eij[a];
+        fj[a] = fj[a] + mi * f_c * eij[a];
+      }
+      const double f_d = 2.0 * eta * gradw / numi / numj / dij;
+      for (int a = 0; a < d; ++a) {
+        fi[a] = fi[a] + mj * f_d * vij[a];
+        fj[a] = fj[a] - mi * f_d * vij[a];
+      }
+      break;
+    }
+    case 2: { /* Espanol-Revenga, rhs_force_ff_Newtonian_Espanol.F90:130-247 */
+      double ev = 0.0;
+      for (int a = 0; a < d; ++a) ev = ev + eij[a] * vij[a];
+      const double f_c = (pi / (numi * numi) + pj / (numj * numj)) * gradw;
+      for (int a = 0; a < d; ++a) {
+        fi[a] = fi[a] - f_c * eij[a] / mi;
+        fj[a] = fj[a] + f_c * eij[a] / mj;
+      }
+      const double f_d1 = (2.0 - 1.0 / d) * eta * gradw / numi / numj / dij;
+      for (int a = 0; a < d; ++a) {
+        fi[a] = fi[a] + f_d1 * vij[a] / mi;
+        fj[a] = fj[a] - f_d1 * vij[a] / mj;
+      }
+      const double f_d2 = eta * (d + 2) / d * gradw * ev / numi / numj / dij;
+      for (int a = 0; a < d; ++a) {
+        fi[a] = fi[a] + f_d2 * eij[a] / mi;
+        fj[a] = fj[a] - f_d2 * eij[a] / mj;
+      }
+      if (brown) {
+        float z[6];
+        double dW[3][3], trace;
+        orc_pair_normals(s->p.seed, fc->step, pidi, pidj, d, z);
+        noise_matrix(s, z, dW, &trace);
+        const double Zij = 4.0 * kt * gradw / dij / numi / numj;
+        const double aa = 5.0 * eta / 3.0;
+        const double bb = ((double)d + 2.0) * eta / 3.0;
+        const double Aij = sqrt(-Zij * aa);
+        const double Bij = sqrt(-Zij * (double)d / 2.0 * (bb + aa * (2.0 / (double)d - 1.0)));
+        for (int a = 0; a < d; ++a) {
+          double We = 0.0;
+          for (int b = 0; b < d; ++b) We = We + dW[a][b] * eij[b];
+          const double fr = (Aij * We + Bij * trace * eij[a]) / fc->sqdt;
+          fi[a] = fi[a] + fr / mi;
+          fj[a] = fj[a] - fr / mj;
+        }
+      }
+      break;
+    }
+    case 3: { /* Hu-Adams, rhs_force_ff_Newtonian_HuAdams.F90:124-237 */
+      const double f_c = (pi / (numi * numi) + pj / (numj * numj)) * gradw;
+      for (int a = 0; a < d; ++a) {
+        fi[a] = fi[a] - f_c * eij[a] / mi;
+        fj[a] = fj[a] + f_c * eij[a] / mj;
+      }
+      const double f_d = eta * (1.0 / (numi * numi) + 1.0 / (numj * numj)) * gradw / dij;
+      for (int a = 0; a < d; ++a) {
+        fi[a] = fi[a] + f_d * vij[a] / mi;
+        fj[a] = fj[a] - f_d * vij[a] / mj;
+      }
+      if (brown) {
+        float z[6];
+        double dW[3][3], trace;
+        orc_pair_normals(s->p.seed, fc->step, pidi, pidj, d, z);
+        noise_matrix(s, z, dW, &trace);
+        const double f_r = sqrt(-4.0 * kt * f_d) / fc->sqdt;
+        for (int a = 0; a < d; ++a) {
+          double We = 0.0;
+          for (int b = 0; b < d; ++b) We = We + dW[a][b] * eij[b];
+          fi[a] = fi[a] + f_r * We / mi;
+          fj[a] = fj[a] - f_r * We / mj;
+        }
+      }
+      break;
+    }
+    case 4: { /* Hu-Adams angular, ..._HuAdams_angular.F90:152-229 */
+      double ev = 0.0;
+      for (int a = 0; a < d; ++a) ev = ev + eij[a] * vij[a];
+      const double pij = (pi + pj) / 2.0;
+      const double Aij = (1.0 / (numi * numi) + 1.0 / (numj * numj)) * gradw;
+      const double f_c = Aij * pij;
+      for (int a = 0; a < d; ++a) {
+        fi[a] = fi[a] - f_c * eij[a] / mi;
+        fj[a] = fj[a] + f_c * eij[a] / mj;
+      }
+      const double f_d = s->p.eta_coef * eta * Aij * ev / dij;
+      for (int a = 0; a < d; ++a) {
+        fi[a] = fi[a] + f_d * eij[a] / mi;
+        fj[a] = fj[a] - f_d * eij[a] / mj;
+      }
+      if (brown) {
+        float z[6];
+        orc_pair_normals(s->p.seed, fc->step, pidi, pidj, d, z);
+        const double eps = (double)z[0];
+        const double f_r = eps * sqrt(2.0 * kt * eta) * sqrt(-s->p.eta_coef * Aij / dij) / fc->sqdt;
+        for (int a = 0; a < d; ++a) {
+          fi[a] = fi[a] + f_r * eij[a] / mi;
+          fj[a] = fj[a] - f_r * eij[a] / mj;
+        }
+      }
+      break;
+    }
+  }
+}
+
+/* Morris no-slip velocity of a wall particle,
+ * boundary_noslip_solid.F90:40-95,137-240; wall sid = -face (1..2d). */
+static void wall_noslip(const orc_state* s, const double* xf, const double* xw,
+                        const double* vf, double* vw, int32_t sid_w) {
+  const int d = s->d;
+  const int index_w = sid_w < 0 ? -sid_w : sid_w;
+  const double* sv = s->p.wall_v[index_w - 1];
+  if (s->p.wall_noslip_type <= 1) {
+    for (int a = 0; a < d; ++a) vw[a] = sv[a];
+    return;
+  }
+  int index;
+  double x_sur;
+  if (index_w % 2 == 1) {
+    index = (index_w + 1) / 2 - 1;
+    x_sur = s->p.min_phys[index];
+  } else {
+    index = index_w / 2 - 1;
+    x_sur = s->p.max_phys[index];
+  }
+  double f_sur = xf[index] - x_sur;
+  double w_sur = xw[index] - x_sur;
+  if (f_sur * w_sur >= 0.0) {
+    for (int a = 0; a < d; ++a) vw[a] = sv[a];
+  } else {
+    f_sur = fabs(f_sur);
+    w_sur = fabs(w_sur);
+    double corr = w_sur / f_sur;
+    if (corr > 0.5) corr = 0.5; /* mcf_wall_dist_ratio, mcf_header.F90:282 */
+    for (int a = 0; a < d; ++a) vw[a] = -corr * (vf[a] - sv[a]) + sv[a];
+  }
+}
+
+static void force_pair(orc_state* s, int64_t ip, int64_t jp, void* ctx) {
+  const force_ctx* fc = (const force_ctx*)ctx;
+  const int d = s->d;
+  const int32_t si = s->sid[ip], sj = s->sid[jp];
+  if (si < 0 && sj < 0) return; /* w-w: no interaction */
+  if (si > 0 && sj > 0) return; /* c-c off (pp_interact_cc = F)     */
+  if ((si > 0 && sj < 0) || (si < 0 && sj > 0)) return; /* c-w off */
+  double rij[3];
+  double dij = 0.0;
+  for (int a = 0; a < d; ++a) {
+    rij[a] = s->x[ip * d + a] - s->x[jp * d + a];
+    dij = dij + rij[a] * rij[a];
+  }
+  if (dij >= s->cut_off2) return; /* pp_interaction.inc:37-50 */
+  dij = sqrt(dij);
+  double gradw;
+  kernel_eval(s, dij, &gradw);
+  double vi[3], vj[3];
+  for (int a = 0; a < d; ++a) {
+    vi[a] = s->v[ip * d + a];
+    vj[a] = s->v[jp * d + a];
+  }
+  double pi = s->pr[ip], pj = s->pr[jp];
+  if (si == 0 && sj < 0) { /* pp_interaction_fw.inc */
+    wall_noslip(s, &s->x[ip * d], &s->x[jp * d], vi, vj, sj);
+    pj = pi;
+  } else if (si < 0 && sj == 0) { /* pp_interaction_wf.inc */
+    wall_noslip(s, &s->x[jp * d], &s->x[ip * d], vj, vi, si);
+    pi = pj;
+  }
+  double fi[3], fj[3];
+  rhs_force_ff(s, fc, &s->x[ip * d], &s->x[jp * d], dij, vi, vj, s->rho[ip], s->rho[jp], pi,
+               pj, s->m[ip], s->m[jp], gradw, s->pid[ip], s->pid[jp], fi, fj);
+  for (int a = 0; a < d; ++a) s->f[ip * d + a] = s->f[ip * d + a] + fi[a];
+  {
+    double ni = 0.0, nj = 0.0;
+    for (int a = 0; a < d; ++a) {
+      ni += fi[a] * fi[a];
+      nj += fj[a] * fj[a];
+    }
+    s->fabs_sum[ip] += sqrt(ni);
+    if (s->p.symmetry) s->fabs_sum[jp] += sqrt(nj);
+  }
+  const int d2 = d * d;
+  if (s->p.stress_tensor) {
+    /* pp_interaction_ff.inc:83-93: sip = rij(a)*fip(b)/2, sjp = sip */
+    for (int b = 0; b < d; ++b)
+      for (int a = 0; a < d; ++a) {
+        const double sab = rij[a] * fi[b] / 2.0;
+        s->s[ip * d2 + b * d + a] = s->s[ip * d2 + b * d + a] + sab;
+        if (s->p.symmetry) s->s[jp * d2 + b * d + a] = s->s[jp * d2 + b * d + a] + sab;
+      }
+  }
+  if (s->p.symmetry)
+    for (int a = 0; a < d; ++a) s->f[jp * d + a] = s->f[jp * d + a] + fj[a];
+}
+
+int orc_compute_interaction(orc_state* s, int64_t step) {
+  if (!s->have_pressure) return fail(s, "orc_compute_interaction: no pressure");
+  const double t0 = now_s();
+  const int d = s->d, d2 = d * d;
+  ghost_refresh(s);
+  for (int64_t j = 0; j < s->nall * d; ++j) s->f[j] = 0.0;
+  for (int64_t j = 0; j < s->nall * d2; ++j) s->s[j] = 0.0;
+  for (int64_t j = 0; j < s->nall; ++j) s->fabs_sum[j] = 0.0;
+  force_ctx fc;
+  fc.step = step;
+  fc.noise = s->p.Brownian && s->p.kt > s->machine_zero;
+  fc.sqdt = 0.0;
+  if (fc.noise) fc.sqdt = sqrt(s->p.dt);
+  for_all_pairs(s, force_pair, &fc);
+  if (s->p.symmetry)
+    for (int64_t g = s->nreal; g < s->nall; ++g) {
+      const int64_t o = s->owner[g];
+      for (int a = 0; a < d; ++a) s->f[o * d + a] = s->f[o * d + a] + s->f[g * d + a];
+      s->fabs_sum[o] += s->fabs_sum[g];
+      if (s->p.stress_tensor)
+        for (int a = 0; a < d2; ++a) s->s[o * d2 + a] = s->s[o * d2 + a] + s->s[g * d2 + a];
+    }
+  s->timers[2] += now_s() - t0;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------
+ * Body force, particles_apply_body_force.F90:96-353.
+ * ---------------------------------------------------------------------- */
+int orc_apply_body_force(orc_state* s) {
+  const int d = s->d;
+  const double* g = s->p.body_force;
+  switch (s->p.body_force_type) {
+    case 0:
+      break;
+    case 1:
+      for (int i = 0; i < d; ++i)
+        if (fabs(g[i]) > s->machine_zero)
+          for (int64_t j = 0; j < s->nreal; ++j)
+            if (s->sid[j] == 0) s->f[j * d + i] = s->f[j * d + i] + g[i];
+      break;
+    case 2:
+      for (int64_t j = 0; j < s->nreal; ++j) {
+        if (!(fabs(g[0]) > s->machine_zero)) continue;
+        const double half = s->p.max_phys[d - 1] * 0.5;
+        const double xl = s->x[j * d + d - 1];
+        if (xl < half && s->sid[j] == 0)
+          s->f[j * d] = s->f[j * d] + g[0];
+        else if (xl > half && s->sid[j] == 0)
+          s->f[j * d] = s->f[j * d] - g[0];
+      }
+      break;
+    case 3: {
+      const double k = 2.0 * MK_PI / (s->p.max_phys[1] - s->p.min_phys[1]);
+      if (fabs(g[0]) > s->machine_zero)
+        for (int64_t j = 0; j < s->nreal; ++j)
+          if (s->sid[j] == 0) s->f[j * d] = s->f[j * d] + g[0] * sin(k * s->x[j * d + 1]);
+      break;
+    }
+    default:
+      return fail(s, "orc_apply_body_force: body_force_type must be 0..3");
+  }
+  return 0;
+}
+
+/* particles_integrate_velocity.F90:84-94 */
+int orc_integrate_velocity(orc_state* s, double dt, double lambda) {
+  const int d = s->d;
+  for (int64_t j = 0; j < s->nreal; ++j)
+    if (s->sid[j] == 0)
+      for (int a = 0; a < d; ++a) s->v[j * d + a] = s->v[j * d + a] + lambda * s->f[j * d + a] * dt;
+  return 0;
+}
+
+/* particles_integrate_position.F90:82-111 (order 1) */
+int orc_integrate_position(orc_state* s, double dt) {
+  const int d = s->d;
+  for (int64_t j = 0; j < s->nreal; ++j)
+    if (s->sid[j] == 0)
+      for (int a = 0; a < d; ++a) s->x[j * d + a] = s->x[j * d + a] + s->v[j * d + a] * dt;
+  return 0;
+}
+
+static void set_dt(orc_state* s, double dt) { s->p.dt = dt; }
+
+static int rhs(orc_state* s, int64_t step) {
+  int rc;
+  if ((rc = orc_build_list(s))) return rc;
+  if ((rc = orc_compute_density(s))) return rc;
+  if ((rc = orc_compute_pressure(s))) return rc;
+  if ((rc = orc_compute_interaction(s, step))) return rc;
+  const double t0 = now_s();
+  rc = orc_apply_body_force(s);
+  s->timers[3] += now_s() - t0;
+  return rc;
+}
+
+/* marching_marching.F90:528-911 (initial right-hand side) */
+int orc_init_force(orc_state* s, int64_t step) {
+  int rc = orc_adjust_particles(s);
+  if (rc) return rc;
+  return rhs(s, step);
+}
+
+/* marching_integrate_VV.F90:303-1620 */
+int orc_step_vv(orc_state* s, int64_t step, double dt) {
+  set_dt(s, dt);
+  double t0 = now_s();
+  orc_integrate_velocity(s, dt, 0.5);
+  orc_integrate_position(s, dt);
+  orc_adjust_particles(s);
+  s->timers[3] += now_s() - t0;
+  int rc = rhs(s, step);
+  if (rc) return rc;
+  t0 = now_s();
+  orc_integrate_velocity(s, dt, 0.5);
+  s->timers[3] += now_s() - t0;
+  return 0;
+}
+
+int orc_run_vv(orc_state* s, int64_t step0, int32_t nsteps, double dt) {
+  for (int32_t k = 1; k <= nsteps; ++k) {
+    int rc = orc_step_vv(s, step0 + k, dt);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+int orc_download(orc_state* s, double* x, double* v, double* rho, double* p,
+                 double* f, double* ct, double* s_out) {
+  const int d = s->d, d2 = d * d;
+  const int64_t n = s->nreal;
+  if (x) memcpy(x, s->x, sizeof(double) * (size_t)(n * d));
+  if (v) memcpy(v, s->v, sizeof(double) * (size_t)(n * d));
+  if (rho) memcpy(rho, s->rho, sizeof(double) * (size_t)n);
+  if (p) memcpy(p, s->pr, sizeof(double) * (size_t)n);
+  if (f) memcpy(f, s->f, sizeof(double) * (size_t)(n * d));
+  if (ct) memcpy(ct, s->ct, sizeof(double) * (size_t)(n * d2));
+  if (s_out) memcpy(s_out, s->s, sizeof(double) * (size_t)(n * d2));
+  return 0;
+}
+
+/* statistic_compute_statistic.F90:230-303 */
+int orc_statistics(orc_state* s, double* k_energy, double* momentum, double* stress) {
+  const int d = s->d, d2 = d * d;
+  double ke = 0.0, mom[3] = {0, 0, 0}, st[9] = {0};
+  for (int64_t j = 0; j < s->nreal; ++j) {
+    if (s->sid[j] == 0) {
+      double v2 = 0.0;
+      for (int a = 0; a < d; ++a) v2 = v2 + s->v[j * d + a] * s->v[j * d + a];
+      ke = ke + 0.5 * s->m[j] * v2;
+      for (int a = 0; a < d; ++a) mom[a] = mom[a] + s->m[j] * s->v[j * d + a];
+    }
+    if (s->p.stress_tensor && s->sid[j] >= 0)
+      for (int a = 0; a < d2; ++a) st[a] = st[a] + s->s[j * d2 + a];
+  }
+  if (k_energy) *k_energy = ke;
+  if (momentum)
+    for (int a = 0; a < 3; ++a) momentum[a] = mom[a];
+  if (stress)
+    for (int a = 0; a < 9; ++a) stress[a] = a < d2 ? st[a] : 0.0;
+  return 0;
+}
+
+int orc_force_scale(const orc_state* s, double* out) {
+  memcpy(out, s->fabs_sum, sizeof(double) * (size_t)s->nreal);
+  return 0;
+}
+
+int orc_counts(const orc_state* s, int64_t* counts) {
+  counts[0] = s->nreal;
+  counts[1] = s->nall - s->nreal;
+  counts[2] = s->npairs;
+  return 0;
+}
+
+int orc_timers(const orc_state* s, double* t) {
+  for (int i = 0; i < 4; ++i) t[i] = s->timers[i];
+  return 0;
+}
+
+/* particles_init_global_inter_cubic.F90 / _square: lattice by repeated
+ * addition starting at min + dx/2 */
+int64_t orc_lattice(int dim, const double* min_t, const double* max_t, const double* dx,
+                    double* x_out, int64_t cap) {
+  int64_t num = 0;
+  double sx[3];
+  if (dim == 3) {
+    sx[2] = min_t[2] + 0.5 * dx[2];
+    while (sx[2] < max_t[2]) {
+      sx[1] = min_t[1] + 0.5 * dx[1];
+      while (sx[1] < max_t[1]) {
+        sx[0] = min_t[0] + 0.5 * dx[0];
+        while (sx[0] < max_t[0]) {
+          if (x_out && num < cap)
+            for (int a = 0; a < 3; ++a) x_out[num * 3 + a] = sx[a];
+          num++;
+          sx[0] = sx[0] + dx[0];
+        }
+        sx[1] = sx[1] + dx[1];
+      }
+      sx[2] = sx[2] + dx[2];
+    }
+  } else {
+    sx[1] = min_t[1] + 0.5 * dx[1];
+    while (sx[1] < max_t[1]) {
+      sx[0] = min_t[0] + 0.5 * dx[0];
+      while (sx[0] < max_t[0]) {
+        if (x_out && num < cap)
+          for (int a = 0; a < 2; ++a) x_out[num * 2 + a] = sx[a];
+        num++;
+        sx[0] = sx[0] + dx[0];
+      }
+      sx[1] = sx[1] + dx[1];
+    }
+  }
+  return num;
+}

@@ -1,0 +1,228 @@
+"""ctypes wrapper of the CPU oracle (oracle/_lib/liborc.so).
+
+TEST INFRASTRUCTURE ONLY.  The oracle restates MCF's Fortran SDPD step in C
+(see mcf_oracle.c for the per-routine citations).  Only tests/, the smoke
+check of __graft_entry__ and the CPU-baseline leg of bench.py use it; the
+product path (mcf_gb300) never imports this module.
+
+Parity status: parity unpinned against outputs of the reference itself (MCF
+cannot be built here and ships no golden vectors); pinned by analytic checks
+and committed fixtures instead (tests/golden).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent))
+
+from mcf_gb300.params import SDPDParams  # noqa: E402  (struct layout only)
+
+from . import build as _build  # noqa: E402
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_h = C.c_void_p
+_LIB = None
+
+
+def load(rebuild: bool = True) -> C.CDLL:
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.build() if rebuild else _build.OUT
+    lib = C.CDLL(str(path))
+    sig = {
+        "orc_create": (_h, [C.POINTER(SDPDParams), C.c_char_p, C.c_int]),
+        "orc_destroy": (None, [_h]),
+        "orc_last_error": (C.c_char_p, [_h]),
+        "orc_set_threads": (C.c_int, [_h, C.c_int]),
+        "orc_upload": (C.c_int, [_h, C.c_int64, _dp, _dp, _dp, _ip, _dp]),
+        "orc_adjust_particles": (C.c_int, [_h]),
+        "orc_build_list": (C.c_int, [_h]),
+        "orc_export_lists": (C.c_int, [_h, _ip, _ip, _ip]),
+        "orc_compute_density": (C.c_int, [_h]),
+        "orc_compute_pressure": (C.c_int, [_h]),
+        "orc_compute_interaction": (C.c_int, [_h, C.c_int64]),
+        "orc_apply_body_force": (C.c_int, [_h]),
+        "orc_integrate_velocity": (C.c_int, [_h, C.c_double, C.c_double]),
+        "orc_integrate_position": (C.c_int, [_h, C.c_double]),
+        "orc_init_force": (C.c_int, [_h, C.c_int64]),
+        "orc_step_vv": (C.c_int, [_h, C.c_int64, C.c_double]),
+        "orc_run_vv": (C.c_int, [_h, C.c_int64, C.c_int32, C.c_double]),
+        "orc_download": (C.c_int, [_h, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+        "orc_statistics": (C.c_int, [_h, _dp, _dp, _dp]),
+        "orc_counts": (C.c_int, [_h, C.POINTER(C.c_int64)]),
+        "orc_force_scale": (C.c_int, [_h, _dp]),
+        "orc_timers": (C.c_int, [_h, _dp]),
+        "orc_lattice": (C.c_int64, [C.c_int, _dp, _dp, _dp, _dp, C.c_int64]),
+        "orc_philox4x32_10": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                     C.POINTER(C.c_uint32)]),
+        "orc_pair_normals": (None, [C.c_uint64, C.c_int64, C.c_int32, C.c_int32, C.c_int,
+                                    C.POINTER(C.c_float)]),
+        "orc_kernel": (C.c_int, [_h, C.c_double, _dp, _dp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _ptr(a, t):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+class Oracle:
+    """CPU FP64 restatement with the same routine names as mcf_gb300.SDPD."""
+
+    def __init__(self, params: SDPDParams, threads: int = 1):
+        self.lib = load()
+        self.params = params.copy()
+        self.dim = int(params.num_dim)
+        err = C.create_string_buffer(256)
+        h = self.lib.orc_create(C.byref(self.params), err, 256)
+        if not h:
+            raise OracleError(err.value.decode())
+        self._h = h
+        self.n = 0
+        self.lib.orc_set_threads(h, int(threads))
+
+    def _check(self, name, rc):
+        if rc != 0:
+            raise OracleError(f"{name}: {self.lib.orc_last_error(self._h).decode()}")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.orc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_threads(self, n: int):
+        self.lib.orc_set_threads(self._h, int(n))
+
+    def upload(self, x, v, m, id_, ct=None):
+        n = int(np.asarray(m).shape[0])
+        d = self.dim
+        self._x = np.ascontiguousarray(x, np.float64).reshape(n, d)
+        self._v = np.ascontiguousarray(v, np.float64).reshape(n, d)
+        self._m = np.ascontiguousarray(m, np.float64).reshape(n)
+        self._id = np.ascontiguousarray(id_, np.int32).reshape(n, 2)
+        ctp = None if ct is None else np.ascontiguousarray(ct, np.float64)
+        self._check("orc_upload", self.lib.orc_upload(self._h, n, _ptr(self._x, C.c_double),
+                                                      _ptr(self._v, C.c_double),
+                                                      _ptr(self._m, C.c_double),
+                                                      _ptr(self._id, C.c_int32),
+                                                      _ptr(ctp, C.c_double)))
+        self.n = n
+
+    def download(self, *fields):
+        n, d = self.n, self.dim
+        shapes = {"x": (n, d), "v": (n, d), "rho": (n,), "p": (n,), "f": (n, d), "s": (n, d * d)}
+        out = {k: np.empty(shapes[k], np.float64) for k in fields}
+        g = lambda k: _ptr(out.get(k), C.c_double)  # noqa: E731
+        self._check("orc_download",
+                    self.lib.orc_download(self._h, g("x"), g("v"), g("rho"), g("p"), g("f"), None,
+                                          g("s")))
+        return out
+
+    def particles_adjust_particles(self):
+        self._check("adjust", self.lib.orc_adjust_particles(self._h))
+
+    def technique_build_list(self, want_lists: bool = True):
+        self._check("build_list", self.lib.orc_build_list(self._h))
+        if not want_lists:
+            return None
+        ncd = np.zeros(3, np.int32)
+        self._check("export", self.lib.orc_export_lists(self._h, _ptr(ncd, C.c_int32), None, None))
+        ncell = int(np.prod(ncd))
+        cs = np.empty(ncell + 1, np.int32)
+        lp = np.empty(max(self.n, 1), np.int32)
+        self._check("export", self.lib.orc_export_lists(self._h, _ptr(ncd, C.c_int32),
+                                                        _ptr(cs, C.c_int32), _ptr(lp, C.c_int32)))
+        return ncd, cs, lp[: int(cs[-1])]
+
+    def particles_compute_density(self):
+        self._check("density", self.lib.orc_compute_density(self._h))
+
+    def particles_compute_pressure(self):
+        self._check("pressure", self.lib.orc_compute_pressure(self._h))
+
+    def particles_compute_interaction(self, step: int = 0):
+        self._check("interaction", self.lib.orc_compute_interaction(self._h, int(step)))
+
+    def particles_apply_body_force(self):
+        self._check("body_force", self.lib.orc_apply_body_force(self._h))
+
+    def particles_integrate_velocity(self, dt, lam):
+        self._check("integrate_velocity", self.lib.orc_integrate_velocity(self._h, dt, lam))
+
+    def particles_integrate_position(self, dt):
+        self._check("integrate_position", self.lib.orc_integrate_position(self._h, dt))
+
+    def marching_init_force(self, step: int = 0):
+        self._check("init_force", self.lib.orc_init_force(self._h, int(step)))
+
+    def marching_integrate_VV(self, step, dt):
+        self._check("step_vv", self.lib.orc_step_vv(self._h, int(step), float(dt)))
+
+    def run_vv(self, step0, nsteps, dt):
+        self._check("run_vv", self.lib.orc_run_vv(self._h, int(step0), int(nsteps), float(dt)))
+
+    def statistic_compute_statistic(self):
+        ke = C.c_double()
+        mom = np.zeros(3)
+        st = np.zeros(9)
+        self._check("statistics", self.lib.orc_statistics(self._h, C.byref(ke),
+                                                          _ptr(mom, C.c_double),
+                                                          _ptr(st, C.c_double)))
+        return ke.value, mom, st
+
+    def force_scale(self) -> np.ndarray:
+        out = np.empty(self.n)
+        self.lib.orc_force_scale(self._h, _ptr(out, C.c_double))
+        return out
+
+    def counts(self):
+        c = (C.c_int64 * 3)()
+        self.lib.orc_counts(self._h, c)
+        return {"real": c[0], "ghost": c[1], "pairs": c[2]}
+
+    def timers(self):
+        t = np.zeros(4)
+        self.lib.orc_timers(self._h, _ptr(t, C.c_double))
+        return {"list": t[0], "density": t[1], "force": t[2], "update": t[3]}
+
+    def kernel(self, r: float):
+        w = C.c_double()
+        g = C.c_double()
+        self.lib.orc_kernel(self._h, float(r), C.byref(w), C.byref(g))
+        return w.value, g.value
+
+
+def pair_normals(seed: int, step: int, pa: int, pb: int, dim: int) -> np.ndarray:
+    z = (C.c_float * 6)()
+    load().orc_pair_normals(seed, step, pa, pb, dim, z)
+    return np.array(z[: (6 if dim == 3 else 3)], dtype=np.float32)
+
+
+def philox(ctr, key) -> list[int]:
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    load().orc_philox4x32_10(c, k, o)
+    return list(o)

@@ -1,0 +1,69 @@
+"""Generate / load the regression fixtures of the oracle (tests/golden/*.npz).
+
+Run `python -m tests.golden.make_golden` to regenerate.  The reference (MCF)
+ships no golden vectors and cannot be built here, so these fixtures pin the
+oracle against its own past outputs; the analytic checks in
+tests/test_oracle.py pin it against MCF's formulas.
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent.parent))
+
+from mcf_gb300 import configs  # noqa: E402
+from mcf_gb300.params import make_params  # noqa: E402
+from oracle.oracle import Oracle  # noqa: E402
+
+CASES = ("c1_small", "c2_small", "walls_small")
+
+
+def workload(name: str) -> configs.Workload:
+    if name == "c1_small":
+        w = configs.c1_poiseuille_2d(n_side=16)
+        rng = np.random.default_rng(11)
+        w.x = w.x + rng.uniform(-0.05, 0.05, w.x.shape) / 16
+        w.v = rng.normal(0, 1e-3, w.v.shape)
+        return w
+    if name == "c2_small":
+        return configs.c2_fluctuating_3d(n_side=9)
+    if name == "walls_small":
+        w = configs.c3_poiseuille_3d(n_side=9)
+        rng = np.random.default_rng(12)
+        fl = w.id[:, 1] == 0
+        w.v[fl] = rng.normal(0, 1e-2, (int(fl.sum()), 3))
+        return w
+    raise KeyError(name)
+
+
+def compute(name: str) -> dict:
+    w = workload(name)
+    o = Oracle(w.params)
+    o.upload(w.x, w.v, w.m, w.id)
+    o.marching_init_force(0)
+    ncd, cs, lp = o.technique_build_list()
+    out = {"num_cell_dim": ncd, "cell_start": cs, "lpdx": lp}
+    d0 = o.download("rho", "p", "f")
+    out.update({"rho0": d0["rho"], "p0": d0["p"], "f0": d0["f"]})
+    o.run_vv(0, 5, w.dt)
+    d1 = o.download("x", "v", "rho", "f")
+    out.update({"x5": d1["x"], "v5": d1["v"], "rho5": d1["rho"], "f5": d1["f"]})
+    return out
+
+
+def load_all() -> dict:
+    res = {}
+    for name in CASES:
+        with np.load(HERE / f"{name}.npz") as z:
+            res[name] = {k: z[k] for k in z.files}
+    return res
+
+
+if __name__ == "__main__":
+    for name in CASES:
+        np.savez_compressed(HERE / f"{name}.npz", **compute(name))
+        print("wrote", name)

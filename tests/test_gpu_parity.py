@@ -1,0 +1,236 @@
+"""GPU parity tests: the CUDA path through the C-ABI against the CPU oracle.
+
+Bars (the benchmark spec of the plain FP64 path):
+  - cell lists bit-exact (per real cell, sorted host indices, PPM order);
+  - per-step density within 1e-12 relative;
+  - per-step acceleration within 1e-12 of the per-particle scale
+    S_i = sum_j |a_ij| (net forces on near-lattice states are sums of large
+    cancelling pair terms, so |a_i| itself is no scale);
+  - with the random force on, the pair normals are FP32 Box-Muller values
+    (CUDA logf/sincospif on the GPU, libm on the CPU): tolerance 1e-5 * S_i;
+  - kT=0 trajectories over 100 steps: positions within 1e-9 of the box
+    length, velocities within 1e-7 of the velocity scale.
+"""
+import numpy as np
+import pytest
+
+from mcf_gb300 import SDPD, configs
+from mcf_gb300.params import PRECISION_FP32_MIXED, PRECISION_FP64
+from oracle.oracle import Oracle
+from tests.golden import make_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def both(w, **over):
+    p = w.params.copy()
+    for k, v in over.items():
+        setattr(p, k, v)
+    g = SDPD(p)
+    g.upload(w.x, w.v, w.m, w.id)
+    o = Oracle(p)
+    o.upload(w.x, w.v, w.m, w.id)
+    return g, o
+
+
+def jittered_2d(n_side=32, amp=0.3, seed=5):
+    w = configs.c1_poiseuille_2d(n_side=n_side)
+    rng = np.random.default_rng(seed)
+    w.x = w.x + rng.uniform(-amp, amp, w.x.shape) / n_side
+    w.v = rng.normal(0, 1e-2, w.v.shape)
+    return w
+
+
+def jittered_3d(n_side=12, amp=0.3, seed=6, **kw):
+    w = configs.c2_fluctuating_3d(n_side=n_side, **kw)
+    rng = np.random.default_rng(seed)
+    w.x = w.x + rng.uniform(-amp, amp, w.x.shape)
+    w.v = rng.normal(0, 1e-2, w.v.shape)
+    return w
+
+
+def compare_lists(g, o):
+    ga = g.technique_build_list()
+    oa = o.technique_build_list()
+    assert np.array_equal(ga[0], oa[0])
+    assert np.array_equal(ga[1], oa[1])
+    assert np.array_equal(ga[2], oa[2])
+
+
+# ---------------------------------------------------------------- cell list
+@pytest.mark.parametrize("maker", ["c1", "jit2d", "jit3d", "walls"])
+def test_cell_list_bit_exact(gpu_lib, maker):
+    w = {"c1": lambda: configs.c1_poiseuille_2d(),
+         "jit2d": jittered_2d,
+         "jit3d": jittered_3d,
+         "walls": lambda: make_golden.workload("walls_small")}[maker]()
+    g, o = both(w)
+    g.particles_adjust_particles()
+    o.particles_adjust_particles()
+    compare_lists(g, o)
+
+
+def test_cell_list_boundary_positions(gpu_lib):
+    # positions on cell faces, on the domain faces and one ulp inside them
+    w = configs.c2_fluctuating_3d(n_side=12)
+    p = w.params
+    n = w.n
+    rng = np.random.default_rng(3)
+    cs = (p.max_phys_t[0] - p.min_phys_t[0]) / int((12.0) / (3.0 * 1.0001))
+    faces = np.array([0.0, cs, 2 * cs, 12.0 - 1e-15, np.nextafter(12.0, 0), np.nextafter(cs, 0),
+                      np.nextafter(cs, 13)])
+    x = w.x.copy()
+    x[: n // 2] = rng.choice(faces, size=(n // 2, 3))
+    w.x = x
+    g, o = both(w)
+    g.particles_adjust_particles()
+    o.particles_adjust_particles()
+    compare_lists(g, o)
+
+
+# ------------------------------------------------------- density and force
+def check_rhs(g, o, noise=False, step=0):
+    g.marching_init_force(step)
+    o.marching_init_force(step)
+    a = g.download("rho", "p", "f")
+    b = o.download("rho", "p", "f")
+    assert np.all(np.abs(a["rho"] - b["rho"]) <= 1e-12 * np.abs(b["rho"]))
+    scale = o.force_scale()[:, None] + np.abs(b["f"])
+    tol = 1e-5 if noise else 1e-12
+    err = np.abs(a["f"] - b["f"])
+    assert np.all(err <= tol * scale), float(np.max(err / scale))
+    return a, b
+
+
+@pytest.mark.parametrize("ftype", [1, 2, 3, 4])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_fp64_density_force(gpu_lib, ftype, dim):
+    w = jittered_2d() if dim == 2 else jittered_3d()
+    over = dict(rhs_force_type=ftype, Brownian=0, kt=0.0)
+    if ftype == 1:
+        over["rhs_density_type"] = 1
+    g, o = both(w, **over)
+    check_rhs(g, o)
+
+
+@pytest.mark.parametrize("ktype,eos", [(2, 1), (1, 2)])
+def test_fp64_kernel_and_eos_variants(gpu_lib, ktype, eos):
+    w = jittered_3d()
+    g, o = both(w, kernel_type=ktype, stateEquation_type=eos, gamma=7.0 if eos == 2 else 1.0,
+                rho_ref=1.0, Brownian=0, kt=0.0)
+    check_rhs(g, o)
+
+
+@pytest.mark.parametrize("ftype", [2, 3, 4])
+def test_fp64_random_force(gpu_lib, ftype):
+    w = jittered_3d()
+    g, o = both(w, rhs_force_type=ftype, Brownian=1, kt=1e-3)
+    a, b = check_rhs(g, o, noise=True, step=17)
+    # the random term is on: the force differs from the deterministic one
+    g2, o2 = both(w, rhs_force_type=ftype, Brownian=0, kt=0.0)
+    g2.marching_init_force(17)
+    c = g2.download("f")["f"]
+    assert np.max(np.abs(a["f"] - c)) > 1e-6
+
+
+def test_fp64_walls(gpu_lib):
+    w = make_golden.workload("walls_small")
+    g, o = both(w, Brownian=0, kt=0.0)
+    check_rhs(g, o)
+
+
+def test_fp64_golden_fixtures(gpu_lib):
+    for name, fx in make_golden.load_all().items():
+        w = make_golden.workload(name)
+        g = SDPD(w.params)
+        g.upload(w.x, w.v, w.m, w.id)
+        g.marching_init_force(0)
+        d = g.download("rho", "f")
+        assert np.all(np.abs(d["rho"] - fx["rho0"]) <= 1e-12 * np.abs(fx["rho0"]))
+        noise = bool(w.params.Brownian and w.params.kt > 0)
+        tol = 1e-5 if noise else 1e-9
+        assert np.all(np.abs(d["f"] - fx["f0"]) <= tol * (np.abs(fx["f0"]).max() + 1.0))
+
+
+def test_stress_tensor_and_statistics(gpu_lib):
+    w = jittered_3d()
+    g, o = both(w, stress_tensor=1, Brownian=0, kt=0.0)
+    g.marching_init_force(0)
+    o.marching_init_force(0)
+    a = g.download("s")["s"]
+    b = o.download("s")["s"]
+    assert np.max(np.abs(a - b)) <= 1e-10 * (np.abs(b).max() + 1e-30)
+    ke_g, mom_g, st_g = g.statistic_compute_statistic()
+    ke_o, mom_o, st_o = o.statistic_compute_statistic()
+    assert abs(ke_g - ke_o) <= 1e-12 * ke_o
+    assert np.allclose(mom_g, mom_o, rtol=1e-12, atol=1e-15)
+    assert np.allclose(st_g, st_o, rtol=1e-10, atol=1e-12 * np.abs(st_o).max())
+
+
+# ------------------------------------------------------------- trajectories
+def test_fp64_trajectory_100_steps_kt0(gpu_lib):
+    w = configs.c1_poiseuille_2d()
+    g, o = both(w)
+    g.marching_init_force(0)
+    o.marching_init_force(0)
+    for s in range(1, 101):
+        g.marching_integrate_VV(s, w.dt)
+        o.marching_integrate_VV(s, w.dt)
+    a = g.download("x", "v", "rho")
+    b = o.download("x", "v", "rho")
+    dx = np.abs(a["x"] - b["x"])
+    dx = np.minimum(dx, 1.0 - dx)  # periodic images
+    assert dx.max() <= 1e-9
+    vs = np.abs(b["v"]).max()
+    assert np.abs(a["v"] - b["v"]).max() <= 1e-7 * vs
+    assert np.all(np.abs(a["rho"] - b["rho"]) <= 1e-10 * b["rho"])
+
+
+def test_run_vv_equals_step_vv_and_is_deterministic(gpu_lib):
+    w = jittered_3d()
+    outs = []
+    for mode in ("step", "run", "run"):
+        g = SDPD(w.params)
+        g.upload(w.x, w.v, w.m, w.id)
+        g.marching_init_force(0)
+        if mode == "step":
+            for s in range(1, 6):
+                g.marching_integrate_VV(s, w.dt)
+        else:
+            g.run_vv(0, 5, w.dt)
+        outs.append(g.download("x", "v", "f"))
+    for k in ("x", "v", "f"):
+        assert np.array_equal(outs[0][k], outs[1][k])
+        assert np.array_equal(outs[1][k], outs[2][k])
+
+
+# --------------------------------------------------------- FP32-mixed path
+def test_fp32_mixed_error_vs_fp64(gpu_lib):
+    w = jittered_3d(amp=0.05)
+    g32, o = both(w, precision=PRECISION_FP32_MIXED, Brownian=0, kt=0.0)
+    g32.marching_init_force(0)
+    o.marching_init_force(0)
+    a = g32.download("rho", "f")
+    b = o.download("rho", "f")
+    rel_rho = np.abs(a["rho"] - b["rho"]) / b["rho"]
+    assert rel_rho.max() < 2e-6
+    scale = o.force_scale()[:, None]
+    assert np.max(np.abs(a["f"] - b["f"]) / scale) < 1e-4
+
+
+# ----------------------------------------------------------- error handling
+def test_neighbour_overflow_is_reported(gpu_lib):
+    from mcf_gb300 import MCFGError
+    from mcf_gb300.params import MCFG_EOVERFLOW
+
+    w = jittered_3d()
+    p = w.params.copy()
+    p.reserved[0] = 8  # far below the ~92 neighbours per particle
+    g = SDPD(p)
+    g.upload(w.x, w.v, w.m, w.id)
+    with pytest.raises(MCFGError) as ei:
+        g.marching_init_force(0)
+    assert ei.value.code == MCFG_EOVERFLOW
+    # the handle stays usable
+    g.upload(w.x, w.v, w.m, w.id)
+    g.technique_build_list()

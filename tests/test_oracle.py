@@ -1,0 +1,151 @@
+"""CPU tests of the oracle (the parity checker): known-answer vectors of the
+random stream, analytic self-checks of MCF's SPH formulas, agreement of
+MCF's two pair-loop modes, PPM's ghost-count test and regression fixtures."""
+import math
+
+import numpy as np
+import pytest
+
+from mcf_gb300 import configs
+from mcf_gb300.params import BC_WALL_SOLID, make_params
+from oracle.oracle import Oracle, pair_normals, philox
+
+
+def test_philox_known_answers():
+    # Philox4x32-10 known-answer vectors published with the Random123
+    # library (Salmon et al., SC'11)
+    assert philox([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert philox([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6,
+                                                          0x6D5451FD]
+    assert philox([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]) == [
+        0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def test_pair_normals_symmetric_and_gaussian():
+    assert np.array_equal(pair_normals(7, 3, 10, 99, 3), pair_normals(7, 3, 99, 10, 3))
+    assert not np.array_equal(pair_normals(7, 3, 10, 99, 3), pair_normals(7, 4, 10, 99, 3))
+    z = np.concatenate([pair_normals(1, s, a, a + 1, 3) for s in range(40) for a in range(250)])
+    assert abs(z.mean()) < 0.03
+    assert abs(z.var() - 1.0) < 0.03
+    assert np.abs(z).max() < 6.0  # mcf_random_Gaussian_max_abs, mcf_header.F90:73
+
+
+@pytest.mark.parametrize("dim,ktype", [(2, 1), (3, 1), (2, 2), (3, 2)])
+def test_kernel_normalisation(dim, ktype):
+    rc = 3.0
+    p = make_params(num_dim=dim, cut_off=rc, kernel_type=ktype,
+                    min_phys=[0, 0, 0], max_phys=[12, 12, 12], min_phys_t=[0, 0, 0],
+                    max_phys_t=[12, 12, 12])
+    o = Oracle(p)
+    r = np.linspace(0.0, rc, 20001)
+    w = np.array([o.kernel(x)[0] for x in r])
+    g = np.array([o.kernel(x)[1] for x in r])
+    shell = 2 * math.pi * r if dim == 2 else 4 * math.pi * r ** 2
+    # MCF's 3D quintic coefficient is 3/(359 pi h^3) (kernel_new.F90:60)
+    # where the normalised spline has 3/(360 pi h^3): its integral is
+    # 360/359, kept as MCF has it
+    expect = 360.0 / 359.0 if (dim == 3 and ktype == 1) else 1.0
+    assert abs(np.trapezoid(w * shell, r) - expect) < 1e-6
+    # dW/dr is the derivative of W
+    dw = np.gradient(w, r)
+    assert np.max(np.abs(dw[5:-5] - g[5:-5])) < 1e-3 * np.max(np.abs(g))
+    assert np.all(g <= 1e-15)
+
+
+def _run_init(w, symmetry=1, **over):
+    p = w.params.copy()
+    p.symmetry = symmetry
+    for k, v in over.items():
+        setattr(p, k, v)
+    o = Oracle(p)
+    o.upload(w.x, w.v, w.m, w.id)
+    o.marching_init_force(0)
+    return o, o.download("rho", "p", "f")
+
+
+def test_lattice_density_is_rho0():
+    w = configs.c1_poiseuille_2d(n_side=32)
+    _, d = _run_init(w)
+    rho_mass = d["rho"] * w.m
+    assert np.allclose(rho_mass, rho_mass[0], rtol=1e-12)
+    assert abs(rho_mass[0] - 1.0) < 1e-3
+
+
+@pytest.mark.parametrize("ftype", [1, 2, 3, 4])
+def test_symmetric_and_full_loops_agree(ftype):
+    # MCF's half-shell loops with ghost put (symmetry=T) and its full
+    # 27-cell loops (symmetry=F) are the same sums in another order
+    w = configs.c2_fluctuating_3d(n_side=10)
+    over = dict(rhs_force_type=ftype, Brownian=1, kt=1e-3)
+    if ftype == 1:
+        over["rhs_density_type"] = 1
+    o1, a = _run_init(w, 1, **over)
+    o2, b = _run_init(w, 0, **over)
+    assert np.allclose(a["rho"], b["rho"], rtol=1e-13, atol=0)
+    scale = o1.force_scale()[:, None]
+    assert np.all(np.abs(a["f"] - b["f"]) <= 1e-12 * scale + 1e-300)
+    assert o1.counts()["pairs"] * 2 == o2.counts()["pairs"]
+
+
+def test_momentum_conservation():
+    w = configs.c2_fluctuating_3d(n_side=10)
+    _, d = _run_init(w)
+    tot = (d["f"] * w.m[:, None]).sum(0)
+    assert np.all(np.abs(tot) < 1e-10)
+
+
+def test_ghost_images_near_periodic_faces():
+    # in the spirit of PPM's ghost-count test
+    # (ppm:test/ppm_module_map_part_ghost_test.F90:64-100): particles inside
+    # the ghost layer of the lower faces get images at +L per face, corner
+    # particles also the diagonal image (symmetry=T, images above only)
+    p = make_params(num_dim=2, min_phys=[0, 0, 0], max_phys=[1, 1, 0], min_phys_t=[0, 0, 0],
+                    max_phys_t=[1, 1, 0], cut_off=0.1, symmetry=1)
+    o = Oracle(p)
+    x = np.array([[0.05, 0.05], [0.5, 0.05]])
+    o.upload(x, np.zeros_like(x), np.ones(2), np.array([[1, 0], [2, 0]], np.int32))
+    o.technique_build_list()
+    c = o.counts()
+    # particle 1: images at (+L,0), (0,+L), (+L,+L); particle 2: (0,+L)
+    assert c["ghost"] == 4
+
+
+def test_body_force_types():
+    w = configs.c1_poiseuille_2d(n_side=32)
+    for bft in (1, 2, 3):
+        p = w.params.copy()
+        p.body_force_type = bft
+        o = Oracle(p)
+        o.upload(w.x, np.zeros_like(w.v), w.m, w.id)
+        o.marching_init_force(0)
+        f = o.download("f")["f"]
+        y = w.x[:, 1]
+        if bft == 1:
+            expect = np.full_like(y, 1.0)
+        elif bft == 2:
+            expect = np.where(y < 0.5, 1.0, -1.0)
+        else:
+            expect = np.sin(2 * math.pi * y)
+        assert np.allclose(f[:, 0], expect, atol=1e-9)
+
+
+def test_walls_channel_setup():
+    w = configs.c3_poiseuille_3d(n_side=12)
+    sid = w.id[:, 1]
+    # 4 wall layers per side (CEILING(1.05*3/1)) in y
+    assert (sid == -3).sum() == 12 * 12 * 4 and (sid == -4).sum() == 12 * 12 * 4
+    assert w.params.bcdef[2] == BC_WALL_SOLID
+    o, d = _run_init(w)
+    rho = d["rho"]
+    assert np.allclose(rho[sid < 0], 1.0)  # init_density / m
+    fl = sid == 0
+    assert np.allclose(rho[fl], rho[fl][0], rtol=1e-9)
+
+
+def test_golden_fixtures_regression():
+    from tests.golden import make_golden
+
+    for name, fx in make_golden.load_all().items():
+        got = make_golden.compute(name)
+        for k, v in fx.items():
+            assert np.array_equal(got[k], v), (name, k)
