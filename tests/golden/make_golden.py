@@ -30,9 +30,9 @@ def workload(name: str) -> configs.Workload:
         w.v = rng.normal(0, 1e-3, w.v.shape)
         return w
     if name == "c2_small":
-        return configs.c2_fluctuating_3d(n_side=9)
+        return configs.c2_fluctuating_3d(n_side=10)
     if name == "walls_small":
-        w = configs.c3_poiseuille_3d(n_side=9)
+        w = configs.c3_poiseuille_3d(n_side=10)
         rng = np.random.default_rng(12)
         fl = w.id[:, 1] == 0
         w.v[fl] = rng.normal(0, 1e-2, (int(fl.sum()), 3))
