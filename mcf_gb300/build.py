@@ -45,9 +45,15 @@ def _flags() -> list[str]:
     ]
 
 
+# Per-file flags.  The pair sweeps run their FP32 path with flush-to-zero and
+# approximate FP32 division / square root (MUFU based, no slow-path calls);
+# these flags do not touch FP64 arithmetic, so the FP64 path is unchanged.
+EXTRA = {"pair_kernels.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]}
+
+
 def _compile(src: str, verbose: bool) -> Path:
     obj = BUILD / (Path(src).stem + ".o")
-    cmd = [nvcc_path(), *_flags(), "-c", str(CSRC / src), "-o", str(obj)]
+    cmd = [nvcc_path(), *_flags(), *EXTRA.get(src, []), "-c", str(CSRC / src), "-o", str(obj)]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -142,7 +142,8 @@ __global__ void k_cell_finalize(Consts k, const int* __restrict__ start,
                                 double4_32a* __restrict__ f_out, double* __restrict__ m_out,
                                 int* __restrict__ pid_out, int* __restrict__ sid_out,
                                 int* __restrict__ hidx_out, float4* __restrict__ off,
-                                int* __restrict__ cell_of, unsigned* __restrict__ err) {
+                                int* __restrict__ cell_of, float2* __restrict__ wd,
+                                unsigned* __restrict__ err) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp > k.ncell) return;
@@ -181,6 +182,13 @@ __global__ void k_cell_finalize(Consts k, const int* __restrict__ start,
     of.z = (D == 3) ? (float)(xp.z - org[2]) : 0.0f;
     of.w = __int_as_float(sid_in[o]);  // species id rides in the w lane
     off[dst] = of;
+    if (wd != nullptr && k.wall_axis >= 0) {
+      // distances to the two faces of the wall axis, formed in FP64 and
+      // rounded once (boundary_noslip_solid.F90:200-206 uses x - x_sur)
+      const double xa = k.wall_axis == 0 ? xp.x : (k.wall_axis == 1 ? xp.y : xp.z);
+      wd[dst] = make_float2((float)(xa - k.min_phys[k.wall_axis]),
+                            (float)(xa - k.max_phys[k.wall_axis]));
+    }
   }
 }
 
@@ -212,11 +220,11 @@ int build_cell_list(Handle* h) {
     if (k.d == 3)
       k_cell_finalize<3><<<gw, warps_per_block * 32, 0, s>>>(
           k, h->cell_start, h->order, h->hidx, h->x, h->v, h->f, h->m, h->pid, h->sid, h->x2,
-          h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->off, h->cell_of, h->d_err);
+          h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->off, h->cell_of, h->wd, h->d_err);
     else
       k_cell_finalize<2><<<gw, warps_per_block * 32, 0, s>>>(
           k, h->cell_start, h->order, h->hidx, h->x, h->v, h->f, h->m, h->pid, h->sid, h->x2,
-          h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->off, h->cell_of, h->d_err);
+          h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->off, h->cell_of, h->wd, h->d_err);
     h->launches += 2;
     std::swap(h->x, h->x2);
     std::swap(h->v, h->v2);

@@ -110,7 +110,7 @@ void free_all(Handle* h) {
   void* ptrs[] = {h->x, h->v, h->f, h->m, h->pid, h->sid, h->hidx, h->rho, h->pr, h->st,
                   h->x2, h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->key, h->rank,
                   h->cnt, h->cell_start, h->scan_part, h->order, h->off, h->cell_of, h->nl,
-                  h->ncount, h->pc, h->pcf, h->vf, h->red, h->d_err, h->d_stats, h->d_pairs,
+                  h->ncount, h->pc, h->pcf, h->vf, h->wd, h->red, h->d_err, h->d_stats, h->d_pairs,
                   h->up_x, h->up_v, h->up_m, h->up_id};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -120,6 +120,7 @@ void free_all(Handle* h) {
   h->key = h->rank = h->cnt = h->cell_start = h->scan_part = h->order = h->cell_of = nullptr;
   h->ncount = h->d_stats = h->up_id = nullptr;
   h->off = h->pcf = h->vf = nullptr;
+  h->wd = nullptr;
   h->pc = nullptr;
   h->nl = nullptr;
   h->d_err = nullptr;
@@ -209,6 +210,12 @@ void fill_consts(Handle* h) {
   k.coeff = (float)k.coef;
   k.coef_gradf = (float)k.coef_grad;
   k.w0f = (float)k.w0;
+  k.etaf = (float)p.eta;
+  k.eta_coeff = (float)p.eta_coef;
+  k.ktf = (float)p.kt;
+  k.wall_axis = -1;
+  for (int a = 0; a < k.d; ++a)
+    if (p.bcdef[2 * a] == MCFG_BC_WALL_SOLID) k.wall_axis = (k.wall_axis == -1) ? a : -2;
   k.rhs_density_type = p.rhs_density_type;
   k.rhs_force_type = p.rhs_force_type;
   k.eos_type = p.stateEquation_type;
@@ -315,7 +322,9 @@ int ensure_capacity(Handle* h, int64_t n64) {
     if (h->p.precision == MCFG_PRECISION_FP64) {
       if ((rc = dalloc(h, &h->pc, cap))) return rc;
     } else {
-      if ((rc = dalloc(h, &h->pcf, cap)) || (rc = dalloc(h, &h->vf, cap))) return rc;
+      if ((rc = dalloc(h, &h->pcf, cap)) || (rc = dalloc(h, &h->vf, cap)) ||
+          (rc = dalloc(h, &h->wd, cap)))
+        return rc;
     }
     if (h->p.stress_tensor)
       if ((rc = dalloc(h, &h->st, cap * (size_t)(d * d)))) return rc;

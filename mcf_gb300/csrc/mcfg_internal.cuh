@@ -46,6 +46,10 @@ struct Consts {
   int kernel_type;
   double h, inv_h, coef, coef_grad, w0;
   float hf, inv_hf, coeff, coef_gradf, w0f;
+  // FP32 copies of the pair constants (the FP32 path never converts from
+  // double inside a pair loop: GB300's FP64 pipe is narrow)
+  float etaf, eta_coeff, ktf;
+  int wall_axis;         // the single solid-wall axis, -1 if none, -2 if several
   // physics
   int rhs_density_type, rhs_force_type, eos_type;
   double c2, rho_ref, gamma, p0;
@@ -111,6 +115,7 @@ struct Handle {
   double4_32a* pc = nullptr;     // FP64 path: (p/n^2 or p, 1/n^2, 1/m, rho)
   float4* pcf = nullptr;     // FP32 path: same in float
   float4* vf = nullptr;      // FP32 path: velocity (w = packed id bits)
+  float2* wd = nullptr;      // FP32 path: signed distances to the wall-axis faces
   // ---- reductions & errors ----
   double* red = nullptr;     // block partials
   unsigned* d_err = nullptr; // device error bitmask

@@ -133,26 +133,49 @@ __device__ __forceinline__ bool dyn_rho(const Consts& k, int sid) {
   return false;
 }
 
-// prologue shared by k_density (fused) and k_pressure
+// Per-particle prologue of the force sweep: pressure from the equation of
+// state and the pair coefficients (fused into k_density or run as
+// k_pressure).  The FP32 path forms them in FP32.
 template <bool FP64>
 __device__ __forceinline__ void write_particle_records(const Consts& k, int i, double rho, double m,
-                                                       int sid, int pid, const double4_32a& v,
+                                                       int pid, const double4_32a& v,
                                                        double* __restrict__ pr,
                                                        double4_32a* __restrict__ pc,
                                                        float4* __restrict__ pcf,
                                                        float4* __restrict__ vf) {
-  const double r_eos = (k.rhs_density_type == 1) ? rho : rho * m;
-  const double p = eos_pressure(k, r_eos);
-  pr[i] = p;
-  const double4_32a c = pair_coeffs(k, rho, p, m);
   if (FP64) {
-    pc[i] = c;
+    const double r_eos = (k.rhs_density_type == 1) ? rho : rho * m;
+    const double p = eos_pressure(k, r_eos);
+    pr[i] = p;
+    pc[i] = pair_coeffs(k, rho, p, m);
   } else {
-    pcf[i] = make_float4((float)c.x, (float)c.y, (float)c.z, (float)c.w);
+    const float rf = (float)rho, mf = (float)m;
+    const float r_eos = (k.rhs_density_type == 1) ? rf : rf * mf;
+    float p;
+    if (k.eos_type == 1) {
+      const float rg = (k.gamma == 1.0) ? r_eos : powf(r_eos, (float)k.gamma);
+      p = (float)k.c2 * (rg - (float)k.rho_ref);
+    } else {
+      const float q = r_eos / (float)k.rho_ref;
+      const float qg = (k.gamma == 1.0) ? q : powf(q, (float)k.gamma);
+      p = (float)k.p0 * (qg - 1.0f);
+    }
+    pr[i] = (double)p;
+    const float inv = 1.0f / rf;
+    float4 cc;
+    switch (k.rhs_force_type) {
+      case 1: cc = make_float4(p * inv * inv, inv, mf, p); break;
+      case 2: cc = make_float4(p * inv * inv, inv, 1.0f / mf, p); break;
+      case 3: cc = make_float4(p * inv * inv, inv * inv, 1.0f / mf, p); break;
+      default: cc = make_float4(p, inv * inv, 1.0f / mf, p); break;
+    }
+    pcf[i] = cc;
     vf[i] = make_float4((float)v.x, (float)v.y, (float)v.z, __int_as_float(pid));
   }
-  (void)sid;
 }
+
+constexpr int kStage = 64;      // neighbour-cell offsets staged per pass
+constexpr int kListStage = 96;  // neighbour entries staged in shared memory per lane
 
 template <int D, bool FP64>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
@@ -167,6 +190,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   constexpr int NS = (D == 3) ? 27 : 9;
   constexpr int CENTER = (D == 3) ? 13 : 4;
   __shared__ NbTable tab[kWarpsPerBlock];
+  __shared__ float4 sb[kWarpsPerBlock][kStage];
+  __shared__ uint16_t ls[kWarpsPerBlock][kListStage][32];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = k.n;
   int my_max = 0;
@@ -182,43 +207,56 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       const float4 oi = active ? off[i] : make_float4(0.f, 0.f, 0.f, 0.f);
       const float rlim = FP64 ? k.rc2f_hi : k.rc2f;
       int cnt = 0;
+      // phase 1: candidate scan, offsets of each neighbour cell staged in
+      // shared memory by coalesced loads, then broadcast to the lanes
       for (int sl = 0; sl < NS; ++sl) {
         const int js = t.start[sl], jn = t.count[sl];
         const float ox = (float)(sl % 3 - 1) * k.csf[0];
         const float oy = (float)((sl / 3) % 3 - 1) * k.csf[1];
         const float oz = (D == 3) ? (float)(sl / 9 - 1) * k.csf[2] : 0.0f;
-        for (int q = 0; q < jn; ++q) {
-          const float4 oj = off[js + q];
-          const float rx = (oi.x - oj.x) - ox;
-          const float ry = (oi.y - oj.y) - oy;
-          float d2 = rx * rx + ry * ry;
-          if (D == 3) {
-            const float rz = (oi.z - oj.z) - oz;
-            d2 += rz * rz;
-          }
-          if (active && d2 < rlim && !(sl == CENTER && js + q == i)) {
-            if (cnt < cap) nl[(size_t)cnt * n + i] = (uint16_t)((sl << kLocalBits) | q);
-            ++cnt;
+        const float px = oi.x - ox, py = oi.y - oy, pz = oi.z - oz;
+        for (int b2 = 0; b2 < jn; b2 += kStage) {
+          const int mm = min(kStage, jn - b2);
+          __syncwarp();
+          for (int q = lane; q < mm; q += 32) sb[wib][q] = off[js + b2 + q];
+          __syncwarp();
+#pragma unroll 4
+          for (int q2 = 0; q2 < mm; ++q2) {
+            const float4 oj = sb[wib][q2];
+            const float rx = px - oj.x, ry = py - oj.y;
+            float d2 = rx * rx + ry * ry;
+            if (D == 3) {
+              const float rz = pz - oj.z;
+              d2 += rz * rz;
+            }
+            const int q = b2 + q2;
+            if (active && d2 < rlim && !(sl == CENTER && js + q == i)) {
+              const uint16_t ent = (uint16_t)((sl << kLocalBits) | q);
+              if (cnt < kListStage)
+                ls[wib][cnt][lane] = ent;
+              else if (cnt < cap)
+                nl[(size_t)cnt * n + i] = ent;
+              ++cnt;
+            }
           }
         }
       }
-      if (!active) continue;
-      if (cnt > cap) {
+      if (active && cnt > cap) {
         atomicOr(err, kErrNeighOverflow);
         my_max = max(my_max, cnt);
-        cnt = cap;
       }
-      // phase 2: exact test (FP64) and the density sum
-      const int si = sid[i];
+      cnt = min(cnt, cap);
+      // phase 2: exact test (FP64 path), density sum, final list rows
+      const int si = active ? sid[i] : 0;
       const bool acc_i = dyn_rho(k, si);
-      double rho_i;
+      double rho_i = 0.0;
       int kept = 0;
       if (FP64) {
-        const double4_32a xi4 = x[i];
+        double4_32a xi4 = active ? x[i] : make_double4_32a(0, 0, 0, 0);
         const double xi[3] = {xi4.x, xi4.y, xi4.z};
         double sum = 0.0;
         for (int e = 0; e < cnt; ++e) {
-          const int ent = nl[(size_t)e * n + i];
+          const int ent = (e < kListStage) ? ls[wib][e][lane] : nl[(size_t)e * n + i];
           const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
           const int j = t.start[sl] + q;
           const double4_32a xj4 = x[j];
@@ -237,30 +275,32 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       } else {
         // Kahan-compensated FP32 sum of W
         float sum = 0.0f, comp = 0.0f;
+        const bool mass = k.rhs_density_type == 1;
         for (int e = 0; e < cnt; ++e) {
-          const int ent = nl[(size_t)e * n + i];
+          const int ent = (e < kListStage) ? ls[wib][e][lane] : nl[(size_t)e * n + i];
+          if (e < kListStage) nl[(size_t)e * n + i] = (uint16_t)ent;
+          if (!acc_i) continue;
           const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
           const int j = t.start[sl] + q;
-          if (acc_i) {
-            const float4 oj = off[j];
-            const float rx = (oi.x - oj.x) - (float)(sl % 3 - 1) * k.csf[0];
-            const float ry = (oi.y - oj.y) - (float)((sl / 3) % 3 - 1) * k.csf[1];
-            float d2 = rx * rx + ry * ry;
-            if (D == 3) {
-              const float rz = (oi.z - oj.z) - (float)(sl / 9 - 1) * k.csf[2];
-              d2 += rz * rz;
-            }
-            float w = kernel_w<float>(k, sqrtf(d2));
-            if (k.rhs_density_type == 1) w *= (float)m[j];
-            const float y = w - comp;
-            const float tt = sum + y;
-            comp = (tt - sum) - y;
-            sum = tt;
+          const float4 oj = off[j];
+          const float rx = (oi.x - oj.x) - (float)(sl % 3 - 1) * k.csf[0];
+          const float ry = (oi.y - oj.y) - (float)((sl / 3) % 3 - 1) * k.csf[1];
+          float d2 = rx * rx + ry * ry;
+          if (D == 3) {
+            const float rz = (oi.z - oj.z) - (float)(sl / 9 - 1) * k.csf[2];
+            d2 += rz * rz;
           }
+          float w = kernel_w<float>(k, sqrtf(d2));
+          if (mass) w *= (float)m[j];
+          const float y = w - comp;
+          const float tt = sum + y;
+          comp = (tt - sum) - y;
+          sum = tt;
         }
         kept = cnt;
         rho_i = (double)sum;
       }
+      if (!active) continue;
       ncount[i] = kept;
       my_max = max(my_max, kept);
       my_pairs += (unsigned long long)kept;
@@ -274,10 +314,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       rho[i] = rho_out;
       if (!(rho_out > 0.0)) atomicOr(err, kErrZeroDensity);
       if (with_pressure)
-        write_particle_records<FP64>(k, i, rho_out, mi, si, pid[i], v[i], pr, pc, pcf, vf);
+        write_particle_records<FP64>(k, i, rho_out, mi, pid[i], v[i], pr, pc, pcf, vf);
     }
   }
-  // warp reductions of the counters
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     my_max = max(my_max, __shfl_xor_sync(0xffffffffu, my_max, o));
@@ -291,35 +330,80 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 
 template <bool FP64>
 __global__ void k_pressure(Consts k, const double* __restrict__ rho, const double* __restrict__ m,
-                           const int* __restrict__ sid, const int* __restrict__ pid,
-                           const double4_32a* __restrict__ v, double* __restrict__ pr,
-                           double4_32a* __restrict__ pc, float4* __restrict__ pcf,
-                           float4* __restrict__ vf) {
+                           const int* __restrict__ pid, const double4_32a* __restrict__ v,
+                           double* __restrict__ pr, double4_32a* __restrict__ pc,
+                           float4* __restrict__ pcf, float4* __restrict__ vf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= k.n) return;
-  write_particle_records<FP64>(k, i, rho[i], m[i], sid[i], pid[i], v[i], pr, pc, pcf, vf);
+  write_particle_records<FP64>(k, i, rho[i], m[i], pid[i], v[i], pr, pc, pcf, vf);
 }
 
 // ---------------------------------------------------------------------------
-// Force sweep
+// Epilogue shared by both force sweeps: body force, store, second half kick.
 // ---------------------------------------------------------------------------
-template <int D, bool FP64>
+template <int D>
+__device__ __forceinline__ void force_epilogue(const Consts& k, int i, int si, const double* xi,
+                                               double ax, double ay, double az,
+                                               int fuse_mode, double dt,
+                                               const double4_32a* __restrict__ v,
+                                               double4_32a* __restrict__ f,
+                                               double4_32a* __restrict__ v_out,
+                                               unsigned* __restrict__ err) {
+  if (!isfinite(ax) || !isfinite(ay) || !isfinite(az)) atomicOr(err, kErrNonFinite);
+  if (fuse_mode >= kForceBody && si == 0) {
+    // particles_apply_body_force.F90:96-353
+    const double g[3] = {k.body_force[0], k.body_force[1], k.body_force[2]};
+    if (k.body_force_type == 1) {
+      if (fabs(g[0]) > k.machine_zero) ax += g[0];
+      if (fabs(g[1]) > k.machine_zero) ay += g[1];
+      if (D == 3 && fabs(g[2]) > k.machine_zero) az += g[2];
+    } else if (k.body_force_type == 2) {
+      if (fabs(g[0]) > k.machine_zero) {
+        const double half = k.max_phys[D - 1] * 0.5;
+        const double xl = xi[D - 1];
+        if (xl < half)
+          ax += g[0];
+        else if (xl > half)
+          ax -= g[0];
+      }
+    } else if (k.body_force_type == 3) {
+      if (fabs(g[0]) > k.machine_zero) {
+        const double kw = 2.0 * kPi / (k.max_phys[1] - k.min_phys[1]);
+        ax += g[0] * sin(kw * xi[1]);
+      }
+    }
+  }
+  f[i] = make_double4_32a(ax, ay, az, 0.0);
+  if (fuse_mode == kForceBodyKick) {
+    // second half kick, particles_integrate_velocity.F90:84-94
+    double4_32a vv = v[i];
+    if (si == 0) {
+      vv.x = vv.x + 0.5 * ax * dt;
+      vv.y = vv.y + 0.5 * ay * dt;
+      if (D == 3) vv.z = vv.z + 0.5 * az * dt;
+    }
+    v_out[i] = vv;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 force sweep
+// ---------------------------------------------------------------------------
+template <int D>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
-    k_force(Consts k, const int* __restrict__ cell_start, const uint16_t* __restrict__ nl,
-            const int* __restrict__ ncount, const float4* __restrict__ off,
-            const double4_32a* __restrict__ x, const double4_32a* __restrict__ v,
-            const double4_32a* __restrict__ pc, const float4* __restrict__ pcf,
-            const float4* __restrict__ vf, const int* __restrict__ sid,
-            const int* __restrict__ pid, double4_32a* __restrict__ f, double* __restrict__ st,
-            int fuse_mode, double dt, double4_32a* __restrict__ v_out, uint32_t step,
-            double inv_sqdt, unsigned* __restrict__ err) {
+    k_force64(Consts k, const int* __restrict__ cell_start, const uint16_t* __restrict__ nl,
+              const int* __restrict__ ncount, const double4_32a* __restrict__ x,
+              const double4_32a* __restrict__ v, const double4_32a* __restrict__ pc,
+              const int* __restrict__ sid, const int* __restrict__ pid,
+              double4_32a* __restrict__ f, double* __restrict__ st, int fuse_mode, double dt,
+              double4_32a* __restrict__ v_out, uint32_t step, double inv_sqdt,
+              unsigned* __restrict__ err) {
   constexpr int CENTER = (D == 3) ? 13 : 4;
-  using T = typename std::conditional<FP64, double, float>::type;
+  using T = double;
   __shared__ NbTable tab[kWarpsPerBlock];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = k.n;
   const bool noise = k.noise != 0;
-  const T isq = (T)inv_sqdt;
   for (int cell = blockIdx.x * kWarpsPerBlock + wib; cell <= k.ncell;
        cell += gridDim.x * kWarpsPerBlock) {
     NbTable& t = tab[wib];
@@ -330,91 +414,50 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       if (i >= c1) continue;
       const int si = sid[i];
       const int pidi = pid[i];
-      T ri[3], vi[3];
-      T Ai, Bi, Ci, Pi;
       const double4_32a xi4 = x[i];
       const double xi[3] = {xi4.x, xi4.y, xi4.z};
-      if (FP64) {
-        const double4_32a v4 = v[i];
-        vi[0] = (T)v4.x; vi[1] = (T)v4.y; vi[2] = (T)v4.z;
-        const double4_32a c = pc[i];
-        Ai = (T)c.x; Bi = (T)c.y; Ci = (T)c.z; Pi = (T)c.w;
-      } else {
-        const float4 o = off[i];
-        ri[0] = (T)o.x; ri[1] = (T)o.y; ri[2] = (T)o.z;
-        const float4 v4 = vf[i];
-        vi[0] = (T)v4.x; vi[1] = (T)v4.y; vi[2] = (T)v4.z;
-        const float4 c = pcf[i];
-        Ai = (T)c.x; Bi = (T)c.y; Ci = (T)c.z; Pi = (T)c.w;
-      }
-      T acc[3] = {T(0), T(0), T(0)};
-      T comp[3] = {T(0), T(0), T(0)};  // Kahan terms (FP32 path)
+      const double4_32a v4i = v[i];
+      const double4_32a ci = pc[i];
+      T acc[3] = {0, 0, 0};
       T sacc[9];
 #pragma unroll
-      for (int a = 0; a < 9; ++a) sacc[a] = T(0);
+      for (int a = 0; a < 9; ++a) sacc[a] = 0;
       const int cnt = ncount[i];
       for (int e = 0; e < cnt; ++e) {
         const int ent = nl[(size_t)e * n + i];
         const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
         const int j = t.start[sl] + q;
-        T r[3], vj[3];
-        T Aj, Bj, Cj, Pj;
-        T d;
-        int sj, pidj = 0;
-        if (FP64) {
-          sj = sid[j];
-          if (si != 0 && sj != 0) continue;  // w-w, c-c, c-w: no interaction here
-          const double4_32a xj4 = x[j];
-          const double xj[3] = {xj4.x, xj4.y, xj4.z};
-          double rr[3];
-          const double d2 = exact_sep<D>(k, xi, xj, t.shift[sl], rr);
-#pragma unroll
-          for (int a = 0; a < D; ++a) r[a] = (T)rr[a];
-          d = (T)sqrt(d2);
-          const double4_32a v4 = v[j];
-          vj[0] = (T)v4.x; vj[1] = (T)v4.y; vj[2] = (T)v4.z;
-          const double4_32a c = pc[j];
-          Aj = (T)c.x; Bj = (T)c.y; Cj = (T)c.z; Pj = (T)c.w;
-          if (noise) pidj = pid[j];
-        } else {
-          const float4 oj = off[j];
-          sj = __float_as_int(oj.w);
-          if (si != 0 && sj != 0) continue;
-          r[0] = (ri[0] - (T)oj.x) - (T)(sl % 3 - 1) * (T)k.csf[0];
-          r[1] = (ri[1] - (T)oj.y) - (T)((sl / 3) % 3 - 1) * (T)k.csf[1];
-          r[2] = (D == 3) ? (ri[2] - (T)oj.z) - (T)(sl / 9 - 1) * (T)k.csf[2] : T(0);
-          T d2 = r[0] * r[0] + r[1] * r[1];
-          if (D == 3) d2 += r[2] * r[2];
-          d = my_sqrt<T>(d2);
-          const float4 v4 = vf[j];
-          vj[0] = (T)v4.x; vj[1] = (T)v4.y; vj[2] = (T)v4.z;
-          pidj = __float_as_int(v4.w);
-          const float4 c = pcf[j];
-          Aj = (T)c.x; Bj = (T)c.y; Cj = (T)c.z; Pj = (T)c.w;
-        }
-        T vi_save[3] = {vi[0], vi[1], vi[2]};
-        T Ai_save = Ai;
+        const int sj = sid[j];
+        if (si != 0 && sj != 0) continue;  // w-w, c-c, c-w: no interaction here
+        const double4_32a xj4 = x[j];
+        const double xj[3] = {xj4.x, xj4.y, xj4.z};
+        T r[3];
+        const double d2 = exact_sep<D>(k, xi, xj, t.shift[sl], r);
+        const T inv_d = rsqrt(d2);
+        const T d = d2 * inv_d;
+        const double4_32a v4 = v[j];
+        T vi[3] = {v4i.x, v4i.y, v4i.z};
+        T vj[3] = {v4.x, v4.y, v4.z};
+        const double4_32a cj = pc[j];
+        T Ai = ci.x, Aj = cj.x;
         if (si < 0 || sj < 0) {
-          // fluid-wall pair: the wall particle takes the Morris no-slip
-          // velocity and the fluid particle's pressure
-          // (pp_interaction_fw.inc, pp_interaction_wf.inc)
+          // fluid-wall pair: wall particle takes the Morris no-slip velocity
+          // and the fluid pressure (pp_interaction_fw.inc / _wf.inc)
           const int sw = (sj < 0) ? sj : si;
           const int axis = (-sw - 1) >> 1;
-          const double4_32a xj4 = x[j];
-          const double xjn = axis == 0 ? xj4.x : axis == 1 ? xj4.y : xj4.z;
           const double xin = axis == 0 ? xi[0] : axis == 1 ? xi[1] : xi[2];
+          const double xjn = axis == 0 ? xj[0] : axis == 1 ? xj[1] : xj[2];
           T vw[3];
-          int ax_unused;
           if (sj < 0) {
-            wall_noslip<T, D>(k, xin, xjn, vi, sj, vw, ax_unused);
+            wall_noslip<T, D>(k, xin, xjn, vi, sj, vw);
 #pragma unroll
             for (int a = 0; a < D; ++a) vj[a] = vw[a];
-            Aj = boundary_A<T>(k.rhs_force_type, Pi, Bj);
+            Aj = boundary_A<T>(k.rhs_force_type, ci.w, cj.y);
           } else {
-            wall_noslip<T, D>(k, xjn, xin, vj, si, vw, ax_unused);
+            wall_noslip<T, D>(k, xjn, xin, vj, si, vw);
 #pragma unroll
             for (int a = 0; a < D; ++a) vi[a] = vw[a];
-            Ai = boundary_A<T>(k.rhs_force_type, Pj, Bi);
+            Ai = boundary_A<T>(k.rhs_force_type, cj.w, ci.y);
           }
         }
         const T gw = kernel_gradw<T>(k, d);
@@ -422,22 +465,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 #pragma unroll
         for (int a = 0; a < D; ++a) vij[a] = vi[a] - vj[a];
         float z[6];
-        if (noise) pair_normals<D>(k.key0, k.key1, step, pidi, pidj, z);
+        if (noise) pair_normals<D>(k.key0, k.key1, step, pidi, pid[j], z);
         T pa[3];
-        pair_accel<T, D>(k, r, d, vij, Ai, Bi, Ci, Aj, Bj, Cj, gw, noise, z, isq, pa);
-        vi[0] = vi_save[0]; vi[1] = vi_save[1]; vi[2] = vi_save[2];
-        Ai = Ai_save;
+        pair_accel<T, D>(k, r, inv_d, vij, Ai, ci.y, ci.z, Aj, cj.y, cj.z, gw, noise, z, inv_sqdt,
+                         pa);
 #pragma unroll
-        for (int a = 0; a < D; ++a) {
-          if (FP64) {
-            acc[a] += pa[a];
-          } else {
-            const T y = pa[a] - comp[a];
-            const T tt = acc[a] + y;
-            comp[a] = (tt - acc[a]) - y;
-            acc[a] = tt;
-          }
-        }
+        for (int a = 0; a < D; ++a) acc[a] += pa[a];
         if (k.stress) {
           // pp_interaction_ff.inc:83-93: s_ab += r_a * f_b / 2
 #pragma unroll
@@ -446,46 +479,167 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
             for (int a = 0; a < D; ++a) sacc[b * D + a] += r[a] * pa[b] * T(0.5);
         }
       }
-      double ax = (double)acc[0], ay = (double)acc[1], az = (D == 3) ? (double)acc[2] : 0.0;
-      if (!isfinite(ax) || !isfinite(ay) || !isfinite(az)) atomicOr(err, kErrNonFinite);
-      if (fuse_mode >= kForceBody && si == 0) {
-        // particles_apply_body_force.F90:96-353
-        const double* g = k.body_force;
-        if (k.body_force_type == 1) {
-          if (fabs(g[0]) > k.machine_zero) ax += g[0];
-          if (fabs(g[1]) > k.machine_zero) ay += g[1];
-          if (D == 3 && fabs(g[2]) > k.machine_zero) az += g[2];
-        } else if (k.body_force_type == 2) {
-          if (fabs(g[0]) > k.machine_zero) {
-            const double half = k.max_phys[D - 1] * 0.5;
-            const double xl = xi[D - 1];
-            if (xl < half)
-              ax += g[0];
-            else if (xl > half)
-              ax -= g[0];
+      if (k.stress) {
+#pragma unroll
+        for (int a = 0; a < D * D; ++a) st[(size_t)a * n + i] = sacc[a];
+      }
+      force_epilogue<D>(k, i, si, xi, acc[0], acc[1], D == 3 ? acc[2] : 0.0, fuse_mode, dt, v,
+                        f, v_out, err);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP32-mixed force sweep: pair arithmetic in FP32 on cell offsets, Kahan
+// sums, the next pair's data loaded while the current one is computed.
+// ---------------------------------------------------------------------------
+struct JData {
+  float4 o, v, c;
+  int sl, j;
+};
+
+template <int D>
+__device__ __forceinline__ JData load_j(const NbTable& t, int ent, const float4* __restrict__ off,
+                                        const float4* __restrict__ vf,
+                                        const float4* __restrict__ pcf) {
+  JData d;
+  d.sl = ent >> kLocalBits;
+  d.j = t.start[d.sl] + (ent & (kMaxCellCount - 1));
+  d.o = off[d.j];
+  d.v = vf[d.j];
+  d.c = pcf[d.j];
+  return d;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
+    k_force32(Consts k, const int* __restrict__ cell_start, const uint16_t* __restrict__ nl,
+              const int* __restrict__ ncount, const float4* __restrict__ off,
+              const double4_32a* __restrict__ x, const double4_32a* __restrict__ v,
+              const float4* __restrict__ pcf, const float4* __restrict__ vf,
+              const float2* __restrict__ wd, double4_32a* __restrict__ f,
+              double* __restrict__ st, int fuse_mode, double dt,
+              double4_32a* __restrict__ v_out, uint32_t step, float inv_sqdt,
+              unsigned* __restrict__ err) {
+  constexpr int CENTER = (D == 3) ? 13 : 4;
+  using T = float;
+  __shared__ NbTable tab[kWarpsPerBlock];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = k.n;
+  const bool noise = k.noise != 0;
+  const bool walls = k.wall_axis != -1;
+  for (int cell = blockIdx.x * kWarpsPerBlock + wib; cell <= k.ncell;
+       cell += gridDim.x * kWarpsPerBlock) {
+    NbTable& t = tab[wib];
+    build_table<D>(k, cell, cell_start, t);
+    const int c0 = t.start[CENTER], c1 = c0 + t.count[CENTER];
+    for (int base = c0; base < c1; base += 32) {
+      const int i = base + lane;
+      if (i >= c1) continue;
+      const float4 oi = off[i];
+      const int si = __float_as_int(oi.w);
+      const float4 v4i = vf[i];
+      const int pidi = __float_as_int(v4i.w);
+      const float4 ci = pcf[i];
+      const float2 wdi = (walls && k.wall_axis >= 0) ? wd[i] : make_float2(0.f, 0.f);
+      T acc[3] = {0.f, 0.f, 0.f}, comp[3] = {0.f, 0.f, 0.f};
+      T sacc[9];
+#pragma unroll
+      for (int a = 0; a < 9; ++a) sacc[a] = 0.f;
+      const int cnt = ncount[i];
+      JData nxt;
+      int ent_n1 = 0;
+      if (cnt > 0) nxt = load_j<D>(t, nl[i], off, vf, pcf);
+      if (cnt > 1) ent_n1 = nl[(size_t)n + i];
+      for (int e = 0; e < cnt; ++e) {
+        const JData cur = nxt;
+        if (e + 1 < cnt) {
+          nxt = load_j<D>(t, ent_n1, off, vf, pcf);
+          if (e + 2 < cnt) ent_n1 = nl[(size_t)(e + 2) * n + i];
+        }
+        const int sj = __float_as_int(cur.o.w);
+        if (si != 0 && sj != 0) continue;
+        const int sl = cur.sl;
+        T r[3];
+        r[0] = (oi.x - cur.o.x) - (float)(sl % 3 - 1) * k.csf[0];
+        r[1] = (oi.y - cur.o.y) - (float)((sl / 3) % 3 - 1) * k.csf[1];
+        r[2] = (D == 3) ? (oi.z - cur.o.z) - (float)(sl / 9 - 1) * k.csf[2] : 0.f;
+        T d2 = r[0] * r[0] + r[1] * r[1];
+        if (D == 3) d2 += r[2] * r[2];
+        const T inv_d = rsqrtf(d2);
+        const T d = d2 * inv_d;
+        T vi[3] = {v4i.x, v4i.y, v4i.z};
+        T vj[3] = {cur.v.x, cur.v.y, cur.v.z};
+        T Ai = ci.x, Aj = cur.c.x;
+        if (si < 0 || sj < 0) {
+          // fluid-wall pair: the wall particle takes the Morris no-slip
+          // velocity and the fluid pressure (pp_interaction_fw.inc / _wf.inc);
+          // face distances come from the FP64-rounded per-particle values
+          // (one wall axis) or from the FP64 positions (several)
+          const int sw = (sj < 0) ? sj : si;
+          const int face = -sw;
+          const bool lower = (face & 1) != 0;
+          float df, dw;
+          if (k.wall_axis >= 0) {
+            const float2 wj = wd[cur.j];
+            const float di = lower ? wdi.x : wdi.y, dj = lower ? wj.x : wj.y;
+            df = (sj < 0) ? di : dj;
+            dw = (sj < 0) ? dj : di;
+          } else {
+            const int axis = (face - 1) >> 1;
+            const double x_sur = axis == 0 ? (lower ? k.min_phys[0] : k.max_phys[0])
+                                 : axis == 1 ? (lower ? k.min_phys[1] : k.max_phys[1])
+                                             : (lower ? k.min_phys[2] : k.max_phys[2]);
+            const double4_32a a4 = x[i], b4 = x[cur.j];
+            const double xa = axis == 0 ? a4.x : axis == 1 ? a4.y : a4.z;
+            const double xb = axis == 0 ? b4.x : axis == 1 ? b4.y : b4.z;
+            df = (float)(((sj < 0) ? xa : xb) - x_sur);
+            dw = (float)(((sj < 0) ? xb : xa) - x_sur);
           }
-        } else if (k.body_force_type == 3) {
-          if (fabs(g[0]) > k.machine_zero) {
-            const double kw = 2.0 * kPi / (k.max_phys[1] - k.min_phys[1]);
-            ax += g[0] * sin(kw * xi[1]);
+          T vw[3];
+          if (sj < 0) {
+            wall_noslip_dist<T, D>(k, df, dw, vi, sj, vw);
+#pragma unroll
+            for (int a = 0; a < D; ++a) vj[a] = vw[a];
+            Aj = boundary_A<T>(k.rhs_force_type, ci.w, cur.c.y);
+          } else {
+            wall_noslip_dist<T, D>(k, df, dw, vj, si, vw);
+#pragma unroll
+            for (int a = 0; a < D; ++a) vi[a] = vw[a];
+            Ai = boundary_A<T>(k.rhs_force_type, cur.c.w, ci.y);
           }
         }
+        const T gw = kernel_gradw<T>(k, d);
+        T vij[3];
+#pragma unroll
+        for (int a = 0; a < D; ++a) vij[a] = vi[a] - vj[a];
+        float z[6];
+        if (noise) pair_normals<D>(k.key0, k.key1, step, pidi, __float_as_int(cur.v.w), z);
+        T pa[3];
+        pair_accel<T, D>(k, r, inv_d, vij, Ai, ci.y, ci.z, Aj, cur.c.y, cur.c.z, gw, noise, z,
+                         inv_sqdt, pa);
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          const T y = pa[a] - comp[a];
+          const T tt = acc[a] + y;
+          comp[a] = (tt - acc[a]) - y;
+          acc[a] = tt;
+        }
+        if (k.stress) {
+#pragma unroll
+          for (int b = 0; b < D; ++b)
+#pragma unroll
+            for (int a = 0; a < D; ++a) sacc[b * D + a] += r[a] * pa[b] * 0.5f;
+        }
       }
-      f[i] = make_double4_32a(ax, ay, az, 0.0);
       if (k.stress) {
 #pragma unroll
         for (int a = 0; a < D * D; ++a) st[(size_t)a * n + i] = (double)sacc[a];
       }
-      if (fuse_mode == kForceBodyKick) {
-        // second half kick, particles_integrate_velocity.F90:84-94
-        double4_32a vv = v[i];
-        if (si == 0) {
-          vv.x = vv.x + 0.5 * ax * dt;
-          vv.y = vv.y + 0.5 * ay * dt;
-          if (D == 3) vv.z = vv.z + 0.5 * az * dt;
-        }
-        v_out[i] = vv;
-      }
+      const double4_32a xi4 = x[i];
+      const double xi[3] = {xi4.x, xi4.y, xi4.z};
+      force_epilogue<D>(k, i, si, xi, (double)acc[0], (double)acc[1],
+                        D == 3 ? (double)acc[2] : 0.0, fuse_mode, dt, v, f, v_out, err);
     }
   }
 }
@@ -526,11 +680,11 @@ int compute_pressure(Handle* h) {
   if (n == 0) return MCFG_OK;
   const int tb = 256, gb = (n + tb - 1) / tb;
   if (h->p.precision == MCFG_PRECISION_FP64)
-    k_pressure<true><<<gb, tb, 0, h->stream>>>(h->k, h->rho, h->m, h->sid, h->pid, h->v, h->pr,
-                                               h->pc, h->pcf, h->vf);
+    k_pressure<true><<<gb, tb, 0, h->stream>>>(h->k, h->rho, h->m, h->pid, h->v, h->pr, h->pc,
+                                               h->pcf, h->vf);
   else
-    k_pressure<false><<<gb, tb, 0, h->stream>>>(h->k, h->rho, h->m, h->sid, h->pid, h->v, h->pr,
-                                                h->pc, h->pcf, h->vf);
+    k_pressure<false><<<gb, tb, 0, h->stream>>>(h->k, h->rho, h->m, h->pid, h->v, h->pr, h->pc,
+                                                h->pcf, h->vf);
   h->launches++;
   if (cuda_check(h, cudaGetLastError(), "pressure launch")) return MCFG_ECUDA;
   return MCFG_OK;
@@ -541,18 +695,28 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
   cudaStream_t s = h->stream;
   const int g = grid_for(h);
   const bool fp64 = h->p.precision == MCFG_PRECISION_FP64;
-  const double inv_sqdt = (k.noise && dt > 0.0) ? 1.0 / sqrt(dt) : 0.0;
   if (k.noise && !(dt > 0.0)) return set_error(h, MCFG_EINVAL, "random force needs dt > 0");
-#define LAUNCH_F(DD, PP)                                                                       \
-  k_force<DD, PP><<<g, kWarpsPerBlock * 32, 0, s>>>(                                            \
-      k, h->cell_start, h->nl, h->ncount, h->off, h->x, h->v, h->pc, h->pcf, h->vf, h->sid,     \
-      h->pid, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step, inv_sqdt, h->d_err)
-  if (k.d == 3) {
-    if (fp64) LAUNCH_F(3, true); else LAUNCH_F(3, false);
+  const double inv_sqdt = (k.noise && dt > 0.0) ? 1.0 / sqrt(dt) : 0.0;
+  const int bs = kWarpsPerBlock * 32;
+  if (fp64) {
+    if (k.d == 3)
+      k_force64<3><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->x, h->v, h->pc, h->sid,
+                                    h->pid, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step,
+                                    inv_sqdt, h->d_err);
+    else
+      k_force64<2><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->x, h->v, h->pc, h->sid,
+                                    h->pid, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step,
+                                    inv_sqdt, h->d_err);
   } else {
-    if (fp64) LAUNCH_F(2, true); else LAUNCH_F(2, false);
+    if (k.d == 3)
+      k_force32<3><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->off, h->x, h->v,
+                                    h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2,
+                                    (uint32_t)step, (float)inv_sqdt, h->d_err);
+    else
+      k_force32<2><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->off, h->x, h->v,
+                                    h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2,
+                                    (uint32_t)step, (float)inv_sqdt, h->d_err);
   }
-#undef LAUNCH_F
   h->launches++;
   if (cuda_check(h, cudaGetLastError(), "force launch")) return MCFG_ECUDA;
   if (fuse_mode == kForceBodyKick) std::swap(h->v, h->v2);

@@ -6,18 +6,24 @@
 namespace mcfg {
 
 template <typename T>
-struct KC;  // kernel constants in T
+struct KC;  // kernel and pair constants in T
 template <>
 struct KC<double> {
   __device__ static double inv_h(const Consts& k) { return k.inv_h; }
   __device__ static double coef(const Consts& k) { return k.coef; }
   __device__ static double coef_grad(const Consts& k) { return k.coef_grad; }
+  __device__ static double eta(const Consts& k) { return k.eta; }
+  __device__ static double kt(const Consts& k) { return k.kt; }
+  __device__ static double eta_coef(const Consts& k) { return k.eta_coef; }
 };
 template <>
 struct KC<float> {
   __device__ static float inv_h(const Consts& k) { return k.inv_hf; }
   __device__ static float coef(const Consts& k) { return k.coeff; }
   __device__ static float coef_grad(const Consts& k) { return k.coef_gradf; }
+  __device__ static float eta(const Consts& k) { return k.etaf; }
+  __device__ static float kt(const Consts& k) { return k.ktf; }
+  __device__ static float eta_coef(const Consts& k) { return k.eta_coeff; }
 };
 
 // W(r): kernel_kernel_quintic_spline.F90:69-99 (h = rc/3, W = coef*[(3-s)^5
@@ -138,17 +144,18 @@ __device__ __forceinline__ float my_sqrt<float>(float a) { return sqrtf(a); }
 
 // Acceleration of particle i from partner j (i side of the symmetric pair
 // forces of rhs_force_ff_Newtonian_{Morris,Espanol,HuAdams,HuAdams_angular}
-// .F90).  r = x_i - x_j (image), d = |r|, vij = v_i - v_j.  Returns the pair
-// acceleration in acc[].
+// .F90).  r = x_i - x_j (image), inv_d = 1/|r|, vij = v_i - v_j.  Returns
+// the pair acceleration in acc[].
 template <typename T, int D>
-__device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T d, const T* vij,
+__device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T inv_d, const T* vij,
                                            T Ai, T Bi, T Ci, T Aj, T Bj, T Cj, T gw,
                                            bool noise, const float* z, T inv_sqdt, T* acc) {
-  const T inv_d = T(1) / d;
   T e[3];
 #pragma unroll
   for (int a = 0; a < D; ++a) e[a] = r[a] * inv_d;
-  const T eta = (T)k.eta;
+  const T eta = KC<T>::eta(k);
+  const T kt = KC<T>::kt(k);
+  const T eta_coef = KC<T>::eta_coef(k);
   switch (k.rhs_force_type) {
     case 1: {
       const T f_c = (Ai + Aj) * gw;
@@ -186,7 +193,7 @@ __device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T d, con
         }
 #pragma unroll
         for (int a = 0; a < D; ++a) dW[a][a] -= tr;
-        const T Zij = T(4) * (T)k.kt * gw * inv_d * Bi * Bj;
+        const T Zij = T(4) * kt * gw * inv_d * Bi * Bj;
         const T aa = T(5) * eta / T(3);
         const T bq = (T(D) + T(2)) * eta / T(3);
         const T Aij = my_sqrt<T>(-Zij * aa);
@@ -225,7 +232,7 @@ __device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T d, con
         }
 #pragma unroll
         for (int a = 0; a < D; ++a) dW[a][a] -= tr;
-        const T f_r = my_sqrt<T>(T(-4) * (T)k.kt * f_d) * inv_sqdt;
+        const T f_r = my_sqrt<T>(T(-4) * kt * f_d) * inv_sqdt;
 #pragma unroll
         for (int a = 0; a < D; ++a) {
           T We = T(0);
@@ -243,11 +250,11 @@ __device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T d, con
       const T pij = (Ai + Aj) * T(0.5);
       const T Aij = (Bi + Bj) * gw;
       const T f_c = Aij * pij;
-      const T f_d = (T)k.eta_coef * eta * Aij * ev * inv_d;
+      const T f_d = eta_coef * eta * Aij * ev * inv_d;
       T fe = f_d - f_c;
       if (noise) {
         const T eps = (T)z[0];
-        fe += eps * my_sqrt<T>(T(2) * (T)k.kt * eta) * my_sqrt<T>(-(T)k.eta_coef * Aij * inv_d) *
+        fe += eps * my_sqrt<T>(T(2) * kt * eta) * my_sqrt<T>(-eta_coef * Aij * inv_d) *
               inv_sqdt;
       }
 #pragma unroll
@@ -258,32 +265,45 @@ __device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T d, con
 }
 
 // Morris no-slip velocity of a solid-wall particle,
-// boundary_noslip_solid.F90:40-95 (frozen) and :137-240 (Morris): wall
-// particles carry sid = -face (1..2d); x_f, x_w are the coordinates along the
-// wall-normal axis.
+// boundary_noslip_solid.F90:40-95 (frozen) and :137-240 (Morris).  Wall
+// particles carry sid = -face (face 1..2d: axis (face-1)/2, lower if odd);
+// f_sur / w_sur are the fluid / wall coordinates minus the face coordinate
+// along that axis.
 template <typename T, int D>
-__device__ __forceinline__ void wall_noslip(const Consts& k, double xf_n, double xw_n,
-                                            const T* vf, int sid_w, T* vw, int& axis) {
-  const int index_w = -sid_w;
-  axis = (index_w - 1) >> 1;
-  const double* sv = k.wall_v[index_w - 1];
-  if (k.wall_noslip_type <= 1) {
+__device__ __forceinline__ void wall_noslip_dist(const Consts& k, T f_sur, T w_sur, const T* vf,
+                                                 int sid_w, T* vw) {
+  // face velocity, selected with constant indices (a dynamic index into the
+  // kernel-parameter block would force a local-memory copy of it)
+  T sv[3] = {T(0), T(0), T(0)};
+  const int fi = -sid_w - 1;
 #pragma unroll
-    for (int a = 0; a < D; ++a) vw[a] = (T)sv[a];
+  for (int f = 0; f < 6; ++f)
+    if (f == fi) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) sv[a] = (T)k.wall_v[f][a];
+    }
+  if (k.wall_noslip_type <= 1 || f_sur * w_sur >= T(0)) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) vw[a] = sv[a];
     return;
   }
-  const double x_sur = (index_w & 1) ? k.min_phys[axis] : k.max_phys[axis];
-  double f_sur = xf_n - x_sur, w_sur = xw_n - x_sur;
-  if (f_sur * w_sur >= 0.0) {
+  T corr = fabs(w_sur) / fabs(f_sur);
+  if (corr > T(0.5)) corr = T(0.5);  // mcf_wall_dist_ratio, mcf_header.F90:282
 #pragma unroll
-    for (int a = 0; a < D; ++a) vw[a] = (T)sv[a];
-  } else {
-    double corr = fabs(w_sur) / fabs(f_sur);
-    if (corr > 0.5) corr = 0.5;  // mcf_wall_dist_ratio, mcf_header.F90:282
-    const T c = (T)corr;
+  for (int a = 0; a < D; ++a) vw[a] = -corr * (vf[a] - sv[a]) + sv[a];
+}
+
+// same from FP64 coordinates along the wall-normal axis
+template <typename T, int D>
+__device__ __forceinline__ void wall_noslip(const Consts& k, double xf_n, double xw_n,
+                                            const T* vf, int sid_w, T* vw) {
+  const int index_w = -sid_w;
+  const int axis = (index_w - 1) >> 1;
+  double x_sur = 0.0;
 #pragma unroll
-    for (int a = 0; a < D; ++a) vw[a] = -c * (vf[a] - (T)sv[a]) + (T)sv[a];
-  }
+  for (int a = 0; a < D; ++a)
+    if (a == axis) x_sur = (index_w & 1) ? k.min_phys[a] : k.max_phys[a];
+  wall_noslip_dist<T, D>(k, (T)(xf_n - x_sur), (T)(xw_n - x_sur), vf, sid_w, vw);
 }
 
 }  // namespace mcfg
