@@ -110,7 +110,7 @@ void free_all(Handle* h) {
   void* ptrs[] = {h->x, h->v, h->f, h->m, h->pid, h->sid, h->hidx, h->rho, h->pr, h->st,
                   h->x2, h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->key, h->rank,
                   h->cnt, h->cell_start, h->scan_part, h->order, h->off, h->cell_of, h->nl,
-                  h->ncount, h->pc, h->pcf, h->vf, h->wd, h->red, h->d_err, h->d_stats, h->d_pairs,
+                  h->ncount, h->nhs, h->jp, h->pc, h->pcf, h->vf, h->wd, h->red, h->d_err, h->d_stats, h->d_pairs,
                   h->up_x, h->up_v, h->up_m, h->up_id};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -118,7 +118,8 @@ void free_all(Handle* h) {
   h->m = h->m2 = h->rho = h->pr = h->st = h->red = h->up_x = h->up_v = h->up_m = nullptr;
   h->pid = h->sid = h->hidx = h->pid2 = h->sid2 = h->hidx2 = nullptr;
   h->key = h->rank = h->cnt = h->cell_start = h->scan_part = h->order = h->cell_of = nullptr;
-  h->ncount = h->d_stats = h->up_id = nullptr;
+  h->ncount = h->d_stats = h->up_id = h->nhs = nullptr;
+  h->jp = nullptr;
   h->off = h->pcf = h->vf = nullptr;
   h->wd = nullptr;
   h->pc = nullptr;
@@ -233,7 +234,10 @@ void fill_consts(Handle* h) {
   k.wall_noslip_type = p.wall_noslip_type;
   k.init_density = p.init_density;
   for (int f = 0; f < 6; ++f)
-    for (int a = 0; a < 3; ++a) k.wall_v[f][a] = p.wall_v[f][a];
+    for (int a = 0; a < 3; ++a) {
+      k.wall_v[f][a] = p.wall_v[f][a];
+      k.wall_vf[f][a] = (float)p.wall_v[f][a];
+    }
   k.stress = p.stress_tensor ? 1 : 0;
   k.key0 = (uint32_t)p.seed;
   k.key1 = (uint32_t)(p.seed >> 32);
@@ -311,6 +315,7 @@ int ensure_capacity(Handle* h, int64_t n64) {
         (rc = dalloc(h, &h->key, cap)) || (rc = dalloc(h, &h->rank, cap)) ||
         (rc = dalloc(h, &h->order, cap)) || (rc = dalloc(h, &h->off, cap)) ||
         (rc = dalloc(h, &h->cell_of, cap)) || (rc = dalloc(h, &h->ncount, cap)) ||
+        (rc = dalloc(h, &h->nhs, cap)) ||
         (rc = dalloc(h, &h->nl, cap * (size_t)neigh)) ||
         (rc = dalloc(h, &h->cnt, (size_t)nbins + 1)) ||
         (rc = dalloc(h, &h->cell_start, (size_t)nbins + 2)) ||
@@ -326,8 +331,16 @@ int ensure_capacity(Handle* h, int64_t n64) {
           (rc = dalloc(h, &h->wd, cap)))
         return rc;
     }
-    if (h->p.stress_tensor)
+    if (h->p.stress_tensor) {
       if ((rc = dalloc(h, &h->st, cap * (size_t)(d * d)))) return rc;
+    } else {
+      // symmetric force partial sums: (forward slots + owner) x 3 planes
+      const size_t planes = (size_t)((d == 3 ? 14 : 5) + 1) * 3;
+      const size_t elt = (h->p.precision == MCFG_PRECISION_FP64) ? 8 : 4;
+      char* pj = nullptr;
+      if ((rc = dalloc(h, &pj, cap * planes * elt))) return rc;
+      h->jp = pj;
+    }
     if ((rc = dalloc(h, &h->up_x, cap * 9)) || (rc = dalloc(h, &h->up_v, cap * 3)) ||
         (rc = dalloc(h, &h->up_m, cap)) || (rc = dalloc(h, &h->up_id, cap * 2)))
       return rc;

@@ -49,6 +49,7 @@ struct Consts {
   // FP32 copies of the pair constants (the FP32 path never converts from
   // double inside a pair loop: GB300's FP64 pipe is narrow)
   float etaf, eta_coeff, ktf;
+  float wall_vf[6][3];   // FP32 copy of wall_v
   int wall_axis;         // the single solid-wall axis, -1 if none, -2 if several
   // physics
   int rhs_density_type, rhs_force_type, eos_type;
@@ -111,6 +112,8 @@ struct Handle {
   // ---- neighbours ----
   uint16_t* nl = nullptr;    // [neigh_cap][cap] entries slot<<11|local
   int* ncount = nullptr;     // [cap]
+  int* nhs = nullptr;        // [cap] first entry of the owned (forward) half
+  void* jp = nullptr;        // symmetric force partial sums [(NSF+1)*3][cap] (T)
   // ---- pair records ----
   double4_32a* pc = nullptr;     // FP64 path: (p/n^2 or p, 1/n^2, 1/m, rho)
   float4* pcf = nullptr;     // FP32 path: same in float
@@ -208,9 +211,10 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1
   return c;
 }
 
-// odd multiple of 2^-24 in (0,1), exact in FP32
+// odd multiple of 2^-24 in (0,1), exact in FP32: (2*(r>>9)+1)*2^-24 formed
+// from the bits of 1 + (r>>9)*2^-23 (no integer-to-float conversion)
 __device__ __forceinline__ float u01(uint32_t r) {
-  return (float)((r >> 9) * 2u + 1u) * (1.0f / 16777216.0f);
+  return (__uint_as_float(0x3f800000u | (r >> 9)) - 1.0f) + 5.9604644775390625e-8f;
 }
 
 __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {

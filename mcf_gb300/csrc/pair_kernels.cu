@@ -35,6 +35,7 @@ struct NbTable {
   int start[kMaxStencil];
   int count[kMaxStencil];
   int shift[kMaxStencil];  // 2 bits per axis: 0 none, 1 image at x+L, 2 at x-L
+  float4 o[kMaxStencil];   // stencil offset x cell side (FP32), per slot
 };
 
 // cell == k.ncell is the bin of particles without a real cell: it has no
@@ -52,6 +53,7 @@ __device__ __forceinline__ void build_table(const Consts& k, int cell,
       t.start[lane] = s0;
       t.count[lane] = (lane == CENTER) ? cell_start[cell + 1] - s0 : 0;
       t.shift[lane] = 0;
+      t.o[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncwarp();
     return;
@@ -97,6 +99,8 @@ __device__ __forceinline__ void build_table(const Consts& k, int cell,
       t.count[lane] = 0;
     }
     t.shift[lane] = sh;
+    t.o[lane] = make_float4((float)o[0] * k.csf[0], (float)o[1] * k.csf[1],
+                            D == 3 ? (float)o[2] * k.csf[2] : 0.0f, 0.0f);
   }
   __syncwarp();
 }
@@ -183,7 +187,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
               const double4_32a* __restrict__ x, const double4_32a* __restrict__ v,
               const double* __restrict__ m, const int* __restrict__ sid,
               const int* __restrict__ pid, uint16_t* __restrict__ nl, int* __restrict__ ncount,
-              int cap, double* __restrict__ rho, double* __restrict__ pr,
+              int* __restrict__ nhs, int cap, double* __restrict__ rho, double* __restrict__ pr,
               double4_32a* __restrict__ pc, float4* __restrict__ pcf, float4* __restrict__ vf,
               int with_pressure, unsigned* __restrict__ err, int* __restrict__ stats,
               unsigned long long* __restrict__ pairs) {
@@ -211,10 +215,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       // shared memory by coalesced loads, then broadcast to the lanes
       for (int sl = 0; sl < NS; ++sl) {
         const int js = t.start[sl], jn = t.count[sl];
-        const float ox = (float)(sl % 3 - 1) * k.csf[0];
-        const float oy = (float)((sl / 3) % 3 - 1) * k.csf[1];
-        const float oz = (D == 3) ? (float)(sl / 9 - 1) * k.csf[2] : 0.0f;
-        const float px = oi.x - ox, py = oi.y - oy, pz = oi.z - oz;
+        const float4 so = t.o[sl];
+        const float px = oi.x - so.x, py = oi.y - so.y, pz = oi.z - so.z;
         for (int b2 = 0; b2 < jn; b2 += kStage) {
           const int mm = min(kStage, jn - b2);
           __syncwarp();
@@ -249,8 +251,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       // phase 2: exact test (FP64 path), density sum, final list rows
       const int si = active ? sid[i] : 0;
       const bool acc_i = dyn_rho(k, si);
+      const int li = i - c0;  // local index in the cell
       double rho_i = 0.0;
       int kept = 0;
+      int hs = -1;  // first entry of the forward half (pairs this particle owns)
       if (FP64) {
         double4_32a xi4 = active ? x[i] : make_double4_32a(0, 0, 0, 0);
         const double xi[3] = {xi4.x, xi4.y, xi4.z};
@@ -264,6 +268,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
           double r[3];
           const double d2 = exact_sep<D>(k, xi, xj, t.shift[sl], r);
           if (d2 >= k.rc2) continue;
+          if (hs < 0 && (sl > CENTER || (sl == CENTER && q > li))) hs = kept;
           nl[(size_t)kept * n + i] = (uint16_t)ent;
           ++kept;
           if (acc_i) {
@@ -279,15 +284,17 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         for (int e = 0; e < cnt; ++e) {
           const int ent = (e < kListStage) ? ls[wib][e][lane] : nl[(size_t)e * n + i];
           if (e < kListStage) nl[(size_t)e * n + i] = (uint16_t)ent;
-          if (!acc_i) continue;
           const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
+          if (hs < 0 && (sl > CENTER || (sl == CENTER && q > li))) hs = e;
+          if (!acc_i) continue;
           const int j = t.start[sl] + q;
           const float4 oj = off[j];
-          const float rx = (oi.x - oj.x) - (float)(sl % 3 - 1) * k.csf[0];
-          const float ry = (oi.y - oj.y) - (float)((sl / 3) % 3 - 1) * k.csf[1];
+          const float4 so = t.o[sl];
+          const float rx = (oi.x - oj.x) - so.x;
+          const float ry = (oi.y - oj.y) - so.y;
           float d2 = rx * rx + ry * ry;
           if (D == 3) {
-            const float rz = (oi.z - oj.z) - (float)(sl / 9 - 1) * k.csf[2];
+            const float rz = (oi.z - oj.z) - so.z;
             d2 += rz * rz;
           }
           float w = kernel_w<float>(k, sqrtf(d2));
@@ -302,6 +309,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       }
       if (!active) continue;
       ncount[i] = kept;
+      nhs[i] = (hs < 0) ? kept : hs;
       my_max = max(my_max, kept);
       my_pairs += (unsigned long long)kept;
       const double mi = m[i];
@@ -466,9 +474,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         for (int a = 0; a < D; ++a) vij[a] = vi[a] - vj[a];
         float z[6];
         if (noise) pair_normals<D>(k.key0, k.key1, step, pidi, pid[j], z);
-        T pa[3];
-        pair_accel<T, D>(k, r, inv_d, vij, Ai, ci.y, ci.z, Aj, cj.y, cj.z, gw, noise, z, inv_sqdt,
-                         pa);
+        T pa[3], si_s, sj_s;
+        pair_force<T, D>(k, r, inv_d, vij, Ai, ci.y, Aj, cj.y, gw, noise, z, inv_sqdt, pa);
+        pair_scales<T>(k.rhs_force_type, ci.z, cj.z, si_s, sj_s);
+#pragma unroll
+        for (int a = 0; a < D; ++a) pa[a] *= si_s;
 #pragma unroll
         for (int a = 0; a < D; ++a) acc[a] += pa[a];
         if (k.stress) {
@@ -561,9 +571,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
         if (si != 0 && sj != 0) continue;
         const int sl = cur.sl;
         T r[3];
-        r[0] = (oi.x - cur.o.x) - (float)(sl % 3 - 1) * k.csf[0];
-        r[1] = (oi.y - cur.o.y) - (float)((sl / 3) % 3 - 1) * k.csf[1];
-        r[2] = (D == 3) ? (oi.z - cur.o.z) - (float)(sl / 9 - 1) * k.csf[2] : 0.f;
+        const float4 so = t.o[sl];
+        r[0] = (oi.x - cur.o.x) - so.x;
+        r[1] = (oi.y - cur.o.y) - so.y;
+        r[2] = (D == 3) ? (oi.z - cur.o.z) - so.z : 0.f;
         T d2 = r[0] * r[0] + r[1] * r[1];
         if (D == 3) d2 += r[2] * r[2];
         const T inv_d = rsqrtf(d2);
@@ -615,9 +626,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
         for (int a = 0; a < D; ++a) vij[a] = vi[a] - vj[a];
         float z[6];
         if (noise) pair_normals<D>(k.key0, k.key1, step, pidi, __float_as_int(cur.v.w), z);
-        T pa[3];
-        pair_accel<T, D>(k, r, inv_d, vij, Ai, ci.y, ci.z, Aj, cur.c.y, cur.c.z, gw, noise, z,
-                         inv_sqdt, pa);
+        T pa[3], si_s, sj_s;
+        pair_force<T, D>(k, r, inv_d, vij, Ai, ci.y, Aj, cur.c.y, gw, noise, z, inv_sqdt, pa);
+        pair_scales<T>(k.rhs_force_type, ci.z, cur.c.z, si_s, sj_s);
+#pragma unroll
+        for (int a = 0; a < D; ++a) pa[a] *= si_s;
 #pragma unroll
         for (int a = 0; a < D; ++a) {
           const T y = pa[a] - comp[a];
@@ -644,6 +657,325 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Symmetric force sweep: every pair is evaluated once, by the particle whose
+// cell owns it (partner in one of the 13 forward cells, or later in the same
+// cell: the half-shell of ppm_neighlist_MkNeighIdx.F90:198-249).  The owner
+// keeps its share in registers (Kahan in FP32); the partner's share is
+// summed per (forward slot, partner) in shared memory.  Lanes of a round that
+// hit the same partner are combined with __match_any_sync, in lane order,
+// by the lowest such lane, so every sum has a fixed order and the result is
+// deterministic without atomics.  The per-slot partial sums go to planes
+// jp[slot][c][n] that k_force_gather adds up per particle.
+// ---------------------------------------------------------------------------
+template <bool FP64>
+struct SymT;
+template <>
+struct SymT<true> {
+  using T = double;
+  static constexpr int CC = 32;  // partners per slot held in shared memory
+};
+template <>
+struct SymT<false> {
+  using T = float;
+  static constexpr int CC = 64;
+};
+
+template <int D, bool FP64>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+    k_force_sym(Consts k, const int* __restrict__ cell_start, const uint16_t* __restrict__ nl,
+                const int* __restrict__ ncount, const int* __restrict__ nhs,
+                const float4* __restrict__ off, const double4_32a* __restrict__ x,
+                const double4_32a* __restrict__ v, const double4_32a* __restrict__ pc,
+                const float4* __restrict__ pcf, const float4* __restrict__ vf,
+                const float2* __restrict__ wd, const int* __restrict__ sid,
+                const int* __restrict__ pid, typename SymT<FP64>::T* __restrict__ jp,
+                uint32_t step, typename SymT<FP64>::T inv_sqdt) {
+  using T = typename SymT<FP64>::T;
+  constexpr int CC = SymT<FP64>::CC;
+  constexpr int CENTER = (D == 3) ? 13 : 4;
+  constexpr int NSF = (D == 3) ? 14 : 5;  // forward slots CENTER..NS-1
+  __shared__ NbTable tab[kWarpsPerBlock];
+  __shared__ T part[kWarpsPerBlock][NSF][3][CC];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = k.n;
+  const bool noise = k.noise != 0;
+  const bool walls = k.wall_axis != -1;
+  for (int cell = blockIdx.x * kWarpsPerBlock + wib; cell <= k.ncell;
+       cell += gridDim.x * kWarpsPerBlock) {
+    NbTable& t = tab[wib];
+    build_table<D>(k, cell, cell_start, t);
+    // zero the partner sums this cell owns (shared, or global when a cell
+    // holds more than CC particles)
+    for (int s = 0; s < NSF; ++s) {
+      const int cs_ = t.count[CENTER + s], st_ = t.start[CENTER + s];
+      for (int q = lane; q < cs_; q += 32)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          if (cs_ <= CC)
+            part[wib][s][a][q] = T(0);
+          else
+            jp[((size_t)s * 3 + a) * n + st_ + q] = T(0);
+        }
+    }
+    __syncwarp();
+    const int c0 = t.start[CENTER], c1 = c0 + t.count[CENTER];
+    for (int base = c0; base < c1; base += 32) {
+      const int i = base + lane;
+      const bool act = i < c1;
+      const int e0 = act ? nhs[i] : 0, e1 = act ? ncount[i] : 0;
+      int rounds = e1 - e0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) rounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, o));
+      // own data
+      int si = 0, pidi = 0;
+      T vi0[3] = {0, 0, 0};
+      T Ai0 = 0, Bi = 0, Ci = 0, Pi = 0;
+      float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+      double xi[3] = {0.0, 0.0, 0.0};
+      float2 wdi = make_float2(0.f, 0.f);
+      if (act) {
+        if (FP64) {
+          si = sid[i];
+          pidi = pid[i];
+          const double4_32a x4 = x[i], v4 = v[i], c4 = pc[i];
+          xi[0] = x4.x; xi[1] = x4.y; xi[2] = x4.z;
+          vi0[0] = (T)v4.x; vi0[1] = (T)v4.y; vi0[2] = (T)v4.z;
+          Ai0 = (T)c4.x; Bi = (T)c4.y; Ci = (T)c4.z; Pi = (T)c4.w;
+        } else {
+          oi = off[i];
+          si = __float_as_int(oi.w);
+          const float4 v4 = vf[i], c4 = pcf[i];
+          pidi = __float_as_int(v4.w);
+          vi0[0] = (T)v4.x; vi0[1] = (T)v4.y; vi0[2] = (T)v4.z;
+          Ai0 = (T)c4.x; Bi = (T)c4.y; Ci = (T)c4.z; Pi = (T)c4.w;
+          if (walls && k.wall_axis >= 0) wdi = wd[i];
+        }
+      }
+      T acc[3] = {0, 0, 0}, comp[3] = {0, 0, 0};
+      for (int r = 0; r < rounds; ++r) {
+        const int e = e0 + r;
+        const bool has_e = e < e1;
+        int key = 0;
+        T vjs[3] = {0, 0, 0};
+        bool has = false;
+        int jsl = 0, jq = 0;
+        if (has_e) {
+          const int ent = nl[(size_t)e * n + i];
+          jsl = ent >> kLocalBits;
+          jq = ent & (kMaxCellCount - 1);
+          const int j = t.start[jsl] + jq;
+          T rr[3], vj[3], vi[3] = {vi0[0], vi0[1], vi0[2]};
+          T Aj, Bj, Cj, Pj, inv_d, d;
+          int sj, pidj;
+          double xj[3] = {0.0, 0.0, 0.0};
+          if (FP64) {
+            sj = sid[j];
+            const double4_32a x4 = x[j];
+            xj[0] = x4.x; xj[1] = x4.y; xj[2] = x4.z;
+            double r64[3];
+            const double d2 = exact_sep<D>(k, xi, xj, t.shift[jsl], r64);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) rr[a] = (T)r64[a];
+            inv_d = (T)rsqrt(d2);
+            d = (T)(d2 * (double)inv_d);
+            const double4_32a v4 = v[j], c4 = pc[j];
+            vj[0] = (T)v4.x; vj[1] = (T)v4.y; vj[2] = (T)v4.z;
+            Aj = (T)c4.x; Bj = (T)c4.y; Cj = (T)c4.z; Pj = (T)c4.w;
+            pidj = noise ? pid[j] : 0;
+          } else {
+            const float4 o4 = off[j], v4 = vf[j], c4 = pcf[j];
+            sj = __float_as_int(o4.w);
+            const float4 so = t.o[jsl];
+            rr[0] = (T)((oi.x - o4.x) - so.x);
+            rr[1] = (T)((oi.y - o4.y) - so.y);
+            rr[2] = (D == 3) ? (T)((oi.z - o4.z) - so.z) : T(0);
+            T d2 = rr[0] * rr[0] + rr[1] * rr[1];
+            if (D == 3) d2 += rr[2] * rr[2];
+            inv_d = (T)rsqrtf((float)d2);
+            d = d2 * inv_d;
+            vj[0] = (T)v4.x; vj[1] = (T)v4.y; vj[2] = (T)v4.z;
+            Aj = (T)c4.x; Bj = (T)c4.y; Cj = (T)c4.z; Pj = (T)c4.w;
+            pidj = __float_as_int(v4.w);
+          }
+          has = !(si != 0 && sj != 0);  // w-w, c-c, c-w: no interaction
+          if (has) {
+            T Ai = Ai0;
+            if (si < 0 || sj < 0) {
+              // fluid-wall pair (pp_interaction_fw.inc / _wf.inc)
+              const int sw = (sj < 0) ? sj : si;
+              const int face = -sw;
+              const bool lower = (face & 1) != 0;
+              const int axis = (face - 1) >> 1;
+              T df, dw;
+              if (!FP64 && k.wall_axis >= 0) {
+                const float2 wj = wd[j];
+                const float a_ = lower ? wdi.x : wdi.y, b_ = lower ? wj.x : wj.y;
+                df = (T)((sj < 0) ? a_ : b_);
+                dw = (T)((sj < 0) ? b_ : a_);
+              } else {
+                const double x_sur = axis == 0 ? (lower ? k.min_phys[0] : k.max_phys[0])
+                                     : axis == 1 ? (lower ? k.min_phys[1] : k.max_phys[1])
+                                                 : (lower ? k.min_phys[2] : k.max_phys[2]);
+                double xa, xb;
+                if (FP64) {
+                  xa = axis == 0 ? xi[0] : axis == 1 ? xi[1] : xi[2];
+                  xb = axis == 0 ? xj[0] : axis == 1 ? xj[1] : xj[2];
+                } else {
+                  const double4_32a a4 = x[i], b4 = x[j];
+                  xa = axis == 0 ? a4.x : axis == 1 ? a4.y : a4.z;
+                  xb = axis == 0 ? b4.x : axis == 1 ? b4.y : b4.z;
+                }
+                df = (T)(((sj < 0) ? xa : xb) - x_sur);
+                dw = (T)(((sj < 0) ? xb : xa) - x_sur);
+              }
+              T vw[3];
+              if (sj < 0) {
+                wall_noslip_dist<T, D>(k, df, dw, vi, sj, vw);
+#pragma unroll
+                for (int a = 0; a < D; ++a) vj[a] = vw[a];
+                Aj = boundary_A<T>(k.rhs_force_type, Pi, Bj);
+              } else {
+                wall_noslip_dist<T, D>(k, df, dw, vj, si, vw);
+#pragma unroll
+                for (int a = 0; a < D; ++a) vi[a] = vw[a];
+                Ai = boundary_A<T>(k.rhs_force_type, Pj, Bi);
+              }
+            }
+            const T gw = kernel_gradw<T>(k, d);
+            T vij[3];
+#pragma unroll
+            for (int a = 0; a < D; ++a) vij[a] = vi[a] - vj[a];
+            float z[6];
+            if (noise) pair_normals<D>(k.key0, k.key1, step, pidi, pidj, z);
+            T g[3], s_i, s_j;
+            pair_force<T, D>(k, rr, inv_d, vij, Ai, Bi, Aj, Bj, gw, noise, z, inv_sqdt, g);
+            pair_scales<T>(k.rhs_force_type, Ci, Cj, s_i, s_j);
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+              const T pa = g[a] * s_i;
+              if (FP64) {
+                acc[a] += pa;
+              } else {
+                const T y = pa - comp[a];
+                const T tt = acc[a] + y;
+                comp[a] = (tt - acc[a]) - y;
+                acc[a] = tt;
+              }
+              vjs[a] = -g[a] * s_j;
+            }
+            key = (jsl - CENTER) * kMaxCellCount + jq;
+          }
+        }
+        // deterministic combination of the partner shares of this round
+        const unsigned amask = __ballot_sync(0xffffffffu, has);
+        if (has) {
+          const unsigned peers = __match_any_sync(amask, key);
+          const int leader = __ffs(peers) - 1;
+          T s0 = vjs[0], s1 = vjs[1], s2 = vjs[2];
+          if (peers != (1u << lane)) {
+            s0 = s1 = s2 = T(0);
+            for (unsigned mm = peers; mm; mm &= mm - 1) {
+              const int src = __ffs(mm) - 1;
+              s0 += __shfl_sync(peers, vjs[0], src);
+              s1 += __shfl_sync(peers, vjs[1], src);
+              s2 += __shfl_sync(peers, vjs[2], src);
+            }
+          }
+          if (lane == leader) {
+            const int s = jsl - CENTER;
+            const int cs_ = t.count[jsl];
+            if (cs_ <= CC) {
+              part[wib][s][0][jq] += s0;
+              part[wib][s][1][jq] += s1;
+              part[wib][s][2][jq] += s2;
+            } else {
+              const size_t b0 = (size_t)t.start[jsl] + jq;
+              jp[((size_t)s * 3 + 0) * n + b0] += s0;
+              jp[((size_t)s * 3 + 1) * n + b0] += s1;
+              jp[((size_t)s * 3 + 2) * n + b0] += s2;
+            }
+          }
+        }
+        __syncwarp();
+      }
+      if (act) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) jp[((size_t)NSF * 3 + a) * n + i] = acc[a];
+      }
+    }
+    __syncwarp();
+    for (int s = 0; s < NSF; ++s) {
+      const int cs_ = t.count[CENTER + s], st_ = t.start[CENTER + s];
+      if (cs_ > CC) continue;
+      for (int q = lane; q < cs_; q += 32)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) jp[((size_t)s * 3 + a) * n + st_ + q] = part[wib][s][a][q];
+    }
+  }
+}
+
+// Sum of the per-slot partner shares and the owner share of every particle
+// (fixed order, Kahan in FP32), then body force and the second half kick.
+template <int D, bool FP64>
+__global__ void k_force_gather(Consts k, const int* __restrict__ cell_of,
+                               const typename SymT<FP64>::T* __restrict__ jp,
+                               const double4_32a* __restrict__ x,
+                               const double4_32a* __restrict__ v, const int* __restrict__ sid,
+                               double4_32a* __restrict__ f, int fuse_mode, double dt,
+                               double4_32a* __restrict__ v_out, unsigned* __restrict__ err) {
+  using T = typename SymT<FP64>::T;
+  constexpr int CENTER = (D == 3) ? 13 : 4;
+  constexpr int NSF = (D == 3) ? 14 : 5;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = k.n;
+  if (j >= n) return;
+  const int cj = cell_of[j];
+  int cc[3] = {0, 0, 0};
+  if (cj < k.ncell) {
+    int rem = cj;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      cc[a] = rem % k.nm[a];
+      rem /= k.nm[a];
+    }
+  }
+  T acc[3], comp[3] = {0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) acc[a] = jp[((size_t)NSF * 3 + a) * n + j];
+  if (cj < k.ncell) {
+#pragma unroll
+    for (int s = 0; s < NSF; ++s) {
+      // the owner cell of plane s is cell(j) - offset(CENTER + s)
+      const int sl = CENTER + s;
+      const int o[3] = {sl % 3 - 1, (sl / 3) % 3 - 1, sl / 9 - 1};
+      bool ok = true;
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        const int h = cc[a] - o[a];
+        if ((h < 0 || h >= k.nm[a]) && !k.periodic[a]) ok = false;
+      }
+      if (!ok) continue;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const T val = jp[((size_t)s * 3 + a) * n + j];
+        if (FP64) {
+          acc[a] += val;
+        } else {
+          const T y = val - comp[a];
+          const T tt = acc[a] + y;
+          comp[a] = (tt - acc[a]) - y;
+          acc[a] = tt;
+        }
+      }
+    }
+  }
+  const double4_32a x4 = x[j];
+  const double xj[3] = {x4.x, x4.y, x4.z};
+  force_epilogue<D>(k, j, sid[j], xj, (double)acc[0], (double)acc[1],
+                    D == 3 ? (double)acc[2] : 0.0, fuse_mode, dt, v, f, v_out, err);
+}
+
 static int grid_for(Handle* h) {
   const int warps = h->k.ncell + 1;  // + bin of particles without a cell
   int g = (warps + kWarpsPerBlock - 1) / kWarpsPerBlock;
@@ -661,7 +993,7 @@ int compute_density(Handle* h, bool with_pressure) {
   const bool fp64 = h->p.precision == MCFG_PRECISION_FP64;
 #define LAUNCH_D(DD, PP)                                                                       \
   k_density<DD, PP><<<g, kWarpsPerBlock * 32, 0, s>>>(                                          \
-      k, h->cell_start, h->off, h->x, h->v, h->m, h->sid, h->pid, h->nl, h->ncount,            \
+      k, h->cell_start, h->off, h->x, h->v, h->m, h->sid, h->pid, h->nl, h->ncount, h->nhs,    \
       h->neigh_cap, h->rho, h->pr, h->pc, h->pcf, h->vf, with_pressure ? 1 : 0, h->d_err,      \
       h->d_stats, h->d_pairs)
   if (k.d == 3) {
@@ -698,7 +1030,47 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
   if (k.noise && !(dt > 0.0)) return set_error(h, MCFG_EINVAL, "random force needs dt > 0");
   const double inv_sqdt = (k.noise && dt > 0.0) ? 1.0 / sqrt(dt) : 0.0;
   const int bs = kWarpsPerBlock * 32;
-  if (fp64) {
+  if (!k.stress && h->jp) {
+    // symmetric sweep + per-particle gather
+    const int n = (int)h->n;
+    const int gbn = (n + 255) / 256;
+    if (fp64) {
+      double* jp = (double*)h->jp;
+      if (k.d == 3) {
+        k_force_sym<3, true><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
+                                              h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
+                                              h->pid, jp, (uint32_t)step, inv_sqdt);
+        if (n > 0)
+          k_force_gather<3, true><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid, h->f,
+                                                      fuse_mode, dt, h->v2, h->d_err);
+      } else {
+        k_force_sym<2, true><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
+                                              h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
+                                              h->pid, jp, (uint32_t)step, inv_sqdt);
+        if (n > 0)
+          k_force_gather<2, true><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid, h->f,
+                                                      fuse_mode, dt, h->v2, h->d_err);
+      }
+    } else {
+      float* jp = (float*)h->jp;
+      if (k.d == 3) {
+        k_force_sym<3, false><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
+                                               h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
+                                               h->pid, jp, (uint32_t)step, (float)inv_sqdt);
+        if (n > 0)
+          k_force_gather<3, false><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid,
+                                                       h->f, fuse_mode, dt, h->v2, h->d_err);
+      } else {
+        k_force_sym<2, false><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
+                                               h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
+                                               h->pid, jp, (uint32_t)step, (float)inv_sqdt);
+        if (n > 0)
+          k_force_gather<2, false><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid,
+                                                       h->f, fuse_mode, dt, h->v2, h->d_err);
+      }
+    }
+    h->launches++;
+  } else if (fp64) {
     if (k.d == 3)
       k_force64<3><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->x, h->v, h->pc, h->sid,
                                     h->pid, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step,

@@ -142,14 +142,15 @@ __device__ __forceinline__ double my_sqrt<double>(double a) { return sqrt(a); }
 template <>
 __device__ __forceinline__ float my_sqrt<float>(float a) { return sqrtf(a); }
 
-// Acceleration of particle i from partner j (i side of the symmetric pair
-// forces of rhs_force_ff_Newtonian_{Morris,Espanol,HuAdams,HuAdams_angular}
-// .F90).  r = x_i - x_j (image), inv_d = 1/|r|, vij = v_i - v_j.  Returns
-// the pair acceleration in acc[].
+// Pair force of rhs_force_ff_Newtonian_{Morris,Espanol,HuAdams,
+// HuAdams_angular}.F90 before the mass factor: the acceleration of i is
+// g * scale_i, that of j is -g * scale_j, with (scale_i, scale_j) =
+// (m_j, m_i) for Morris (C = m) and (1/m_i, 1/m_j) otherwise (C = 1/m); see
+// pair_scales.  r = x_i - x_j (image), inv_d = 1/|r|, vij = v_i - v_j.
 template <typename T, int D>
-__device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T inv_d, const T* vij,
-                                           T Ai, T Bi, T Ci, T Aj, T Bj, T Cj, T gw,
-                                           bool noise, const float* z, T inv_sqdt, T* acc) {
+__device__ __forceinline__ void pair_force(const Consts& k, const T* r, T inv_d, const T* vij,
+                                           T Ai, T Bi, T Aj, T Bj, T gw, bool noise,
+                                           const float* z, T inv_sqdt, T* g) {
   T e[3];
 #pragma unroll
   for (int a = 0; a < D; ++a) e[a] = r[a] * inv_d;
@@ -161,7 +162,7 @@ __device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T inv_d,
       const T f_c = (Ai + Aj) * gw;
       const T f_d = T(2) * eta * gw * Bi * Bj * inv_d;
 #pragma unroll
-      for (int a = 0; a < D; ++a) acc[a] = Cj * (f_d * vij[a] - f_c * e[a]);
+      for (int a = 0; a < D; ++a) g[a] = f_d * vij[a] - f_c * e[a];
       break;
     }
     case 2: {
@@ -173,7 +174,7 @@ __device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T inv_d,
       const T f_d1 = (T(2) - T(1) / T(D)) * bb;
       const T f_d2 = (T(D + 2) / T(D)) * bb * ev;
 #pragma unroll
-      for (int a = 0; a < D; ++a) acc[a] = Ci * (f_d1 * vij[a] + (f_d2 - f_c) * e[a]);
+      for (int a = 0; a < D; ++a) g[a] = f_d1 * vij[a] + (f_d2 - f_c) * e[a];
       if (noise) {
         T dW[3][3];
         T tr = T(0);
@@ -203,7 +204,7 @@ __device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T inv_d,
           T We = T(0);
 #pragma unroll
           for (int b = 0; b < D; ++b) We += dW[a][b] * e[b];
-          acc[a] += Ci * (Aij * We + Bij * tr * e[a]) * inv_sqdt;
+          g[a] += (Aij * We + Bij * tr * e[a]) * inv_sqdt;
         }
       }
       break;
@@ -212,7 +213,7 @@ __device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T inv_d,
       const T f_c = (Ai + Aj) * gw;
       const T f_d = eta * (Bi + Bj) * gw * inv_d;
 #pragma unroll
-      for (int a = 0; a < D; ++a) acc[a] = Ci * (f_d * vij[a] - f_c * e[a]);
+      for (int a = 0; a < D; ++a) g[a] = f_d * vij[a] - f_c * e[a];
       if (noise) {
         T dW[3][3];
         T tr = T(0);
@@ -238,7 +239,7 @@ __device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T inv_d,
           T We = T(0);
 #pragma unroll
           for (int b = 0; b < D; ++b) We += dW[a][b] * e[b];
-          acc[a] += Ci * f_r * We;
+          g[a] += f_r * We;
         }
       }
       break;
@@ -254,15 +255,37 @@ __device__ __forceinline__ void pair_accel(const Consts& k, const T* r, T inv_d,
       T fe = f_d - f_c;
       if (noise) {
         const T eps = (T)z[0];
-        fe += eps * my_sqrt<T>(T(2) * kt * eta) * my_sqrt<T>(-eta_coef * Aij * inv_d) *
-              inv_sqdt;
+        fe += eps * my_sqrt<T>(T(2) * kt * eta) * my_sqrt<T>(-eta_coef * Aij * inv_d) * inv_sqdt;
       }
 #pragma unroll
-      for (int a = 0; a < D; ++a) acc[a] = Ci * fe * e[a];
+      for (int a = 0; a < D; ++a) g[a] = fe * e[a];
       break;
     }
   }
 }
+
+// (scale_i, scale_j) of pair_force from the C coefficients
+template <typename T>
+__device__ __forceinline__ void pair_scales(int type, T Ci, T Cj, T& si, T& sj) {
+  if (type == 1) {
+    si = Cj;
+    sj = Ci;
+  } else {
+    si = Ci;
+    sj = Cj;
+  }
+}
+
+template <typename T>
+struct WallV;
+template <>
+struct WallV<double> {
+  __device__ static double get(const Consts& k, int f, int a) { return k.wall_v[f][a]; }
+};
+template <>
+struct WallV<float> {
+  __device__ static float get(const Consts& k, int f, int a) { return k.wall_vf[f][a]; }
+};
 
 // Morris no-slip velocity of a solid-wall particle,
 // boundary_noslip_solid.F90:40-95 (frozen) and :137-240 (Morris).  Wall
@@ -280,7 +303,7 @@ __device__ __forceinline__ void wall_noslip_dist(const Consts& k, T f_sur, T w_s
   for (int f = 0; f < 6; ++f)
     if (f == fi) {
 #pragma unroll
-      for (int a = 0; a < 3; ++a) sv[a] = (T)k.wall_v[f][a];
+      for (int a = 0; a < 3; ++a) sv[a] = WallV<T>::get(k, f, a);
     }
   if (k.wall_noslip_type <= 1 || f_sur * w_sur >= T(0)) {
 #pragma unroll

@@ -167,6 +167,29 @@ def test_stress_tensor_and_statistics(gpu_lib):
     assert np.allclose(st_g, st_o, rtol=1e-10, atol=1e-12 * np.abs(st_o).max())
 
 
+@pytest.mark.parametrize("precision", [PRECISION_FP64, PRECISION_FP32_MIXED])
+@pytest.mark.parametrize("maker", ["jit3d", "walls", "jit2d"])
+def test_symmetric_sweep_matches_gather_sweep(gpu_lib, precision, maker):
+    # the stress tensor selects the two-sided gather sweep, without it the
+    # symmetric (each pair once) sweep runs: same accelerations
+    w = {"jit3d": jittered_3d, "walls": lambda: make_golden.workload("walls_small"),
+         "jit2d": jittered_2d}[maker]()
+    res = []
+    for stress in (0, 1):
+        p = w.params.copy()
+        p.precision = precision
+        p.stress_tensor = stress
+        p.Brownian = 1
+        p.kt = 1e-3
+        g = SDPD(p)
+        g.upload(w.x, w.v, w.m, w.id)
+        g.marching_init_force(3)
+        res.append(g.download("f")["f"])
+    scale = np.abs(res[1]).max()
+    tol = 1e-13 if precision == PRECISION_FP64 else 2e-5
+    assert np.max(np.abs(res[0] - res[1])) <= tol * scale
+
+
 # ------------------------------------------------------------- trajectories
 def test_fp64_trajectory_100_steps_kt0(gpu_lib):
     w = configs.c1_poiseuille_2d()
