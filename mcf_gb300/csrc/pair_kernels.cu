@@ -681,6 +681,21 @@ struct SymT<false> {
   static constexpr int CC = 64;
 };
 
+
+// Per-warp dynamic shared memory of k_force_sym (bytes), see the layout in
+// the kernel.
+template <int D, bool FP64>
+__host__ __device__ constexpr int sym_warp_bytes() {
+  using T = typename SymT<FP64>::T;
+  constexpr int NSF = (D == 3) ? 14 : 5;
+  constexpr int CC = SymT<FP64>::CC;
+  constexpr int part = NSF * 3 * CC * (int)sizeof(T);
+  constexpr int accs = 2 * 3 * 32 * (int)sizeof(T);
+  constexpr int idx = 96 * 4;  // ex[33], e0[32], pad
+  constexpr int own = FP64 ? (3 * 32 * 32 + 2 * 32 * 4) : (3 * 32 * 16 + 32 * 8);
+  return ((part + accs + idx + own) + 31) / 32 * 32;
+}
+
 template <int D, bool FP64>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     k_force_sym(Consts k, const int* __restrict__ cell_start, const uint16_t* __restrict__ nl,
@@ -695,9 +710,19 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   constexpr int CC = SymT<FP64>::CC;
   constexpr int CENTER = (D == 3) ? 13 : 4;
   constexpr int NSF = (D == 3) ? 14 : 5;  // forward slots CENTER..NS-1
+  extern __shared__ __align__(32) unsigned char smem_raw[];
   __shared__ NbTable tab[kWarpsPerBlock];
-  __shared__ T part[kWarpsPerBlock][NSF][3][CC];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // per-warp layout: part[NSF][3][CC] | acc[3][32] | comp[3][32] | ex[33] e0[32] |
+  //                  owner data (FP32: off, vf, pcf float4 + wd float2;
+  //                              FP64: x, v, pc double4 + sid, pid int)
+  unsigned char* wb = smem_raw + (size_t)wib * sym_warp_bytes<D, FP64>();
+  T* part = reinterpret_cast<T*>(wb);
+  T* acc_s = part + NSF * 3 * CC;
+  T* comp_s = acc_s + 3 * 32;
+  int* ex = reinterpret_cast<int*>(comp_s + 3 * 32);
+  int* e0s = ex + 33;
+  unsigned char* own = reinterpret_cast<unsigned char*>(ex + 96);
   const int n = k.n;
   const bool noise = k.noise != 0;
   const bool walls = k.wall_axis != -1;
@@ -713,94 +738,131 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
           if (cs_ <= CC)
-            part[wib][s][a][q] = T(0);
+            part[(s * 3 + a) * CC + q] = T(0);
           else
             jp[((size_t)s * 3 + a) * n + st_ + q] = T(0);
         }
     }
-    __syncwarp();
     const int c0 = t.start[CENTER], c1 = c0 + t.count[CENTER];
     for (int base = c0; base < c1; base += 32) {
       const int i = base + lane;
       const bool act = i < c1;
       const int e0 = act ? nhs[i] : 0, e1 = act ? ncount[i] : 0;
-      int rounds = e1 - e0;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) rounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, o));
-      // own data
-      int si = 0, pidi = 0;
-      T vi0[3] = {0, 0, 0};
-      T Ai0 = 0, Bi = 0, Ci = 0, Pi = 0;
-      float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
-      double xi[3] = {0.0, 0.0, 0.0};
-      float2 wdi = make_float2(0.f, 0.f);
-      if (act) {
-        if (FP64) {
-          si = sid[i];
-          pidi = pid[i];
-          const double4_32a x4 = x[i], v4 = v[i], c4 = pc[i];
-          xi[0] = x4.x; xi[1] = x4.y; xi[2] = x4.z;
-          vi0[0] = (T)v4.x; vi0[1] = (T)v4.y; vi0[2] = (T)v4.z;
-          Ai0 = (T)c4.x; Bi = (T)c4.y; Ci = (T)c4.z; Pi = (T)c4.w;
-        } else {
-          oi = off[i];
-          si = __float_as_int(oi.w);
-          const float4 v4 = vf[i], c4 = pcf[i];
-          pidi = __float_as_int(v4.w);
-          vi0[0] = (T)v4.x; vi0[1] = (T)v4.y; vi0[2] = (T)v4.z;
-          Ai0 = (T)c4.x; Bi = (T)c4.y; Ci = (T)c4.z; Pi = (T)c4.w;
-          if (walls && k.wall_axis >= 0) wdi = wd[i];
+      const int len = e1 - e0;
+      // owner data and accumulators of this chunk in shared memory
+      if (FP64) {
+        double4_32a* ox = reinterpret_cast<double4_32a*>(own);
+        double4_32a* ov = ox + 32;
+        double4_32a* oc = ov + 32;
+        int* os = reinterpret_cast<int*>(oc + 32);
+        int* op = os + 32;
+        if (act) {
+          ox[lane] = x[i];
+          ov[lane] = v[i];
+          oc[lane] = pc[i];
+          os[lane] = sid[i];
+          op[lane] = pid[i];
+        }
+      } else {
+        float4* oo = reinterpret_cast<float4*>(own);
+        float4* ov = oo + 32;
+        float4* oc = ov + 32;
+        float2* ow = reinterpret_cast<float2*>(oc + 32);
+        if (act) {
+          oo[lane] = off[i];
+          ov[lane] = vf[i];
+          oc[lane] = pcf[i];
+          if (walls && k.wall_axis >= 0) ow[lane] = wd[i];
         }
       }
-      T acc[3] = {0, 0, 0}, comp[3] = {0, 0, 0};
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        acc_s[a * 32 + lane] = T(0);
+        comp_s[a * 32 + lane] = T(0);
+      }
+      // exclusive prefix of the owned-pair counts: the warp's pairs are
+      // spread evenly over the lanes, 32 per round
+      int incl = len;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int tt = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += tt;
+      }
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      ex[lane] = incl - len;
+      e0s[lane] = e0;
+      if (lane == 31) ex[32] = total;
+      __syncwarp();
+      const int rounds = (total + 31) >> 5;
       for (int r = 0; r < rounds; ++r) {
-        const int e = e0 + r;
-        const bool has_e = e < e1;
-        int key = 0;
-        T vjs[3] = {0, 0, 0};
+        const int fidx = r * 32 + lane;
+        const bool valid = fidx < total;
+        int ow_l = 0;
+#pragma unroll
+        for (int stp = 16; stp > 0; stp >>= 1)
+          if (ex[ow_l + stp] <= fidx) ow_l += stp;
         bool has = false;
-        int jsl = 0, jq = 0;
-        if (has_e) {
-          const int ent = nl[(size_t)e * n + i];
+        int keyj = 0, jsl = 0, jq = 0;
+        T vjs[3] = {0, 0, 0}, vis[3] = {0, 0, 0};
+        if (valid) {
+          const int ii = base + ow_l;
+          const int e = e0s[ow_l] + (fidx - ex[ow_l]);
+          const int ent = nl[(size_t)e * n + ii];
           jsl = ent >> kLocalBits;
           jq = ent & (kMaxCellCount - 1);
           const int j = t.start[jsl] + jq;
-          T rr[3], vj[3], vi[3] = {vi0[0], vi0[1], vi0[2]};
-          T Aj, Bj, Cj, Pj, inv_d, d;
-          int sj, pidj;
-          double xj[3] = {0.0, 0.0, 0.0};
+          T rr[3], vi[3], vj[3];
+          T Ai, Bi, Ci, Pi, Aj, Bj, Cj, Pj, inv_d, d;
+          int si, sj, pidi, pidj;
+          double xi[3] = {0.0, 0.0, 0.0}, xj[3] = {0.0, 0.0, 0.0};
+          float2 wdi = make_float2(0.f, 0.f);
           if (FP64) {
+            const double4_32a* ox = reinterpret_cast<const double4_32a*>(own);
+            const int* os = reinterpret_cast<const int*>(ox + 96);
+            const double4_32a x4 = ox[ow_l], v4 = ox[32 + ow_l], c4 = ox[64 + ow_l];
+            si = os[ow_l];
+            pidi = os[32 + ow_l];
+            xi[0] = x4.x; xi[1] = x4.y; xi[2] = x4.z;
+            vi[0] = (T)v4.x; vi[1] = (T)v4.y; vi[2] = (T)v4.z;
+            Ai = (T)c4.x; Bi = (T)c4.y; Ci = (T)c4.z; Pi = (T)c4.w;
             sj = sid[j];
-            const double4_32a x4 = x[j];
-            xj[0] = x4.x; xj[1] = x4.y; xj[2] = x4.z;
+            const double4_32a xj4 = x[j];
+            xj[0] = xj4.x; xj[1] = xj4.y; xj[2] = xj4.z;
             double r64[3];
             const double d2 = exact_sep<D>(k, xi, xj, t.shift[jsl], r64);
 #pragma unroll
             for (int a = 0; a < 3; ++a) rr[a] = (T)r64[a];
             inv_d = (T)rsqrt(d2);
             d = (T)(d2 * (double)inv_d);
-            const double4_32a v4 = v[j], c4 = pc[j];
-            vj[0] = (T)v4.x; vj[1] = (T)v4.y; vj[2] = (T)v4.z;
-            Aj = (T)c4.x; Bj = (T)c4.y; Cj = (T)c4.z; Pj = (T)c4.w;
+            const double4_32a vj4 = v[j], cj4 = pc[j];
+            vj[0] = (T)vj4.x; vj[1] = (T)vj4.y; vj[2] = (T)vj4.z;
+            Aj = (T)cj4.x; Bj = (T)cj4.y; Cj = (T)cj4.z; Pj = (T)cj4.w;
             pidj = noise ? pid[j] : 0;
           } else {
-            const float4 o4 = off[j], v4 = vf[j], c4 = pcf[j];
-            sj = __float_as_int(o4.w);
+            const float4* oo = reinterpret_cast<const float4*>(own);
+            const float2* ow = reinterpret_cast<const float2*>(oo + 96);
+            const float4 o4 = oo[ow_l], v4 = oo[32 + ow_l], c4 = oo[64 + ow_l];
+            si = __float_as_int(o4.w);
+            pidi = __float_as_int(v4.w);
+            vi[0] = (T)v4.x; vi[1] = (T)v4.y; vi[2] = (T)v4.z;
+            Ai = (T)c4.x; Bi = (T)c4.y; Ci = (T)c4.z; Pi = (T)c4.w;
+            if (walls && k.wall_axis >= 0) wdi = ow[ow_l];
+            const float4 oj = off[j], vj4 = vf[j], cj4 = pcf[j];
+            sj = __float_as_int(oj.w);
             const float4 so = t.o[jsl];
-            rr[0] = (T)((oi.x - o4.x) - so.x);
-            rr[1] = (T)((oi.y - o4.y) - so.y);
-            rr[2] = (D == 3) ? (T)((oi.z - o4.z) - so.z) : T(0);
+            rr[0] = (T)((o4.x - oj.x) - so.x);
+            rr[1] = (T)((o4.y - oj.y) - so.y);
+            rr[2] = (D == 3) ? (T)((o4.z - oj.z) - so.z) : T(0);
             T d2 = rr[0] * rr[0] + rr[1] * rr[1];
             if (D == 3) d2 += rr[2] * rr[2];
             inv_d = (T)rsqrtf((float)d2);
             d = d2 * inv_d;
-            vj[0] = (T)v4.x; vj[1] = (T)v4.y; vj[2] = (T)v4.z;
-            Aj = (T)c4.x; Bj = (T)c4.y; Cj = (T)c4.z; Pj = (T)c4.w;
-            pidj = __float_as_int(v4.w);
+            vj[0] = (T)vj4.x; vj[1] = (T)vj4.y; vj[2] = (T)vj4.z;
+            Aj = (T)cj4.x; Bj = (T)cj4.y; Cj = (T)cj4.z; Pj = (T)cj4.w;
+            pidj = __float_as_int(vj4.w);
           }
-          has = !(si != 0 && sj != 0);  // w-w, c-c, c-w: no interaction
+          has = !(si != 0 && sj != 0);  // w-w, c-c, c-w: no interaction here
           if (has) {
-            T Ai = Ai0;
             if (si < 0 || sj < 0) {
               // fluid-wall pair (pp_interaction_fw.inc / _wf.inc)
               const int sw = (sj < 0) ? sj : si;
@@ -822,7 +884,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
                   xa = axis == 0 ? xi[0] : axis == 1 ? xi[1] : xi[2];
                   xb = axis == 0 ? xj[0] : axis == 1 ? xj[1] : xj[2];
                 } else {
-                  const double4_32a a4 = x[i], b4 = x[j];
+                  const double4_32a a4 = x[ii], b4 = x[j];
                   xa = axis == 0 ? a4.x : axis == 1 ? a4.y : a4.z;
                   xb = axis == 0 ? b4.x : axis == 1 ? b4.y : b4.z;
                 }
@@ -853,47 +915,71 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
             pair_scales<T>(k.rhs_force_type, Ci, Cj, s_i, s_j);
 #pragma unroll
             for (int a = 0; a < D; ++a) {
-              const T pa = g[a] * s_i;
-              if (FP64) {
-                acc[a] += pa;
-              } else {
-                const T y = pa - comp[a];
-                const T tt = acc[a] + y;
-                comp[a] = (tt - acc[a]) - y;
-                acc[a] = tt;
-              }
+              vis[a] = g[a] * s_i;
               vjs[a] = -g[a] * s_j;
             }
-            key = (jsl - CENTER) * kMaxCellCount + jq;
+            keyj = (jsl - CENTER) * kMaxCellCount + jq;
           }
         }
-        // deterministic combination of the partner shares of this round
+        // deterministic combination: lanes of this round with the same
+        // target are summed in lane order by the lowest of them
         const unsigned amask = __ballot_sync(0xffffffffu, has);
         if (has) {
-          const unsigned peers = __match_any_sync(amask, key);
-          const int leader = __ffs(peers) - 1;
-          T s0 = vjs[0], s1 = vjs[1], s2 = vjs[2];
-          if (peers != (1u << lane)) {
-            s0 = s1 = s2 = T(0);
-            for (unsigned mm = peers; mm; mm &= mm - 1) {
-              const int src = __ffs(mm) - 1;
-              s0 += __shfl_sync(peers, vjs[0], src);
-              s1 += __shfl_sync(peers, vjs[1], src);
-              s2 += __shfl_sync(peers, vjs[2], src);
+          // partner side
+          {
+            const unsigned peers = __match_any_sync(amask, keyj);
+            T s0 = vjs[0], s1 = vjs[1], s2 = vjs[2];
+            if (peers != (1u << lane)) {
+              s0 = s1 = s2 = T(0);
+              for (unsigned mm = peers; mm; mm &= mm - 1) {
+                const int src = __ffs(mm) - 1;
+                s0 += __shfl_sync(peers, vjs[0], src);
+                s1 += __shfl_sync(peers, vjs[1], src);
+                s2 += __shfl_sync(peers, vjs[2], src);
+              }
+            }
+            if (lane == __ffs(peers) - 1) {
+              const int s = jsl - CENTER;
+              if (t.count[jsl] <= CC) {
+                part[(s * 3 + 0) * CC + jq] += s0;
+                part[(s * 3 + 1) * CC + jq] += s1;
+                part[(s * 3 + 2) * CC + jq] += s2;
+              } else {
+                const size_t b0 = (size_t)t.start[jsl] + jq;
+                jp[((size_t)s * 3 + 0) * n + b0] += s0;
+                jp[((size_t)s * 3 + 1) * n + b0] += s1;
+                jp[((size_t)s * 3 + 2) * n + b0] += s2;
+              }
             }
           }
-          if (lane == leader) {
-            const int s = jsl - CENTER;
-            const int cs_ = t.count[jsl];
-            if (cs_ <= CC) {
-              part[wib][s][0][jq] += s0;
-              part[wib][s][1][jq] += s1;
-              part[wib][s][2][jq] += s2;
-            } else {
-              const size_t b0 = (size_t)t.start[jsl] + jq;
-              jp[((size_t)s * 3 + 0) * n + b0] += s0;
-              jp[((size_t)s * 3 + 1) * n + b0] += s1;
-              jp[((size_t)s * 3 + 2) * n + b0] += s2;
+          // owner side (Kahan-compensated in FP32)
+          {
+            const unsigned peers = __match_any_sync(amask, ow_l);
+            T s0 = vis[0], s1 = vis[1], s2 = vis[2];
+            if (peers != (1u << lane)) {
+              s0 = s1 = s2 = T(0);
+              for (unsigned mm = peers; mm; mm &= mm - 1) {
+                const int src = __ffs(mm) - 1;
+                s0 += __shfl_sync(peers, vis[0], src);
+                s1 += __shfl_sync(peers, vis[1], src);
+                s2 += __shfl_sync(peers, vis[2], src);
+              }
+            }
+            if (lane == __ffs(peers) - 1) {
+              const T sv[3] = {s0, s1, s2};
+#pragma unroll
+              for (int a = 0; a < 3; ++a) {
+                T& acc = acc_s[a * 32 + ow_l];
+                if (FP64) {
+                  acc += sv[a];
+                } else {
+                  T& cmp = comp_s[a * 32 + ow_l];
+                  const T y = sv[a] - cmp;
+                  const T tt = acc + y;
+                  cmp = (tt - acc) - y;
+                  acc = tt;
+                }
+              }
             }
           }
         }
@@ -901,8 +987,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       }
       if (act) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) jp[((size_t)NSF * 3 + a) * n + i] = acc[a];
+        for (int a = 0; a < 3; ++a) jp[((size_t)NSF * 3 + a) * n + i] = acc_s[a * 32 + lane];
       }
+      __syncwarp();
     }
     __syncwarp();
     for (int s = 0; s < NSF; ++s) {
@@ -910,8 +997,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       if (cs_ > CC) continue;
       for (int q = lane; q < cs_; q += 32)
 #pragma unroll
-        for (int a = 0; a < 3; ++a) jp[((size_t)s * 3 + a) * n + st_ + q] = part[wib][s][a][q];
+        for (int a = 0; a < 3; ++a)
+          jp[((size_t)s * 3 + a) * n + st_ + q] = part[(s * 3 + a) * CC + q];
     }
+    __syncwarp();
   }
 }
 
@@ -1034,17 +1123,29 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
     // symmetric sweep + per-particle gather
     const int n = (int)h->n;
     const int gbn = (n + 255) / 256;
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaFuncSetAttribute(k_force_sym<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kWarpsPerBlock * sym_warp_bytes<3, true>());
+      cudaFuncSetAttribute(k_force_sym<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kWarpsPerBlock * sym_warp_bytes<2, true>());
+      cudaFuncSetAttribute(k_force_sym<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kWarpsPerBlock * sym_warp_bytes<3, false>());
+      cudaFuncSetAttribute(k_force_sym<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kWarpsPerBlock * sym_warp_bytes<2, false>());
+      attr_set = true;
+    }
     if (fp64) {
       double* jp = (double*)h->jp;
       if (k.d == 3) {
-        k_force_sym<3, true><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
+        k_force_sym<3, true><<<g, bs, kWarpsPerBlock * sym_warp_bytes<3, true>(), s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
                                               h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
                                               h->pid, jp, (uint32_t)step, inv_sqdt);
         if (n > 0)
           k_force_gather<3, true><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid, h->f,
                                                       fuse_mode, dt, h->v2, h->d_err);
       } else {
-        k_force_sym<2, true><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
+        k_force_sym<2, true><<<g, bs, kWarpsPerBlock * sym_warp_bytes<2, true>(), s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
                                               h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
                                               h->pid, jp, (uint32_t)step, inv_sqdt);
         if (n > 0)
@@ -1054,14 +1155,14 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
     } else {
       float* jp = (float*)h->jp;
       if (k.d == 3) {
-        k_force_sym<3, false><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
+        k_force_sym<3, false><<<g, bs, kWarpsPerBlock * sym_warp_bytes<3, false>(), s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
                                                h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
                                                h->pid, jp, (uint32_t)step, (float)inv_sqdt);
         if (n > 0)
           k_force_gather<3, false><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid,
                                                        h->f, fuse_mode, dt, h->v2, h->d_err);
       } else {
-        k_force_sym<2, false><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
+        k_force_sym<2, false><<<g, bs, kWarpsPerBlock * sym_warp_bytes<2, false>(), s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
                                                h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
                                                h->pid, jp, (uint32_t)step, (float)inv_sqdt);
         if (n > 0)
