@@ -1119,8 +1119,10 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
   if (k.noise && !(dt > 0.0)) return set_error(h, MCFG_EINVAL, "random force needs dt > 0");
   const double inv_sqdt = (k.noise && dt > 0.0) ? 1.0 / sqrt(dt) : 0.0;
   const int bs = kWarpsPerBlock * 32;
-  if (!k.stress && h->jp) {
-    // symmetric sweep + per-particle gather
+  if (!k.stress && h->jp && fp64) {
+    // symmetric sweep + per-particle gather: halves the FP64 pair work; the
+    // FP32 path keeps the two-sided sweep, which is faster there (the
+    // symmetric sweep's shared-memory partner sums cap its occupancy)
     const int n = (int)h->n;
     const int gbn = (n + 255) / 256;
     static bool attr_set = false;

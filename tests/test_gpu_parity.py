@@ -171,7 +171,7 @@ def test_stress_tensor_and_statistics(gpu_lib):
 @pytest.mark.parametrize("maker", ["jit3d", "walls", "jit2d"])
 def test_symmetric_sweep_matches_gather_sweep(gpu_lib, precision, maker):
     # the stress tensor selects the two-sided gather sweep, without it the
-    # symmetric (each pair once) sweep runs: same accelerations
+    # FP64 path runs the symmetric (each pair once) sweep: same accelerations
     w = {"jit3d": jittered_3d, "walls": lambda: make_golden.workload("walls_small"),
          "jit2d": jittered_2d}[maker]()
     res = []
