@@ -225,6 +225,26 @@ void* mcfg_get_stream(mcfg_handle* h);
 int mcfg_set_profiling(mcfg_handle* h, int mode);
 int mcfg_get_phase_times(mcfg_handle* h, double* ms, int64_t* counts);
 
+/* Number density of n particles for callers that cannot allocate device
+ * memory (a caching allocator holding its lock, a host that hands over only
+ * buffers it registered itself, a fixed device-memory budget).  This entry
+ * point has no counterpart in the reference: it is an allocation-free
+ * variant of mcfg_compute_density.  x [n*d], m [n], id [n*2] and the output
+ * rho [n] are DEVICE pointers owned by the caller, laid out like the host
+ * arrays of mcfg_upload; stream is a cudaStream_t (NULL = default stream)
+ * and the call is asynchronous on it.  Nothing is allocated: the cell list
+ * lives in a fixed array inside the library (about 1.3 MB, held on every GPU
+ * that loads the library until the process exits), so n <= 65,536 and the
+ * mesh may have at most 65,536 real cells; larger inputs return MCFG_EINVAL.
+ * The first call on a device looks up that array's device address (with the
+ * device current); make that first call before any stream capture.  All
+ * calls share the array: calls whose GPU work overlaps race, so serialise
+ * them.  Errors: mcfg_noalloc_error(). */
+int mcfg_density_noalloc(const mcfg_params* params, int32_t n, const double* x,
+                         const double* m, const int32_t* id, double* rho,
+                         void* stream);
+const char* mcfg_noalloc_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,7 +19,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libmcfg.so"
-SOURCES = ["mcfg_api.cu", "cell_list.cu", "pair_kernels.cu", "update.cu"]
+SOURCES = ["mcfg_api.cu", "cell_list.cu", "pair_kernels.cu", "update.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

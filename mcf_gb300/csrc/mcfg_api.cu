@@ -129,7 +129,11 @@ void free_all(Handle* h) {
   h->device_bytes = 0;
 }
 
-const char* validate(const mcfg_params* p) {
+}  // namespace
+
+namespace mcfg {
+
+const char* validate_params(const mcfg_params* p) {
   if (!p) return "params is NULL";
   if (p->num_dim != 2 && p->num_dim != 3) return "num_dim must be 2 or 3";
   if (!(p->cut_off > 0.0)) return "cut_off must be positive";
@@ -160,9 +164,15 @@ const char* validate(const mcfg_params* p) {
   return nullptr;
 }
 
-void fill_consts(Handle* h) {
-  const mcfg_params& p = h->p;
-  Consts& k = h->k;
+}  // namespace mcfg
+
+namespace {
+
+}  // namespace
+
+namespace mcfg {
+
+void make_consts(const mcfg_params& p, Consts& k) {
   memset(&k, 0, sizeof k);
   k.d = p.num_dim;
   const double cf = p.cell_factor > 0.0 ? p.cell_factor : 1.0001;
@@ -244,6 +254,12 @@ void fill_consts(Handle* h) {
   k.body_force_type = p.body_force_type;
   for (int a = 0; a < 3; ++a) k.body_force[a] = p.body_force[a];
 }
+
+}  // namespace mcfg
+
+namespace {
+
+void fill_consts(Handle* h) { make_consts(h->p, h->k); }
 
 __global__ void k_upload(int n, int d, const double* __restrict__ hx, const double* __restrict__ hv,
                          const double* __restrict__ hm, const int* __restrict__ hid,
@@ -415,7 +431,7 @@ const char* mcfg_create_error(void) {
 int mcfg_create(const mcfg_params* params, mcfg_handle** out) {
   if (!out) return MCFG_EINVAL;
   *out = nullptr;
-  const char* msg = validate(params);
+  const char* msg = validate_params(params);
   if (msg) {
     std::lock_guard<std::mutex> lk(g_create_mu);
     g_create_err = msg;

@@ -171,6 +171,10 @@ struct PhaseScope {
 // accumulate completed phase events (call after a stream synchronize)
 void resolve_phases(Handle* h);
 
+// parameter checks and derived constants shared by all entry points
+const char* validate_params(const mcfg_params* p);
+void make_consts(const mcfg_params& p, Consts& k);
+
 // set err and return code
 int set_error(Handle* h, int code, const std::string& msg);
 int cuda_check(Handle* h, cudaError_t e, const char* what);
