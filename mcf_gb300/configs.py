@@ -161,4 +161,20 @@ def c3_poiseuille_3d(n_side: int = 100, precision: int = PRECISION_FP64, walls: 
     return _finish(f"C3 3D {n_side}^3 Poiseuille", p, [1.0] * 3, 0.0, 0.0, seed, 5e-5, 5000)
 
 
-WORKLOADS = {"c1": c1_poiseuille_2d, "c2": c2_fluctuating_3d, "c3": c3_poiseuille_3d}
+def c5_oldroyd_b_2d(n_side: int = 128, precision: int = PRECISION_FP64, seed: int = BASE_SEED + 5,
+                    amplitude: float = 0.01) -> Workload:
+    """2D 128x128 periodic Oldroyd-B shear: dx = 1 (L = 128; with L = 1 the
+    explicit scheme at dt = 1e-3 is 65x past MCF's viscous limit), solvent
+    eta_s = 0.5, G = n_p kt_p = 0.5 and tau = 1 (eta_p = G tau = 0.5), c = 10,
+    kT = 1e-4 with the Philox increments, body force g_x sin(2 pi y / L_y)
+    (body_force_type 3; amplitude 0.01 keeps the Mach number small on the
+    L = 128 box), dt = 1e-3, 200 steps; conformation tensor starts at I."""
+    L = float(n_side)
+    p = make_params(**_box(2, 0.0, L), cut_off=3.0, c=10.0, eta=0.5, kt=1e-4, Brownian=1,
+                    Newtonian=0, tau=1.0, n_p=1.0, kt_p=0.5, body_force_type=3,
+                    body_force=[amplitude, 0.0, 0.0], dt=1e-3, precision=precision, seed=seed)
+    return _finish(f"C5 2D {n_side}^2 Oldroyd-B", p, [1.0, 1.0], 0.0, 0.0, seed, 1e-3, 200)
+
+
+WORKLOADS = {"c1": c1_poiseuille_2d, "c2": c2_fluctuating_3d, "c3": c3_poiseuille_3d,
+             "c5": c5_oldroyd_b_2d}

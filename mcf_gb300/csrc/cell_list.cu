@@ -143,6 +143,8 @@ __global__ void k_cell_finalize(Consts k, const int* __restrict__ start,
                                 int* __restrict__ pid_out, int* __restrict__ sid_out,
                                 int* __restrict__ hidx_out, float4* __restrict__ off,
                                 int* __restrict__ cell_of, float2* __restrict__ wd,
+                                const double* __restrict__ ct_in, const double* __restrict__ act_in,
+                                double* __restrict__ ct_out, double* __restrict__ act_out,
                                 unsigned* __restrict__ err) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -182,6 +184,13 @@ __global__ void k_cell_finalize(Consts k, const int* __restrict__ start,
     of.z = (D == 3) ? (float)(xp.z - org[2]) : 0.0f;
     of.w = __int_as_float(sid_in[o]);  // species id rides in the w lane
     off[dst] = of;
+    if (ct_in != nullptr) {
+      const int n = k.n;
+      for (int cc = 0; cc < D * D; ++cc) {
+        ct_out[(size_t)cc * n + dst] = ct_in[(size_t)cc * n + o];
+        act_out[(size_t)cc * n + dst] = act_in[(size_t)cc * n + o];
+      }
+    }
     if (wd != nullptr && k.wall_axis >= 0) {
       // distances to the two faces of the wall axis, formed in FP64 and
       // rounded once (boundary_noslip_solid.F90:200-206 uses x - x_sur)
@@ -220,11 +229,13 @@ int build_cell_list(Handle* h) {
     if (k.d == 3)
       k_cell_finalize<3><<<gw, warps_per_block * 32, 0, s>>>(
           k, h->cell_start, h->order, h->hidx, h->x, h->v, h->f, h->m, h->pid, h->sid, h->x2,
-          h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->off, h->cell_of, h->wd, h->d_err);
+          h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->off, h->cell_of, h->wd, h->ct, h->act,
+          h->ct2, h->act2, h->d_err);
     else
       k_cell_finalize<2><<<gw, warps_per_block * 32, 0, s>>>(
           k, h->cell_start, h->order, h->hidx, h->x, h->v, h->f, h->m, h->pid, h->sid, h->x2,
-          h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->off, h->cell_of, h->wd, h->d_err);
+          h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->off, h->cell_of, h->wd, h->ct, h->act,
+          h->ct2, h->act2, h->d_err);
     h->launches += 2;
     std::swap(h->x, h->x2);
     std::swap(h->v, h->v2);
@@ -233,6 +244,10 @@ int build_cell_list(Handle* h) {
     std::swap(h->pid, h->pid2);
     std::swap(h->sid, h->sid2);
     std::swap(h->hidx, h->hidx2);
+    if (h->ct) {
+      std::swap(h->ct, h->ct2);
+      std::swap(h->act, h->act2);
+    }
   }
   if (cuda_check(h, cudaGetLastError(), "cell list launch")) return MCFG_ECUDA;
   return MCFG_OK;

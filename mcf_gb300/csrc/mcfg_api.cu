@@ -111,7 +111,8 @@ void free_all(Handle* h) {
                   h->x2, h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->key, h->rank,
                   h->cnt, h->cell_start, h->scan_part, h->order, h->off, h->cell_of, h->nl,
                   h->ncount, h->nhs, h->jp, h->pc, h->pcf, h->vf, h->wd, h->red, h->d_err, h->d_stats, h->d_pairs,
-                  h->up_x, h->up_v, h->up_m, h->up_id};
+                  h->up_x, h->up_v, h->up_m, h->up_id, h->ct, h->act, h->vgt, h->ct2,
+                  h->act2, h->qq};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   h->x = h->v = h->f = h->x2 = h->v2 = h->f2 = nullptr;
@@ -120,6 +121,8 @@ void free_all(Handle* h) {
   h->key = h->rank = h->cnt = h->cell_start = h->scan_part = h->order = h->cell_of = nullptr;
   h->ncount = h->d_stats = h->up_id = h->nhs = nullptr;
   h->jp = nullptr;
+  h->ct = h->act = h->vgt = h->ct2 = h->act2 = nullptr;
+  h->qq = nullptr;
   h->off = h->pcf = h->vf = nullptr;
   h->wd = nullptr;
   h->pc = nullptr;
@@ -146,7 +149,9 @@ const char* validate_params(const mcfg_params* p) {
   if (p->body_force_type < 0 || p->body_force_type > 3) return "body_force_type must be 0..3";
   if (p->precision != MCFG_PRECISION_FP64 && p->precision != MCFG_PRECISION_FP32_MIXED)
     return "precision must be MCFG_PRECISION_FP64 or MCFG_PRECISION_FP32_MIXED";
-  if (!p->Newtonian) return "non-Newtonian (Oldroyd-B) model is not in this build";
+  if (!p->Newtonian && p->rhs_force_type != 3)
+    return "the Oldroyd-B model needs rhs_force_type 3 (Hu-Adams)";
+  if (!p->Newtonian && !(std::fabs(p->tau) > 1e-14)) return "tau should not be zero";
   for (int a = 0; a < p->num_dim; ++a) {
     const int lo = p->bcdef[2 * a], hi = p->bcdef[2 * a + 1];
     if ((lo != MCFG_BC_PERIODIC && lo != MCFG_BC_WALL_SOLID) ||
@@ -249,6 +254,10 @@ void make_consts(const mcfg_params& p, Consts& k) {
       k.wall_vf[f][a] = (float)p.wall_v[f][a];
     }
   k.stress = p.stress_tensor ? 1 : 0;
+  k.newtonian = p.Newtonian ? 1 : 0;
+  k.G = p.n_p * p.kt_p;
+  k.tau = p.tau;
+  k.inv_tau = p.Newtonian ? 0.0 : 1.0 / p.tau;
   k.key0 = (uint32_t)p.seed;
   k.key1 = (uint32_t)(p.seed >> 32);
   k.body_force_type = p.body_force_type;
@@ -260,6 +269,19 @@ void make_consts(const mcfg_params& p, Consts& k) {
 namespace {
 
 void fill_consts(Handle* h) { make_consts(h->p, h->k); }
+
+// conformation tensor: host (d*d, N) interleaved -> device [c][n]; identity
+// when no host array is given (particles_init_partial_inter.F90:145-148)
+__global__ void k_upload_ct(int n, int d, const double* __restrict__ hct, double* __restrict__ ct,
+                            double* __restrict__ act) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int d2 = d * d;
+  for (int c = 0; c < d2; ++c) {
+    ct[(size_t)c * n + i] = hct ? hct[(size_t)i * d2 + c] : ((c % (d + 1)) == 0 ? 1.0 : 0.0);
+    act[(size_t)c * n + i] = 0.0;
+  }
+}
 
 __global__ void k_upload(int n, int d, const double* __restrict__ hx, const double* __restrict__ hv,
                          const double* __restrict__ hm, const int* __restrict__ hid,
@@ -346,6 +368,16 @@ int ensure_capacity(Handle* h, int64_t n64) {
       if ((rc = dalloc(h, &h->pcf, cap)) || (rc = dalloc(h, &h->vf, cap)) ||
           (rc = dalloc(h, &h->wd, cap)))
         return rc;
+    }
+    if (!h->p.Newtonian) {
+      const size_t d2 = (size_t)d * d;
+      const size_t elt = (h->p.precision == MCFG_PRECISION_FP64) ? 8 : 4;
+      char* q = nullptr;
+      if ((rc = dalloc(h, &h->ct, cap * d2)) || (rc = dalloc(h, &h->act, cap * d2)) ||
+          (rc = dalloc(h, &h->vgt, cap * d2)) || (rc = dalloc(h, &h->ct2, cap * d2)) ||
+          (rc = dalloc(h, &h->act2, cap * d2)) || (rc = dalloc(h, &q, cap * (1 + d2) * elt)))
+        return rc;
+      h->qq = q;
     }
     if (h->p.stress_tensor) {
       if ((rc = dalloc(h, &h->st, cap * (size_t)(d * d)))) return rc;
@@ -510,7 +542,7 @@ int mcfg_upload(mcfg_handle* h, int64_t n, const double* x, const double* v, con
   GUARD(h);
   if (n < 0 || (n > 0 && (!x || !v || !m || !id)))
     return set_error(h, MCFG_EINVAL, "mcfg_upload: NULL array");
-  if (ct && h->p.Newtonian == 0) return set_error(h, MCFG_ENOTSUP, "conformation tensor");
+  if (ct && h->p.Newtonian) return set_error(h, MCFG_EINVAL, "conformation tensor of a Newtonian run");
   TRY(ensure_capacity(h, n));
   const int d = h->p.num_dim;
   h->n = n;
@@ -530,6 +562,19 @@ int mcfg_upload(mcfg_handle* h, int64_t n, const double* x, const double* v, con
     k_upload<<<gb, tb, 0, s>>>((int)n, d, h->up_x, h->up_v, h->up_m, h->up_id, h->x, h->v, h->f,
                                h->m, h->pid, h->sid, h->hidx);
     h->launches++;
+    if (!h->p.Newtonian) {
+      double* hct = nullptr;
+      if (ct) {
+        // staged through up_x (n*9 doubles)
+        if (cuda_check(h, cudaStreamSynchronize(s), "upload sync") ||
+            cuda_check(h, cudaMemcpyAsync(h->up_x, ct, sizeof(double) * (size_t)(n * d * d),
+                                          cudaMemcpyHostToDevice, s), "upload ct"))
+          return MCFG_ECUDA;
+        hct = h->up_x;
+      }
+      k_upload_ct<<<gb, tb, 0, s>>>((int)n, d, hct, h->ct, h->act);
+      h->launches++;
+    }
     if (cuda_check(h, cudaGetLastError(), "upload kernel")) return MCFG_ECUDA;
     if (h->p.stress_tensor)
       if (cuda_check(h, cudaMemsetAsync(h->st, 0, sizeof(double) * (size_t)(n * d * d), s),
@@ -681,7 +726,7 @@ int mcfg_download(mcfg_handle* h, double* x, double* v, double* rho, double* p, 
                   double* ct, double* s) {
   GUARD(h);
   if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
-  if (ct) return set_error(h, MCFG_ENOTSUP, "conformation tensor not in this build");
+  if (ct && h->p.Newtonian) return set_error(h, MCFG_EINVAL, "no conformation tensor (Newtonian)");
   if (s && !h->p.stress_tensor) return set_error(h, MCFG_EINVAL, "stress_tensor is off");
   const int n = (int)h->n, d = h->p.num_dim;
   if (n == 0) return MCFG_OK;
@@ -709,6 +754,14 @@ int mcfg_download(mcfg_handle* h, double* x, double* v, double* rho, double* p, 
   if (f) TRY(vec_out(h->f, f));
   if (rho) TRY(sca_out(h->rho, rho));
   if (p) TRY(sca_out(h->pr, p));
+  if (ct) {
+    k_download_tensor<<<gb, tb, 0, st>>>(n, d * d, h->hidx, h->ct, stage);
+    h->launches++;
+    if (cuda_check(h, cudaMemcpyAsync(ct, stage, sizeof(double) * (size_t)n * d * d,
+                                      cudaMemcpyDeviceToHost, st), "download ct") ||
+        cuda_check(h, cudaStreamSynchronize(st), "download sync"))
+      return MCFG_ECUDA;
+  }
   if (s) {
     k_download_tensor<<<gb, tb, 0, st>>>(n, d * d, h->hidx, h->st, stage);
     h->launches++;

@@ -61,6 +61,9 @@ struct Consts {
   double min_phys[3], max_phys[3];
   double wall_v[6][3];
   int stress;
+  // Oldroyd-B conformation model (Newtonian == 0)
+  int newtonian;
+  double G, tau, inv_tau;  // G = n_p kt_p
   uint32_t key0, key1;   // Philox key (seed)
   int body_force_type;
   double body_force[3];
@@ -96,6 +99,12 @@ struct Handle {
   double* rho = nullptr;
   double* pr = nullptr;
   double* st = nullptr;   // stress, [d*d][cap] component-major
+  // Oldroyd-B state, [d*d][cap] component-major (component a + d*b)
+  double* ct = nullptr;   // conformation tensor
+  double* act = nullptr;  // d(ct)/dt of the last right-hand side
+  double* vgt = nullptr;  // velocity gradient tensor
+  double *ct2 = nullptr, *act2 = nullptr;
+  void* qq = nullptr;     // per-particle 1/n and G*ct/n^2, [1+d*d][cap] (T)
   // double buffers for the permutation
   double4_32a *x2 = nullptr, *v2 = nullptr, *f2 = nullptr;
   double* m2 = nullptr;

@@ -38,6 +38,14 @@ struct NbTable {
   float4 o[kMaxStencil];   // stencil offset x cell side (FP32), per slot
 };
 
+// Oldroyd-B arrays handed to the sweeps (all null for a Newtonian run).
+struct NN {
+  const double* ct;  // conformation tensor [d*d][n]
+  double* act;       // d(ct)/dt [d*d][n]
+  double* vgt;       // velocity gradient [d*d][n]
+  void* qq;          // 1/n and G*ct/n^2, [1+d*d][n] in the path's type
+};
+
 // cell == k.ncell is the bin of particles without a real cell: it has no
 // neighbours (PPM gives such particles no box, ppm_util_rank3d.F90:463-473).
 template <int D>
@@ -146,7 +154,32 @@ __device__ __forceinline__ void write_particle_records(const Consts& k, int i, d
                                                        double* __restrict__ pr,
                                                        double4_32a* __restrict__ pc,
                                                        float4* __restrict__ pcf,
-                                                       float4* __restrict__ vf) {
+                                                       float4* __restrict__ vf, const NN& nn) {
+  if (!k.newtonian) {
+    // Oldroyd-B: pressure tensor (p + G) I - G c
+    // (particles_compute_pressure_tensor.F90:88-133) as A = (p + G)/n^2 and
+    // Q = G c / n^2, with 1/n for the velocity gradient
+    const double r_eos = (k.rhs_density_type == 1) ? rho : rho * m;
+    const double p = eos_pressure(k, r_eos);
+    pr[i] = p;
+    const double inv = 1.0 / rho;
+    const double inv2 = inv * inv;
+    const int n = k.n, d2 = k.d * k.d;
+    if (FP64) {
+      pc[i] = make_double4_32a((p + k.G) * inv2, inv2, 1.0 / m, p);
+      double* q = (double*)nn.qq;
+      q[i] = inv;
+      for (int cc = 0; cc < d2; ++cc) q[(size_t)(1 + cc) * n + i] = k.G * nn.ct[(size_t)cc * n + i] * inv2;
+    } else {
+      pcf[i] = make_float4((float)((p + k.G) * inv2), (float)inv2, (float)(1.0 / m), (float)p);
+      vf[i] = make_float4((float)v.x, (float)v.y, (float)v.z, __int_as_float(pid));
+      float* q = (float*)nn.qq;
+      q[i] = (float)inv;
+      for (int cc = 0; cc < d2; ++cc)
+        q[(size_t)(1 + cc) * n + i] = (float)(k.G * nn.ct[(size_t)cc * n + i] * inv2);
+    }
+    return;
+  }
   if (FP64) {
     const double r_eos = (k.rhs_density_type == 1) ? rho : rho * m;
     const double p = eos_pressure(k, r_eos);
@@ -190,7 +223,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
               int* __restrict__ nhs, int cap, double* __restrict__ rho, double* __restrict__ pr,
               double4_32a* __restrict__ pc, float4* __restrict__ pcf, float4* __restrict__ vf,
               int with_pressure, unsigned* __restrict__ err, int* __restrict__ stats,
-              unsigned long long* __restrict__ pairs) {
+              unsigned long long* __restrict__ pairs, NN nn) {
   constexpr int NS = (D == 3) ? 27 : 9;
   constexpr int CENTER = (D == 3) ? 13 : 4;
   __shared__ NbTable tab[kWarpsPerBlock];
@@ -322,7 +355,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       rho[i] = rho_out;
       if (!(rho_out > 0.0)) atomicOr(err, kErrZeroDensity);
       if (with_pressure)
-        write_particle_records<FP64>(k, i, rho_out, mi, pid[i], v[i], pr, pc, pcf, vf);
+        write_particle_records<FP64>(k, i, rho_out, mi, pid[i], v[i], pr, pc, pcf, vf, nn);
     }
   }
 #pragma unroll
@@ -340,10 +373,10 @@ template <bool FP64>
 __global__ void k_pressure(Consts k, const double* __restrict__ rho, const double* __restrict__ m,
                            const int* __restrict__ pid, const double4_32a* __restrict__ v,
                            double* __restrict__ pr, double4_32a* __restrict__ pc,
-                           float4* __restrict__ pcf, float4* __restrict__ vf) {
+                           float4* __restrict__ pcf, float4* __restrict__ vf, NN nn) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= k.n) return;
-  write_particle_records<FP64>(k, i, rho[i], m[i], pid[i], v[i], pr, pc, pcf, vf);
+  write_particle_records<FP64>(k, i, rho[i], m[i], pid[i], v[i], pr, pc, pcf, vf, nn);
 }
 
 // ---------------------------------------------------------------------------
@@ -394,10 +427,39 @@ __device__ __forceinline__ void force_epilogue(const Consts& k, int i, int si, c
   }
 }
 
+// Oldroyd-B per-particle update after the pair sweep: store the velocity
+// gradient L, act = c L^T + L c - (c - I)/tau (particles_compute_act.F90:
+// 112-156) and, inside a VV step, the second half step ct += act dt/2
+// (particles_integrate_ct.F90:66-68), all in FP64.
+template <int D>
+__device__ __forceinline__ void nn_epilogue(const Consts& k, const NN& nn, int i, const double* L,
+                                            int fuse_mode, double dt) {
+  const int n = k.n;
+#pragma unroll
+  for (int cc = 0; cc < D * D; ++cc) nn.vgt[(size_t)cc * n + i] = L[cc];
+  if (fuse_mode < kForceBody) return;
+  double cm[D * D];
+#pragma unroll
+  for (int cc = 0; cc < D * D; ++cc) cm[cc] = nn.ct[(size_t)cc * n + i];
+#pragma unroll
+  for (int b = 0; b < D; ++b)
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      double t = 0.0;
+#pragma unroll
+      for (int q = 0; q < D; ++q) t = t + cm[a + D * q] * L[b + D * q] + L[a + D * q] * cm[q + D * b];
+      const double act = t - (cm[a + D * b] - (a == b ? 1.0 : 0.0)) * k.inv_tau;
+      nn.act[(size_t)(a + D * b) * n + i] = act;
+      if (fuse_mode == kForceBodyKick)
+        ((double*)nn.ct)[(size_t)(a + D * b) * n + i] =
+            __dadd_rn(cm[a + D * b], __dmul_rn(__dmul_rn(act, dt), 0.5));
+    }
+}
+
 // ---------------------------------------------------------------------------
 // FP64 force sweep
 // ---------------------------------------------------------------------------
-template <int D>
+template <int D, bool NNW>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     k_force64(Consts k, const int* __restrict__ cell_start, const uint16_t* __restrict__ nl,
               const int* __restrict__ ncount, const double4_32a* __restrict__ x,
@@ -405,8 +467,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
               const int* __restrict__ sid, const int* __restrict__ pid,
               double4_32a* __restrict__ f, double* __restrict__ st, int fuse_mode, double dt,
               double4_32a* __restrict__ v_out, uint32_t step, double inv_sqdt,
-              unsigned* __restrict__ err) {
+              unsigned* __restrict__ err, NN nn) {
   constexpr int CENTER = (D == 3) ? 13 : 4;
+  constexpr int D2 = D * D;
   using T = double;
   __shared__ NbTable tab[kWarpsPerBlock];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -426,6 +489,15 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       const double xi[3] = {xi4.x, xi4.y, xi4.z};
       const double4_32a v4i = v[i];
       const double4_32a ci = pc[i];
+      constexpr bool nnw = NNW;  // Oldroyd-B terms compiled only when used
+      const double* qq = (const double*)nn.qq;
+      T qi[1 + D2], L[D2];
+#pragma unroll
+      for (int cc = 0; cc < D2; ++cc) L[cc] = 0;
+      if (nnw) {
+#pragma unroll
+        for (int cc = 0; cc <= D2; ++cc) qi[cc] = qq[(size_t)cc * n + i];
+      }
       T acc[3] = {0, 0, 0};
       T sacc[9];
 #pragma unroll
@@ -447,10 +519,19 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         T vi[3] = {v4i.x, v4i.y, v4i.z};
         T vj[3] = {v4.x, v4.y, v4.z};
         const double4_32a cj = pc[j];
-        T Ai = ci.x, Aj = cj.x;
+        T Ai = ci.x, Aj = cj.x, Bi = ci.y, Bj = cj.y;
+        T qj[1 + D2], qie[1 + D2];
+        if (nnw) {
+#pragma unroll
+          for (int cc = 0; cc <= D2; ++cc) {
+            qj[cc] = qq[(size_t)cc * n + j];
+            qie[cc] = qi[cc];
+          }
+        }
         if (si < 0 || sj < 0) {
           // fluid-wall pair: wall particle takes the Morris no-slip velocity
-          // and the fluid pressure (pp_interaction_fw.inc / _wf.inc)
+          // and the fluid pressure (pp_interaction_fw.inc / _wf.inc); in the
+          // Oldroyd-B model also the fluid density and pressure tensor
           const int sw = (sj < 0) ? sj : si;
           const int axis = (-sw - 1) >> 1;
           const double xin = axis == 0 ? xi[0] : axis == 1 ? xi[1] : xi[2];
@@ -460,12 +541,26 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
             wall_noslip<T, D>(k, xin, xjn, vi, sj, vw);
 #pragma unroll
             for (int a = 0; a < D; ++a) vj[a] = vw[a];
-            Aj = boundary_A<T>(k.rhs_force_type, ci.w, cj.y);
+            if (nnw) {
+              Aj = Ai;
+              Bj = Bi;
+#pragma unroll
+              for (int cc = 0; cc <= D2; ++cc) qj[cc] = qi[cc];
+            } else {
+              Aj = boundary_A<T>(k.rhs_force_type, ci.w, cj.y);
+            }
           } else {
             wall_noslip<T, D>(k, xjn, xin, vj, si, vw);
 #pragma unroll
             for (int a = 0; a < D; ++a) vi[a] = vw[a];
-            Ai = boundary_A<T>(k.rhs_force_type, cj.w, ci.y);
+            if (nnw) {
+              Ai = Aj;
+              Bi = Bj;
+#pragma unroll
+              for (int cc = 0; cc <= D2; ++cc) qie[cc] = qj[cc];
+            } else {
+              Ai = boundary_A<T>(k.rhs_force_type, cj.w, ci.y);
+            }
           }
         }
         const T gw = kernel_gradw<T>(k, d);
@@ -475,7 +570,24 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         float z[6];
         if (noise) pair_normals<D>(k.key0, k.key1, step, pidi, pid[j], z);
         T pa[3], si_s, sj_s;
-        pair_force<T, D>(k, r, inv_d, vij, Ai, ci.y, Aj, cj.y, gw, noise, z, inv_sqdt, pa);
+        pair_force<T, D>(k, r, inv_d, vij, Ai, Bi, Aj, Bj, gw, noise, z, inv_sqdt, pa);
+        if (nnw) {
+          // polymer part of the pressure-tensor force,
+          // rhs_force_ff_non_Newtonian_HuAdams.F90:95-110, and the velocity
+          // gradient of pp_vgt_ip.inc
+#pragma unroll
+          for (int b = 0; b < D; ++b) {
+            T s_ = 0;
+#pragma unroll
+            for (int a = 0; a < D; ++a) s_ += (qie[1 + a + D * b] + qj[1 + a + D * b]) * r[a];
+            pa[b] += gw * inv_d * s_;
+          }
+          const T fac = gw * qie[0] * inv_d;
+#pragma unroll
+          for (int b = 0; b < D; ++b)
+#pragma unroll
+            for (int a = 0; a < D; ++a) L[a + D * b] += (vj[a] - vi[a]) * r[b] * fac;
+        }
         pair_scales<T>(k.rhs_force_type, ci.z, cj.z, si_s, sj_s);
 #pragma unroll
         for (int a = 0; a < D; ++a) pa[a] *= si_s;
@@ -493,6 +605,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 #pragma unroll
         for (int a = 0; a < D * D; ++a) st[(size_t)a * n + i] = sacc[a];
       }
+      if (nnw) nn_epilogue<D>(k, nn, i, L, fuse_mode, dt);
       force_epilogue<D>(k, i, si, xi, acc[0], acc[1], D == 3 ? acc[2] : 0.0, fuse_mode, dt, v,
                         f, v_out, err);
     }
@@ -521,7 +634,7 @@ __device__ __forceinline__ JData load_j(const NbTable& t, int ent, const float4*
   return d;
 }
 
-template <int D>
+template <int D, bool NNW>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
     k_force32(Consts k, const int* __restrict__ cell_start, const uint16_t* __restrict__ nl,
               const int* __restrict__ ncount, const float4* __restrict__ off,
@@ -530,8 +643,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
               const float2* __restrict__ wd, double4_32a* __restrict__ f,
               double* __restrict__ st, int fuse_mode, double dt,
               double4_32a* __restrict__ v_out, uint32_t step, float inv_sqdt,
-              unsigned* __restrict__ err) {
+              unsigned* __restrict__ err, NN nn) {
   constexpr int CENTER = (D == 3) ? 13 : 4;
+  constexpr int D2 = D * D;
   using T = float;
   __shared__ NbTable tab[kWarpsPerBlock];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -552,6 +666,15 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
       const int pidi = __float_as_int(v4i.w);
       const float4 ci = pcf[i];
       const float2 wdi = (walls && k.wall_axis >= 0) ? wd[i] : make_float2(0.f, 0.f);
+      constexpr bool nnw = NNW;  // Oldroyd-B terms compiled only when used
+      const float* qq = (const float*)nn.qq;
+      T qi[1 + D2], L[D2];
+#pragma unroll
+      for (int cc = 0; cc < D2; ++cc) L[cc] = 0.f;
+      if (nnw) {
+#pragma unroll
+        for (int cc = 0; cc <= D2; ++cc) qi[cc] = qq[(size_t)cc * n + i];
+      }
       T acc[3] = {0.f, 0.f, 0.f}, comp[3] = {0.f, 0.f, 0.f};
       T sacc[9];
 #pragma unroll
@@ -581,12 +704,21 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
         const T d = d2 * inv_d;
         T vi[3] = {v4i.x, v4i.y, v4i.z};
         T vj[3] = {cur.v.x, cur.v.y, cur.v.z};
-        T Ai = ci.x, Aj = cur.c.x;
+        T Ai = ci.x, Aj = cur.c.x, Bi = ci.y, Bj = cur.c.y;
+        T qj[1 + D2], qie[1 + D2];
+        if (nnw) {
+#pragma unroll
+          for (int cc = 0; cc <= D2; ++cc) {
+            qj[cc] = qq[(size_t)cc * n + cur.j];
+            qie[cc] = qi[cc];
+          }
+        }
         if (si < 0 || sj < 0) {
           // fluid-wall pair: the wall particle takes the Morris no-slip
-          // velocity and the fluid pressure (pp_interaction_fw.inc / _wf.inc);
-          // face distances come from the FP64-rounded per-particle values
-          // (one wall axis) or from the FP64 positions (several)
+          // velocity and the fluid pressure (pp_interaction_fw.inc / _wf.inc),
+          // in the Oldroyd-B model also the fluid density and pressure
+          // tensor; face distances come from the FP64-rounded per-particle
+          // values (one wall axis) or from the FP64 positions (several)
           const int sw = (sj < 0) ? sj : si;
           const int face = -sw;
           const bool lower = (face & 1) != 0;
@@ -612,12 +744,26 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
             wall_noslip_dist<T, D>(k, df, dw, vi, sj, vw);
 #pragma unroll
             for (int a = 0; a < D; ++a) vj[a] = vw[a];
-            Aj = boundary_A<T>(k.rhs_force_type, ci.w, cur.c.y);
+            if (nnw) {
+              Aj = Ai;
+              Bj = Bi;
+#pragma unroll
+              for (int cc = 0; cc <= D2; ++cc) qj[cc] = qi[cc];
+            } else {
+              Aj = boundary_A<T>(k.rhs_force_type, ci.w, cur.c.y);
+            }
           } else {
             wall_noslip_dist<T, D>(k, df, dw, vj, si, vw);
 #pragma unroll
             for (int a = 0; a < D; ++a) vi[a] = vw[a];
-            Ai = boundary_A<T>(k.rhs_force_type, cur.c.w, ci.y);
+            if (nnw) {
+              Ai = Aj;
+              Bi = Bj;
+#pragma unroll
+              for (int cc = 0; cc <= D2; ++cc) qie[cc] = qj[cc];
+            } else {
+              Ai = boundary_A<T>(k.rhs_force_type, cur.c.w, ci.y);
+            }
           }
         }
         const T gw = kernel_gradw<T>(k, d);
@@ -627,7 +773,22 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
         float z[6];
         if (noise) pair_normals<D>(k.key0, k.key1, step, pidi, __float_as_int(cur.v.w), z);
         T pa[3], si_s, sj_s;
-        pair_force<T, D>(k, r, inv_d, vij, Ai, ci.y, Aj, cur.c.y, gw, noise, z, inv_sqdt, pa);
+        pair_force<T, D>(k, r, inv_d, vij, Ai, Bi, Aj, Bj, gw, noise, z, inv_sqdt, pa);
+        if (nnw) {
+          // polymer pressure-tensor force and velocity gradient (FP32 pairs)
+#pragma unroll
+          for (int b = 0; b < D; ++b) {
+            T s_ = 0.f;
+#pragma unroll
+            for (int a = 0; a < D; ++a) s_ += (qie[1 + a + D * b] + qj[1 + a + D * b]) * r[a];
+            pa[b] += gw * inv_d * s_;
+          }
+          const T fac = gw * qie[0] * inv_d;
+#pragma unroll
+          for (int b = 0; b < D; ++b)
+#pragma unroll
+            for (int a = 0; a < D; ++a) L[a + D * b] += (vj[a] - vi[a]) * r[b] * fac;
+        }
         pair_scales<T>(k.rhs_force_type, ci.z, cur.c.z, si_s, sj_s);
 #pragma unroll
         for (int a = 0; a < D; ++a) pa[a] *= si_s;
@@ -651,6 +812,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
       }
       const double4_32a xi4 = x[i];
       const double xi[3] = {xi4.x, xi4.y, xi4.z};
+      if (nnw) {
+        double Ld[D2];
+#pragma unroll
+        for (int cc = 0; cc < D2; ++cc) Ld[cc] = (double)L[cc];
+        nn_epilogue<D>(k, nn, i, Ld, fuse_mode, dt);
+      }
       force_epilogue<D>(k, i, si, xi, (double)acc[0], (double)acc[1],
                         D == 3 ? (double)acc[2] : 0.0, fuse_mode, dt, v, f, v_out, err);
     }
@@ -1084,7 +1251,7 @@ int compute_density(Handle* h, bool with_pressure) {
   k_density<DD, PP><<<g, kWarpsPerBlock * 32, 0, s>>>(                                          \
       k, h->cell_start, h->off, h->x, h->v, h->m, h->sid, h->pid, h->nl, h->ncount, h->nhs,    \
       h->neigh_cap, h->rho, h->pr, h->pc, h->pcf, h->vf, with_pressure ? 1 : 0, h->d_err,      \
-      h->d_stats, h->d_pairs)
+      h->d_stats, h->d_pairs, NN{h->ct, h->act, h->vgt, h->qq})
   if (k.d == 3) {
     if (fp64) LAUNCH_D(3, true); else LAUNCH_D(3, false);
   } else {
@@ -1102,10 +1269,10 @@ int compute_pressure(Handle* h) {
   const int tb = 256, gb = (n + tb - 1) / tb;
   if (h->p.precision == MCFG_PRECISION_FP64)
     k_pressure<true><<<gb, tb, 0, h->stream>>>(h->k, h->rho, h->m, h->pid, h->v, h->pr, h->pc,
-                                               h->pcf, h->vf);
+                                               h->pcf, h->vf, NN{h->ct, h->act, h->vgt, h->qq});
   else
     k_pressure<false><<<gb, tb, 0, h->stream>>>(h->k, h->rho, h->m, h->pid, h->v, h->pr, h->pc,
-                                                h->pcf, h->vf);
+                                                h->pcf, h->vf, NN{h->ct, h->act, h->vgt, h->qq});
   h->launches++;
   if (cuda_check(h, cudaGetLastError(), "pressure launch")) return MCFG_ECUDA;
   return MCFG_OK;
@@ -1119,7 +1286,8 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
   if (k.noise && !(dt > 0.0)) return set_error(h, MCFG_EINVAL, "random force needs dt > 0");
   const double inv_sqdt = (k.noise && dt > 0.0) ? 1.0 / sqrt(dt) : 0.0;
   const int bs = kWarpsPerBlock * 32;
-  if (!k.stress && h->jp && fp64) {
+  const NN nn{h->ct, h->act, h->vgt, h->qq};
+  if (!k.stress && h->jp && fp64 && k.newtonian) {
     // symmetric sweep + per-particle gather: halves the FP64 pair work; the
     // FP32 path keeps the two-sided sweep, which is faster there (the
     // symmetric sweep's shared-memory partner sums cap its occupancy)
@@ -1174,23 +1342,27 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
     }
     h->launches++;
   } else if (fp64) {
-    if (k.d == 3)
-      k_force64<3><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->x, h->v, h->pc, h->sid,
-                                    h->pid, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step,
-                                    inv_sqdt, h->d_err);
-    else
-      k_force64<2><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->x, h->v, h->pc, h->sid,
-                                    h->pid, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step,
-                                    inv_sqdt, h->d_err);
+#define LAUNCH_F64(DD, NW)                                                                      \
+  k_force64<DD, NW><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->x, h->v, h->pc,      \
+                                     h->sid, h->pid, h->f, h->st, fuse_mode, dt, h->v2,          \
+                                     (uint32_t)step, inv_sqdt, h->d_err, nn)
+    if (k.d == 3) {
+      if (k.newtonian) LAUNCH_F64(3, false); else LAUNCH_F64(3, true);
+    } else {
+      if (k.newtonian) LAUNCH_F64(2, false); else LAUNCH_F64(2, true);
+    }
+#undef LAUNCH_F64
   } else {
-    if (k.d == 3)
-      k_force32<3><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->off, h->x, h->v,
-                                    h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2,
-                                    (uint32_t)step, (float)inv_sqdt, h->d_err);
-    else
-      k_force32<2><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->off, h->x, h->v,
-                                    h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2,
-                                    (uint32_t)step, (float)inv_sqdt, h->d_err);
+#define LAUNCH_F32(DD, NW)                                                                      \
+  k_force32<DD, NW><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->off, h->x, h->v,    \
+                                     h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2,    \
+                                     (uint32_t)step, (float)inv_sqdt, h->d_err, nn)
+    if (k.d == 3) {
+      if (k.newtonian) LAUNCH_F32(3, false); else LAUNCH_F32(3, true);
+    } else {
+      if (k.newtonian) LAUNCH_F32(2, false); else LAUNCH_F32(2, true);
+    }
+#undef LAUNCH_F32
   }
   h->launches++;
   if (cuda_check(h, cudaGetLastError(), "force launch")) return MCFG_ECUDA;

@@ -36,14 +36,24 @@ __device__ __forceinline__ void wrap_axis(const Consts& k, int a,
   }
 }
 
-// flags: 1 half kick, 2 drift, 4 wrap.  The arithmetic is rounded exactly
-// like MCF's: v + (lambda*f)*dt, x + v*dt (no fused multiply-add).
+// flags: 1 half kick, 2 drift, 4 wrap, 8 conformation-tensor half step.
+// The arithmetic is rounded exactly like MCF's: v + (lambda*f)*dt,
+// x + v*dt, ct + act*dt*lambda (no fused multiply-add).
 template <int D>
 __global__ void k_integrate(Consts k, int flags, double dt, double lambda,
                             double4_32a* __restrict__ x, double4_32a* __restrict__ v,
-                            const double4_32a* __restrict__ f, const int* __restrict__ sid) {
+                            const double4_32a* __restrict__ f, const int* __restrict__ sid,
+                            double* __restrict__ ct, const double* __restrict__ act) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= k.n) return;
+  if ((flags & 8) && ct != nullptr) {
+    // particles_integrate_ct.F90:66-68 (all real particles)
+#pragma unroll
+    for (int cc = 0; cc < D * D; ++cc) {
+      const size_t q = (size_t)cc * k.n + i;
+      ct[q] = __dadd_rn(ct[q], __dmul_rn(__dmul_rn(act[q], dt), 0.5));
+    }
+  }
   const int s = sid[i];
   double4_32a xv = x[i], vv = v[i];
   double xs[3] = {xv.x, xv.y, xv.z}, vs[3] = {vv.x, vv.y, vv.z};
@@ -154,10 +164,10 @@ static int launch_integrate(Handle* h, int flags, double dt, double lambda) {
   const int tb = 256, gb = (n + tb - 1) / tb;
   if (h->k.d == 3)
     k_integrate<3><<<gb, tb, 0, h->stream>>>(h->k, flags, dt, lambda, h->x, h->v, h->f,
-                                             h->sid);
+                                             h->sid, h->ct, h->act);
   else
     k_integrate<2><<<gb, tb, 0, h->stream>>>(h->k, flags, dt, lambda, h->x, h->v, h->f,
-                                             h->sid);
+                                             h->sid, h->ct, h->act);
   h->launches++;
   return cuda_check(h, cudaGetLastError(), "integrate launch") ? MCFG_ECUDA : MCFG_OK;
 }
@@ -167,7 +177,9 @@ int integrate_velocity(Handle* h, double dt, double lambda) {
 }
 int integrate_position(Handle* h, double dt) { return launch_integrate(h, 2, dt, 0.0); }
 int adjust_particles(Handle* h) { return launch_integrate(h, 4, 0.0, 0.0); }
-int kick_drift_wrap(Handle* h, double dt) { return launch_integrate(h, 7, dt, 0.5); }
+int kick_drift_wrap(Handle* h, double dt) {
+  return launch_integrate(h, h->p.Newtonian ? 7 : 15, dt, 0.5);
+}
 
 int apply_body_force(Handle* h) {
   const int n = (int)h->n;

@@ -163,12 +163,14 @@ class SDPD:
         self.n = n
 
     def download(self, *fields: str) -> dict:
-        """fields among x, v, rho, p, f, s; arrays in host particle order."""
+        """fields among x, v, rho, p, f, s, ct; arrays in host particle order."""
         n, d = self.n, self.dim
-        shapes = {"x": (n, d), "v": (n, d), "rho": (n,), "p": (n,), "f": (n, d), "s": (n, d * d)}
+        shapes = {"x": (n, d), "v": (n, d), "rho": (n,), "p": (n,), "f": (n, d), "s": (n, d * d),
+                  "ct": (n, d * d)}
         out = {k: np.empty(shapes[k], np.float64) for k in fields}
         g = lambda k: _ptr(out.get(k), C.c_double)  # noqa: E731
-        rc = self.lib.mcfg_download(self._h, g("x"), g("v"), g("rho"), g("p"), g("f"), None, g("s"))
+        rc = self.lib.mcfg_download(self._h, g("x"), g("v"), g("rho"), g("p"), g("f"), g("ct"),
+                                    g("s"))
         self._check("mcfg_download", rc)
         return out
 

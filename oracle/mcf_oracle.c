@@ -40,6 +40,7 @@ struct orc_state {
   int64_t nreal, nall, cap;
   double *x, *v, *f, *rho, *pr, *m, *s, *ct;
   double* fabs_sum; /* per particle sum of |pair acceleration| (test scale) */
+  double *vgt, *act; /* Oldroyd-B: velocity gradient, d(ct)/dt (d*d per particle) */
   int32_t *pid, *sid;
   int64_t* owner;
   /* cell list (ppm_util_rank3d.F90 / rank2d) */
@@ -232,6 +233,10 @@ orc_state* orc_create(const mcfg_params* p, char* err, int errlen) {
     msg = "rhs_force_type must be 1..4";
   else if (p->stateEquation_type != 1 && p->stateEquation_type != 2)
     msg = "stateEquation_type must be 1 or 2";
+  else if (!p->Newtonian && p->rhs_force_type != 3)
+    msg = "the Oldroyd-B model needs rhs_force_type 3 (Hu-Adams)";
+  else if (!p->Newtonian && !(fabs(p->tau) > 1e-14))
+    msg = "tau should not be zero";
   if (msg) {
     if (err) snprintf(err, (size_t)errlen, "%s", msg);
     return NULL;
@@ -258,7 +263,9 @@ orc_state* orc_create(const mcfg_params* p, char* err, int errlen) {
 static void free_arrays(orc_state* s) {
   free(s->x); free(s->v); free(s->f); free(s->rho); free(s->pr); free(s->m);
   free(s->s); free(s->ct); free(s->pid); free(s->sid); free(s->owner); free(s->fabs_sum);
+  free(s->vgt); free(s->act);
   s->x = s->v = s->f = s->rho = s->pr = s->m = s->s = s->ct = s->fabs_sum = NULL;
+  s->vgt = s->act = NULL;
   s->pid = s->sid = NULL;
   s->owner = NULL;
 }
@@ -291,6 +298,8 @@ static void ensure_cap(orc_state* s, int64_t need) {
   s->sid = (int32_t*)realloc(s->sid, sizeof(int32_t) * (size_t)cap);
   s->owner = (int64_t*)realloc(s->owner, sizeof(int64_t) * (size_t)cap);
   s->fabs_sum = (double*)realloc(s->fabs_sum, sizeof(double) * (size_t)cap);
+  s->vgt = (double*)realloc(s->vgt, sizeof(double) * (size_t)(cap * d2));
+  s->act = (double*)realloc(s->act, sizeof(double) * (size_t)(cap * d2));
   s->cap = cap;
 }
 
@@ -316,6 +325,8 @@ int orc_upload(orc_state* s, int64_t n, const double* x, const double* v,
   memset(s->rho, 0, sizeof(double) * (size_t)n);
   memset(s->pr, 0, sizeof(double) * (size_t)n);
   memset(s->s, 0, sizeof(double) * (size_t)(n * d2));
+  memset(s->vgt, 0, sizeof(double) * (size_t)(n * d2));
+  memset(s->act, 0, sizeof(double) * (size_t)(n * d2));
   s->nreal = s->nall = n;
   s->have_list = s->have_density = s->have_pressure = 0;
   return 0;
@@ -931,6 +942,60 @@ static void wall_noslip(const orc_state* s, const double* xf, const double* xw,
   }
 }
 
+/* particles_compute_pressure_tensor.F90:88-133: pt(i,j) = -G ct(i,j) +
+ * delta_ij (p + G), G = n_p kt_p; pt[i + d*j] */
+static void pressure_tensor(const orc_state* s, int64_t k, double* pt) {
+  const int d = s->d;
+  const double G = s->p.n_p * s->p.kt_p;
+  for (int j = 0; j < d; ++j)
+    for (int i = 0; i < d; ++i) {
+      pt[i + d * j] = -G * s->ct[k * d * d + i + d * j];
+      if (i == j) pt[i + d * j] = pt[i + d * j] + s->pr[k] + G;
+    }
+}
+
+/* rhs_force_ff_non_Newtonian_HuAdams.F90:95-201 */
+static void rhs_force_nn(orc_state* s, const force_ctx* fc, const double* xi, const double* xj,
+                         double dij, const double* vi, const double* vj, double numi,
+                         double numj, const double* pti, const double* ptj, double mi, double mj,
+                         double gradw, int32_t pidi, int32_t pidj, double* fi, double* fj) {
+  const int d = s->d;
+  double eij[3], vij[3], f_c[3];
+  for (int a = 0; a < d; ++a) {
+    fi[a] = 0.0;
+    fj[a] = 0.0;
+    eij[a] = (xi[a] - xj[a]) / dij;
+    vij[a] = vi[a] - vj[a];
+    f_c[a] = 0.0;
+  }
+  for (int j = 0; j < d; ++j)
+    for (int i = 0; i < d; ++i)
+      f_c[j] = f_c[j] + pti[i + d * j] * eij[i] / (numi * numi) +
+               ptj[i + d * j] * eij[i] / (numj * numj);
+  for (int a = 0; a < d; ++a) {
+    fi[a] = fi[a] - f_c[a] * gradw / mi;
+    fj[a] = fj[a] + f_c[a] * gradw / mj;
+  }
+  const double f_d = s->p.eta * (1.0 / (numi * numi) + 1.0 / (numj * numj)) * gradw / dij;
+  for (int a = 0; a < d; ++a) {
+    fi[a] = fi[a] + f_d * vij[a] / mi;
+    fj[a] = fj[a] - f_d * vij[a] / mj;
+  }
+  if (fc->noise) {
+    float z[6];
+    double dW[3][3], trace;
+    orc_pair_normals(s->p.seed, fc->step, pidi, pidj, d, z);
+    noise_matrix(s, z, dW, &trace);
+    const double f_r = sqrt(-4.0 * s->p.kt * f_d) / fc->sqdt;
+    for (int a = 0; a < d; ++a) {
+      double We = 0.0;
+      for (int b = 0; b < d; ++b) We = We + dW[a][b] * eij[b];
+      fi[a] = fi[a] + f_r * We / mi;
+      fj[a] = fj[a] - f_r * We / mj;
+    }
+  }
+}
+
 static void force_pair(orc_state* s, int64_t ip, int64_t jp, void* ctx) {
   const force_ctx* fc = (const force_ctx*)ctx;
   const int d = s->d;
@@ -962,8 +1027,31 @@ static void force_pair(orc_state* s, int64_t ip, int64_t jp, void* ctx) {
     pi = pj;
   }
   double fi[3], fj[3];
-  rhs_force_ff(s, fc, &s->x[ip * d], &s->x[jp * d], dij, vi, vj, s->rho[ip], s->rho[jp], pi,
-               pj, s->m[ip], s->m[jp], gradw, s->pid[ip], s->pid[jp], fi, fj);
+  if (s->p.Newtonian) {
+    rhs_force_ff(s, fc, &s->x[ip * d], &s->x[jp * d], dij, vi, vj, s->rho[ip], s->rho[jp], pi,
+                 pj, s->m[ip], s->m[jp], gradw, s->pid[ip], s->pid[jp], fi, fj);
+  } else {
+    /* pp_interaction_ff/fw/wf.inc, non-Newtonian branch: a boundary
+     * partner takes the fluid particle's density and pressure tensor */
+    const int64_t pf = (si < 0) ? jp : ip; /* the fluid one of a f-w pair */
+    const double rho_ip = (si == 0 && sj == 0) ? s->rho[ip] : s->rho[pf];
+    const double rho_jp = (si == 0 && sj == 0) ? s->rho[jp] : s->rho[pf];
+    /* pp_vgt_ip.inc / pp_vgt_jp.inc */
+    const int d2v = d * d;
+    for (int b = 0; b < d; ++b)
+      for (int a = 0; a < d; ++a) {
+        s->vgt[ip * d2v + a + d * b] += (vj[a] - vi[a]) * rij[b] * gradw / rho_ip / dij;
+        if (s->p.symmetry)
+          s->vgt[jp * d2v + a + d * b] += (vi[a] - vj[a]) * (-rij[b]) * gradw / rho_jp / dij;
+      }
+    double pti[9], ptj[9];
+    const int64_t ci_ = (si == 0 && sj == 0) ? ip : pf;
+    const int64_t cj_ = (si == 0 && sj == 0) ? jp : pf;
+    pressure_tensor(s, ci_, pti);
+    pressure_tensor(s, cj_, ptj);
+    rhs_force_nn(s, fc, &s->x[ip * d], &s->x[jp * d], dij, vi, vj, rho_ip, rho_jp, pti, ptj,
+                 s->m[ip], s->m[jp], gradw, s->pid[ip], s->pid[jp], fi, fj);
+  }
   for (int a = 0; a < d; ++a) s->f[ip * d + a] = s->f[ip * d + a] + fi[a];
   {
     double ni = 0.0, nj = 0.0;
@@ -996,6 +1084,8 @@ int orc_compute_interaction(orc_state* s, int64_t step) {
   for (int64_t j = 0; j < s->nall * d; ++j) s->f[j] = 0.0;
   for (int64_t j = 0; j < s->nall * d2; ++j) s->s[j] = 0.0;
   for (int64_t j = 0; j < s->nall; ++j) s->fabs_sum[j] = 0.0;
+  if (!s->p.Newtonian)
+    for (int64_t j = 0; j < s->nall * d2; ++j) s->vgt[j] = 0.0;
   force_ctx fc;
   fc.step = step;
   fc.noise = s->p.Brownian && s->p.kt > s->machine_zero;
@@ -1007,6 +1097,8 @@ int orc_compute_interaction(orc_state* s, int64_t step) {
       const int64_t o = s->owner[g];
       for (int a = 0; a < d; ++a) s->f[o * d + a] = s->f[o * d + a] + s->f[g * d + a];
       s->fabs_sum[o] += s->fabs_sum[g];
+      if (!s->p.Newtonian)
+        for (int a = 0; a < d2; ++a) s->vgt[o * d2 + a] = s->vgt[o * d2 + a] + s->vgt[g * d2 + a];
       if (s->p.stress_tensor)
         for (int a = 0; a < d2; ++a) s->s[o * d2 + a] = s->s[o * d2 + a] + s->s[g * d2 + a];
     }
@@ -1073,6 +1165,30 @@ int orc_integrate_position(orc_state* s, double dt) {
 
 static void set_dt(orc_state* s, double dt) { s->p.dt = dt; }
 
+/* particles_compute_act.F90:112-156: act = c L^T + L c - (c - I)/tau with
+ * L = vgt, L(a,b) = vgt[a + d*b] */
+static void compute_act(orc_state* s) {
+  const int d = s->d, d2 = d * d;
+  const double tau = s->p.tau;
+  for (int64_t p = 0; p < s->nreal; ++p) {
+    const double* c_ = &s->ct[p * d2];
+    const double* L = &s->vgt[p * d2];
+    for (int j = 0; j < d; ++j)
+      for (int i = 0; i < d; ++i) {
+        double t_act = 0.0;
+        for (int k = 0; k < d; ++k)
+          t_act = t_act + c_[i + d * k] * L[j + d * k] + L[i + d * k] * c_[k + d * j];
+        s->act[p * d2 + i + d * j] = t_act - (c_[i + d * j] - (i == j ? 1.0 : 0.0)) / tau;
+      }
+  }
+}
+
+/* particles_integrate_ct.F90:66-68 */
+static void integrate_ct(orc_state* s, double dt, double lambda) {
+  const int d2 = s->d * s->d;
+  for (int64_t p = 0; p < s->nreal * d2; ++p) s->ct[p] = s->ct[p] + s->act[p] * dt * lambda;
+}
+
 static int rhs(orc_state* s, int64_t step) {
   int rc;
   if ((rc = orc_build_list(s))) return rc;
@@ -1081,6 +1197,7 @@ static int rhs(orc_state* s, int64_t step) {
   if ((rc = orc_compute_interaction(s, step))) return rc;
   const double t0 = now_s();
   rc = orc_apply_body_force(s);
+  if (!s->p.Newtonian) compute_act(s); /* marching_integrate_VV.F90:1496 */
   s->timers[3] += now_s() - t0;
   return rc;
 }
@@ -1098,11 +1215,13 @@ int orc_step_vv(orc_state* s, int64_t step, double dt) {
   double t0 = now_s();
   orc_integrate_velocity(s, dt, 0.5);
   orc_integrate_position(s, dt);
+  if (!s->p.Newtonian) integrate_ct(s, dt, 0.5); /* marching_integrate_VV.F90:413 */
   orc_adjust_particles(s);
   s->timers[3] += now_s() - t0;
   int rc = rhs(s, step);
   if (rc) return rc;
   t0 = now_s();
+  if (!s->p.Newtonian) integrate_ct(s, dt, 0.5); /* :1511 */
   orc_integrate_velocity(s, dt, 0.5);
   s->timers[3] += now_s() - t0;
   return 0;

@@ -132,12 +132,13 @@ class Oracle:
 
     def download(self, *fields):
         n, d = self.n, self.dim
-        shapes = {"x": (n, d), "v": (n, d), "rho": (n,), "p": (n,), "f": (n, d), "s": (n, d * d)}
+        shapes = {"x": (n, d), "v": (n, d), "rho": (n,), "p": (n,), "f": (n, d), "s": (n, d * d),
+                  "ct": (n, d * d)}
         out = {k: np.empty(shapes[k], np.float64) for k in fields}
         g = lambda k: _ptr(out.get(k), C.c_double)  # noqa: E731
         self._check("orc_download",
-                    self.lib.orc_download(self._h, g("x"), g("v"), g("rho"), g("p"), g("f"), None,
-                                          g("s")))
+                    self.lib.orc_download(self._h, g("x"), g("v"), g("rho"), g("p"), g("f"),
+                                          g("ct"), g("s")))
         return out
 
     def particles_adjust_particles(self):

@@ -257,3 +257,46 @@ def test_neighbour_overflow_is_reported(gpu_lib):
     # the handle stays usable
     g.upload(w.x, w.v, w.m, w.id)
     g.technique_build_list()
+
+
+# ------------------------------------------------------------ Oldroyd-B model
+def oldroyd_case(n_side=24, seed=8):
+    w = configs.c5_oldroyd_b_2d(n_side=n_side)
+    rng = np.random.default_rng(seed)
+    w.x = w.x + rng.uniform(-0.2, 0.2, w.x.shape)
+    w.v = rng.normal(0, 1e-2, w.v.shape)
+    return w
+
+
+@pytest.mark.parametrize("noise", [0, 1])
+def test_oldroyd_b_fp64_steps(gpu_lib, noise):
+    w = oldroyd_case()
+    g, o = both(w, Brownian=noise, kt=1e-4 if noise else 0.0)
+    g.marching_init_force(0)
+    o.marching_init_force(0)
+    a = g.download("f")["f"]
+    b = o.download("f")["f"]
+    scale = o.force_scale()[:, None] + np.abs(b)
+    assert np.all(np.abs(a - b) <= (1e-5 if noise else 1e-12) * scale)
+    for s in range(1, 6):
+        g.marching_integrate_VV(s, w.dt)
+        o.marching_integrate_VV(s, w.dt)
+    a = g.download("x", "v", "ct")
+    b = o.download("x", "v", "ct")
+    tol_x, tol_v, tol_c = (1e-9, 1e-6, 1e-9) if noise else (1e-12, 1e-10, 1e-12)
+    assert np.max(np.abs(a["x"] - b["x"])) <= tol_x * 24
+    assert np.max(np.abs(a["v"] - b["v"])) <= tol_v * (np.abs(b["v"]).max() + 1e-30)
+    assert np.max(np.abs(a["ct"] - b["ct"])) <= tol_c
+
+
+def test_oldroyd_b_fp32_mixed_ct_error(gpu_lib):
+    w = oldroyd_case()
+    g, o = both(w, precision=PRECISION_FP32_MIXED, Brownian=0, kt=0.0)
+    g.marching_init_force(0)
+    o.marching_init_force(0)
+    g.run_vv(0, 5, w.dt)
+    o.run_vv(0, 5, w.dt)
+    a = g.download("ct")["ct"]
+    b = o.download("ct")["ct"]
+    dev = np.abs(b - np.array([1.0, 0, 0, 1.0]))
+    assert np.max(np.abs(a - b)) <= 1e-3 * dev.max() + 1e-9
