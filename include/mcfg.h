@@ -102,6 +102,25 @@ typedef struct mcfg_handle mcfg_handle;
  * (iso_c_binding, ctypes) can verify their copy of the layout. */
 int64_t mcfg_sizeof_params(void);
 
+/* Rigid colloids made of boundary particles (sid = colloid number 1..nc),
+ * the Colloid object's parameters (mcf/src/Class_Colloid.F90); spheres in
+ * 3D, disks in 2D. */
+typedef struct mcfg_colloid_params {
+  int32_t num_colloid;
+  int32_t noslip_type;      /* 1 frozen (rigid velocity), 2 Morris extrapolation */
+  int32_t rho_type;         /* 0 constant density, 1 dynamic                 */
+  int32_t translate;        /* colloid translates (V used)                    */
+  int32_t rotate;           /* colloid rotates (Omega used)                   */
+  int32_t pp_interact_cc;   /* boundary particles of different colloids
+                               interact (pp_interaction_cc.inc)              */
+  int32_t cc_repul_type;    /* 0 none, 1 Hookean, 2 DLVO                      */
+  int32_t reserved0;
+  double dout;              /* outer layer, mcf_colloid_out_layer_coeff*dx   */
+  double cc_repul_F0;
+  double cc_repul_cut_off;  /* hn */
+  double cc_repul_cut_on;   /* hm */
+} mcfg_colloid_params;
+
 /* Per-handle counters, readable at any time. */
 typedef struct mcfg_info {
   int64_t num_part;       /* particles uploaded                              */
@@ -201,6 +220,28 @@ int mcfg_run_vv(mcfg_handle* h, int64_t step0, int32_t nsteps, double dt);
  * x,v,f: [n*d]; rho,p: [n]; ct: [n*d*d]; s: [n*d*d] (stress_tensor). */
 int mcfg_download(mcfg_handle* h, double* x, double* v, double* rho,
                   double* p, double* f, double* ct, double* s);
+
+/* Colloid state for the pair terms: centres x[nc*d], velocities v[nc*d],
+ * angular velocities omega[nc*3], radii radius[nc].  The colloid pair
+ * terms are pp_interaction_fc.inc / pp_interaction_cf.inc with the Morris
+ * no-slip velocity of colloid_noslip_Morris_sphere.F90:129-300 (disk in
+ * 2D) or the frozen one (colloid_noslip_frozen.F90); boundary-particle
+ * velocities follow particles_set_colloid_velocity.F90:73-95.  Call after
+ * mcfg_upload (the boundary particles are the uploaded sid > 0 ones) and
+ * again whenever the colloids move. */
+int mcfg_set_colloids(mcfg_handle* h, const mcfg_colloid_params* cp,
+                      const double* x, const double* v, const double* omega,
+                      const double* radius);
+
+/* Drag and torque of every colloid from its boundary particles' last
+ * accelerations, particles_collect_colloid_interaction.F90:93-136:
+ * drag[nc*d] = sum m f, torque[nc*3] = sum r x (m f). */
+int mcfg_colloid_drag(mcfg_handle* h, double* drag, double* torque);
+
+/* Colloid-colloid repulsion force[nc*d] (Hookean or DLVO),
+ * colloid_compute_repulsion_cc.F90:95-164 over the nearest periodic image
+ * of each colloid pair (colloid_compute_interaction.F90:532-576). */
+int mcfg_colloid_repulsion(mcfg_handle* h, double* force);
 
 /* Global FP64 sums of statistic_compute_statistic.F90:230-303: kinetic
  * energy and momentum over fluid particles, stress sum over sid >= 0.

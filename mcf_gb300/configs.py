@@ -16,7 +16,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .params import BC_PERIODIC, BC_WALL_SOLID, PRECISION_FP64, SDPDParams, make_params
+from .params import (BC_PERIODIC, BC_WALL_SOLID, PRECISION_FP64, ColloidParams, SDPDParams,
+                     make_params)
 
 BASE_SEED = 20261203
 
@@ -176,5 +177,80 @@ def c5_oldroyd_b_2d(n_side: int = 128, precision: int = PRECISION_FP64, seed: in
     return _finish(f"C5 2D {n_side}^2 Oldroyd-B", p, [1.0, 1.0], 0.0, 0.0, seed, 1e-3, 200)
 
 
+@dataclass
+class ColloidSet:
+    params: ColloidParams
+    x: np.ndarray
+    v: np.ndarray
+    omega: np.ndarray
+    radius: np.ndarray
+
+
+def c4_colloids(n_side: int = 96, n_colloid: int = 200, radius: float = 4.0,
+                precision: int = PRECISION_FP64, seed: int = BASE_SEED + 4,
+                min_gap: float = 1.0, v_scale: float = 0.0, omega_scale: float = 0.0):
+    """3D colloidal suspension: periodic cube of n_side^3 lattice sites, dx = 1,
+    n_colloid rigid spheres of the given radius at seeded non-overlapping
+    centres.  Lattice sites inside a sphere within din = 1.05 rc of its
+    surface are its boundary particles (sid = colloid number), deeper ones
+    are dropped, the rest are solvent (colloid_check_boundary_particle.F90
+    with coll_place lattice).  Morris no-slip, constant boundary density,
+    eta = 1, c = 10, kT = 1e-3, g_x = 0.05, dt = 5e-5; colloid-colloid
+    repulsion is MCF's DLVO form with hn = 0.1 a (the closest MCF has to
+    F0 exp(-r / 0.1 a)), F0 = 10.  Returns (Workload, ColloidSet)."""
+    L = float(n_side)
+    rng = np.random.default_rng(seed)
+    centres = []
+    tries = 0
+    while len(centres) < n_colloid and tries < 200000:
+        tries += 1
+        cand = rng.uniform(0.0, L, 3)
+        ok = True
+        for c in centres:
+            dd = cand - c
+            dd -= L * np.round(dd / L)
+            if np.sqrt(dd @ dd) < 2 * radius + min_gap:
+                ok = False
+                break
+        if ok:
+            centres.append(cand)
+    cx = np.array(centres).reshape(-1, 3)
+    nc = cx.shape[0]
+    p = make_params(**_box(3, 0.0, L), cut_off=3.0, c=10.0, eta=1.0, kt=1e-3, Brownian=1,
+                    body_force_type=1, body_force=[0.05, 0.0, 0.0], dt=5e-5, precision=precision,
+                    seed=seed, init_density=1.0)
+    x = lattice(3, [0.0] * 3, [L] * 3, [1.0] * 3)
+    din = 1.05 * 3.0
+    sid = np.zeros(x.shape[0], np.int32)
+    keep = np.ones(x.shape[0], bool)
+    for ci in range(nc):
+        dd = x - cx[ci]
+        dd -= L * np.round(dd / L)
+        dist = np.sqrt((dd * dd).sum(1))
+        inside = dist <= radius
+        sid[inside] = ci + 1
+        keep[dist <= radius - din] = False
+    x, sid = x[keep], sid[keep]
+    n = x.shape[0]
+    m = np.ones(n)
+    ids = np.stack([np.arange(1, n + 1, dtype=np.int32), sid], axis=1).astype(np.int32)
+    w = Workload(f"C4 3D {n_side}^3 + {nc} colloids", p, x, np.zeros((n, 3)), m, ids, 5e-5, 2000)
+    cp = ColloidParams()
+    cp.num_colloid = nc
+    cp.noslip_type = 2
+    cp.rho_type = 0
+    cp.translate = 1
+    cp.rotate = 1
+    cp.pp_interact_cc = 0
+    cp.cc_repul_type = 2
+    cp.dout = 0.05 * 1.0  # mcf_colloid_out_layer_coeff * dx
+    cp.cc_repul_F0 = 10.0
+    cp.cc_repul_cut_off = 0.1 * radius
+    cp.cc_repul_cut_on = 0.01 * radius
+    cv = rng.normal(0.0, v_scale, (nc, 3)) if v_scale else np.zeros((nc, 3))
+    om = rng.normal(0.0, omega_scale, (nc, 3)) if omega_scale else np.zeros((nc, 3))
+    return w, ColloidSet(cp, cx, cv, om, np.full(nc, radius))
+
+
 WORKLOADS = {"c1": c1_poiseuille_2d, "c2": c2_fluctuating_3d, "c3": c3_poiseuille_3d,
-             "c5": c5_oldroyd_b_2d}
+             "c4": c4_colloids, "c5": c5_oldroyd_b_2d}

@@ -145,7 +145,7 @@ __global__ void k_cell_finalize(Consts k, const int* __restrict__ start,
                                 int* __restrict__ cell_of, float2* __restrict__ wd,
                                 const double* __restrict__ ct_in, const double* __restrict__ act_in,
                                 double* __restrict__ ct_out, double* __restrict__ act_out,
-                                unsigned* __restrict__ err) {
+                                int* __restrict__ slot_of, unsigned* __restrict__ err) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp > k.ncell) return;
@@ -177,6 +177,7 @@ __global__ void k_cell_finalize(Consts k, const int* __restrict__ start,
     pid_out[dst] = pid_in[o];
     sid_out[dst] = sid_in[o];
     hidx_out[dst] = hm;
+    slot_of[hm] = dst;
     cell_of[dst] = warp;
     float4 of;
     of.x = (float)(xp.x - org[0]);
@@ -230,12 +231,12 @@ int build_cell_list(Handle* h) {
       k_cell_finalize<3><<<gw, warps_per_block * 32, 0, s>>>(
           k, h->cell_start, h->order, h->hidx, h->x, h->v, h->f, h->m, h->pid, h->sid, h->x2,
           h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->off, h->cell_of, h->wd, h->ct, h->act,
-          h->ct2, h->act2, h->d_err);
+          h->ct2, h->act2, h->slot_of, h->d_err);
     else
       k_cell_finalize<2><<<gw, warps_per_block * 32, 0, s>>>(
           k, h->cell_start, h->order, h->hidx, h->x, h->v, h->f, h->m, h->pid, h->sid, h->x2,
           h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->off, h->cell_of, h->wd, h->ct, h->act,
-          h->ct2, h->act2, h->d_err);
+          h->ct2, h->act2, h->slot_of, h->d_err);
     h->launches += 2;
     std::swap(h->x, h->x2);
     std::swap(h->v, h->v2);

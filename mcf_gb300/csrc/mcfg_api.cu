@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 #include <string>
 
@@ -112,7 +113,8 @@ void free_all(Handle* h) {
                   h->cnt, h->cell_start, h->scan_part, h->order, h->off, h->cell_of, h->nl,
                   h->ncount, h->nhs, h->jp, h->pc, h->pcf, h->vf, h->wd, h->red, h->d_err, h->d_stats, h->d_pairs,
                   h->up_x, h->up_v, h->up_m, h->up_id, h->ct, h->act, h->vgt, h->ct2,
-                  h->act2, h->qq};
+                  h->act2, h->qq, h->coll, h->coll_start, h->coll_mem, h->slot_of, h->rxc,
+                  h->rxcf, h->coll_out};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   h->x = h->v = h->f = h->x2 = h->v2 = h->f2 = nullptr;
@@ -123,6 +125,12 @@ void free_all(Handle* h) {
   h->jp = nullptr;
   h->ct = h->act = h->vgt = h->ct2 = h->act2 = nullptr;
   h->qq = nullptr;
+  h->coll = h->coll_out = nullptr;
+  h->coll_start = h->coll_mem = h->slot_of = nullptr;
+  h->rxc = nullptr;
+  h->rxcf = nullptr;
+  h->k.coll = nullptr;
+  h->k.ncoll = 0;
   h->off = h->pcf = h->vf = nullptr;
   h->wd = nullptr;
   h->pc = nullptr;
@@ -287,7 +295,7 @@ __global__ void k_upload(int n, int d, const double* __restrict__ hx, const doub
                          const double* __restrict__ hm, const int* __restrict__ hid,
                          double4_32a* __restrict__ x, double4_32a* __restrict__ v,
                          double4_32a* __restrict__ f, double* __restrict__ m, int* __restrict__ pid,
-                         int* __restrict__ sid, int* __restrict__ hidx) {
+                         int* __restrict__ sid, int* __restrict__ hidx, int* __restrict__ slot_of) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double* xp = hx + (size_t)i * d;
@@ -299,6 +307,7 @@ __global__ void k_upload(int n, int d, const double* __restrict__ hx, const doub
   pid[i] = hid[2 * i];
   sid[i] = hid[2 * i + 1];
   hidx[i] = i;
+  slot_of[i] = i;
 }
 
 // scatter sorted state back to host order: interleaved (d, N) layout
@@ -353,7 +362,7 @@ int ensure_capacity(Handle* h, int64_t n64) {
         (rc = dalloc(h, &h->key, cap)) || (rc = dalloc(h, &h->rank, cap)) ||
         (rc = dalloc(h, &h->order, cap)) || (rc = dalloc(h, &h->off, cap)) ||
         (rc = dalloc(h, &h->cell_of, cap)) || (rc = dalloc(h, &h->ncount, cap)) ||
-        (rc = dalloc(h, &h->nhs, cap)) ||
+        (rc = dalloc(h, &h->nhs, cap)) || (rc = dalloc(h, &h->slot_of, cap)) ||
         (rc = dalloc(h, &h->nl, cap * (size_t)neigh)) ||
         (rc = dalloc(h, &h->cnt, (size_t)nbins + 1)) ||
         (rc = dalloc(h, &h->cell_start, (size_t)nbins + 2)) ||
@@ -363,8 +372,9 @@ int ensure_capacity(Handle* h, int64_t n64) {
         (rc = dalloc(h, &h->d_pairs, 1)))
       return rc;
     if (h->p.precision == MCFG_PRECISION_FP64) {
-      if ((rc = dalloc(h, &h->pc, cap))) return rc;
+      if ((rc = dalloc(h, &h->pc, cap)) || (rc = dalloc(h, &h->rxc, cap))) return rc;
     } else {
+      if ((rc = dalloc(h, &h->rxcf, cap))) return rc;
       if ((rc = dalloc(h, &h->pcf, cap)) || (rc = dalloc(h, &h->vf, cap)) ||
           (rc = dalloc(h, &h->wd, cap)))
         return rc;
@@ -560,7 +570,7 @@ int mcfg_upload(mcfg_handle* h, int64_t n, const double* x, const double* v, con
       return MCFG_ECUDA;
     const int tb = 256, gb = (int)((n + tb - 1) / tb);
     k_upload<<<gb, tb, 0, s>>>((int)n, d, h->up_x, h->up_v, h->up_m, h->up_id, h->x, h->v, h->f,
-                               h->m, h->pid, h->sid, h->hidx);
+                               h->m, h->pid, h->sid, h->hidx, h->slot_of);
     h->launches++;
     if (!h->p.Newtonian) {
       double* hct = nullptr;
@@ -586,6 +596,34 @@ int mcfg_upload(mcfg_handle* h, int64_t n, const double* x, const double* v, con
   }
   // pageable host buffers: the copies above are complete only after a sync
   if (cuda_check(h, cudaStreamSynchronize(h->stream), "upload sync")) return MCFG_ECUDA;
+  // boundary particles of each colloid (host indices), for the drag sums
+  {
+    int maxc = 0;
+    for (int64_t i = 0; i < n; ++i) maxc = std::max(maxc, (int)id[2 * i + 1]);
+    h->h_coll_start.assign((size_t)maxc + 1, 0);
+    h->h_coll_mem.clear();
+    if (maxc > 0) {
+      for (int64_t i = 0; i < n; ++i)
+        if (id[2 * i + 1] > 0) h->h_coll_start[(size_t)id[2 * i + 1]]++;
+      for (int c = 0; c < maxc; ++c) h->h_coll_start[(size_t)c + 1] += h->h_coll_start[(size_t)c];
+      h->h_coll_mem.assign((size_t)h->h_coll_start[(size_t)maxc], 0);
+      std::vector<int> pos(h->h_coll_start.begin(), h->h_coll_start.end() - 1);
+      for (int64_t i = 0; i < n; ++i)
+        if (id[2 * i + 1] > 0) h->h_coll_mem[(size_t)pos[(size_t)id[2 * i + 1] - 1]++] = (int)i;
+      int rc2;
+      if ((rc2 = dalloc(h, &h->coll_start, (size_t)maxc + 1)) ||
+          (rc2 = dalloc(h, &h->coll_mem, h->h_coll_mem.size())))
+        return rc2;
+      if (cuda_check(h, cudaMemcpy(h->coll_start, h->h_coll_start.data(),
+                                   sizeof(int) * h->h_coll_start.size(), cudaMemcpyHostToDevice),
+                     "upload colloid lists") ||
+          cuda_check(h, cudaMemcpy(h->coll_mem, h->h_coll_mem.data(),
+                                   sizeof(int) * h->h_coll_mem.size(), cudaMemcpyHostToDevice),
+                     "upload colloid lists"))
+        return MCFG_ECUDA;
+    }
+    h->coll_nmem = (int)h->h_coll_mem.size();
+  }
   h->have_particles = true;
   h->have_list = h->have_density = h->have_pressure = h->have_force = false;
   return MCFG_OK;
@@ -770,6 +808,104 @@ int mcfg_download(mcfg_handle* h, double* x, double* v, double* rho, double* p, 
         cuda_check(h, cudaStreamSynchronize(st), "download sync"))
       return MCFG_ECUDA;
   }
+  return MCFG_OK;
+}
+
+int mcfg_set_colloids(mcfg_handle* h, const mcfg_colloid_params* cp, const double* x,
+                      const double* v, const double* omega, const double* radius) {
+  GUARD(h);
+  if (!cp || cp->num_colloid < 0) return set_error(h, MCFG_EINVAL, "bad colloid parameters");
+  const int nc = cp->num_colloid, d = h->p.num_dim;
+  if (nc > 0 && (!x || !v || !omega || !radius))
+    return set_error(h, MCFG_EINVAL, "mcfg_set_colloids: NULL array");
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "upload the particles first");
+  if ((int)h->h_coll_start.size() - 1 > nc)
+    return set_error(h, MCFG_EINVAL, "a particle's sid exceeds num_colloid");
+  if (cp->noslip_type < 1 || cp->noslip_type > 2)
+    return set_error(h, MCFG_ENOTSUP, "colloid noslip_type must be 1 (frozen) or 2 (Morris)");
+  h->cp = *cp;
+  h->cx.assign(x, x + (size_t)nc * d);
+  h->cv.assign(v, v + (size_t)nc * d);
+  h->com.assign(omega, omega + (size_t)nc * 3);
+  h->crad.assign(radius, radius + nc);
+  std::vector<double> buf((size_t)nc * 12, 0.0);
+  for (int c = 0; c < nc; ++c) {
+    for (int a = 0; a < d; ++a) {
+      buf[(size_t)c * 12 + a] = x[(size_t)c * d + a];
+      buf[(size_t)c * 12 + 3 + a] = v[(size_t)c * d + a];
+    }
+    for (int a = 0; a < 3; ++a) buf[(size_t)c * 12 + 6 + a] = omega[(size_t)c * 3 + a];
+    buf[(size_t)c * 12 + 9] = radius[c];
+  }
+  if (nc > 0) {
+    int rc;
+    if ((rc = dalloc(h, &h->coll, buf.size())) || (rc = dalloc(h, &h->coll_out, (size_t)nc * 6)))
+      return rc;
+    if (cuda_check(h, cudaMemcpyAsync(h->coll, buf.data(), sizeof(double) * buf.size(),
+                                      cudaMemcpyHostToDevice, h->stream), "upload colloids") ||
+        cuda_check(h, cudaStreamSynchronize(h->stream), "upload colloids"))
+      return MCFG_ECUDA;
+  }
+  Consts& k = h->k;
+  k.ncoll = nc;
+  k.coll = h->coll;
+  k.coll_noslip = cp->noslip_type;
+  k.coll_rho_type = cp->rho_type;
+  k.coll_translate = cp->translate;
+  k.coll_rotate = cp->rotate;
+  k.pp_cc = cp->pp_interact_cc;
+  k.coll_dout = cp->dout;
+  h->have_density = h->have_pressure = false;
+  return MCFG_OK;
+}
+
+int mcfg_colloid_drag(mcfg_handle* h, double* drag, double* torque) {
+  GUARD(h);
+  if (!h->have_force) return set_error(h, MCFG_ESTATE, "no force computed yet");
+  return colloid_drag(h, drag, torque);
+}
+
+int mcfg_colloid_repulsion(mcfg_handle* h, double* force) {
+  GUARD(h);
+  if (!force) return set_error(h, MCFG_EINVAL, "NULL output");
+  const int nc = h->k.ncoll, d = h->p.num_dim;
+  const mcfg_colloid_params& cp = h->cp;
+  for (int q = 0; q < nc * d; ++q) force[q] = 0.0;
+  if (cp.cc_repul_type < 1) return MCFG_OK;
+  const double hn = cp.cc_repul_cut_off, hm = cp.cc_repul_cut_on, F0 = cp.cc_repul_F0;
+  for (int i = 0; i < nc; ++i)
+    for (int j = i + 1; j < nc; ++j) {
+      double R12[3] = {0, 0, 0}, rr = 0.0;
+      for (int a = 0; a < d; ++a) {
+        double r = h->cx[(size_t)i * d + a] - h->cx[(size_t)j * d + a];
+        if (h->k.periodic[a]) {
+          if (r > 0.5 * h->k.len[a])
+            r -= h->k.len[a];
+          else if (r < -0.5 * h->k.len[a])
+            r += h->k.len[a];
+        }
+        R12[a] = r;
+        rr += r * r;
+      }
+      const double r = std::sqrt(rr);
+      double gap = r - (h->crad[i] + h->crad[j]);
+      if (!(gap < 5.0 * hn)) continue;
+      double F = 0.0;
+      if (cp.cc_repul_type == 1) {  // Hookean
+        if (gap < hn) {
+          if (gap < hm) gap = hm;
+          F = F0 - F0 * gap / hn;
+        }
+      } else {  // DLVO
+        if (gap < hm) gap = hm;
+        F = F0 / hn * std::exp(-gap / hn) / (1.0 - std::exp(-gap / hn)) -
+            F0 / hn * std::exp(-5.0) / (1.0 - std::exp(-5.0));
+      }
+      for (int a = 0; a < d; ++a) {
+        force[(size_t)i * d + a] += F * R12[a] / r;
+        force[(size_t)j * d + a] -= F * R12[a] / r;
+      }
+    }
   return MCFG_OK;
 }
 

@@ -61,6 +61,10 @@ struct Consts {
   double min_phys[3], max_phys[3];
   double wall_v[6][3];
   int stress;
+  // colloids (boundary particles sid = 1..ncoll)
+  int ncoll, coll_noslip, coll_rho_type, coll_translate, coll_rotate, pp_cc;
+  double coll_dout;
+  const double* coll;    // device [ncoll][12]: X(3) V(3) Omega(3) R pad(2)
   // Oldroyd-B conformation model (Newtonian == 0)
   int newtonian;
   double G, tau, inv_tau;  // G = n_p kt_p
@@ -105,6 +109,18 @@ struct Handle {
   double* vgt = nullptr;  // velocity gradient tensor
   double *ct2 = nullptr, *act2 = nullptr;
   void* qq = nullptr;     // per-particle 1/n and G*ct/n^2, [1+d*d][cap] (T)
+  // colloids
+  mcfg_colloid_params cp{};
+  std::vector<double> cx, cv, com, crad;  // host copies (repulsion)
+  double* coll = nullptr;      // device [nc][12]
+  int* coll_start = nullptr;   // [nc+1] CSR of boundary particles (host indices)
+  int* coll_mem = nullptr;
+  int coll_nmem = 0;
+  std::vector<int> h_coll_start, h_coll_mem;
+  int* slot_of = nullptr;      // host index -> sorted slot
+  double4_32a* rxc = nullptr;  // FP64 path: boundary particle minus its colloid image centre
+  float4* rxcf = nullptr;      // FP32 path: same in FP32
+  double* coll_out = nullptr;  // [nc][6] drag + torque
   // double buffers for the permutation
   double4_32a *x2 = nullptr, *v2 = nullptr, *f2 = nullptr;
   double* m2 = nullptr;
@@ -199,6 +215,7 @@ int integrate_position(Handle* h, double dt);
 int adjust_particles(Handle* h);
 int kick_drift_wrap(Handle* h, double dt);
 int statistics(Handle* h, double* ke, double* mom, double* stress);
+int colloid_drag(Handle* h, double* drag, double* torque);
 int check_device_errors(Handle* h);
 
 // fuse_mode of compute_force

@@ -142,7 +142,46 @@ __device__ __forceinline__ double exact_sep(const Consts& k, const double* xi, c
 __device__ __forceinline__ bool dyn_rho(const Consts& k, int sid) {
   if (sid == 0) return true;
   if (sid < 0) return k.wall_rho_type == 1;
-  return false;
+  return k.coll_rho_type == 1;
+}
+
+// colloid arrays handed to the sweeps
+struct CollArgs {
+  double4_32a* v;      // state velocity (boundary particles get the rigid one)
+  double4_32a* rxc;    // FP64 path: boundary particle - colloid image centre
+  float4* rxcf;        // FP32 path: same
+};
+
+// particles_set_colloid_velocity.F90:73-95 with colloid_particle_velocity.F90:
+// the boundary particle moves with its colloid, V + Omega x rx.  Also keeps
+// rx for the no-slip pair term.  Returns the new velocity.
+template <int D>
+__device__ __forceinline__ double4_32a colloid_particle_update(const Consts& k, int i, int si,
+                                                               const double4_32a& xi4,
+                                                               const CollArgs& ca) {
+  const double x[3] = {xi4.x, xi4.y, xi4.z};
+  double rx[3] = {0.0, 0.0, 0.0};
+  colloid_rx<D>(k, x, si - 1, rx);
+  if (ca.rxc) ca.rxc[i] = make_double4_32a(rx[0], rx[1], rx[2], 0.0);
+  if (ca.rxcf) ca.rxcf[i] = make_float4((float)rx[0], (float)rx[1], (float)rx[2], 0.f);
+  double vn[3] = {0.0, 0.0, 0.0};
+  if (k.coll_translate || k.coll_rotate) {
+    const double* cd = k.coll + (size_t)(si - 1) * 12;
+    vn[0] = cd[3];
+    vn[1] = cd[4];
+    vn[2] = D == 3 ? cd[5] : 0.0;
+    if (k.coll_rotate) {
+      const double r3[3] = {rx[0], rx[1], D == 3 ? rx[2] : 0.0};
+      const double om[3] = {cd[6], cd[7], cd[8]};
+      double w[3];
+      cross3t<double>(om, r3, w);
+#pragma unroll
+      for (int a = 0; a < D; ++a) vn[a] += w[a];
+    }
+  }
+  const double4_32a out = make_double4_32a(vn[0], vn[1], D == 3 ? vn[2] : 0.0, 0.0);
+  ca.v[i] = out;
+  return out;
 }
 
 // Per-particle prologue of the force sweep: pressure from the equation of
@@ -223,7 +262,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
               int* __restrict__ nhs, int cap, double* __restrict__ rho, double* __restrict__ pr,
               double4_32a* __restrict__ pc, float4* __restrict__ pcf, float4* __restrict__ vf,
               int with_pressure, unsigned* __restrict__ err, int* __restrict__ stats,
-              unsigned long long* __restrict__ pairs, NN nn) {
+              unsigned long long* __restrict__ pairs, NN nn, CollArgs ca) {
   constexpr int NS = (D == 3) ? 27 : 9;
   constexpr int CENTER = (D == 3) ? 13 : 4;
   __shared__ NbTable tab[kWarpsPerBlock];
@@ -354,8 +393,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       }
       rho[i] = rho_out;
       if (!(rho_out > 0.0)) atomicOr(err, kErrZeroDensity);
-      if (with_pressure)
-        write_particle_records<FP64>(k, i, rho_out, mi, pid[i], v[i], pr, pc, pcf, vf, nn);
+      if (with_pressure) {
+        const double4_32a vi4 =
+            (si > 0 && k.ncoll > 0) ? colloid_particle_update<D>(k, i, si, x[i], ca) : v[i];
+        write_particle_records<FP64>(k, i, rho_out, mi, pid[i], vi4, pr, pc, pcf, vf, nn);
+      }
     }
   }
 #pragma unroll
@@ -369,14 +411,19 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   }
 }
 
-template <bool FP64>
+template <int D, bool FP64>
 __global__ void k_pressure(Consts k, const double* __restrict__ rho, const double* __restrict__ m,
                            const int* __restrict__ pid, const double4_32a* __restrict__ v,
                            double* __restrict__ pr, double4_32a* __restrict__ pc,
-                           float4* __restrict__ pcf, float4* __restrict__ vf, NN nn) {
+                           float4* __restrict__ pcf, float4* __restrict__ vf, NN nn,
+                           const int* __restrict__ sid, const double4_32a* __restrict__ x,
+                           CollArgs ca) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= k.n) return;
-  write_particle_records<FP64>(k, i, rho[i], m[i], pid[i], v[i], pr, pc, pcf, vf, nn);
+  const int si = sid[i];
+  const double4_32a vi4 =
+      (si > 0 && k.ncoll > 0) ? colloid_particle_update<D>(k, i, si, x[i], ca) : v[i];
+  write_particle_records<FP64>(k, i, rho[i], m[i], pid[i], vi4, pr, pc, pcf, vf, nn);
 }
 
 // ---------------------------------------------------------------------------
@@ -467,7 +514,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
               const int* __restrict__ sid, const int* __restrict__ pid,
               double4_32a* __restrict__ f, double* __restrict__ st, int fuse_mode, double dt,
               double4_32a* __restrict__ v_out, uint32_t step, double inv_sqdt,
-              unsigned* __restrict__ err, NN nn) {
+              unsigned* __restrict__ err, NN nn, CollArgs ca) {
   constexpr int CENTER = (D == 3) ? 13 : 4;
   constexpr int D2 = D * D;
   using T = double;
@@ -508,7 +555,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
         const int j = t.start[sl] + q;
         const int sj = sid[j];
-        if (si != 0 && sj != 0) continue;  // w-w, c-c, c-w: no interaction here
+        // pp_interaction.inc:63-223: w-w and c-w never interact, c-c only
+        // between different colloids with pp_interact_cc
+        if (si != 0 && sj != 0 && !(si > 0 && sj > 0 && si != sj && k.pp_cc)) continue;
         const double4_32a xj4 = x[j];
         const double xj[3] = {xj4.x, xj4.y, xj4.z};
         T r[3];
@@ -553,6 +602,46 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
             wall_noslip<T, D>(k, xjn, xin, vj, si, vw);
 #pragma unroll
             for (int a = 0; a < D; ++a) vi[a] = vw[a];
+            if (nnw) {
+              Ai = Aj;
+              Bi = Bj;
+#pragma unroll
+              for (int cc = 0; cc <= D2; ++cc) qie[cc] = qj[cc];
+            } else {
+              Ai = boundary_A<T>(k.rhs_force_type, cj.w, ci.y);
+            }
+          }
+        } else if ((si > 0) != (sj > 0)) {
+          // fluid-colloid pair (pp_interaction_fc.inc / _cf.inc): the
+          // boundary particle takes the Morris no-slip velocity and the
+          // fluid pressure (Oldroyd-B: also its density and pressure tensor)
+          if (sj > 0) {
+            if (k.coll_noslip == 2) {
+              const double4_32a rc4 = ca.rxc[j];
+              const T rxc_[3] = {rc4.x, rc4.y, rc4.z};
+              T vw[3];
+              colloid_noslip<T, D>(k, sj - 1, rxc_, r, vi, vw);
+#pragma unroll
+              for (int a = 0; a < D; ++a) vj[a] = vw[a];
+            }
+            if (nnw) {
+              Aj = Ai;
+              Bj = Bi;
+#pragma unroll
+              for (int cc = 0; cc <= D2; ++cc) qj[cc] = qi[cc];
+            } else {
+              Aj = boundary_A<T>(k.rhs_force_type, ci.w, cj.y);
+            }
+          } else {
+            if (k.coll_noslip == 2) {
+              const double4_32a rc4 = ca.rxc[i];
+              const T rxc_[3] = {rc4.x, rc4.y, rc4.z};
+              const T rfc[3] = {-r[0], -r[1], -r[2]};
+              T vw[3];
+              colloid_noslip<T, D>(k, si - 1, rxc_, rfc, vj, vw);
+#pragma unroll
+              for (int a = 0; a < D; ++a) vi[a] = vw[a];
+            }
             if (nnw) {
               Ai = Aj;
               Bi = Bj;
@@ -643,7 +732,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
               const float2* __restrict__ wd, double4_32a* __restrict__ f,
               double* __restrict__ st, int fuse_mode, double dt,
               double4_32a* __restrict__ v_out, uint32_t step, float inv_sqdt,
-              unsigned* __restrict__ err, NN nn) {
+              unsigned* __restrict__ err, NN nn, CollArgs ca) {
   constexpr int CENTER = (D == 3) ? 13 : 4;
   constexpr int D2 = D * D;
   using T = float;
@@ -691,7 +780,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
           if (e + 2 < cnt) ent_n1 = nl[(size_t)(e + 2) * n + i];
         }
         const int sj = __float_as_int(cur.o.w);
-        if (si != 0 && sj != 0) continue;
+        if (si != 0 && sj != 0 && !(si > 0 && sj > 0 && si != sj && k.pp_cc)) continue;
         const int sl = cur.sl;
         T r[3];
         const float4 so = t.o[sl];
@@ -756,6 +845,44 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
             wall_noslip_dist<T, D>(k, df, dw, vj, si, vw);
 #pragma unroll
             for (int a = 0; a < D; ++a) vi[a] = vw[a];
+            if (nnw) {
+              Ai = Aj;
+              Bi = Bj;
+#pragma unroll
+              for (int cc = 0; cc <= D2; ++cc) qie[cc] = qj[cc];
+            } else {
+              Ai = boundary_A<T>(k.rhs_force_type, cur.c.w, ci.y);
+            }
+          }
+        } else if ((si > 0) != (sj > 0)) {
+          // fluid-colloid pair (pp_interaction_fc.inc / _cf.inc)
+          if (sj > 0) {
+            if (k.coll_noslip == 2) {
+              const float4 rc4 = ca.rxcf[cur.j];
+              const T rxc_[3] = {rc4.x, rc4.y, rc4.z};
+              T vw[3];
+              colloid_noslip<T, D>(k, sj - 1, rxc_, r, vi, vw);
+#pragma unroll
+              for (int a = 0; a < D; ++a) vj[a] = vw[a];
+            }
+            if (nnw) {
+              Aj = Ai;
+              Bj = Bi;
+#pragma unroll
+              for (int cc = 0; cc <= D2; ++cc) qj[cc] = qi[cc];
+            } else {
+              Aj = boundary_A<T>(k.rhs_force_type, ci.w, cur.c.y);
+            }
+          } else {
+            if (k.coll_noslip == 2) {
+              const float4 rc4 = ca.rxcf[i];
+              const T rxc_[3] = {rc4.x, rc4.y, rc4.z};
+              const T rfc[3] = {-r[0], -r[1], -r[2]};
+              T vw[3];
+              colloid_noslip<T, D>(k, si - 1, rxc_, rfc, vj, vw);
+#pragma unroll
+              for (int a = 0; a < D; ++a) vi[a] = vw[a];
+            }
             if (nnw) {
               Ai = Aj;
               Bi = Bj;
@@ -1251,7 +1378,7 @@ int compute_density(Handle* h, bool with_pressure) {
   k_density<DD, PP><<<g, kWarpsPerBlock * 32, 0, s>>>(                                          \
       k, h->cell_start, h->off, h->x, h->v, h->m, h->sid, h->pid, h->nl, h->ncount, h->nhs,    \
       h->neigh_cap, h->rho, h->pr, h->pc, h->pcf, h->vf, with_pressure ? 1 : 0, h->d_err,      \
-      h->d_stats, h->d_pairs, NN{h->ct, h->act, h->vgt, h->qq})
+      h->d_stats, h->d_pairs, NN{h->ct, h->act, h->vgt, h->qq}, CollArgs{h->v, h->rxc, h->rxcf})
   if (k.d == 3) {
     if (fp64) LAUNCH_D(3, true); else LAUNCH_D(3, false);
   } else {
@@ -1267,12 +1394,17 @@ int compute_pressure(Handle* h) {
   const int n = (int)h->n;
   if (n == 0) return MCFG_OK;
   const int tb = 256, gb = (n + tb - 1) / tb;
-  if (h->p.precision == MCFG_PRECISION_FP64)
-    k_pressure<true><<<gb, tb, 0, h->stream>>>(h->k, h->rho, h->m, h->pid, h->v, h->pr, h->pc,
-                                               h->pcf, h->vf, NN{h->ct, h->act, h->vgt, h->qq});
-  else
-    k_pressure<false><<<gb, tb, 0, h->stream>>>(h->k, h->rho, h->m, h->pid, h->v, h->pr, h->pc,
-                                                h->pcf, h->vf, NN{h->ct, h->act, h->vgt, h->qq});
+  const NN nn{h->ct, h->act, h->vgt, h->qq};
+  const CollArgs ca{h->v, h->rxc, h->rxcf};
+#define LAUNCH_P(DD, PP)                                                                        \
+  k_pressure<DD, PP><<<gb, tb, 0, h->stream>>>(h->k, h->rho, h->m, h->pid, h->v, h->pr, h->pc,   \
+                                               h->pcf, h->vf, nn, h->sid, h->x, ca)
+  if (h->p.precision == MCFG_PRECISION_FP64) {
+    if (h->k.d == 3) LAUNCH_P(3, true); else LAUNCH_P(2, true);
+  } else {
+    if (h->k.d == 3) LAUNCH_P(3, false); else LAUNCH_P(2, false);
+  }
+#undef LAUNCH_P
   h->launches++;
   if (cuda_check(h, cudaGetLastError(), "pressure launch")) return MCFG_ECUDA;
   return MCFG_OK;
@@ -1287,7 +1419,8 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
   const double inv_sqdt = (k.noise && dt > 0.0) ? 1.0 / sqrt(dt) : 0.0;
   const int bs = kWarpsPerBlock * 32;
   const NN nn{h->ct, h->act, h->vgt, h->qq};
-  if (!k.stress && h->jp && fp64 && k.newtonian) {
+  const CollArgs ca{h->v, h->rxc, h->rxcf};
+  if (!k.stress && h->jp && fp64 && k.newtonian && k.ncoll == 0) {
     // symmetric sweep + per-particle gather: halves the FP64 pair work; the
     // FP32 path keeps the two-sided sweep, which is faster there (the
     // symmetric sweep's shared-memory partner sums cap its occupancy)
@@ -1345,7 +1478,7 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
 #define LAUNCH_F64(DD, NW)                                                                      \
   k_force64<DD, NW><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->x, h->v, h->pc,      \
                                      h->sid, h->pid, h->f, h->st, fuse_mode, dt, h->v2,          \
-                                     (uint32_t)step, inv_sqdt, h->d_err, nn)
+                                     (uint32_t)step, inv_sqdt, h->d_err, nn, ca)
     if (k.d == 3) {
       if (k.newtonian) LAUNCH_F64(3, false); else LAUNCH_F64(3, true);
     } else {
@@ -1356,7 +1489,7 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
 #define LAUNCH_F32(DD, NW)                                                                      \
   k_force32<DD, NW><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->off, h->x, h->v,    \
                                      h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2,    \
-                                     (uint32_t)step, (float)inv_sqdt, h->d_err, nn)
+                                     (uint32_t)step, (float)inv_sqdt, h->d_err, nn, ca)
     if (k.d == 3) {
       if (k.newtonian) LAUNCH_F32(3, false); else LAUNCH_F32(3, true);
     } else {

@@ -329,4 +329,85 @@ __device__ __forceinline__ void wall_noslip(const Consts& k, double xf_n, double
   wall_noslip_dist<T, D>(k, (T)(xf_n - x_sur), (T)(xw_n - x_sur), vf, sid_w, vw);
 }
 
+// ---------------------------------------------------------------------------
+// Colloids (spheres in 3D, disks in 2D)
+// ---------------------------------------------------------------------------
+// colloid_in_nearest_image.F90 (periodic part), FP64: rx = x - nearest image
+// of colloid c's centre, looked for within radius + dout per axis
+template <int D>
+__device__ __forceinline__ void colloid_rx(const Consts& k, const double* x, int c, double* rx) {
+  const double* cd = k.coll + (size_t)c * 12;
+  const double dmax = cd[9] + k.coll_dout;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    double xi = cd[a];
+    const double r = x[a] - xi;
+    if (r > dmax && k.periodic[a])
+      xi = xi + k.len[a];
+    else if (-r > dmax && k.periodic[a])
+      xi = xi - k.len[a];
+    rx[a] = x[a] - xi;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void cross3t(const T* a, const T* b, T* o) {
+  o[0] = a[1] * b[2] - a[2] * b[1];
+  o[1] = a[2] * b[0] - a[0] * b[2];
+  o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Morris no-slip velocity of a colloid boundary particle seen from a fluid
+// particle, colloid_noslip_Morris_sphere.F90:129-300 (disk alike in 2D):
+// r_xc = boundary particle - colloid image centre, r_fc = fluid - boundary
+// particle (pair separation), vf the fluid velocity.
+template <typename T, int D>
+__device__ __forceinline__ void colloid_noslip(const Consts& k, int c, const T* r_xc,
+                                               const T* r_fc, const T* vf, T* vc) {
+  const double* cd = k.coll + (size_t)c * 12;
+  const T R = (T)cd[9];
+  T V[3] = {(T)cd[3], (T)cd[4], (T)cd[5]};
+  const T om[3] = {(T)cd[6], (T)cd[7], (T)cd[8]};
+  T r_xf[3] = {0, 0, 0};
+  T dd = 0;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    r_xf[a] = r_xc[a] + r_fc[a];
+    dd += r_xf[a] * r_xf[a];
+  }
+  const T d_fcoll = my_sqrt<T>(dd);
+  if (d_fcoll <= R) {
+    T w[3] = {0, 0, 0};
+    if (k.coll_rotate) {
+      const T r3[3] = {r_xc[0], r_xc[1], D == 3 ? r_xc[2] : T(0)};
+      cross3t<T>(om, r3, w);
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) vc[a] = V[a] + w[a];
+    return;
+  }
+  T d_cn = 0;
+#pragma unroll
+  for (int a = 0; a < D; ++a) d_cn += r_xc[a] * r_xf[a] / d_fcoll;
+  const T d_cs = R - d_cn;
+  const T d_fs = d_fcoll - R;
+  T corr;
+  if (fabs(d_fs) < (T)k.machine_zero) {
+    corr = T(0.5);  // mcf_colloid_dist_ratio_max
+  } else {
+    corr = d_cs / d_fs;
+    if (corr > T(0.5)) corr = T(0.5);
+    else if (corr < T(-0.5)) corr = T(-0.5);
+  }
+  T r_vs[3] = {0, 0, 0};
+  if (k.coll_rotate) {
+    T r_xs[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) r_xs[a] = R / d_fcoll * r_xf[a];
+    cross3t<T>(om, r_xs, r_vs);
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) vc[a] = -corr * (vf[a] - V[a] - r_vs[a]) + V[a] + r_vs[a];
+}
+
 }  // namespace mcfg

@@ -6,6 +6,7 @@
 // particles_apply_body_force.F90:96-353, marching_integrate_VV.F90:303-322,
 // statistic_compute_statistic.F90:230-303.
 #include "mcfg_internal.cuh"
+#include "sph.cuh"
 
 namespace mcfg {
 
@@ -156,6 +157,68 @@ __global__ void k_stats_final(const double* __restrict__ part, int nparts, doubl
   double s = 0.0;
   for (int b = 0; b < nparts; ++b) s += part[(size_t)b * kRedVals + q];
   out[q] = s;
+}
+
+// particles_collect_colloid_interaction.F90:93-136: one warp per colloid
+// sums m f and r x (m f) over its boundary particles in a fixed order.
+template <int D>
+__global__ void k_colloid_drag(Consts k, const int* __restrict__ cstart,
+                               const int* __restrict__ cmem, const int* __restrict__ slot_of,
+                               const double4_32a* __restrict__ x,
+                               const double4_32a* __restrict__ f, const double* __restrict__ m,
+                               double* __restrict__ out) {
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= k.ncoll) return;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int q = cstart[c] + lane; q < cstart[c + 1]; q += 32) {
+    const int s = slot_of[cmem[q]];
+    const double4_32a fv = f[s], xv = x[s];
+    const double mi = m[s];
+    const double F[3] = {fv.x * mi, fv.y * mi, D == 3 ? fv.z * mi : 0.0};
+    const double xs[3] = {xv.x, xv.y, xv.z};
+    double rx[3] = {0.0, 0.0, 0.0};
+    colloid_rx<D>(k, xs, c, rx);
+    double T[3];
+    cross3t<double>(rx, F, T);
+    for (int a = 0; a < 3; ++a) {
+      acc[a] += F[a];
+      acc[3 + a] += T[a];
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int a = 0; a < 6; ++a) acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], o);
+  if (lane == 0)
+    for (int a = 0; a < 6; ++a) out[(size_t)c * 6 + a] = acc[a];
+}
+
+int colloid_drag(Handle* h, double* drag, double* torque) {
+  const int nc = h->k.ncoll, d = h->k.d;
+  if (nc == 0) return MCFG_OK;
+  const int warps_per_block = 4;
+  const int g = (nc + warps_per_block - 1) / warps_per_block;
+  if (d == 3)
+    k_colloid_drag<3><<<g, 32 * warps_per_block, 0, h->stream>>>(
+        h->k, h->coll_start, h->coll_mem, h->slot_of, h->x, h->f, h->m, h->coll_out);
+  else
+    k_colloid_drag<2><<<g, 32 * warps_per_block, 0, h->stream>>>(
+        h->k, h->coll_start, h->coll_mem, h->slot_of, h->x, h->f, h->m, h->coll_out);
+  h->launches++;
+  std::vector<double> buf((size_t)nc * 6);
+  if (cuda_check(h, cudaMemcpyAsync(buf.data(), h->coll_out, sizeof(double) * buf.size(),
+                                    cudaMemcpyDeviceToHost, h->stream),
+                 "drag copy") ||
+      cuda_check(h, cudaStreamSynchronize(h->stream), "drag sync"))
+    return MCFG_ECUDA;
+  for (int c = 0; c < nc; ++c) {
+    for (int a = 0; a < d; ++a)
+      if (drag) drag[(size_t)c * d + a] = buf[(size_t)c * 6 + a];
+    for (int a = 0; a < 3; ++a)
+      if (torque) torque[(size_t)c * 3 + a] = buf[(size_t)c * 6 + 3 + a];
+  }
+  return MCFG_OK;
 }
 
 static int launch_integrate(Handle* h, int flags, double dt, double lambda) {

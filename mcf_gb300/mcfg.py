@@ -14,7 +14,7 @@ from pathlib import Path
 
 import numpy as np
 
-from .params import STATUS_NAMES, SDPDInfo, SDPDParams
+from .params import STATUS_NAMES, ColloidParams, SDPDInfo, SDPDParams
 
 _LIB = None
 LIB_PATH = Path(__file__).resolve().parent / "libmcfg.so"
@@ -71,6 +71,9 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "mcfg_density_noalloc": (C.c_int, [C.POINTER(SDPDParams), C.c_int32, C.c_void_p,
                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
         "mcfg_noalloc_error": (C.c_char_p, []),
+        "mcfg_set_colloids": (C.c_int, [_h, C.POINTER(ColloidParams), _dp, _dp, _dp, _dp]),
+        "mcfg_colloid_drag": (C.c_int, [_h, _dp, _dp]),
+        "mcfg_colloid_repulsion": (C.c_int, [_h, _dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -231,6 +234,34 @@ class SDPD:
                     self.lib.mcfg_statistics(self._h, C.byref(ke), _ptr(mom, C.c_double),
                                              _ptr(st, C.c_double)))
         return ke.value, mom, st
+
+    # -- colloids (Class_Colloid) -------------------------------------------
+    def set_colloids(self, cp: ColloidParams, x, v, omega, radius) -> None:
+        self._cp = cp
+        self._cx = _as(x, np.float64)
+        self._cv = _as(v, np.float64)
+        self._com = _as(omega, np.float64)
+        self._crad = _as(radius, np.float64)
+        self._check("mcfg_set_colloids", self.lib.mcfg_set_colloids(
+            self._h, C.byref(cp), _ptr(self._cx, C.c_double), _ptr(self._cv, C.c_double),
+            _ptr(self._com, C.c_double), _ptr(self._crad, C.c_double)))
+
+    def colloid_drag(self):
+        """particles_collect_colloid_interaction: (drag[nc, d], torque[nc, 3])"""
+        nc = self._cp.num_colloid
+        drag = np.zeros((nc, self.dim))
+        torque = np.zeros((nc, 3))
+        self._check("particles_collect_colloid_interaction",
+                    self.lib.mcfg_colloid_drag(self._h, _ptr(drag, C.c_double),
+                                               _ptr(torque, C.c_double)))
+        return drag, torque
+
+    def colloid_repulsion(self):
+        """colloid_compute_repulsion_cc summed per colloid: force[nc, d]"""
+        out = np.zeros((self._cp.num_colloid, self.dim))
+        self._check("colloid_compute_repulsion_cc",
+                    self.lib.mcfg_colloid_repulsion(self._h, _ptr(out, C.c_double)))
+        return out
 
     def upload_force(self, f) -> None:
         self._f = _as(f, np.float64, (self.n, self.dim))

@@ -85,6 +85,25 @@ class SDPDParams(C.Structure):
         return out
 
 
+class ColloidParams(C.Structure):
+    """mcfg_colloid_params: the Colloid object's pair-term parameters."""
+
+    _fields_ = [
+        ("num_colloid", C.c_int32),
+        ("noslip_type", C.c_int32),
+        ("rho_type", C.c_int32),
+        ("translate", C.c_int32),
+        ("rotate", C.c_int32),
+        ("pp_interact_cc", C.c_int32),
+        ("cc_repul_type", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("dout", C.c_double),
+        ("cc_repul_F0", C.c_double),
+        ("cc_repul_cut_off", C.c_double),
+        ("cc_repul_cut_on", C.c_double),
+    ]
+
+
 class SDPDInfo(C.Structure):
     _fields_ = [
         ("num_part", C.c_int64),

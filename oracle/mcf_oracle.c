@@ -54,6 +54,9 @@ struct orc_state {
   int have_list, have_density, have_pressure;
   int64_t npairs;
   int nthreads;
+  /* colloids (Class_Colloid): centre, velocity, angular velocity, radius */
+  mcfg_colloid_params cp;
+  double *cx, *cv, *com, *crad;
   double timers[4];
   char err[256];
 };
@@ -273,6 +276,7 @@ static void free_arrays(orc_state* s) {
 void orc_destroy(orc_state* s) {
   if (!s) return;
   free_arrays(s);
+  free(s->cx); free(s->cv); free(s->com); free(s->crad);
   free(s->lhbx); free(s->lpdx); free(s->pbox);
   free(s);
 }
@@ -679,7 +683,174 @@ static void for_all_pairs(orc_state* s, pair_fn fn, void* ctx) {
 static int dyn_rho(const orc_state* s, int32_t sid) {
   if (sid == 0) return 1;
   if (sid < 0) return s->p.wall_rho_type == 1;
-  return 0; /* colloid boundary particles: constant density in this build */
+  return s->cp.rho_type == 1;
+}
+
+/* colloid_in_nearest_image.F90 (periodic part): image of colloid c's centre
+ * nearest to x (within radius + dout per axis), its velocity, and
+ * rx = x - image */
+static void colloid_nearest_image(const orc_state* s, const double* x, int c, double* ximg,
+                                  double* rx, double* vimg) {
+  const int d = s->d;
+  const double dmax = s->crad[c] + s->cp.dout;
+  for (int a = 0; a < d; ++a) {
+    ximg[a] = s->cx[c * d + a];
+    vimg[a] = s->cv[c * d + a];
+    const double r = x[a] - ximg[a];
+    if (r > dmax && s->periodic[a]) ximg[a] = ximg[a] + s->len[a];
+    else if (-r > dmax && s->periodic[a]) ximg[a] = ximg[a] - s->len[a];
+    rx[a] = x[a] - ximg[a];
+  }
+}
+
+static void cross3(const double* a, const double* b, double* o) {
+  o[0] = a[1] * b[2] - a[2] * b[1];
+  o[1] = a[2] * b[0] - a[0] * b[2];
+  o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+/* colloid_particle_velocity.F90: V + Omega x rx of a boundary particle */
+static void colloid_particle_velocity(const orc_state* s, const double* x, int c, double* vout) {
+  const int d = s->d;
+  for (int a = 0; a < d; ++a) vout[a] = 0.0;
+  if (!(s->cp.translate || s->cp.rotate)) return;
+  double ximg[3], rx[3] = {0, 0, 0}, vimg[3];
+  colloid_nearest_image(s, x, c, ximg, rx, vimg);
+  for (int a = 0; a < d; ++a) vout[a] = vimg[a];
+  if (s->cp.rotate) {
+    double r3[3] = {rx[0], rx[1], d == 3 ? rx[2] : 0.0}, w[3];
+    cross3(&s->com[c * 3], r3, w);
+    for (int a = 0; a < d; ++a) vout[a] = vout[a] + w[a];
+  }
+}
+
+/* colloid_noslip_Morris_sphere.F90:129-300 (disk in 2D) and
+ * colloid_noslip_frozen.F90: velocity given to boundary particle xc of
+ * colloid c seen from fluid particle xf with velocity vf */
+static void colloid_noslip(const orc_state* s, const double* xf, const double* xc,
+                           const double* vf, int c, double* vc) {
+  const int d = s->d;
+  double xcoll[3], r_xc[3] = {0, 0, 0}, vcoll[3];
+  colloid_nearest_image(s, xc, c, xcoll, r_xc, vcoll);
+  const double* om = &s->com[c * 3];
+  if (s->cp.noslip_type <= 1) {
+    for (int a = 0; a < d; ++a) vc[a] = vcoll[a];
+    if (s->cp.rotate) {
+      double r3[3] = {r_xc[0], r_xc[1], d == 3 ? r_xc[2] : 0.0}, w[3];
+      cross3(om, r3, w);
+      for (int a = 0; a < d; ++a) vc[a] = vc[a] + w[a];
+    }
+    return;
+  }
+  const double R = s->crad[c];
+  double r_xf[3] = {0, 0, 0};
+  for (int a = 0; a < d; ++a) r_xf[a] = xf[a] - xcoll[a];
+  double dd = 0.0;
+  for (int a = 0; a < d; ++a) dd = dd + r_xf[a] * r_xf[a];
+  const double d_fcoll = sqrt(dd);
+  if (d_fcoll <= R) {
+    for (int a = 0; a < d; ++a) vc[a] = vcoll[a];
+    if (s->cp.rotate) {
+      double r3[3] = {r_xc[0], r_xc[1], d == 3 ? r_xc[2] : 0.0}, w[3];
+      cross3(om, r3, w);
+      for (int a = 0; a < d; ++a) vc[a] = vc[a] + w[a];
+    }
+    return;
+  }
+  double nvec[3] = {0, 0, 0}, d_cn = 0.0;
+  for (int a = 0; a < d; ++a) nvec[a] = r_xf[a] / d_fcoll;
+  for (int a = 0; a < d; ++a) d_cn = d_cn + r_xc[a] * nvec[a];
+  const double d_cs = R - d_cn;
+  double d_fs = d_fcoll - R;
+  double r_xs[3] = {0, 0, 0};
+  for (int a = 0; a < d; ++a) r_xs[a] = R / d_fcoll * r_xf[a];
+  double corr;
+  if (fabs(d_fs) < s->machine_zero) {
+    d_fs = s->machine_zero;
+    corr = 0.5; /* mcf_colloid_dist_ratio_max */
+  } else {
+    corr = d_cs / d_fs;
+    if (corr > 0.5) corr = 0.5;
+    else if (corr < -0.5) corr = -0.5;
+  }
+  double r_vs[3] = {0, 0, 0};
+  if (s->cp.rotate) cross3(om, r_xs, r_vs);
+  for (int a = 0; a < d; ++a) vc[a] = -corr * (vf[a] - vcoll[a] - r_vs[a]) + vcoll[a] + r_vs[a];
+}
+
+int orc_set_colloids(orc_state* s, const mcfg_colloid_params* cp, const double* x,
+                     const double* v, const double* omega, const double* radius) {
+  const int nc = cp->num_colloid, d = s->d;
+  s->cp = *cp;
+  free(s->cx); free(s->cv); free(s->com); free(s->crad);
+  s->cx = (double*)malloc(sizeof(double) * (size_t)(nc * d + 1));
+  s->cv = (double*)malloc(sizeof(double) * (size_t)(nc * d + 1));
+  s->com = (double*)malloc(sizeof(double) * (size_t)(nc * 3 + 1));
+  s->crad = (double*)malloc(sizeof(double) * (size_t)(nc + 1));
+  memcpy(s->cx, x, sizeof(double) * (size_t)(nc * d));
+  memcpy(s->cv, v, sizeof(double) * (size_t)(nc * d));
+  memcpy(s->com, omega, sizeof(double) * (size_t)(nc * 3));
+  memcpy(s->crad, radius, sizeof(double) * (size_t)nc);
+  return 0;
+}
+
+/* particles_collect_colloid_interaction.F90:93-136 */
+int orc_colloid_drag(orc_state* s, double* drag, double* torque) {
+  const int d = s->d, nc = s->cp.num_colloid;
+  for (int k = 0; k < nc * d; ++k) drag[k] = 0.0;
+  for (int k = 0; k < nc * 3; ++k) torque[k] = 0.0;
+  for (int64_t j = 0; j < s->nreal; ++j) {
+    const int c = s->sid[j] - 1;
+    if (s->sid[j] <= 0 || c >= nc) continue;
+    double F[3] = {0, 0, 0};
+    for (int a = 0; a < d; ++a) F[a] = s->f[j * d + a] * s->m[j];
+    for (int a = 0; a < d; ++a) drag[c * d + a] = drag[c * d + a] + F[a];
+    double ximg[3], rx[3] = {0, 0, 0}, vimg[3], T[3];
+    colloid_nearest_image(s, &s->x[j * d], c, ximg, rx, vimg);
+    cross3(rx, F, T);
+    for (int a = 0; a < 3; ++a) torque[c * 3 + a] = torque[c * 3 + a] + T[a];
+  }
+  return 0;
+}
+
+/* colloid_compute_repulsion_cc.F90:95-164, nearest periodic image */
+int orc_colloid_repulsion(orc_state* s, double* force) {
+  const int d = s->d, nc = s->cp.num_colloid;
+  for (int k = 0; k < nc * d; ++k) force[k] = 0.0;
+  if (s->cp.cc_repul_type < 1) return 0;
+  const double hn = s->cp.cc_repul_cut_off, hm = s->cp.cc_repul_cut_on, F0 = s->cp.cc_repul_F0;
+  for (int i = 0; i < nc; ++i)
+    for (int j = i + 1; j < nc; ++j) {
+      double R12[3] = {0, 0, 0}, rr = 0.0;
+      for (int a = 0; a < d; ++a) {
+        double r = s->cx[i * d + a] - s->cx[j * d + a];
+        if (s->periodic[a]) {
+          if (r > 0.5 * s->len[a]) r -= s->len[a];
+          else if (r < -0.5 * s->len[a]) r += s->len[a];
+        }
+        R12[a] = r;
+        rr += r * r;
+      }
+      const double r = sqrt(rr);
+      double h = r - (s->crad[i] + s->crad[j]);
+      if (!(h < 5.0 * hn)) continue;
+      double F = 0.0;
+      if (s->cp.cc_repul_type == 1) {
+        if (h < hn) {
+          if (h < hm) h = hm;
+          F = F0 - F0 * h / hn;
+        }
+      } else {
+        if (h < hm) h = hm;
+        F = F0 / hn * exp(-h / hn) / (1.0 - exp(-h / hn)) -
+            F0 / hn * exp(-5.0) / (1.0 - exp(-5.0));
+      }
+      for (int a = 0; a < d; ++a) {
+        force[i * d + a] += F * R12[a] / r;
+        force[j * d + a] -= F * R12[a] / r;
+      }
+    }
+  return 0;
 }
 
 static void density_pair(orc_state* s, int64_t ip, int64_t jp, void* ctx) {
@@ -729,6 +900,9 @@ int orc_compute_density(orc_state* s) {
       const int64_t o = s->owner[g];
       if (dyn_rho(s, s->sid[o])) s->rho[o] = s->rho[o] + s->rho[g];
     }
+  if (s->cp.num_colloid > 0) /* marching_integrate_VV.F90:1074 */
+    for (int64_t j = 0; j < s->nreal; ++j)
+      if (s->sid[j] > 0) colloid_particle_velocity(s, &s->x[j * s->d], s->sid[j] - 1, &s->v[j * s->d]);
   ghost_refresh(s);
   s->have_density = 1;
   s->timers[1] += now_s() - t0;
@@ -1001,7 +1175,7 @@ static void force_pair(orc_state* s, int64_t ip, int64_t jp, void* ctx) {
   const int d = s->d;
   const int32_t si = s->sid[ip], sj = s->sid[jp];
   if (si < 0 && sj < 0) return; /* w-w: no interaction */
-  if (si > 0 && sj > 0) return; /* c-c off (pp_interact_cc = F)     */
+  if (si > 0 && sj > 0 && (si == sj || !s->cp.pp_interact_cc)) return; /* c-c */
   if ((si > 0 && sj < 0) || (si < 0 && sj > 0)) return; /* c-w off */
   double rij[3];
   double dij = 0.0;
@@ -1025,6 +1199,12 @@ static void force_pair(orc_state* s, int64_t ip, int64_t jp, void* ctx) {
   } else if (si < 0 && sj == 0) { /* pp_interaction_wf.inc */
     wall_noslip(s, &s->x[jp * d], &s->x[ip * d], vj, vi, si);
     pi = pj;
+  } else if (si == 0 && sj > 0) { /* pp_interaction_fc.inc */
+    if (s->cp.noslip_type == 2) colloid_noslip(s, &s->x[ip * d], &s->x[jp * d], vi, sj - 1, vj);
+    pj = pi;
+  } else if (si > 0 && sj == 0) { /* pp_interaction_cf.inc */
+    if (s->cp.noslip_type == 2) colloid_noslip(s, &s->x[jp * d], &s->x[ip * d], vj, si - 1, vi);
+    pi = pj;
   }
   double fi[3], fj[3];
   if (s->p.Newtonian) {
@@ -1033,7 +1213,7 @@ static void force_pair(orc_state* s, int64_t ip, int64_t jp, void* ctx) {
   } else {
     /* pp_interaction_ff/fw/wf.inc, non-Newtonian branch: a boundary
      * partner takes the fluid particle's density and pressure tensor */
-    const int64_t pf = (si < 0) ? jp : ip; /* the fluid one of a f-w pair */
+    const int64_t pf = (si != 0) ? jp : ip; /* the fluid one of a fluid-boundary pair */
     const double rho_ip = (si == 0 && sj == 0) ? s->rho[ip] : s->rho[pf];
     const double rho_jp = (si == 0 && sj == 0) ? s->rho[jp] : s->rho[pf];
     /* pp_vgt_ip.inc / pp_vgt_jp.inc */

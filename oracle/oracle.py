@@ -20,7 +20,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent))
 
-from mcf_gb300.params import SDPDParams  # noqa: E402  (struct layout only)
+from mcf_gb300.params import ColloidParams, SDPDParams  # noqa: E402  (struct layouts only)
 
 from . import build as _build  # noqa: E402
 
@@ -65,6 +65,9 @@ def load(rebuild: bool = True) -> C.CDLL:
         "orc_pair_normals": (None, [C.c_uint64, C.c_int64, C.c_int32, C.c_int32, C.c_int,
                                     C.POINTER(C.c_float)]),
         "orc_kernel": (C.c_int, [_h, C.c_double, _dp, _dp]),
+        "orc_set_colloids": (C.c_int, [_h, C.POINTER(ColloidParams), _dp, _dp, _dp, _dp]),
+        "orc_colloid_drag": (C.c_int, [_h, _dp, _dp]),
+        "orc_colloid_repulsion": (C.c_int, [_h, _dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -196,6 +199,30 @@ class Oracle:
     def force_scale(self) -> np.ndarray:
         out = np.empty(self.n)
         self.lib.orc_force_scale(self._h, _ptr(out, C.c_double))
+        return out
+
+    def set_colloids(self, cp, x, v, omega, radius):
+        self._cp = cp
+        self._cx = np.ascontiguousarray(x, np.float64)
+        self._cv = np.ascontiguousarray(v, np.float64)
+        self._com = np.ascontiguousarray(omega, np.float64)
+        self._crad = np.ascontiguousarray(radius, np.float64)
+        self._check("set_colloids", self.lib.orc_set_colloids(
+            self._h, C.byref(cp), _ptr(self._cx, C.c_double), _ptr(self._cv, C.c_double),
+            _ptr(self._com, C.c_double), _ptr(self._crad, C.c_double)))
+
+    def colloid_drag(self):
+        nc = self._cp.num_colloid
+        drag = np.zeros((nc, self.dim))
+        torque = np.zeros((nc, 3))
+        self._check("colloid_drag", self.lib.orc_colloid_drag(self._h, _ptr(drag, C.c_double),
+                                                               _ptr(torque, C.c_double)))
+        return drag, torque
+
+    def colloid_repulsion(self):
+        out = np.zeros((self._cp.num_colloid, self.dim))
+        self._check("colloid_repulsion", self.lib.orc_colloid_repulsion(self._h,
+                                                                         _ptr(out, C.c_double)))
         return out
 
     def counts(self):

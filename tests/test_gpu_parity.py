@@ -300,3 +300,55 @@ def test_oldroyd_b_fp32_mixed_ct_error(gpu_lib):
     b = o.download("ct")["ct"]
     dev = np.abs(b - np.array([1.0, 0, 0, 1.0]))
     assert np.max(np.abs(a - b)) <= 1e-3 * dev.max() + 1e-9
+
+
+# ------------------------------------------------------------------ colloids
+def colloid_case(precision=PRECISION_FP64, noslip=2):
+    w, cs = configs.c4_colloids(n_side=24, n_colloid=4, radius=3.0, precision=precision,
+                                v_scale=0.05, omega_scale=0.02)
+    rng = np.random.default_rng(13)
+    fl = w.id[:, 1] == 0
+    w.v[fl] = rng.normal(0, 1e-2, (int(fl.sum()), 3))
+    w.x[fl] += rng.uniform(-0.1, 0.1, (int(fl.sum()), 3))
+    cs.params.noslip_type = noslip
+    return w, cs
+
+
+@pytest.mark.parametrize("noslip", [1, 2])
+def test_colloid_pair_terms_fp64(gpu_lib, noslip):
+    w, cs = colloid_case(noslip=noslip)
+    assert (w.id[:, 1] > 0).sum() > 100
+    g, o = both(w, Brownian=0, kt=0.0)
+    for h in (g, o):
+        h.set_colloids(cs.params, cs.x, cs.v, cs.omega, cs.radius)
+    a, b = check_rhs(g, o)
+    va = g.download("v")["v"]
+    vb = o.download("v")["v"]
+    bp = w.id[:, 1] > 0
+    assert np.allclose(va[bp], vb[bp], rtol=0, atol=1e-14)  # rigid boundary velocities
+    da, ta = g.colloid_drag()
+    db, tb = o.colloid_drag()
+    scale = np.abs(db).max() + np.abs(tb).max()
+    assert np.max(np.abs(da - db)) <= 1e-10 * scale
+    assert np.max(np.abs(ta - tb)) <= 1e-10 * scale
+    assert np.allclose(g.colloid_repulsion(), o.colloid_repulsion(), rtol=1e-12, atol=1e-14)
+
+
+def test_colloid_steps_fp64_and_fp32(gpu_lib):
+    w, cs = colloid_case()
+    g, o = both(w, Brownian=0, kt=0.0)
+    p32 = w.params.copy()
+    p32.precision = PRECISION_FP32_MIXED
+    p32.Brownian = 0
+    p32.kt = 0.0
+    g32 = SDPD(p32)
+    g32.upload(w.x, w.v, w.m, w.id)
+    for h in (g, o, g32):
+        h.set_colloids(cs.params, cs.x, cs.v, cs.omega, cs.radius)
+        h.marching_init_force(0)
+        h.run_vv(0, 5, w.dt)
+    a, b, c32 = (h.download("x", "v") for h in (g, o, g32))
+    assert np.max(np.abs(a["x"] - b["x"])) <= 1e-11
+    vs = np.abs(b["v"]).max()
+    assert np.max(np.abs(a["v"] - b["v"])) <= 1e-9 * vs
+    assert np.max(np.abs(c32["v"] - b["v"])) <= 2e-4 * vs

@@ -172,3 +172,75 @@ def test_oldroyd_b_loop_modes_agree_and_act():
     ct = outs[0]["ct"]
     assert np.max(np.abs(ct - np.array([1.0, 0, 0, 1.0]))) > 1e-8  # it evolved
     assert np.max(np.abs(ct[:, 1] - ct[:, 2])) < 1e-12  # stays symmetric
+
+
+def _colloid_oracle(symmetry, noslip, **over):
+    w, cs = configs.c4_colloids(n_side=24, n_colloid=4, radius=3.0, v_scale=0.05,
+                                omega_scale=0.02)
+    rng = np.random.default_rng(13)
+    fl = w.id[:, 1] == 0
+    w.v[fl] = rng.normal(0, 1e-2, (int(fl.sum()), 3))
+    w.x[fl] += rng.uniform(-0.1, 0.1, (int(fl.sum()), 3))
+    cs.params.noslip_type = noslip
+    p = w.params.copy()
+    p.symmetry = symmetry
+    for k, v in over.items():
+        setattr(p, k, v)
+    o = Oracle(p)
+    o.upload(w.x, w.v, w.m, w.id)
+    o.set_colloids(cs.params, cs.x, cs.v, cs.omega, cs.radius)
+    o.marching_init_force(0)
+    return w, cs, o
+
+
+@pytest.mark.parametrize("noslip", [1, 2])
+def test_colloid_loop_modes_agree(noslip):
+    # the fluid-colloid pair term (Morris sphere no-slip) computed once per
+    # pair with the ghost put, and from both sides in the full loops
+    res = []
+    for sym in (1, 0):
+        w, cs, o = _colloid_oracle(sym, noslip)
+        d = o.download("rho", "f", "v")
+        res.append((d, o.force_scale(), o.colloid_drag()))
+    (a, sa, (da, ta)), (b, _, (db, tb)) = res
+    assert np.allclose(a["rho"], b["rho"], rtol=1e-13, atol=0)
+    assert np.all(np.abs(a["f"] - b["f"]) <= 1e-12 * (sa[:, None] + np.abs(a["f"])))
+    assert np.allclose(da, db, rtol=1e-10, atol=1e-12)
+    assert np.allclose(ta, tb, rtol=1e-10, atol=1e-12)
+    # boundary particles carry the rigid-body velocity V + Omega x r
+    bp = w.id[:, 1] > 0
+    ci = w.id[bp, 1] - 1
+    L = 24.0
+    r = w.x[bp] - cs.x[ci]
+    r -= L * np.round(r / L)
+    expect = cs.v[ci] + np.cross(cs.omega[ci], r)
+    assert np.allclose(a["v"][bp], expect, rtol=0, atol=1e-14)
+
+
+def test_colloid_momentum_balance():
+    # pair forces are equal and opposite: what the fluid gains the colloids
+    # lose (drag = sum of m f over each colloid's boundary particles)
+    w, cs, o = _colloid_oracle(1, 2, body_force_type=0, Brownian=0, kt=0.0)
+    d = o.download("f")
+    fl = w.id[:, 1] == 0
+    fluid = (d["f"][fl] * w.m[fl, None]).sum(0)
+    drag, torque = o.colloid_drag()
+    assert np.abs(drag).max() > 1e-6
+    assert np.allclose(fluid + drag.sum(0), 0.0, atol=1e-9 * np.abs(drag).max() + 1e-10)
+    bp = ~fl
+    assert np.allclose(drag.sum(0), (d["f"][bp] * w.m[bp, None]).sum(0), rtol=1e-10, atol=1e-12)
+
+
+def test_colloid_repulsion_is_pairwise_antisymmetric():
+    w, cs = configs.c4_colloids(n_side=24, n_colloid=2, radius=3.0, min_gap=0.05)
+    # place the two spheres 0.2 apart through the periodic x face
+    cs.x[0] = [0.5, 12.0, 12.0]
+    cs.x[1] = [24.0 - 5.7, 12.0, 12.0]
+    o = Oracle(w.params)
+    o.upload(w.x, w.v, w.m, w.id)
+    for t in (1, 2):
+        cs.params.cc_repul_type = t
+        o.set_colloids(cs.params, cs.x, cs.v, cs.omega, cs.radius)
+        fr = o.colloid_repulsion()
+        assert np.allclose(fr[0] + fr[1], 0.0, atol=1e-12)
+        assert fr[0, 0] > 0.0 and abs(fr[0, 1]) < 1e-12  # pushed apart along x
