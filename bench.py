@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     return ap.parse_args()
 
@@ -275,6 +276,44 @@ def roofline_for(sd, torch, w, prec_idx, peaks, step0):
             "peak_source": peaks.get("source"), "phase_share": share}
 
 
+def adjoint_cost(torch, w, T, K, local, wts):
+    """Wall time of mcfg_adjoint_run (J and dJ/d(eta, tau, c) over T steps,
+    checkpoints every K) against the forward trajectory it differentiates
+    (mcfg_init_force + mcfg_run_vv of the same T steps), both after a warm-up
+    call; returns the ratio and both times."""
+    from mcf_gb300 import SDPD
+
+    w.params.device = local
+    w.params.stress_tensor = 1
+    sd = SDPD(w.params)
+
+    def fwd():
+        sd.upload(w.x, w.v, w.m, w.id)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sd.marching_init_force(0)
+        sd.run_vv(0, T, w.dt)
+        sd.synchronize()
+        return time.perf_counter() - t0
+
+    def adj():
+        sd.upload(w.x, w.v, w.m, w.id)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        J, g = sd.adjoint_run(0, T, w.dt, wts, checkpoint_every=K)
+        return time.perf_counter() - t0, J, g
+
+    fwd()
+    adj()
+    tf = min(fwd() for _ in range(3))
+    ta, J, g = min((adj() for _ in range(3)), key=lambda r: r[0])
+    return {"workload": w.name, "n": w.n, "steps": T, "checkpoint_every": K,
+            "forward_ms": 1e3 * tf, "adjoint_ms": 1e3 * ta, "adjoint_over_forward": ta / tf,
+            "J": J, "dJ_deta_tau_c": [float(x) for x in g],
+            "timing": "wall clock, best of 3 after a warm-up call; adjoint includes its own "
+                      "forward pass, checkpoints and segment recomputation"}
+
+
 def run_ours(args, ws, rank, local):
     import numpy as np
     import torch
@@ -371,6 +410,14 @@ def run_ours(args, ws, rank, local):
                "h2d_bytes_per_step": int(n * (3 * 8 * 3 + 8 + 8)),
                "d2h_bytes_per_step": int(n * 3 * 8 * 3), "steps": ke,
                "path": "mcfg_upload + mcfg_upload_force + mcfg_step_vv + mcfg_download per step"}
+    adjoint = None
+    if not args.no_adjoint:
+        w5 = configs.c5_oldroyd_b_2d()
+        w5.v = np.random.default_rng(55).normal(0, 1e-3, w5.v.shape)
+        adjoint = adjoint_cost(torch, w5, 200, 20, local, [0.0, 0.5, 0.5, 0.0])
+        w3 = configs.c2_fluctuating_3d(n_side=args.n_side)
+        adjoint["periodic_3d"] = adjoint_cost(torch, w3, 20, 10, local,
+                                              [0, 0.5, 0, 0.5, 0, 0, 0, 0, 0])
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(w, args.cpu_sample_steps)
@@ -389,6 +436,7 @@ def run_ours(args, ws, rank, local):
                    "neighbour_capacity": info["neigh_capacity"], "max_neigh": info["max_neigh"],
                    "pairs_per_step": info["num_pairs"]},
         "roofline": roof, "fp64": fp64, "fp32_error_vs_fp64": err, "e2e": e2e,
+        "adjoint": adjoint,
         "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
         "pair_interactions_per_s": info["num_pairs"] * args.steps * ws / tmax,
     }

@@ -256,6 +256,33 @@ int mcfg_synchronize(mcfg_handle* h);
  * callers that time or order work around them; NULL on error. */
 void* mcfg_get_stream(mcfg_handle* h);
 
+/* Adjoint of the time-averaged stress (differentiation form; MCF has no
+ * counterpart, it differentiates the VV step of marching_integrate_VV.F90:
+ * 303-1620 as this library computes it).  From the state the handle holds
+ * (x0, v0, ct0 as uploaded) the call runs the initial right-hand side at
+ * step0 (as mcfg_init_force) and nsteps VV steps step0+1 ... (as
+ * mcfg_run_vv) and evaluates
+ *     J = (1/nsteps) sum_{t=1..nsteps} sum_q w[q] S_t[q],
+ * S_t being the stress mcfg_statistics reports after step t (d*d entries,
+ * the same layout; stress_tensor must be on).  The reverse sweep replays
+ * the Philox noise of every pair from the same keys, keeps a checkpoint of
+ * the state every checkpoint_every steps (<= 0: 20) and recomputes each
+ * segment forward before walking it backwards; the pair and density sums
+ * have hand-written adjoint kernels.  Outputs (any may be NULL): J;
+ * dJ_dparams[3] = dJ/d(eta, tau, c) (c the sound speed of the equation of
+ * state, tau at fixed G = n_p kt_p; tau's entry is 0 for a Newtonian run);
+ * dJ_dx0, dJ_dv0 [n*d] and dJ_dct0 [n*d*d] (Oldroyd-B only) in host particle
+ * order.  Afterwards the handle holds the state after the last step, as
+ * mcfg_run_vv would leave it.  Supported: FP64 precision, all-fluid
+ * periodic boxes (no walls or colloids), number density (rhs_density_type
+ * 2), Hu-Adams force (rhs_force_type 3) with or without the random term,
+ * either kernel, either equation of state, body force types 0-3, Newtonian
+ * or Oldroyd-B; anything else returns MCFG_ENOTSUP. */
+int mcfg_adjoint_run(mcfg_handle* h, int64_t step0, int32_t nsteps, double dt,
+                     int32_t checkpoint_every, const double* w, double* J,
+                     double* dJ_dparams, double* dJ_dx0, double* dJ_dv0,
+                     double* dJ_dct0);
+
 /* Per-phase device timers (CUDA events on the handle's stream), the
  * GPU counterpart of MCF's __DEBUG_INTEGRATE_VV phase times
  * (marching_integrate_VV.F90:131-143,1679-1709).  Phases: 0 cell list,

@@ -19,7 +19,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libmcfg.so"
-SOURCES = ["mcfg_api.cu", "cell_list.cu", "pair_kernels.cu", "update.cu", "noalloc.cu"]
+SOURCES = ["mcfg_api.cu", "cell_list.cu", "pair_kernels.cu", "update.cu", "noalloc.cu", "adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -48,7 +48,10 @@ def _flags() -> list[str]:
 # Per-file flags.  The pair sweeps run their FP32 path with flush-to-zero and
 # approximate FP32 division / square root (MUFU based, no slow-path calls);
 # these flags do not touch FP64 arithmetic, so the FP64 path is unchanged.
-EXTRA = {"pair_kernels.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]}
+# The adjoint replays the pair normals (FP32 Box-Muller), so it is compiled
+# with the same flags to draw the same bits.
+_PAIR_FLAGS = ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
+EXTRA = {"pair_kernels.cu": _PAIR_FLAGS, "adjoint.cu": _PAIR_FLAGS}
 
 
 def _compile(src: str, verbose: bool) -> Path:

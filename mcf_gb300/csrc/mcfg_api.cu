@@ -13,8 +13,6 @@
 
 using namespace mcfg;
 
-struct mcfg_handle : public Handle {};
-
 namespace mcfg {
 
 int set_error(Handle* h, int code, const std::string& msg) {
@@ -108,6 +106,7 @@ int dalloc(Handle* h, T** p, size_t count) {
 }
 
 void free_all(Handle* h) {
+  free_adjoint(h);
   void* ptrs[] = {h->x, h->v, h->f, h->m, h->pid, h->sid, h->hidx, h->rho, h->pr, h->st,
                   h->x2, h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->key, h->rank,
                   h->cnt, h->cell_start, h->scan_part, h->order, h->off, h->cell_of, h->nl,
@@ -427,6 +426,10 @@ int set_device(Handle* h) {
     if (_rc) return _rc;   \
   } while (0)
 
+}  // namespace
+
+namespace mcfg {
+
 int rhs(Handle* h, int64_t step, int fuse_mode, double dt) {
   {
     PhaseScope ps(h, kPhaseList);
@@ -450,6 +453,10 @@ int kdw(Handle* h, double dt) {
   PhaseScope ps(h, kPhaseUpdate);
   return kick_drift_wrap(h, dt);
 }
+
+}  // namespace mcfg
+
+namespace {
 
 __global__ void k_upload_force(int n, int d, const double* __restrict__ hf,
                                const int* __restrict__ hidx, double4_32a* __restrict__ f) {
@@ -599,7 +606,12 @@ int mcfg_upload(mcfg_handle* h, int64_t n, const double* x, const double* v, con
   // boundary particles of each colloid (host indices), for the drag sums
   {
     int maxc = 0;
-    for (int64_t i = 0; i < n; ++i) maxc = std::max(maxc, (int)id[2 * i + 1]);
+    int64_t nb = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      maxc = std::max(maxc, (int)id[2 * i + 1]);
+      nb += (id[2 * i + 1] != 0) ? 1 : 0;
+    }
+    h->n_boundary = nb;
     h->h_coll_start.assign((size_t)maxc + 1, 0);
     h->h_coll_mem.clear();
     if (maxc > 0) {

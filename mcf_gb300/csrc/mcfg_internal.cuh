@@ -83,6 +83,7 @@ struct Handle {
   bool have_particles = false, have_list = false, have_density = false,
        have_pressure = false, have_force = false;
   int64_t n = 0;
+  int64_t n_boundary = 0;  // uploaded particles with sid != 0 (walls, colloids)
   int cap_n = 0;           // allocated particle capacity
   int neigh_cap = 0;       // neighbour list capacity per particle
   double dt = 0.0;
@@ -156,6 +157,8 @@ struct Handle {
   double* up_m = nullptr;
   int* up_id = nullptr;
   size_t up_cap = 0;
+  // ---- adjoint buffers (adjoint.cu), null until mcfg_adjoint_run ----
+  struct AdjBuffers* adj = nullptr;
   // ---- per-phase device timers ----
   bool profiling = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
@@ -204,6 +207,13 @@ void make_consts(const mcfg_params& p, Consts& k);
 int set_error(Handle* h, int code, const std::string& msg);
 int cuda_check(Handle* h, cudaError_t e, const char* what);
 
+}  // namespace mcfg
+
+// the opaque handle of the C ABI
+struct mcfg_handle : public mcfg::Handle {};
+
+namespace mcfg {
+
 // launches (implemented in the .cu files)
 int build_cell_list(Handle* h);
 int compute_density(Handle* h, bool with_pressure);
@@ -215,6 +225,14 @@ int integrate_position(Handle* h, double dt);
 int adjust_particles(Handle* h);
 int kick_drift_wrap(Handle* h, double dt);
 int statistics(Handle* h, double* ke, double* mom, double* stress);
+// second half kick v += (0.5 a) dt and, Oldroyd-B, ct += (act dt) 0.5 (the
+// unfused tail of a VV step, bit-identical to the fused force epilogue)
+int kick_ct_half(Handle* h, double dt);
+// right-hand side (cell list, density, pressure, force) and the first half
+// of a VV step (kick, drift, wrap, ct half step), with phase timers
+int rhs(Handle* h, int64_t step, int fuse_mode, double dt);
+int kdw(Handle* h, double dt);
+void free_adjoint(Handle* h);
 int colloid_drag(Handle* h, double* drag, double* torque);
 int check_device_errors(Handle* h);
 

@@ -82,6 +82,26 @@ __device__ __forceinline__ T kernel_gradw(const Consts& k, T r) {
   }
 }
 
+// d2W/dr2 for the adjoint: the derivative in r of kernel_gradw's
+// polynomials (quintic: coef/h^2 [20(3-s)^3 - 120(2-s)^3 + 300(1-s)^3]
+// piecewise; Lucy: -12 coef/h^2 (1-s)(1-3s)).
+template <typename T>
+__device__ __forceinline__ T kernel_grad2w(const Consts& k, T r) {
+  const T s = r * KC<T>::inv_h(k);
+  const T cg = KC<T>::coef_grad(k) * KC<T>::inv_h(k);  // -coef/h^2
+  if (k.kernel_type == 1) {
+    const T s3 = T(3) - s, s2 = T(2) - s, s1 = T(1) - s;
+    T g = T(0);
+    if (s < T(3)) g = T(-20) * (s3 * s3 * s3);
+    if (s < T(2)) g = g + T(120) * (s2 * s2 * s2);
+    if (s < T(1)) g = g - T(300) * (s1 * s1 * s1);
+    return cg * g;
+  } else {
+    if (s > T(1)) return T(0);
+    return cg * T(12) * (T(1) - s) * (T(1) - T(3) * s);
+  }
+}
+
 // Pressure, stateEquation_compute_pressure.F90:147-180 (vector forms):
 // Morris p = c^2 (rho^gamma - rho_ref), Batchelor p = p0((rho/rho_ref)^gamma - 1).
 __device__ __forceinline__ double eos_pressure(const Consts& k, double rho) {

@@ -240,6 +240,9 @@ int integrate_velocity(Handle* h, double dt, double lambda) {
 }
 int integrate_position(Handle* h, double dt) { return launch_integrate(h, 2, dt, 0.0); }
 int adjust_particles(Handle* h) { return launch_integrate(h, 4, 0.0, 0.0); }
+int kick_ct_half(Handle* h, double dt) {
+  return launch_integrate(h, h->p.Newtonian ? 1 : 9, dt, 0.5);
+}
 int kick_drift_wrap(Handle* h, double dt) {
   return launch_integrate(h, h->p.Newtonian ? 7 : 15, dt, 0.5);
 }

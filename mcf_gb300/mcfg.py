@@ -61,6 +61,8 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "mcfg_init_force": (C.c_int, [_h, C.c_int64]),
         "mcfg_step_vv": (C.c_int, [_h, C.c_int64, C.c_double]),
         "mcfg_run_vv": (C.c_int, [_h, C.c_int64, C.c_int32, C.c_double]),
+        "mcfg_adjoint_run": (C.c_int, [_h, C.c_int64, C.c_int32, C.c_double, C.c_int32, _dp, _dp,
+                                       _dp, _dp, _dp, _dp]),
         "mcfg_download": (C.c_int, [_h, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
         "mcfg_statistics": (C.c_int, [_h, _dp, _dp, _dp]),
         "mcfg_synchronize": (C.c_int, [_h]),
@@ -225,6 +227,30 @@ class SDPD:
 
     def run_vv(self, step0: int, nsteps: int, dt: float) -> None:
         self._check("marching_marching", self.lib.mcfg_run_vv(self._h, int(step0), int(nsteps), float(dt)))
+
+    def adjoint_run(self, step0: int, nsteps: int, dt: float, w, checkpoint_every: int = 20,
+                    state_grads: bool = False):
+        """Time-averaged stress J = mean_t sum_q w[q] S_t[q] over nsteps VV steps from
+        the uploaded state, and its gradient by the hand-written adjoint.
+        Returns (J, dJ/d(eta, tau, c)) or, with state_grads, also a dict of
+        dJ/dx0, dJ/dv0 (and dJ/dct0 for Oldroyd-B) in host order."""
+        d = self.dim
+        wv = np.zeros(9)
+        wv[: d * d] = np.asarray(w, np.float64).reshape(-1)[: d * d]
+        J = C.c_double()
+        g = np.zeros(3)
+        out = {}
+        if state_grads:
+            out["x"] = np.zeros((self.n, d))
+            out["v"] = np.zeros((self.n, d))
+            if not self.params.Newtonian:
+                out["ct"] = np.zeros((self.n, d * d))
+        self._check("mcfg_adjoint_run", self.lib.mcfg_adjoint_run(
+            self._h, int(step0), int(nsteps), float(dt), int(checkpoint_every),
+            _ptr(wv, C.c_double), C.byref(J), _ptr(g, C.c_double),
+            _ptr(out.get("x"), C.c_double), _ptr(out.get("v"), C.c_double),
+            _ptr(out.get("ct"), C.c_double)))
+        return (J.value, g, out) if state_grads else (J.value, g)
 
     def statistic_compute_statistic(self):
         ke = C.c_double()

@@ -217,6 +217,13 @@ void orc_pair_normals(uint64_t seed, int64_t step, int32_t pid_a, int32_t pid_b,
   }
 }
 
+/* the normals of many pairs (z[k*6 ...]) for checkers that evaluate pairs
+ * in their own order */
+void orc_pair_normals_batch(uint64_t seed, int64_t step, int64_t npairs, const int32_t* pa,
+                            const int32_t* pb, int dim, float* z) {
+  for (int64_t k = 0; k < npairs; ++k) orc_pair_normals(seed, step, pa[k], pb[k], dim, z + 6 * k);
+}
+
 /* ------------------------------------------------------------------------
  * Create / destroy
  * ---------------------------------------------------------------------- */

@@ -84,6 +84,8 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
 /* the six (3D) / three (2D) pair normals of one (seed, step, pid pair) */
 void orc_pair_normals(uint64_t seed, int64_t step, int32_t pid_a,
                       int32_t pid_b, int dim, float* z);
+void orc_pair_normals_batch(uint64_t seed, int64_t step, int64_t npairs, const int32_t* pa,
+                            const int32_t* pb, int dim, float* z);
 
 /* kernel value and derivative (kernel_kernel_*), for unit tests */
 int orc_kernel(const orc_state* s, double r, double* w, double* gradw);

@@ -64,6 +64,9 @@ def load(rebuild: bool = True) -> C.CDLL:
                                      C.POINTER(C.c_uint32)]),
         "orc_pair_normals": (None, [C.c_uint64, C.c_int64, C.c_int32, C.c_int32, C.c_int,
                                     C.POINTER(C.c_float)]),
+        "orc_pair_normals_batch": (None, [C.c_uint64, C.c_int64, C.c_int64,
+                                          C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int,
+                                          C.POINTER(C.c_float)]),
         "orc_kernel": (C.c_int, [_h, C.c_double, _dp, _dp]),
         "orc_set_colloids": (C.c_int, [_h, C.POINTER(ColloidParams), _dp, _dp, _dp, _dp]),
         "orc_colloid_drag": (C.c_int, [_h, _dp, _dp]),
@@ -246,6 +249,16 @@ def pair_normals(seed: int, step: int, pa: int, pb: int, dim: int) -> np.ndarray
     z = (C.c_float * 6)()
     load().orc_pair_normals(seed, step, pa, pb, dim, z)
     return np.array(z[: (6 if dim == 3 else 3)], dtype=np.float32)
+
+
+def pair_normals_batch(seed: int, step: int, pa, pb, dim: int) -> np.ndarray:
+    """normals of the pairs (pa[k], pb[k]): float32 [npairs, 6]"""
+    pa = np.ascontiguousarray(pa, np.int32)
+    pb = np.ascontiguousarray(pb, np.int32)
+    z = np.zeros((pa.size, 6), np.float32)
+    load().orc_pair_normals_batch(seed, step, pa.size, _ptr(pa, C.c_int32), _ptr(pb, C.c_int32),
+                                  dim, _ptr(z, C.c_float))
+    return z
 
 
 def philox(ctr, key) -> list[int]:
