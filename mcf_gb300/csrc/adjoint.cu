@@ -16,7 +16,8 @@
 //   xbar(prev) = xbar', vbar(prev) = vbar' + dt xbar', cbar(prev) = cbar'.
 // Each step's right-hand-side inputs (cell order, neighbour list included)
 // come from a tape filled while the segment since the last checkpoint is
-// recomputed; checkpoints are taken every K steps in the first pass.  The
+// recomputed (the last segment is taped during the first pass, which also
+// takes the checkpoints, every K steps).  The
 // random term is replayed from the same Philox keys (seed, step, pid pair).
 //
 // Pair VJP of the Hu-Adams force (rhs_force_ff_Newtonian_HuAdams.F90:124-237,
@@ -46,6 +47,7 @@ struct Tape {
   int* pid;
   int* hidx;
   int* ncount;
+  int* cell_of;      // cell of each particle (ncell: outside the mesh)
   int* cell_start;
   uint16_t* nl;      // [neigh][n]
   double* ct;        // [d*d][n] conformation tensor c' (Oldroyd-B)
@@ -86,6 +88,7 @@ void free_adjoint(Handle* h) {
 namespace {
 
 constexpr int kAdjRedThreads = 256;
+constexpr int kAdjTPB = 128;  // threads per block of the thread-per-particle sweeps
 
 template <typename T>
 int aalloc(Handle* h, AdjBuffers* b, T** p, size_t count) {
@@ -150,6 +153,7 @@ int ensure_buffers(Handle* h, int K, int T) {
     ATRY(aalloc(h, b, &t.pid, N));
     ATRY(aalloc(h, b, &t.hidx, N));
     ATRY(aalloc(h, b, &t.ncount, N));
+    ATRY(aalloc(h, b, &t.cell_of, N));
     ATRY(aalloc(h, b, &t.cell_start, (size_t)ncell + 2));
     ATRY(aalloc(h, b, &t.nl, (size_t)neigh * N));
     if (nnw) {
@@ -249,8 +253,8 @@ __global__ void k_ck_restore(int n, int d2, Ckpt in, const double* __restrict__ 
 __global__ void k_tape_record(int n, int ncell2, int d2, Tape out, const double4_32a* x,
                               const double4_32a* v, const double4_32a* pc, const double* rho,
                               const int* pid, const int* hidx, const int* ncount,
-                              const int* cell_start, const uint16_t* nl, const double* ct,
-                              const double* vgt) {
+                              const int* cell_of, const int* cell_start, const uint16_t* nl,
+                              const double* ct, const double* vgt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < ncell2) out.cell_start[i] = cell_start[i];
   if (i >= n) return;
@@ -260,6 +264,7 @@ __global__ void k_tape_record(int n, int ncell2, int d2, Tape out, const double4
   out.rho[i] = rho[i];
   out.pid[i] = pid[i];
   out.hidx[i] = hidx[i];
+  out.cell_of[i] = cell_of[i];
   const int c = ncount[i];
   out.ncount[i] = c;
   for (int e = 0; e < c; ++e) out.nl[(size_t)e * n + i] = nl[(size_t)e * n + i];
@@ -396,16 +401,16 @@ __global__ void k_adj_pre(Consts k, Tape tp, double phi, const double4_32a* __re
 // pair VJP of the force, the velocity gradient and the stress functional;
 // writes nbar (adjoint of the number density) for the density VJP
 template <int D, bool NNW>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+__global__ void __launch_bounds__(kAdjTPB)
     k_adj_force(Consts k, Tape tp, const double4_32a* __restrict__ lam,
                 const double* __restrict__ Lb, const double* __restrict__ w, double wscale,
                 uint32_t step, double inv_sqdt, double4_32a* __restrict__ xbs,
                 double4_32a* __restrict__ vbs, double* __restrict__ cbs,
                 double* __restrict__ nbar, double* __restrict__ gp) {
-  constexpr int CENTER = (D == 3) ? 13 : 4;
+  constexpr int NS = (D == 3) ? 27 : 9;
   constexpr int D2 = D * D;
-  __shared__ NbTable tab[kWarpsPerBlock];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ int s_start[NS * kAdjTPB];
+  __shared__ int s_shift[NS * kAdjTPB];
   const int n = k.n;
   const bool noise = k.noise != 0;
   const double eta = k.eta, kt = k.kt;
@@ -413,256 +418,244 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   double wt[D2];
 #pragma unroll
   for (int q = 0; q < D2; ++q) wt[q] = w[q] * wscale;
-  for (int cell = blockIdx.x * kWarpsPerBlock + wib; cell <= k.ncell;
-       cell += gridDim.x * kWarpsPerBlock) {
-    NbTable& t = tab[wib];
-    build_table<D>(k, cell, tp.cell_start, t);
-    const int c0 = t.start[CENTER], c1 = c0 + t.count[CENTER];
-    for (int base = c0; base < c1; base += 32) {
-      const int i = base + lane;
-      if (i >= c1) continue;
-      const double4_32a xi4 = tp.x[i];
-      const double xi[3] = {xi4.x, xi4.y, xi4.z};
-      const double4_32a vi4 = tp.v[i];
-      const double4_32a pci = tp.pc[i];
-      const double ni = tp.rho[i];
-      const double4_32a li4 = lam[i];
-      const int pidi = tp.pid[i];
-      double ci[D2], Lbi[D2];
-      if (NNW) {
+  const int tid = threadIdx.x;
+  const int i = blockIdx.x * kAdjTPB + tid;
+  if (i >= n) return;
+  build_lane_table<D, kAdjTPB>(k, tp.cell_of[i], tp.cell_start, s_start, s_shift);
+  const double4_32a xi4 = tp.x[i];
+  const double xi[3] = {xi4.x, xi4.y, xi4.z};
+  const double4_32a vi4 = tp.v[i];
+  const double4_32a pci = tp.pc[i];
+  const double ni = tp.rho[i];
+  const double4_32a li4 = lam[i];
+  const int pidi = tp.pid[i];
+  double ci[D2], Lbi[D2];
+  if (NNW) {
 #pragma unroll
-        for (int q = 0; q < D2; ++q) {
-          ci[q] = tp.ct[(size_t)q * n + i];
-          Lbi[q] = Lb[(size_t)q * n + i];
-        }
-      }
-      const double qi = 1.0 / ni;
-      double xb[3] = {0, 0, 0}, vb[3] = {0, 0, 0}, Pbar[D2];
-#pragma unroll
-      for (int q = 0; q < D2; ++q) Pbar[q] = 0.0;
-      double Bbar = 0.0, Abar = 0.0, nbL = 0.0, etab = 0.0;
-      const int cnt = tp.ncount[i];
-      for (int e = 0; e < cnt; ++e) {
-        const int ent = tp.nl[(size_t)e * n + i];
-        const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
-        const int j = t.start[sl] + q;
-        const double4_32a xj4 = tp.x[j];
-        const double xj[3] = {xj4.x, xj4.y, xj4.z};
-        double r[3];
-        const double dd2 = exact_sep<D>(k, xi, xj, t.shift[sl], r);
-        const double u = rsqrt(dd2);
-        const double dist = dd2 * u;
-        double ev[3];
-#pragma unroll
-        for (int a = 0; a < D; ++a) ev[a] = r[a] * u;
-        const double gw = kernel_gradw<double>(k, dist);
-        const double g2 = kernel_grad2w<double>(k, dist);
-        const double4_32a vj4 = tp.v[j];
-        const double4_32a pcj = tp.pc[j];
-        const double4_32a lj4 = lam[j];
-        double vij[3], gb[3], g[3];
-#pragma unroll
-        for (int a = 0; a < D; ++a) vij[a] = d4(vi4, a) - d4(vj4, a);
-        const double SB = pci.y + pcj.y, SA = pci.x + pcj.x;
-        const double f_c = SA * gw;
-        const double f_d = eta * SB * gw * u;
-        double dW[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-        double f_r = 0.0;
-        if (noise) {
-          float z[6];
-          pair_normals<D>(k.key0, k.key1, step, pidi, tp.pid[j], z);
-          noise_dw<D>(z, dW);
-          f_r = sqrt(-4.0 * kt * f_d) * inv_sqdt;
-        }
-        double P[D2], Phi[D2];
-        if (NNW) {
-          const double qj = 1.0 / tp.rho[j];
-#pragma unroll
-          for (int c = 0; c < D2; ++c) {
-            P[c] = G * (ci[c] * pci.y + tp.ct[(size_t)c * n + j] * pcj.y);
-            Phi[c] = Lbi[c] * qi + Lb[(size_t)c * n + j] * qj;
-          }
-        }
-        const double hm = 0.5 * (pci.z + pcj.z);
-        // forward pair value and its seed gbar = lam_i/m_i - lam_j/m_j + h w~ r
-        double We[3], Pr[3];
-#pragma unroll
-        for (int b = 0; b < D; ++b) {
-          We[b] = 0.0;
-#pragma unroll
-          for (int a = 0; a < D; ++a) We[b] += dW[b][a] * ev[a];
-          Pr[b] = 0.0;
-          if (NNW) {
-#pragma unroll
-            for (int a = 0; a < D; ++a) Pr[b] += P[a + D * b] * r[a];
-          }
-          g[b] = f_d * vij[b] - f_c * ev[b] + gw * u * Pr[b] + f_r * We[b];
-          double sw = 0.0;
-#pragma unroll
-          for (int a = 0; a < D; ++a) sw += wt[b * D + a] * r[a];
-          gb[b] = d4(li4, b) * pci.z - d4(lj4, b) * pcj.z + hm * sw;
-        }
-        double gbv = 0.0, gbe = 0.0, gbWe = 0.0, gbPr = 0.0;
-#pragma unroll
-        for (int a = 0; a < D; ++a) {
-          gbv += gb[a] * vij[a];
-          gbe += gb[a] * ev[a];
-          gbWe += gb[a] * We[a];
-          gbPr += gb[a] * Pr[a];
-        }
-        const double fdb = gbv + ((noise && f_d < 0.0) ? gbWe * f_r / (2.0 * f_d) : 0.0);
-        const double fcb = -gbe;
-        double Wb = fdb * eta * SB * u + fcb * SA + u * gbPr;
-        double ub = fdb * eta * SB * gw + gw * gbPr;
-        double rb[3], eb[3];
-#pragma unroll
-        for (int a = 0; a < D; ++a) {
-          double s1 = 0.0, s2 = 0.0, s3 = 0.0;
-#pragma unroll
-          for (int b = 0; b < D; ++b) {
-            s1 += wt[b * D + a] * g[b];
-            s2 += dW[a][b] * gb[b];
-            if (NNW) s3 += P[a + D * b] * gb[b];
-          }
-          rb[a] = hm * s1 + gw * u * s3;
-          eb[a] = -f_c * gb[a] + f_r * s2;
-        }
-        if (NNW) {
-          // L term: W' u sum_ab Phi_ab (v_j - v_i)_a r_b
-          double phv = 0.0, phi_i = 0.0;
-#pragma unroll
-          for (int b = 0; b < D; ++b)
-#pragma unroll
-            for (int a = 0; a < D; ++a) {
-              phv += Phi[a + D * b] * (-vij[a]) * r[b];
-              phi_i += Lbi[a + D * b] * (-vij[a]) * r[b];
-            }
-          Wb += u * phv;
-          ub += gw * phv;
-#pragma unroll
-          for (int b = 0; b < D; ++b) {
-            double s = 0.0, sv = 0.0;
-#pragma unroll
-            for (int a = 0; a < D; ++a) {
-              s += Phi[a + D * b] * (-vij[a]);
-              sv += Phi[b + D * a] * r[a];
-            }
-            rb[b] += gw * u * s;
-            vb[b] -= gw * u * sv;  // d/dv_i of (v_j - v_i)
-          }
-          nbL -= gw * u * phi_i * qi * qi;
-#pragma unroll
-          for (int b = 0; b < D; ++b)
-#pragma unroll
-            for (int a = 0; a < D; ++a) Pbar[a + D * b] += gw * u * r[a] * gb[b];
-        }
-        double ee = 0.0;
-#pragma unroll
-        for (int a = 0; a < D; ++a) ee += eb[a] * ev[a];
-        const double radial = Wb * g2 - ub * u * u;
-#pragma unroll
-        for (int a = 0; a < D; ++a) {
-          xb[a] += rb[a] + u * (eb[a] - ee * ev[a]) + radial * ev[a];
-          vb[a] += f_d * gb[a];
-        }
-        Bbar += fdb * eta * gw * u;
-        Abar += fcb * gw;
-        etab += 0.5 * fdb * SB * gw * u;
-      }
-      // per-particle chain: A = (p + G) B, B = 1/n^2, Q = G c B, p = EOS(n m)
-      const double Bi = pci.y, p = pci.w, mi = 1.0 / pci.z;
-      const double pbar = Abar * Bi;
-      double Bt = Bbar + Abar * (p + G);
-      if (NNW) {
-#pragma unroll
-        for (int q = 0; q < D2; ++q) {
-          Bt += G * ci[q] * Pbar[q];
-          cbs[(size_t)q * n + i] += G * Bi * Pbar[q];
-        }
-      }
-      const double r_eos = ni * mi;
-      double dpdn;
-      if (k.eos_type == 1)
-        dpdn = k.c2 * ((k.gamma == 1.0) ? 1.0 : k.gamma * pow(r_eos, k.gamma - 1.0)) * mi;
-      else
-        dpdn = k.p0 * ((k.gamma == 1.0) ? 1.0 : k.gamma * pow(r_eos / k.rho_ref, k.gamma - 1.0)) *
-               mi / k.rho_ref;
-      nbar[i] = Bt * (-2.0 * Bi * qi) + nbL + pbar * dpdn;
-      double4_32a xo = xbs[i], vo = vbs[i];
-      xo.x += xb[0];
-      xo.y += xb[1];
-      vo.x += vb[0];
-      vo.y += vb[1];
-      if (D == 3) {
-        xo.z += xb[2];
-        vo.z += vb[2];
-      }
-      xbs[i] = xo;
-      vbs[i] = vo;
-      const int hi = tp.hidx[i];
-      const double csound = sqrt(k.c2);
-      gp[hi] += etab;
-      gp[(size_t)2 * n + hi] += (csound > 0.0) ? pbar * 2.0 * p / csound : 0.0;
+    for (int q = 0; q < D2; ++q) {
+      ci[q] = tp.ct[(size_t)q * n + i];
+      Lbi[q] = Lb[(size_t)q * n + i];
     }
   }
+  const double qi = 1.0 / ni;
+  double xb[3] = {0, 0, 0}, vb[3] = {0, 0, 0}, Pbar[D2];
+#pragma unroll
+  for (int q = 0; q < D2; ++q) Pbar[q] = 0.0;
+  double Bbar = 0.0, Abar = 0.0, nbL = 0.0, etab = 0.0;
+  const int cnt = tp.ncount[i];
+  for (int e = 0; e < cnt; ++e) {
+    const int ent = tp.nl[(size_t)e * n + i];
+    const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
+    const int j = s_start[sl * kAdjTPB + tid] + q;
+    const double4_32a xj4 = tp.x[j];
+    const double xj[3] = {xj4.x, xj4.y, xj4.z};
+    double r[3];
+    const double dd2 = exact_sep<D>(k, xi, xj, s_shift[sl * kAdjTPB + tid], r);
+    const double u = rsqrt(dd2);
+    const double dist = dd2 * u;
+    double ev[3];
+#pragma unroll
+    for (int a = 0; a < D; ++a) ev[a] = r[a] * u;
+    const double gw = kernel_gradw<double>(k, dist);
+    const double g2 = kernel_grad2w<double>(k, dist);
+    const double4_32a vj4 = tp.v[j];
+    const double4_32a pcj = tp.pc[j];
+    const double4_32a lj4 = lam[j];
+    double vij[3], gb[3], g[3];
+#pragma unroll
+    for (int a = 0; a < D; ++a) vij[a] = d4(vi4, a) - d4(vj4, a);
+    const double SB = pci.y + pcj.y, SA = pci.x + pcj.x;
+    const double f_c = SA * gw;
+    const double f_d = eta * SB * gw * u;
+    double dW[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double f_r = 0.0;
+    if (noise) {
+      float z[6];
+      pair_normals<D>(k.key0, k.key1, step, pidi, tp.pid[j], z);
+      noise_dw<D>(z, dW);
+      f_r = sqrt(-4.0 * kt * f_d) * inv_sqdt;
+    }
+    double P[D2], Phi[D2];
+    if (NNW) {
+      const double qj = 1.0 / tp.rho[j];
+#pragma unroll
+      for (int c = 0; c < D2; ++c) {
+        P[c] = G * (ci[c] * pci.y + tp.ct[(size_t)c * n + j] * pcj.y);
+        Phi[c] = Lbi[c] * qi + Lb[(size_t)c * n + j] * qj;
+      }
+    }
+    const double hm = 0.5 * (pci.z + pcj.z);
+    // forward pair value and its seed gbar = lam_i/m_i - lam_j/m_j + h w~ r
+    double We[3], Pr[3];
+#pragma unroll
+    for (int b = 0; b < D; ++b) {
+      We[b] = 0.0;
+#pragma unroll
+      for (int a = 0; a < D; ++a) We[b] += dW[b][a] * ev[a];
+      Pr[b] = 0.0;
+      if (NNW) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) Pr[b] += P[a + D * b] * r[a];
+      }
+      g[b] = f_d * vij[b] - f_c * ev[b] + gw * u * Pr[b] + f_r * We[b];
+      double sw = 0.0;
+#pragma unroll
+      for (int a = 0; a < D; ++a) sw += wt[b * D + a] * r[a];
+      gb[b] = d4(li4, b) * pci.z - d4(lj4, b) * pcj.z + hm * sw;
+    }
+    double gbv = 0.0, gbe = 0.0, gbWe = 0.0, gbPr = 0.0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      gbv += gb[a] * vij[a];
+      gbe += gb[a] * ev[a];
+      gbWe += gb[a] * We[a];
+      gbPr += gb[a] * Pr[a];
+    }
+    const double fdb = gbv + ((noise && f_d < 0.0) ? gbWe * f_r / (2.0 * f_d) : 0.0);
+    const double fcb = -gbe;
+    double Wb = fdb * eta * SB * u + fcb * SA + u * gbPr;
+    double ub = fdb * eta * SB * gw + gw * gbPr;
+    double rb[3], eb[3];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+#pragma unroll
+      for (int b = 0; b < D; ++b) {
+        s1 += wt[b * D + a] * g[b];
+        s2 += dW[a][b] * gb[b];
+        if (NNW) s3 += P[a + D * b] * gb[b];
+      }
+      rb[a] = hm * s1 + gw * u * s3;
+      eb[a] = -f_c * gb[a] + f_r * s2;
+    }
+    if (NNW) {
+      // L term: W' u sum_ab Phi_ab (v_j - v_i)_a r_b
+      double phv = 0.0, phi_i = 0.0;
+#pragma unroll
+      for (int b = 0; b < D; ++b)
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          phv += Phi[a + D * b] * (-vij[a]) * r[b];
+          phi_i += Lbi[a + D * b] * (-vij[a]) * r[b];
+        }
+      Wb += u * phv;
+      ub += gw * phv;
+#pragma unroll
+      for (int b = 0; b < D; ++b) {
+        double s = 0.0, sv = 0.0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          s += Phi[a + D * b] * (-vij[a]);
+          sv += Phi[b + D * a] * r[a];
+        }
+        rb[b] += gw * u * s;
+        vb[b] -= gw * u * sv;  // d/dv_i of (v_j - v_i)
+      }
+      nbL -= gw * u * phi_i * qi * qi;
+#pragma unroll
+      for (int b = 0; b < D; ++b)
+#pragma unroll
+        for (int a = 0; a < D; ++a) Pbar[a + D * b] += gw * u * r[a] * gb[b];
+    }
+    double ee = 0.0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) ee += eb[a] * ev[a];
+    const double radial = Wb * g2 - ub * u * u;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      xb[a] += rb[a] + u * (eb[a] - ee * ev[a]) + radial * ev[a];
+      vb[a] += f_d * gb[a];
+    }
+    Bbar += fdb * eta * gw * u;
+    Abar += fcb * gw;
+    etab += 0.5 * fdb * SB * gw * u;
+  }
+  // per-particle chain: A = (p + G) B, B = 1/n^2, Q = G c B, p = EOS(n m)
+  const double Bi = pci.y, p = pci.w, mi = 1.0 / pci.z;
+  const double pbar = Abar * Bi;
+  double Bt = Bbar + Abar * (p + G);
+  if (NNW) {
+#pragma unroll
+    for (int q = 0; q < D2; ++q) {
+      Bt += G * ci[q] * Pbar[q];
+      cbs[(size_t)q * n + i] += G * Bi * Pbar[q];
+    }
+  }
+  const double r_eos = ni * mi;
+  double dpdn;
+  if (k.eos_type == 1)
+    dpdn = k.c2 * ((k.gamma == 1.0) ? 1.0 : k.gamma * pow(r_eos, k.gamma - 1.0)) * mi;
+  else
+    dpdn = k.p0 * ((k.gamma == 1.0) ? 1.0 : k.gamma * pow(r_eos / k.rho_ref, k.gamma - 1.0)) *
+           mi / k.rho_ref;
+  nbar[i] = Bt * (-2.0 * Bi * qi) + nbL + pbar * dpdn;
+  double4_32a xo = xbs[i], vo = vbs[i];
+  xo.x += xb[0];
+  xo.y += xb[1];
+  vo.x += vb[0];
+  vo.y += vb[1];
+  if (D == 3) {
+    xo.z += xb[2];
+    vo.z += vb[2];
+  }
+  xbs[i] = xo;
+  vbs[i] = vo;
+  const int hi = tp.hidx[i];
+  const double csound = sqrt(k.c2);
+  gp[hi] += etab;
+  gp[(size_t)2 * n + hi] += (csound > 0.0) ? pbar * 2.0 * p / csound : 0.0;
 }
 
 // density VJP, x_i gets sum_j (nbar_i + nbar_j) W'(r_ij) e_ij, then the
 // drift: the carried adjoints of the previous step, in host order
 template <int D, bool NNW>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+__global__ void __launch_bounds__(kAdjTPB)
     k_adj_density(Consts k, Tape tp, const double* __restrict__ nbar,
                   const double4_32a* __restrict__ xbs, const double4_32a* __restrict__ vbs,
                   const double* __restrict__ cbs, int drift, double dt,
                   double4_32a* __restrict__ xb_h, double4_32a* __restrict__ vb_h,
                   double* __restrict__ cb_h) {
-  constexpr int CENTER = (D == 3) ? 13 : 4;
-  __shared__ NbTable tab[kWarpsPerBlock];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int NS = (D == 3) ? 27 : 9;
+  __shared__ int s_start[NS * kAdjTPB];
+  __shared__ int s_shift[NS * kAdjTPB];
   const int n = k.n;
-  for (int cell = blockIdx.x * kWarpsPerBlock + wib; cell <= k.ncell;
-       cell += gridDim.x * kWarpsPerBlock) {
-    NbTable& t = tab[wib];
-    build_table<D>(k, cell, tp.cell_start, t);
-    const int c0 = t.start[CENTER], c1 = c0 + t.count[CENTER];
-    for (int base = c0; base < c1; base += 32) {
-      const int i = base + lane;
-      if (i >= c1) continue;
-      const double4_32a xi4 = tp.x[i];
-      const double xi[3] = {xi4.x, xi4.y, xi4.z};
-      const double nbi = nbar[i];
-      double acc[3] = {0, 0, 0};
-      const int cnt = tp.ncount[i];
-      for (int e = 0; e < cnt; ++e) {
-        const int ent = tp.nl[(size_t)e * n + i];
-        const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
-        const int j = t.start[sl] + q;
-        const double4_32a xj4 = tp.x[j];
-        const double xj[3] = {xj4.x, xj4.y, xj4.z};
-        double r[3];
-        const double dd2 = exact_sep<D>(k, xi, xj, t.shift[sl], r);
-        const double dist = sqrt(dd2);
-        const double f = (nbi + nbar[j]) * kernel_gradw<double>(k, dist) / dist;
+  const int tid = threadIdx.x;
+  const int i = blockIdx.x * kAdjTPB + tid;
+  if (i >= n) return;
+  build_lane_table<D, kAdjTPB>(k, tp.cell_of[i], tp.cell_start, s_start, s_shift);
+  const double4_32a xi4 = tp.x[i];
+  const double xi[3] = {xi4.x, xi4.y, xi4.z};
+  const double nbi = nbar[i];
+  double acc[3] = {0, 0, 0};
+  const int cnt = tp.ncount[i];
+  for (int e = 0; e < cnt; ++e) {
+    const int ent = tp.nl[(size_t)e * n + i];
+    const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
+    const int j = s_start[sl * kAdjTPB + tid] + q;
+    const double4_32a xj4 = tp.x[j];
+    const double xj[3] = {xj4.x, xj4.y, xj4.z};
+    double r[3];
+    const double dd2 = exact_sep<D>(k, xi, xj, s_shift[sl * kAdjTPB + tid], r);
+    const double dist = sqrt(dd2);
+    const double f = (nbi + nbar[j]) * kernel_gradw<double>(k, dist) / dist;
 #pragma unroll
-        for (int a = 0; a < D; ++a) acc[a] += f * r[a];
-      }
-      const int hi = tp.hidx[i];
-      double4_32a xo = xbs[i], vo = vbs[i];
-      xo.x += acc[0];
-      xo.y += acc[1];
-      if (D == 3) xo.z += acc[2];
-      if (drift) {
-        vo.x += dt * xo.x;
-        vo.y += dt * xo.y;
-        if (D == 3) vo.z += dt * xo.z;
-      }
-      xb_h[hi] = xo;
-      vb_h[hi] = vo;
-      if (NNW) {
+    for (int a = 0; a < D; ++a) acc[a] += f * r[a];
+  }
+  const int hi = tp.hidx[i];
+  double4_32a xo = xbs[i], vo = vbs[i];
+  xo.x += acc[0];
+  xo.y += acc[1];
+  if (D == 3) xo.z += acc[2];
+  if (drift) {
+    vo.x += dt * xo.x;
+    vo.y += dt * xo.y;
+    if (D == 3) vo.z += dt * xo.z;
+  }
+  xb_h[hi] = xo;
+  vb_h[hi] = vo;
+  if (NNW) {
 #pragma unroll
-        for (int q = 0; q < D * D; ++q) cb_h[(size_t)q * n + hi] = cbs[(size_t)q * n + i];
-      }
-    }
+    for (int q = 0; q < D * D; ++q) cb_h[(size_t)q * n + hi] = cbs[(size_t)q * n + i];
   }
 }
 
@@ -694,10 +687,11 @@ int restore_ckpt(Handle* h, const Ckpt& c) {
 }
 
 int record_tape(Handle* h, const Tape& t) {
+  PhaseScope ps(h, kPhaseOther);
   const int n = (int)h->n, d2 = h->k.d * h->k.d, nc2 = h->k.ncell + 2;
   k_tape_record<<<grid1(std::max(n, nc2)), 256, 0, h->stream>>>(
-      n, nc2, d2, t, h->x, h->v, h->pc, h->rho, h->pid, h->hidx, h->ncount, h->cell_start,
-      h->nl, h->ct, h->vgt);
+      n, nc2, d2, t, h->x, h->v, h->pc, h->rho, h->pid, h->hidx, h->ncount, h->cell_of,
+      h->cell_start, h->nl, h->ct, h->vgt);
   return launched(h, "tape record");
 }
 
@@ -718,21 +712,21 @@ int forward_step(Handle* h, int64_t step, double dt, const Tape* tape, double* j
 
 int adjoint_step(Handle* h, const Tape& tp, int64_t step, double dt, double phi, int drift,
                  double wscale) {
+  PhaseScope ps(h, kPhaseOther);
   AdjBuffers* b = h->adj;
   const Consts& k = h->k;
   const int n = (int)h->n;
   cudaStream_t s = h->stream;
   const double inv_sqdt = k.noise ? 1.0 / sqrt(dt) : 0.0;
-  const int gcell = std::max(1, (k.ncell + 1 + kWarpsPerBlock - 1) / kWarpsPerBlock);
-  const int bs = kWarpsPerBlock * 32;
+  const int gp_ = std::max(1, (n + kAdjTPB - 1) / kAdjTPB);
 #define ADJ_LAUNCH(DD, NW)                                                                     \
   do {                                                                                         \
     k_adj_pre<DD, NW><<<grid1(n), 256, 0, s>>>(k, tp, phi, b->xb_h, b->vb_h, b->cb_h, b->lam,  \
                                                b->xbs, b->vbs, b->cbs, b->Lb, b->gp);          \
-    k_adj_force<DD, NW><<<gcell, bs, 0, s>>>(k, tp, b->lam, b->Lb, b->w, wscale,               \
+    k_adj_force<DD, NW><<<gp_, kAdjTPB, 0, s>>>(k, tp, b->lam, b->Lb, b->w, wscale,               \
                                              (uint32_t)step, inv_sqdt, b->xbs, b->vbs, b->cbs, \
                                              b->nbar, b->gp);                                  \
-    k_adj_density<DD, NW><<<gcell, bs, 0, s>>>(k, tp, b->nbar, b->xbs, b->vbs, b->cbs, drift,  \
+    k_adj_density<DD, NW><<<gp_, kAdjTPB, 0, s>>>(k, tp, b->nbar, b->xbs, b->vbs, b->cbs, drift,  \
                                                dt, b->xb_h, b->vb_h, b->cb_h);                 \
   } while (0)
   if (k.d == 3) {
@@ -816,9 +810,14 @@ extern "C" int mcfg_adjoint_run(mcfg_handle* h, int64_t step0, int32_t nsteps, d
   ATRY(launched(h, "save constants"));
   ATRY(save_ckpt(h, b->ck[0]));
   ATRY(rhs(h, step0, kForceBody, dt));
+  // the last segment is taped on the way (it is walked back first, with no
+  // recomputation)
+  const int klast = (nseg - 1) * K;
+  if (nseg == 1) ATRY(record_tape(h, b->tape[(size_t)K]));
   for (int t = 1; t <= T; ++t) {
     if (t > 1 && (t - 1) % K == 0) ATRY(save_ckpt(h, b->ck[(size_t)((t - 1) / K)]));
-    ATRY(forward_step(h, step0 + t, dt, nullptr, b->jpart + (size_t)(t - 1) * b->nb));
+    const Tape* tp = (t > klast) ? &b->tape[(size_t)(t - klast - 1)] : nullptr;
+    ATRY(forward_step(h, step0 + t, dt, tp, b->jpart + (size_t)(t - 1) * b->nb));
   }
   ATRY(save_ckpt(h, b->last));
   ATRY(check_device_errors(h));
@@ -833,13 +832,15 @@ extern "C" int mcfg_adjoint_run(mcfg_handle* h, int64_t step0, int32_t nsteps, d
   const double wscale = 1.0 / (double)T;
   for (int sg = nseg - 1; sg >= 0; --sg) {
     const int k0 = sg * K, k1 = std::min(k0 + K, T);
-    ATRY(restore_ckpt(h, b->ck[(size_t)sg]));
-    if (sg == 0) {
-      ATRY(rhs(h, step0, kForceBody, dt));
-      ATRY(record_tape(h, b->tape[(size_t)K]));
+    if (sg < nseg - 1) {
+      ATRY(restore_ckpt(h, b->ck[(size_t)sg]));
+      if (sg == 0) {
+        ATRY(rhs(h, step0, kForceBody, dt));
+        ATRY(record_tape(h, b->tape[(size_t)K]));
+      }
+      for (int t = k0 + 1; t <= k1; ++t)
+        ATRY(forward_step(h, step0 + t, dt, &b->tape[(size_t)(t - k0 - 1)], nullptr));
     }
-    for (int t = k0 + 1; t <= k1; ++t)
-      ATRY(forward_step(h, step0 + t, dt, &b->tape[(size_t)(t - k0 - 1)], nullptr));
     for (int t = k1; t > k0; --t)
       ATRY(adjoint_step(h, b->tape[(size_t)(t - k0 - 1)], step0 + t, dt,
                         t == T ? 0.5 * dt : dt, 1, wscale));

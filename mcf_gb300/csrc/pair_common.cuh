@@ -108,3 +108,65 @@ __device__ __forceinline__ double exact_sep(const Consts& k, const double* xi, c
 }
 
 }  // namespace mcfg
+
+namespace mcfg {
+
+// Per-thread neighbour-cell table for thread-per-particle sweeps: slot s of
+// thread t lives at s * TPB + t (conflict-free).  Same slots, starts and
+// periodic image bits as build_table, so the neighbour-list entries
+// slot<<11 | local index decode the same way.
+template <int D, int TPB>
+__device__ __forceinline__ void build_lane_table(const Consts& k, int cell,
+                                                 const int* __restrict__ cell_start,
+                                                 int* __restrict__ s_start,
+                                                 int* __restrict__ s_shift) {
+  constexpr int NS = (D == 3) ? 27 : 9;
+  constexpr int CENTER = (D == 3) ? 13 : 4;
+  const int t = threadIdx.x;
+  if (cell == k.ncell) {
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      s_start[s * TPB + t] = (s == CENTER) ? cell_start[cell] : 0;
+      s_shift[s * TPB + t] = 0;
+    }
+    return;
+  }
+  int c[3] = {0, 0, 0};
+  int rem = cell;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    c[a] = rem % k.nm[a];
+    rem /= k.nm[a];
+  }
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    const int o[3] = {s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1};
+    int nc = 0, stride = 1, sh = 0;
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      int t2 = c[a] + o[a];
+      if (t2 < 0) {
+        if (k.periodic[a]) {
+          t2 += k.nm[a];
+          sh |= 2 << (2 * a);
+        } else {
+          ok = false;
+        }
+      } else if (t2 >= k.nm[a]) {
+        if (k.periodic[a]) {
+          t2 -= k.nm[a];
+          sh |= 1 << (2 * a);
+        } else {
+          ok = false;
+        }
+      }
+      nc += t2 * stride;
+      stride *= k.nm[a];
+    }
+    s_start[s * TPB + t] = ok ? cell_start[nc] : 0;
+    s_shift[s * TPB + t] = sh;
+  }
+}
+
+}  // namespace mcfg
