@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--accuracy-steps", type=int, default=200)
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     return ap.parse_args()
 
@@ -314,6 +316,68 @@ def adjoint_cost(torch, w, T, K, local, wts):
                       "forward pass, checkpoints and segment recomputation"}
 
 
+def fp32_accuracy(w, steps, local):
+    """FP32-mixed against FP64 after `steps` VV steps from the same state
+    (same Philox keys, so the only difference is FP32 pair arithmetic): bulk
+    mean velocity and the velocity profile u_x(y) in unit slabs at the end,
+    and, averaged over the second half of the run, the wall shear stress
+    (x-force on each wall's particles per area) and the shear stress
+    statistic S_xy."""
+    import numpy as np
+
+    from mcf_gb300 import SDPD
+    from mcf_gb300.params import PRECISION_FP32_MIXED, PRECISION_FP64
+
+    out = {}
+    res = {}
+    sid = w.id[:, 1]
+    fl = sid == 0
+    area = (w.params.max_phys[0] - w.params.min_phys[0]) * (w.params.max_phys[2] -
+                                                            w.params.min_phys[2])
+    for name, prec in (("fp32", PRECISION_FP32_MIXED), ("fp64", PRECISION_FP64)):
+        p = w.params.copy()
+        p.precision = prec
+        p.stress_tensor = 1
+        p.device = local
+        sd = SDPD(p)
+        sd.upload(w.x, w.v, w.m, w.id)
+        sd.marching_init_force(0)
+        half = steps // 2
+        sd.run_vv(0, half, w.dt)
+        walls, sxy = [], []
+        every = max(1, (steps - half) // 10)
+        for s in range(half, steps, every):
+            sd.run_vv(s, every, w.dt)
+            _, _, st = sd.statistic_compute_statistic()
+            f = sd.download("f")["f"]
+            walls.append([float((w.m[sid == q] * f[sid == q, 0]).sum() / area) for q in (-3, -4)])
+            sxy.append(0.5 * (st[1] + st[3]))
+        d = sd.download("x", "v")
+        res[name] = (d, np.mean(walls, axis=0), float(np.mean(sxy)))
+        del sd
+
+    def summary(d, walls, sxy):
+        x, v = d["x"], d["v"]
+        ybin = np.floor(x[fl, 1] - w.params.min_phys[1]).astype(int)
+        nb = int(round(w.params.max_phys[1] - w.params.min_phys[1]))
+        ybin = np.clip(ybin, 0, nb - 1)
+        prof = np.bincount(ybin, weights=v[fl, 0], minlength=nb) / np.maximum(
+            np.bincount(ybin, minlength=nb), 1)
+        return float(v[fl, 0].mean()), prof, list(walls), sxy
+
+    u32, p32, w32, s32 = summary(*res["fp32"])
+    u64, p64, w64, s64 = summary(*res["fp64"])
+    out["steps"] = steps
+    out["mean_velocity_rel"] = abs(u32 - u64) / abs(u64)
+    out["velocity_profile_rel"] = float(np.max(np.abs(p32 - p64)) / np.max(np.abs(p64)))
+    out["wall_shear_stress_rel"] = float(max(abs(a - b) / abs(b) for a, b in zip(w32, w64)))
+    out["shear_stress_rel"] = abs(s32 - s64) / abs(s64)
+    out["mean_velocity_fp64"] = u64
+    out["wall_shear_stress_fp64"] = [float(x) for x in w64]
+    out["reference"] = "the FP64 GPU path (itself within 1e-12 of the CPU oracle per step)"
+    return out
+
+
 def run_ours(args, ws, rank, local):
     import numpy as np
     import torch
@@ -372,6 +436,8 @@ def run_ours(args, ws, rank, local):
         fp64 = {"value": v64, "unit": UNIT, "steps": k64, "ms_per_step": 1e3 * t64 / k64,
                 "fp32_mixed_speedup": value / v64, "roofline": roof64}
         del sd64
+        if not args.no_accuracy:
+            err["long_run"] = fp32_accuracy(w, args.accuracy_steps, local)
     # end to end through the C-ABI with host buffers
     e2e = None
     if not args.no_e2e:
