@@ -272,8 +272,16 @@ def roofline_for(sd, torch, w, prec_idx, peaks, step0):
     achieved = algo / (avg_ms / 1e3) / 1e9
     peak = peaks.get("hbm_gbs")
     share = {k: round(v[0] / sum(x[0] for x in phases.values()), 4) for k, v in phases.items()}
+    # DRAM bytes per particle of this kernel from the committed ncu summary
+    # (a smaller case of the same workload, scaled by the particles)
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        per = json.loads(tf.read_text()).get("fp64" if prec_idx else "fp32", {}).get(top)
+        if per:
+            traffic = per * w.n
     return {"kernel_phase": top, "bound": "hbm", "achieved": achieved, "peak": peak,
-            "unit": "GB/s", "frac": (achieved / peak) if peak else None, "traffic": None,
+            "unit": "GB/s", "frac": (achieved / peak) if peak else None, "traffic": traffic,
             "avg_ms": avg_ms, "algo_bytes_per_launch": algo,
             "peak_source": peaks.get("source"), "phase_share": share}
 
