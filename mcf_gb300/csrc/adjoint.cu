@@ -22,7 +22,7 @@
 //
 // Pair VJP of the Hu-Adams force (rhs_force_ff_Newtonian_HuAdams.F90:124-237,
 // non-Newtonian form rhs_force_ff_non_Newtonian_HuAdams.F90:95-201) with
-// g = f_d v_ij - f_c e + W' u P^T r + f_r dW e, f_c = (A_i + A_j) W',
+// g = f_d v_ij - f_c e + W' u P^T r + f_r We, f_c = (A_i + A_j) W',
 // f_d = eta (B_i + B_j) W' u, f_r = sqrt(-4 kT f_d)/sqrt(dt),
 // A = (p + G)/n^2, B = 1/n^2, P = G (c_i B_i + c_j B_j), u = 1/|r|, and the
 // velocity gradient L_i += (v_j - v_i) (x) r W' u / n_i (pp_vgt_ip.inc).
@@ -318,29 +318,6 @@ __global__ void k_row_sums(int n, int rows, const double* __restrict__ a,
 // adjoint kernels
 // ---------------------------------------------------------------------------
 
-// dW of the pair from its normals, as the forward sweep builds it
-// (diagonal minus its mean, off-diagonals symmetric with weight 1/sqrt 2)
-template <int D>
-__device__ __forceinline__ void noise_dw(const float* z, double (&dW)[3][3]) {
-  double tr = 0.0;
-#pragma unroll
-  for (int a = 0; a < D; ++a) {
-    dW[a][a] = (double)z[a];
-    tr += dW[a][a];
-  }
-  tr = tr / (double)D;
-  const double s2 = 0.70710678118654752440;
-  if (D == 3) {
-    dW[0][1] = dW[1][0] = (double)z[3] * s2;
-    dW[0][2] = dW[2][0] = (double)z[4] * s2;
-    dW[1][2] = dW[2][1] = (double)z[5] * s2;
-  } else {
-    dW[0][1] = dW[1][0] = (double)z[2] * s2;
-  }
-#pragma unroll
-  for (int a = 0; a < D; ++a) dW[a][a] -= tr;
-}
-
 __device__ __forceinline__ double d4(const double4_32a& a, int c) {
   return c == 0 ? a.x : (c == 1 ? a.y : a.z);
 }
@@ -467,14 +444,22 @@ __global__ void __launch_bounds__(kAdjTPB)
     const double SB = pci.y + pcj.y, SA = pci.x + pcj.x;
     const double f_c = SA * gw;
     const double f_d = eta * SB * gw * u;
-    double dW[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-    double f_r = 0.0;
+    // random term We = s (ca (e.g) e + cb (g - (e.g) e)), replayed from
+    // the pair's keys exactly as pair_force draws it
+    double gz[3] = {0, 0, 0}, sg = 0.0, f_r = 0.0;
     if (noise) {
       float z[6];
-      pair_normals<D>(k.key0, k.key1, step, pidi, tp.pid[j], z);
-      noise_dw<D>(z, dW);
+      pair_draw<D>(3, k.key0, k.key1, step, pidi, tp.pid[j], z);
+#pragma unroll
+      for (int a = 0; a < D; ++a) gz[a] = (double)z[a];
+      sg = (double)z[5];
       f_r = sqrt(-4.0 * kt * f_d) * inv_sqdt;
     }
+    const double cbn = 0.70710678118654752440;
+    const double cdn = ((D == 3) ? 0.81649658092772603273 : cbn) - cbn;  // ca - cb
+    double eg = 0.0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) eg += ev[a] * gz[a];
     double P[D2], Phi[D2];
     if (NNW) {
       const double qj = 1.0 / tp.rho[j];
@@ -489,9 +474,7 @@ __global__ void __launch_bounds__(kAdjTPB)
     double We[3], Pr[3];
 #pragma unroll
     for (int b = 0; b < D; ++b) {
-      We[b] = 0.0;
-#pragma unroll
-      for (int a = 0; a < D; ++a) We[b] += dW[b][a] * ev[a];
+      We[b] = sg * (cdn * eg * ev[b] + cbn * gz[b]);
       Pr[b] = 0.0;
       if (NNW) {
 #pragma unroll
@@ -516,17 +499,17 @@ __global__ void __launch_bounds__(kAdjTPB)
     double Wb = fdb * eta * SB * u + fcb * SA + u * gbPr;
     double ub = fdb * eta * SB * gw + gw * gbPr;
     double rb[3], eb[3];
+    const double fre = f_r * sg * cdn;  // d(We)/de = s (ca - cb) ((e.g) I + e g^T)
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+      double s1 = 0.0, s3 = 0.0;
 #pragma unroll
       for (int b = 0; b < D; ++b) {
         s1 += wt[b * D + a] * g[b];
-        s2 += dW[a][b] * gb[b];
         if (NNW) s3 += P[a + D * b] * gb[b];
       }
       rb[a] = hm * s1 + gw * u * s3;
-      eb[a] = -f_c * gb[a] + f_r * s2;
+      eb[a] = -f_c * gb[a] + fre * (gz[a] * gbe + gb[a] * eg);
     }
     if (NNW) {
       // L term: W' u sum_ab Phi_ab (v_j - v_i)_a r_b

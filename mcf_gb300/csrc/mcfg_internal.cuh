@@ -293,4 +293,30 @@ __device__ __forceinline__ void pair_normals(uint32_t k0, uint32_t k1, uint32_t 
   }
 }
 
+// What a pair draws for its random force, by force form, from the stream of
+// pair_normals (the first normals of the same counter):
+//   type 2 (Espanol-Revenga): the 6 (3D) / 3 (2D) normals of the matrix dW;
+//   type 3 (Hu-Adams, also non-Newtonian): d normals g for We = dW e drawn
+//     from its law given e (see pair_force), z[5] = +1 when pa < pb, -1
+//     otherwise (orients We so that the pair's two sides are opposite);
+//   type 4 (angular): one normal.
+template <int D>
+__device__ __forceinline__ void pair_draw(int type, uint32_t k0, uint32_t k1, uint32_t step,
+                                          int pa, int pb, float* z) {
+  if (type == 2) {
+    pair_normals<D>(k0, k1, step, pa, pb, z);
+    return;
+  }
+  const uint32_t a = (uint32_t)min(pa, pb), b = (uint32_t)max(pa, pb);
+  const uint4 r = philox4x32_10(make_uint4(a, b, step, 0u), k0, k1);
+  box_muller(r.x, r.y, z[0], z[1]);
+  if (type == 3) {
+    if (D == 3) {
+      float t1;
+      box_muller(r.z, r.w, z[2], t1);
+    }
+    z[5] = (pa < pb) ? 1.0f : -1.0f;
+  }
+}
+
 }  // namespace mcfg

@@ -235,32 +235,19 @@ __device__ __forceinline__ void pair_force(const Consts& k, const T* r, T inv_d,
 #pragma unroll
       for (int a = 0; a < D; ++a) g[a] = f_d * vij[a] - f_c * e[a];
       if (noise) {
-        T dW[3][3];
-        T tr = T(0);
+        // MCF uses its symmetric traceless dW only through We = dW e, a
+        // Gaussian vector with variance 1 - 1/d along e and 1/2 across e;
+        // drawn directly as s (ca (e.g) e + cb (g - (e.g) e)) from d normals
+        // g (pair_draw), s = +-1 by pid order so both sides get opposite We
+        const T cb = T(0.70710678118654752440);
+        const T ca = (D == 3) ? T(0.81649658092772603273) : cb;  // sqrt(1 - 1/d)
+        T eg = T(0);
 #pragma unroll
-        for (int a = 0; a < D; ++a) {
-          dW[a][a] = (T)z[a];
-          tr += dW[a][a];
-        }
-        tr = tr / T(D);
-        const T s2 = T(0.70710678118654752440);
-        if (D == 3) {
-          dW[0][1] = dW[1][0] = (T)z[3] * s2;
-          dW[0][2] = dW[2][0] = (T)z[4] * s2;
-          dW[1][2] = dW[2][1] = (T)z[5] * s2;
-        } else {
-          dW[0][1] = dW[1][0] = (T)z[2] * s2;
-        }
+        for (int a = 0; a < D; ++a) eg += e[a] * (T)z[a];
+        const T f_r = my_sqrt<T>(T(-4) * kt * f_d) * inv_sqdt * (T)z[5];
+        const T fl = f_r * (ca - cb) * eg, ft = f_r * cb;
 #pragma unroll
-        for (int a = 0; a < D; ++a) dW[a][a] -= tr;
-        const T f_r = my_sqrt<T>(T(-4) * kt * f_d) * inv_sqdt;
-#pragma unroll
-        for (int a = 0; a < D; ++a) {
-          T We = T(0);
-#pragma unroll
-          for (int b = 0; b < D; ++b) We += dW[a][b] * e[b];
-          g[a] += f_r * We;
-        }
+        for (int a = 0; a < D; ++a) g[a] += fl * e[a] + ft * (T)z[a];
       }
       break;
     }

@@ -16,7 +16,8 @@ Physics restated (reference files of MCF):
   - equation of state, vector forms: stateEquation_compute_pressure.F90:
     147-180, p0 of stateEquation_new.F90:102-103;
   - Hu-Adams pair force with the Wiener term: rhs_force_ff_Newtonian_HuAdams.
-    F90:124-239; non-Newtonian form with the pressure tensor:
+    F90:124-239 (We = dW e drawn from its law given e, as the oracle's
+    pair_we); non-Newtonian form with the pressure tensor:
     rhs_force_ff_non_Newtonian_HuAdams.F90:95-201,
     particles_compute_pressure_tensor.F90:88-133;
   - velocity gradient pp_vgt_ip.inc:12-24, act particles_compute_act.F90:
@@ -27,7 +28,7 @@ Physics restated (reference files of MCF):
   - VV order marching_integrate_VV.F90:303-1620.
 Pairs are found by minimum image (the box is at least twice the cut-off);
 the random term uses the oracle's Philox/Box-Muller normals of each pid
-pair (orc_pair_normals), so the noise is the oracle's.
+pair (orc_pair_normals) the same way, so the noise is the oracle's.
 """
 from __future__ import annotations
 
@@ -130,22 +131,18 @@ class RefTrajectory:
             P = Q[I] + Q[J]
             g = g + (gw * u)[:, None] * torch.einsum("kab,ka->kb", P, r)
         if self.noise:
-            z = pair_normals_batch(self.p.seed, step, self.pid[I.numpy()], self.pid[J.numpy()], d)
-            z = torch.as_tensor(z.astype(np.float64))
-            dW = torch.zeros(len(I), d, d, dtype=torch_dtype)
-            for a in range(d):
-                dW[:, a, a] = z[:, a]
-            tr = dW.diagonal(dim1=1, dim2=2).sum(-1) / d
-            s2 = 0.70710678118654752440
-            if d == 3:
-                for (a, b, k) in ((0, 1, 3), (0, 2, 4), (1, 2, 5)):
-                    dW[:, a, b] = dW[:, b, a] = z[:, k] * s2
-            else:
-                dW[:, 0, 1] = dW[:, 1, 0] = z[:, 2] * s2
-            for a in range(d):
-                dW[:, a, a] = dW[:, a, a] - tr
+            # We = s (ca (e.g) e + cb (g - (e.g) e)) with the pair's first d
+            # normals g and s = +1 if pid_i < pid_j (the oracle's pair_we)
+            pi_, pj_ = self.pid[I.numpy()], self.pid[J.numpy()]
+            z = pair_normals_batch(self.p.seed, step, pi_, pj_, d)
+            gz = torch.as_tensor(z[:, :d].astype(np.float64))
+            sg = torch.as_tensor(np.where(pi_ < pj_, 1.0, -1.0))
+            cb = 0.70710678118654752440
+            ca = 0.81649658092772603273 if d == 3 else cb
+            eg = (e * gz).sum(-1)
+            We = sg[:, None] * ((ca - cb) * eg[:, None] * e + cb * gz)
             f_r = torch.sqrt(-4.0 * self.p.kt * f_d) / math.sqrt(dt)
-            g = g + f_r[:, None] * torch.einsum("kab,kb->ka", dW, e)
+            g = g + f_r[:, None] * We
         a = torch.zeros(n, d, dtype=torch_dtype).index_add(0, I, g / self.m[I][:, None])
         # stress S[b, a] = sum over ordered pairs r_a g_b / (2 m_i)
         S = torch.einsum("ka,kb->ba", r, g / (2.0 * self.m[I])[:, None])

@@ -967,6 +967,32 @@ static void noise_matrix(const orc_state* s, const float* z, double dW[3][3],
   for (int a = 0; a < d; ++a) dW[a][a] = dW[a][a] - trace;
 }
 
+/* We = dW e of the Hu-Adams random force (rhs_force_ff_Newtonian_HuAdams.F90:
+ * 176-239): MCF uses its symmetric traceless dW only through this vector, a
+ * Gaussian with variance 1 - 1/d along e and 1/2 across e, so it is drawn
+ * directly, We = s (ca (e.g) e + cb (g - (e.g) e)), ca = sqrt(1 - 1/d),
+ * cb = sqrt(1/2), from the first d normals g of the pair's stream and
+ * s = +1 if pid_i < pid_j else -1 (the pair's two sides get opposite We). */
+static void pair_we(const orc_state* s, int64_t step, int32_t pidi, int32_t pidj,
+                    const double* e, double* We) {
+  const int d = s->d;
+  float z[6];
+  orc_pair_normals(s->p.seed, step, pidi, pidj, d, z);
+  const double cb = 0.70710678118654752440;
+  const double ca = (d == 3) ? 0.81649658092772603273 : cb;
+  const double sg = (pidi < pidj) ? 1.0 : -1.0;
+  double eg = 0.0;
+  for (int a = 0; a < d; ++a) eg = eg + e[a] * (double)z[a];
+  for (int a = 0; a < d; ++a)
+    We[a] = sg * ((ca - cb) * eg * e[a] + cb * (double)z[a]);
+}
+
+int orc_pair_we(const orc_state* s, int64_t step, int32_t pidi, int32_t pidj, const double* e,
+                double* We) {
+  pair_we(s, step, pidi, pidj, e, We);
+  return 0;
+}
+
 static void rhs_force_ff(orc_state* s, const force_ctx* fc, const double* xi,
                          const double* xj, double dij, const double* vi,
                          const double* vj, double numi, double numj, double pi,
@@ -1046,16 +1072,12 @@ static void rhs_force_ff(orc_state* s, const force_ctx* fc, const double* xi,
         fj[a] = fj[a] - f_d * vij[a] / mj;
       }
       if (brown) {
-        float z[6];
-        double dW[3][3], trace;
-        orc_pair_normals(s->p.seed, fc->step, pidi, pidj, d, z);
-        noise_matrix(s, z, dW, &trace);
+        double We[3];
+        pair_we(s, fc->step, pidi, pidj, eij, We);
         const double f_r = sqrt(-4.0 * kt * f_d) / fc->sqdt;
         for (int a = 0; a < d; ++a) {
-          double We = 0.0;
-          for (int b = 0; b < d; ++b) We = We + dW[a][b] * eij[b];
-          fi[a] = fi[a] + f_r * We / mi;
-          fj[a] = fj[a] - f_r * We / mj;
+          fi[a] = fi[a] + f_r * We[a] / mi;
+          fj[a] = fj[a] - f_r * We[a] / mj;
         }
       }
       break;
@@ -1163,16 +1185,12 @@ static void rhs_force_nn(orc_state* s, const force_ctx* fc, const double* xi, co
     fj[a] = fj[a] - f_d * vij[a] / mj;
   }
   if (fc->noise) {
-    float z[6];
-    double dW[3][3], trace;
-    orc_pair_normals(s->p.seed, fc->step, pidi, pidj, d, z);
-    noise_matrix(s, z, dW, &trace);
+    double We[3];
+    pair_we(s, fc->step, pidi, pidj, eij, We);
     const double f_r = sqrt(-4.0 * s->p.kt * f_d) / fc->sqdt;
     for (int a = 0; a < d; ++a) {
-      double We = 0.0;
-      for (int b = 0; b < d; ++b) We = We + dW[a][b] * eij[b];
-      fi[a] = fi[a] + f_r * We / mi;
-      fj[a] = fj[a] - f_r * We / mj;
+      fi[a] = fi[a] + f_r * We[a] / mi;
+      fj[a] = fj[a] - f_r * We[a] / mj;
     }
   }
 }

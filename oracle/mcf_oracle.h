@@ -86,6 +86,9 @@ void orc_pair_normals(uint64_t seed, int64_t step, int32_t pid_a,
                       int32_t pid_b, int dim, float* z);
 void orc_pair_normals_batch(uint64_t seed, int64_t step, int64_t npairs, const int32_t* pa,
                             const int32_t* pb, int dim, float* z);
+/* the Hu-Adams random vector We of pair (pidi, pidj) with unit vector e */
+int orc_pair_we(const orc_state* s, int64_t step, int32_t pidi, int32_t pidj, const double* e,
+                double* We);
 
 /* kernel value and derivative (kernel_kernel_*), for unit tests */
 int orc_kernel(const orc_state* s, double r, double* w, double* gradw);

@@ -68,6 +68,7 @@ def load(rebuild: bool = True) -> C.CDLL:
                                           C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int,
                                           C.POINTER(C.c_float)]),
         "orc_kernel": (C.c_int, [_h, C.c_double, _dp, _dp]),
+        "orc_pair_we": (C.c_int, [_h, C.c_int64, C.c_int32, C.c_int32, _dp, _dp]),
         "orc_set_colloids": (C.c_int, [_h, C.POINTER(ColloidParams), _dp, _dp, _dp, _dp]),
         "orc_colloid_drag": (C.c_int, [_h, _dp, _dp]),
         "orc_colloid_repulsion": (C.c_int, [_h, _dp]),
@@ -227,6 +228,13 @@ class Oracle:
         self._check("colloid_repulsion", self.lib.orc_colloid_repulsion(self._h,
                                                                          _ptr(out, C.c_double)))
         return out
+
+    def pair_we(self, step, pidi, pidj, e):
+        e = np.ascontiguousarray(e, np.float64)
+        out = np.zeros(3)
+        self.lib.orc_pair_we(self._h, int(step), int(pidi), int(pidj), _ptr(e, C.c_double),
+                             _ptr(out, C.c_double))
+        return out[: self.dim]
 
     def counts(self):
         c = (C.c_int64 * 3)()

@@ -5,9 +5,9 @@ References:
   - the FP64 reference gradient: torch autograd of the dense restatement in
     oracle/adjoint_ref.py, itself pinned to the CPU oracle (trajectory and
     central differences, test_adjoint_ref.py);
-  - central finite differences of the GPU's own J (step 1e-6 relative; 1e-3
-    for tau, whose derivative is five orders below J/tau there) on
-    the full 2D 128^2 Oldroyd-B workload, 200 steps, checkpoints every 20.
+  - central finite differences of the GPU's own J on the full 2D 128^2
+    Oldroyd-B workload, 200 steps, checkpoints every 20: step 1e-6 (eta, c)
+    and Richardson-extrapolated steps 1e-2 / 2e-2 (eta, tau, c), see the test.
 Tolerances: without noise the adjoint matches the reference gradient to
 1e-8 relative; with the random term on, the GPU's FP32 Box-Muller normals
 (CUDA logf/sincospif) differ from the CPU's in the last bits, so the bound
@@ -127,12 +127,16 @@ class StressAdjoint(torch.autograd.Function):
 def test_c5_gradient_against_finite_differences(gpu_lib):
     # full 2D 128^2 Oldroyd-B workload: 200 steps, checkpoints every 20, kT =
     # 1e-4 with the Philox increments; a small seeded velocity perturbation
-    # gives the shear stress a signal from step one.  Central differences
-    # with step 1e-6 (relative) for eta and c.  dJ/dtau is five orders below
-    # J/tau here (the conformation tensor starts at I and moves by O(L t)),
-    # so at step 1e-6 the difference quotient is mostly rounding of J; tau
-    # uses step 1e-3, whose truncation error (h^2/6 times the third
-    # derivative) stays below 1e-6 relative.
+    # gives the shear stress a signal from step one.
+    # (1) central differences with step 1e-6 (relative) for eta and c,
+    #     within 1e-4 plus the rounding floor of the quotient: J sums ~3e6
+    #     stress terms over the trajectory and carries ~1e-13 of rounding
+    #     (measured up to 3e-13 here), so the floor is 1e-12 / h;
+    # (2) Richardson-extrapolated central differences (steps 1e-2, 2e-2)
+    #     for all three, within 1e-4: rounding and truncation both far below.
+    #     dJ/dtau is five orders below J/tau here (the conformation tensor
+    #     starts at I and moves by O(L t)), so at step 1e-6 its quotient
+    #     would be mostly rounding; tau is checked by (2) only.
     w = configs.c5_oldroyd_b_2d()
     w.params.stress_tensor = 1
     rng = np.random.default_rng(55)
@@ -142,14 +146,22 @@ def test_c5_gradient_against_finite_differences(gpu_lib):
     J = StressAdjoint.apply(theta, w, 200, 20)
     J.backward()
     g = theta.grad.numpy()
-    for k, rel_step in ((0, 1e-6), (1, 1e-3), (2, 1e-6)):
-        th = float(theta.detach()[k])
-        hstep = rel_step * abs(th)
-        tp = theta.detach().clone()
-        tm = theta.detach().clone()
-        tp[k] += hstep
-        tm[k] -= hstep
-        jp = float(StressAdjoint.apply(tp, w, 200, 20))
-        jm = float(StressAdjoint.apply(tm, w, 200, 20))
-        fd = (jp - jm) / (2 * hstep)
-        assert abs(fd - g[k]) <= 1e-4 * max(abs(fd), abs(g[k])), (k, fd, g[k], float(J))
+    th0 = theta.detach().clone()
+
+    def J_at(k, h):
+        t = th0.clone()
+        t[k] += h
+        return float(StressAdjoint.apply(t, w, 200, 20))
+
+    for k in range(3):
+        th = float(th0[k])
+        if k != 1:
+            h = 1e-6 * abs(th)
+            fd = (J_at(k, h) - J_at(k, -h)) / (2 * h)
+            floor = 1e-12 / h
+            assert abs(fd - g[k]) <= 1e-4 * max(abs(fd), abs(g[k])) + floor, (k, fd, g[k])
+        h1 = 1e-2 * abs(th)
+        d1 = (J_at(k, h1) - J_at(k, -h1)) / (2 * h1)
+        d2 = (J_at(k, 2 * h1) - J_at(k, -2 * h1)) / (4 * h1)
+        fdr = (4 * d1 - d2) / 3
+        assert abs(fdr - g[k]) <= 1e-4 * abs(g[k]), (k, fdr, g[k])

@@ -244,3 +244,33 @@ def test_colloid_repulsion_is_pairwise_antisymmetric():
         fr = o.colloid_repulsion()
         assert np.allclose(fr[0] + fr[1], 0.0, atol=1e-12)
         assert fr[0, 0] > 0.0 and abs(fr[0, 1]) < 1e-12  # pushed apart along x
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_pair_we_has_mcf_law_and_is_antisymmetric(dim):
+    # We = dW e of MCF's Hu-Adams term: the oracle draws it directly; its law
+    # given e must be that of MCF's construction (9 i.i.d. normals, off-
+    # diagonals averaged, trace/d removed): variance 1 - 1/d along e, 1/2
+    # across; and the two sides of a pair must get opposite vectors
+    w = configs.c2_fluctuating_3d(n_side=10) if dim == 3 else configs.c1_poiseuille_2d(n_side=16)
+    o = Oracle(w.params)
+    rng = np.random.default_rng(3)
+    e = rng.normal(size=dim)
+    e /= np.linalg.norm(e)
+    draws = []
+    for k in range(20000):
+        a, b = 1 + 2 * k, 2 + 2 * k
+        we = o.pair_we(7, a, b, e)
+        assert np.array_equal(o.pair_we(7, b, a, -e), -we)
+        draws.append(we)
+    draws = np.array(draws)
+    cov = np.cov(draws.T)
+    # MCF's construction sampled with numpy
+    xi = rng.normal(size=(200000, dim, dim))
+    dW = 0.5 * (xi + xi.transpose(0, 2, 1))
+    for q in range(dim):
+        dW[:, q, q] = xi[:, q, q] - np.trace(xi, axis1=1, axis2=2) / dim
+    ref = np.cov((dW @ e).T)
+    expect = (1 - 1 / dim) * np.outer(e, e) + 0.5 * (np.eye(dim) - np.outer(e, e))
+    assert np.max(np.abs(ref - expect)) < 0.02
+    assert np.max(np.abs(cov - expect)) < 0.04, cov
