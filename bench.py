@@ -13,8 +13,13 @@ wrap, cell list, density, pressure, pair force, body force, kick); the
 metric counts fluid particles.
 
 `value` is the FP32-mixed path with the state resident in HBM (device time,
-CUDA events on the library's stream).  `fp64` is the plain FP64 path on the
-same workload.  `e2e` is the same metric through the C-ABI with host
+CUDA events on the library's stream), with neighbour-list reuse on
+(mcfg_params.reserved[1]): the candidates within rc + skin are rebuilt on the
+device only when a particle has moved more than skin/2, every step re-tests
+them exactly (config.list_reuse gives the skin, the rebuilds inside the timed
+steps and the same step with MCF's cell list rebuilt every step;
+--no-list-reuse times that mode as the headline).  `fp64` is the plain FP64
+path on the same workload.  `e2e` is the same metric through the C-ABI with host
 buffers: every step uploads x, v, f, m, id from pinned host memory, runs
 mcfg_step_vv and downloads x, v, f.  `cpu_baseline` is the CPU restatement
 of MCF's path (the oracle; MCF itself cannot be built here) on the host
@@ -64,6 +69,7 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-list-reuse", action="store_true")
     ap.add_argument("--accuracy-steps", type=int, default=200)
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     return ap.parse_args()
@@ -404,10 +410,13 @@ def run_ours(args, ws, rank, local):
 
     w = configs.c3_poiseuille_3d(n_side=args.n_side, precision=PRECISION_FP32_MIXED)
     w.params.device = local
+    reuse = 0 if args.no_list_reuse else 1
+    w.params.reserved[1] = reuse
     sd = SDPD(w.params)
     sd.upload(w.x, w.v, w.m, w.id)
     sd.marching_init_force(0)
     sd.run_vv(0, args.warmup, w.dt)
+    r0 = sd.info()["list_rebuilds"]
     clk = ClockSampler(local)
     clk.start()
     t, launches = timed_run(sd, torch, args.steps, args.warmup, w.dt, ws)
@@ -415,13 +424,33 @@ def run_ours(args, ws, rank, local):
     tmax = max_over_ranks(t, ws)
     value = aggregate_throughput(w.n_fluid * args.steps, tmax, ws)
     info = sd.info()
+    list_reuse = None
+    if reuse:
+        list_reuse = {"skin": info["skin"], "rebuilds_in_timed_steps": info["list_rebuilds"] - r0,
+                      "rebuilds_total": info["list_rebuilds"]}
     roof = roofline_for(sd, torch, w, 0, peaks, args.warmup + args.steps)
+    # the same FP32-mixed step with MCF's cell list rebuilt every step
+    every_step = None
+    if reuse:
+        p1 = w.params.copy()
+        p1.reserved[1] = 0
+        sd1 = SDPD(p1)
+        sd1.upload(w.x, w.v, w.m, w.id)
+        sd1.marching_init_force(0)
+        sd1.run_vv(0, args.warmup, w.dt)
+        t1, _ = timed_run(sd1, torch, args.steps, args.warmup, w.dt, ws)
+        t1 = max_over_ranks(t1, ws)
+        every_step = {"value": aggregate_throughput(w.n_fluid * args.steps, t1, ws),
+                      "unit": UNIT, "ms_per_step": 1e3 * t1 / args.steps}
+        list_reuse["rebuild_every_step"] = every_step
+        del sd1
     # FP32-mixed error against the FP64 path on the same state
     err = None
     fp64 = None
     if not args.no_fp64:
         w64 = configs.c3_poiseuille_3d(n_side=args.n_side, precision=PRECISION_FP64)
         w64.params.device = local
+        w64.params.reserved[1] = reuse
         sd64 = SDPD(w64.params)
         sd64.upload(w.x, w.v, w.m, w.id)
         sd64.marching_init_force(0)
@@ -508,7 +537,7 @@ def run_ours(args, ws, rank, local):
                    "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2 "
                    f"({info['device_bytes'] / 1e6:.0f} MB device state)",
                    "neighbour_capacity": info["neigh_capacity"], "max_neigh": info["max_neigh"],
-                   "pairs_per_step": info["num_pairs"]},
+                   "pairs_per_step": info["num_pairs"], "list_reuse": list_reuse},
         "roofline": roof, "fp64": fp64, "fp32_error_vs_fp64": err, "e2e": e2e,
         "adjoint": adjoint,
         "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),

@@ -93,6 +93,18 @@ typedef struct mcfg_params {
   double kt_p;                /* polymer kT (G = n_p*kt_p)                   */
   uint64_t seed;              /* Philox key for the Wiener increments        */
   int32_t device;             /* CUDA device ordinal                         */
+  /* reserved[0]: neighbour-list capacity per particle (0: 256 in 3D, 96 in
+   *   2D).
+   * reserved[1]: non-zero enables neighbour-list reuse in mcfg_step_vv /
+   *   mcfg_run_vv: the candidates within rc + skin are listed at a rebuild
+   *   (skin = 0.99 x (smallest cell side - cut_off), so the cell stencil of
+   *   the rebuild holds every pair) and re-tested exactly every step; the
+   *   rebuild -- wrap, MCF's cell list, candidate list -- happens on the
+   *   device when a particle has moved more than skin/2 since the last one.
+   *   The pair set of every step is the same as without reuse; positions
+   *   may sit up to skin/2 past a periodic face between rebuilds (mcfg_download
+   *   returns them wrapped).  Widen the skin with cell_factor.
+   * reserved[2..6]: must be 0. */
   int32_t reserved[7];
 } mcfg_params;
 
@@ -134,6 +146,8 @@ typedef struct mcfg_info {
   int32_t neigh_capacity; /* per-particle neighbour list capacity           */
   int64_t kernel_launches;/* kernels launched by this handle so far          */
   int64_t device_bytes;   /* device memory held by the handle               */
+  int64_t list_rebuilds;  /* candidate-list rebuilds so far (list reuse)    */
+  double skin;            /* list-reuse skin (0: reuse off)                  */
 } mcfg_info;
 
 /* Create a handle on params->device.  Replaces the construction of MCF's

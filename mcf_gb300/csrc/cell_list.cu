@@ -23,7 +23,9 @@ __device__ __forceinline__ int ppm_axis_cell(double xa, double xmin, double xmax
 
 template <int D>
 __global__ void k_cell_key(Consts k, const double4_32a* __restrict__ x, int* __restrict__ key,
-                           int* __restrict__ rank, int* __restrict__ cnt) {
+                           int* __restrict__ rank, int* __restrict__ cnt,
+                           const int* __restrict__ gate) {
+  if (gate && *gate == 0) return;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= k.n) return;
   const double4_32a xp = x[p];
@@ -74,7 +76,9 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* smem, int& total
   return warp_off + inc - v;
 }
 
-__global__ void k_scan_tiles(const int* __restrict__ in, int n, int* __restrict__ part) {
+__global__ void k_scan_tiles(const int* __restrict__ in, int n, int* __restrict__ part,
+                             const int* __restrict__ gate) {
+  if (gate && *gate == 0) return;
   __shared__ int smem[32];
   const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPer;
   int s = 0;
@@ -86,7 +90,8 @@ __global__ void k_scan_tiles(const int* __restrict__ in, int n, int* __restrict_
   if (threadIdx.x == 0) part[blockIdx.x] = total;
 }
 
-__global__ void k_scan_partials(int* part, int nparts) {
+__global__ void k_scan_partials(int* part, int nparts, const int* __restrict__ gate) {
+  if (gate && *gate == 0) return;
   __shared__ int smem[32];
   int carry = 0;
   for (int b0 = 0; b0 < nparts; b0 += blockDim.x) {
@@ -100,7 +105,8 @@ __global__ void k_scan_partials(int* part, int nparts) {
 }
 
 __global__ void k_scan_final(const int* __restrict__ in, int n, const int* __restrict__ part,
-                             int* __restrict__ out) {
+                             int* __restrict__ out, const int* __restrict__ gate) {
+  if (gate && *gate == 0) return;
   __shared__ int smem[32];
   const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPer;
   int vals[kScanPer];
@@ -122,7 +128,9 @@ __global__ void k_scan_final(const int* __restrict__ in, int n, const int* __res
 }
 
 __global__ void k_scatter(int n, const int* __restrict__ key, const int* __restrict__ rank,
-                          const int* __restrict__ start, int* __restrict__ order) {
+                          const int* __restrict__ start, int* __restrict__ order,
+                          const int* __restrict__ gate) {
+  if (gate && *gate == 0) return;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   order[start[key[p]] + rank[p]] = p;
@@ -145,7 +153,9 @@ __global__ void k_cell_finalize(Consts k, const int* __restrict__ start,
                                 int* __restrict__ cell_of, float2* __restrict__ wd,
                                 const double* __restrict__ ct_in, const double* __restrict__ act_in,
                                 double* __restrict__ ct_out, double* __restrict__ act_out,
-                                int* __restrict__ slot_of, unsigned* __restrict__ err) {
+                                int* __restrict__ slot_of, unsigned* __restrict__ err,
+                                const int* __restrict__ gate) {
+  if (gate && *gate == 0) return;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp > k.ncell) return;
@@ -202,56 +212,126 @@ __global__ void k_cell_finalize(Consts k, const int* __restrict__ start,
   }
 }
 
-int build_cell_list(Handle* h) {
+// zero the per-bin counts (a kernel, so that it can be gated)
+__global__ void k_zero_counts(int* __restrict__ cnt, int nbins, const int* __restrict__ gate) {
+  if (gate && *gate == 0) return;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < nbins) cnt[b] = 0;
+}
+
+// after a gated rebuild: the permuted state back into the primary buffers
+// (a host-side pointer swap cannot depend on the device flag) and the
+// reference positions of the new candidate list
+template <int D>
+__global__ void k_copy_back(int n, const int* __restrict__ gate, const double4_32a* __restrict__ x2,
+                            const double4_32a* __restrict__ v2, const double4_32a* __restrict__ f2,
+                            const double* __restrict__ m2, const int* __restrict__ pid2,
+                            const int* __restrict__ sid2, const int* __restrict__ hidx2,
+                            const double* __restrict__ ct2, const double* __restrict__ act2,
+                            double4_32a* __restrict__ x, double4_32a* __restrict__ v,
+                            double4_32a* __restrict__ f, double* __restrict__ m,
+                            int* __restrict__ pid, int* __restrict__ sid, int* __restrict__ hidx,
+                            double* __restrict__ ct, double* __restrict__ act,
+                            double4_32a* __restrict__ x_ref) {
+  if (*gate == 0) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4_32a xp = x2[i];
+  x[i] = xp;
+  x_ref[i] = xp;
+  v[i] = v2[i];
+  f[i] = f2[i];
+  m[i] = m2[i];
+  pid[i] = pid2[i];
+  sid[i] = sid2[i];
+  hidx[i] = hidx2[i];
+  if (ct != nullptr)
+    for (int cc = 0; cc < D * D; ++cc) {
+      ct[(size_t)cc * n + i] = ct2[(size_t)cc * n + i];
+      act[(size_t)cc * n + i] = act2[(size_t)cc * n + i];
+    }
+}
+
+// the cell list proper; with a gate every kernel returns at once when the
+// device flag is zero, and the permuted state is copied back instead of
+// swapping the buffers
+static int cell_list_launches(Handle* h, const int* gate) {
   Consts& k = h->k;
   const int n = (int)h->n;
   cudaStream_t s = h->stream;
   const int nbins = k.ncell + 1;
-  if (cuda_check(h, cudaMemsetAsync(h->cnt, 0, sizeof(int) * (size_t)nbins, s), "memset cnt"))
-    return MCFG_ECUDA;
+  if (gate == nullptr) {
+    if (cuda_check(h, cudaMemsetAsync(h->cnt, 0, sizeof(int) * (size_t)nbins, s), "memset cnt"))
+      return MCFG_ECUDA;
+  } else {
+    k_zero_counts<<<(nbins + 255) / 256, 256, 0, s>>>(h->cnt, nbins, gate);
+    h->launches++;
+  }
   const int tb = 256;
   const int gb = (n + tb - 1) / tb;
   if (n > 0) {
     if (k.d == 3)
-      k_cell_key<3><<<gb, tb, 0, s>>>(k, h->x, h->key, h->rank, h->cnt);
+      k_cell_key<3><<<gb, tb, 0, s>>>(k, h->x, h->key, h->rank, h->cnt, gate);
     else
-      k_cell_key<2><<<gb, tb, 0, s>>>(k, h->x, h->key, h->rank, h->cnt);
+      k_cell_key<2><<<gb, tb, 0, s>>>(k, h->x, h->key, h->rank, h->cnt, gate);
     h->launches++;
   }
   const int ntiles = (nbins + kScanTile - 1) / kScanTile;
-  k_scan_tiles<<<ntiles, kScanThreads, 0, s>>>(h->cnt, nbins, h->scan_part);
-  k_scan_partials<<<1, 1024, 0, s>>>(h->scan_part, ntiles);
-  k_scan_final<<<ntiles, kScanThreads, 0, s>>>(h->cnt, nbins, h->scan_part, h->cell_start);
+  k_scan_tiles<<<ntiles, kScanThreads, 0, s>>>(h->cnt, nbins, h->scan_part, gate);
+  k_scan_partials<<<1, 1024, 0, s>>>(h->scan_part, ntiles, gate);
+  k_scan_final<<<ntiles, kScanThreads, 0, s>>>(h->cnt, nbins, h->scan_part, h->cell_start, gate);
   h->launches += 3;
   if (n > 0) {
-    k_scatter<<<gb, tb, 0, s>>>(n, h->key, h->rank, h->cell_start, h->order);
+    k_scatter<<<gb, tb, 0, s>>>(n, h->key, h->rank, h->cell_start, h->order, gate);
     const int warps_per_block = 8;
     const int gw = (nbins + warps_per_block - 1) / warps_per_block;
     if (k.d == 3)
       k_cell_finalize<3><<<gw, warps_per_block * 32, 0, s>>>(
           k, h->cell_start, h->order, h->hidx, h->x, h->v, h->f, h->m, h->pid, h->sid, h->x2,
           h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->off, h->cell_of, h->wd, h->ct, h->act,
-          h->ct2, h->act2, h->slot_of, h->d_err);
+          h->ct2, h->act2, h->slot_of, h->d_err, gate);
     else
       k_cell_finalize<2><<<gw, warps_per_block * 32, 0, s>>>(
           k, h->cell_start, h->order, h->hidx, h->x, h->v, h->f, h->m, h->pid, h->sid, h->x2,
           h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->off, h->cell_of, h->wd, h->ct, h->act,
-          h->ct2, h->act2, h->slot_of, h->d_err);
+          h->ct2, h->act2, h->slot_of, h->d_err, gate);
     h->launches += 2;
-    std::swap(h->x, h->x2);
-    std::swap(h->v, h->v2);
-    std::swap(h->f, h->f2);
-    std::swap(h->m, h->m2);
-    std::swap(h->pid, h->pid2);
-    std::swap(h->sid, h->sid2);
-    std::swap(h->hidx, h->hidx2);
-    if (h->ct) {
-      std::swap(h->ct, h->ct2);
-      std::swap(h->act, h->act2);
+    if (gate == nullptr) {
+      std::swap(h->x, h->x2);
+      std::swap(h->v, h->v2);
+      std::swap(h->f, h->f2);
+      std::swap(h->m, h->m2);
+      std::swap(h->pid, h->pid2);
+      std::swap(h->sid, h->sid2);
+      std::swap(h->hidx, h->hidx2);
+      if (h->ct) {
+        std::swap(h->ct, h->ct2);
+        std::swap(h->act, h->act2);
+      }
+    } else {
+#define COPY_BACK(DD)                                                                            \
+  k_copy_back<DD><<<gb, tb, 0, s>>>(n, gate, h->x2, h->v2, h->f2, h->m2, h->pid2, h->sid2,       \
+                                    h->hidx2, h->ct2, h->act2, h->x, h->v, h->f, h->m, h->pid,   \
+                                    h->sid, h->hidx, h->ct, h->act, h->x_ref)
+      if (k.d == 3) COPY_BACK(3); else COPY_BACK(2);
+#undef COPY_BACK
+      h->launches++;
     }
   }
   if (cuda_check(h, cudaGetLastError(), "cell list launch")) return MCFG_ECUDA;
   return MCFG_OK;
 }
+
+int build_cell_list(Handle* h) {
+  h->reuse_valid = false;  // the particle order changes under any candidate list
+  if (h->unwrapped) {      // after list-reuse steps: MCF's wrap first
+    const int rc = adjust_particles(h);
+    if (rc) return rc;
+    h->unwrapped = false;
+  }
+  return cell_list_launches(h, nullptr);
+}
+
+int gated_cell_list(Handle* h) { return cell_list_launches(h, h->d_rebuild); }
 
 }  // namespace mcfg

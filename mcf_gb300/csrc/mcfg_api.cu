@@ -107,6 +107,13 @@ int dalloc(Handle* h, T** p, size_t count) {
 
 void free_all(Handle* h) {
   free_adjoint(h);
+  for (void* p : {(void*)h->x_ref, (void*)h->vl, (void*)h->vcount, (void*)h->d_rebuild})
+    if (p) cudaFree(p);
+  h->x_ref = nullptr;
+  h->vl = nullptr;
+  h->vcount = h->d_rebuild = nullptr;
+  h->vcap = 0;
+  h->reuse_valid = false;
   void* ptrs[] = {h->x, h->v, h->f, h->m, h->pid, h->sid, h->hidx, h->rho, h->pr, h->st,
                   h->x2, h->v2, h->f2, h->m2, h->pid2, h->sid2, h->hidx2, h->key, h->rank,
                   h->cnt, h->cell_start, h->scan_part, h->order, h->off, h->cell_of, h->nl,
@@ -213,6 +220,18 @@ void make_consts(const mcfg_params& p, Consts& k) {
   }
   k.rc2 = p.cut_off * p.cut_off;
   k.rc2f = (float)k.rc2;
+  k.reuse = 0;
+  if (p.reserved[1] != 0) {
+    double csmin = 1e300;
+    for (int a = 0; a < k.d; ++a) csmin = std::min(csmin, k.cs[a]);
+    const double skin = 0.99 * (csmin - p.cut_off);
+    if (skin > 0.0) {
+      k.reuse = 1;
+      k.half_skin2 = 0.25 * skin * skin;
+      const double rv = p.cut_off + skin;
+      k.rv2f = (float)(rv * rv * (1.0 + 1e-4));
+    }
+  }
   // FP32 prefilter of the FP64 path: relative slack far above the FP32
   // rounding of cell offsets (|offset| <= cell side)
   k.rc2f_hi = (float)(k.rc2 * (1.0 + 1e-4));
@@ -322,6 +341,22 @@ __global__ void k_download(int n, int d, const int* __restrict__ hidx, const dou
   if (d == 3) o[2] = v.z;
 }
 
+// positions in host order, wrapped into the periodic box (after list-reuse
+// steps the stored positions may lie up to skin/2 outside a periodic face)
+__global__ void k_download_pos(Consts k, int n, const int* __restrict__ hidx,
+                               const double4_32a* __restrict__ x, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4_32a v = x[i];
+  double xs[3] = {v.x, v.y, v.z};
+  for (int a = 0; a < k.d; ++a) {
+    if (xs[a] < k.min_phys[a] && k.bc_lo[a] == MCFG_BC_PERIODIC) xs[a] = __dadd_rn(xs[a], k.len[a]);
+    if (xs[a] >= k.max_phys[a] && k.bc_hi[a] == MCFG_BC_PERIODIC) xs[a] = __dsub_rn(xs[a], k.len[a]);
+  }
+  double* o = out + (size_t)hidx[i] * k.d;
+  for (int a = 0; a < k.d; ++a) o[a] = xs[a];
+}
+
 __global__ void k_download_scalar(int n, const int* __restrict__ hidx, const double* __restrict__ a,
                                   double* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -370,6 +405,17 @@ int ensure_capacity(Handle* h, int64_t n64) {
         (rc = dalloc(h, &h->d_err, 1)) || (rc = dalloc(h, &h->d_stats, 4)) ||
         (rc = dalloc(h, &h->d_pairs, 1)))
       return rc;
+    if (h->k.reuse) {
+      // candidates within rc + skin: the list grows with the volume ratio
+      const double rv = std::sqrt((double)h->k.rv2f) / h->p.cut_off;
+      h->vcap = (int)std::ceil(neigh * std::pow(rv, d) * 1.05) + 8;
+      if ((rc = dalloc(h, &h->x_ref, cap)) || (rc = dalloc(h, &h->vl, cap * (size_t)h->vcap)) ||
+          (rc = dalloc(h, &h->vcount, cap)) || (rc = dalloc(h, &h->d_rebuild, 2)))
+        return rc;
+      if (cuda_check(h, cudaMemsetAsync(h->d_rebuild, 0, 2 * sizeof(int), h->stream),
+                     "memset rebuild"))
+        return MCFG_ECUDA;
+    }
     if (h->p.precision == MCFG_PRECISION_FP64) {
       if ((rc = dalloc(h, &h->pc, cap)) || (rc = dalloc(h, &h->rxc, cap))) return rc;
     } else {
@@ -452,6 +498,51 @@ int rhs(Handle* h, int64_t step, int fuse_mode, double dt) {
 int kdw(Handle* h, double dt) {
   PhaseScope ps(h, kPhaseUpdate);
   return kick_drift_wrap(h, dt);
+}
+
+// the right-hand side in list-reuse mode: the rebuild kernels return at once
+// unless a particle has moved more than skin/2 (or no candidate list matches
+// the particles yet), then the density over the candidate list and the force
+int rhs_reuse(Handle* h, int64_t step, int fuse_mode, double dt) {
+  {
+    PhaseScope ps(h, kPhaseList);
+    if (!h->reuse_valid &&
+        cuda_check(h, cudaMemsetAsync(h->d_rebuild, 0xff, sizeof(int), h->stream), "rebuild flag"))
+      return MCFG_ECUDA;
+    TRY(wrap_gated(h));
+    TRY(gated_cell_list(h));
+    TRY(verlet_build_gated(h));
+    h->reuse_valid = true;
+  }
+  h->have_list = false;  // stage entry points rebuild MCF's list themselves
+  {
+    PhaseScope ps(h, kPhaseDensity);
+    TRY(compute_density(h, true, true));
+  }
+  h->have_density = h->have_pressure = true;
+  {
+    PhaseScope ps(h, kPhaseForce);
+    TRY(compute_force(h, step, fuse_mode, dt));
+  }
+  h->have_force = true;
+  return MCFG_OK;
+}
+
+// one VV step of mcfg_step_vv / mcfg_run_vv
+int vv_step(Handle* h, int64_t step, double dt) {
+  if (!h->k.reuse) {
+    TRY(kdw(h, dt));
+    return rhs(h, step, kForceBodyKick, dt);
+  }
+  if (h->reuse_valid) {
+    PhaseScope ps(h, kPhaseUpdate);
+    h->unwrapped = true;
+    TRY(kick_drift_reuse(h, dt));
+  } else {
+    // no candidate list yet: MCF's kick-drift-wrap; the rebuild follows
+    TRY(kdw(h, dt));
+  }
+  return rhs_reuse(h, step, kForceBodyKick, dt);
 }
 
 }  // namespace mcfg
@@ -551,6 +642,15 @@ int mcfg_get_info(const mcfg_handle* h, mcfg_info* info) {
   info->neigh_capacity = h->neigh_cap;
   info->kernel_launches = h->launches;
   info->device_bytes = h->device_bytes;
+  if (h->k.reuse) {
+    info->skin = 2.0 * std::sqrt(h->k.half_skin2);
+    int cntr[2] = {0, 0};
+    if (h->d_rebuild && cudaSetDevice(h->device) == cudaSuccess &&
+        cudaMemcpyAsync(cntr, h->d_rebuild, sizeof cntr, cudaMemcpyDeviceToHost, h->stream) ==
+            cudaSuccess &&
+        cudaStreamSynchronize(h->stream) == cudaSuccess)
+      info->list_rebuilds = cntr[1];
+  }
   return MCFG_OK;
 }
 
@@ -637,6 +737,8 @@ int mcfg_upload(mcfg_handle* h, int64_t n, const double* x, const double* v, con
     h->coll_nmem = (int)h->h_coll_mem.size();
   }
   h->have_particles = true;
+  h->reuse_valid = false;
+  h->unwrapped = false;
   h->have_list = h->have_density = h->have_pressure = h->have_force = false;
   return MCFG_OK;
 }
@@ -755,8 +857,7 @@ int mcfg_step_vv(mcfg_handle* h, int64_t step, double dt) {
   if (!h->have_force) return set_error(h, MCFG_ESTATE, "mcfg_init_force must come first");
   if (!(dt > 0.0)) return set_error(h, MCFG_EINVAL, "dt must be positive");
   h->dt = dt;
-  TRY(kdw(h, dt));
-  TRY(rhs(h, step, kForceBodyKick, dt));
+  TRY(vv_step(h, step, dt));
   return check_device_errors(h);
 }
 
@@ -765,10 +866,7 @@ int mcfg_run_vv(mcfg_handle* h, int64_t step0, int32_t nsteps, double dt) {
   if (!h->have_force) return set_error(h, MCFG_ESTATE, "mcfg_init_force must come first");
   if (!(dt > 0.0)) return set_error(h, MCFG_EINVAL, "dt must be positive");
   h->dt = dt;
-  for (int32_t q = 1; q <= nsteps; ++q) {
-    TRY(kdw(h, dt));
-    TRY(rhs(h, step0 + q, kForceBodyKick, dt));
-  }
+  for (int32_t q = 1; q <= nsteps; ++q) TRY(vv_step(h, step0 + q, dt));
   return check_device_errors(h);
 }
 
@@ -799,7 +897,14 @@ int mcfg_download(mcfg_handle* h, double* x, double* v, double* rho, double* p, 
       return MCFG_ECUDA;
     return cuda_check(h, cudaStreamSynchronize(st), "download sync") ? MCFG_ECUDA : MCFG_OK;
   };
-  if (x) TRY(vec_out(h->x, x));
+  if (x) {
+    k_download_pos<<<gb, tb, 0, st>>>(h->k, n, h->hidx, h->x, stage);
+    h->launches++;
+    if (cuda_check(h, cudaMemcpyAsync(x, stage, sizeof(double) * (size_t)n * d,
+                                      cudaMemcpyDeviceToHost, st), "download") ||
+        cuda_check(h, cudaStreamSynchronize(st), "download sync"))
+      return MCFG_ECUDA;
+  }
   if (v) TRY(vec_out(h->v, v));
   if (f) TRY(vec_out(h->f, f));
   if (rho) TRY(sca_out(h->rho, rho));

@@ -42,6 +42,14 @@ struct Consts {
   float csf[3];
   double rc2;               // cut_off**2
   float rc2f, rc2f_hi;      // FP32 cut-off^2 and its prefilter bound
+  // neighbour-list reuse (mcfg_params.reserved[1] != 0): the candidates
+  // within rc + skin are listed at a rebuild and re-tested every step; a
+  // rebuild happens when a particle has moved more than skin/2 since the
+  // last one.  skin = 0.99 (smallest cell side - rc), so the 27/9-cell
+  // stencil of the rebuild still holds every pair of the step.
+  int reuse;
+  double half_skin2;        // (skin/2)^2
+  float rv2f;               // FP32 bound of the candidate list, (rc + skin)^2 with slack
   // kernel
   int kernel_type;
   double h, inv_h, coef, coef_grad, w0;
@@ -157,6 +165,14 @@ struct Handle {
   double* up_m = nullptr;
   int* up_id = nullptr;
   size_t up_cap = 0;
+  // ---- neighbour-list reuse ----
+  double4_32a* x_ref = nullptr;  // positions at the last rebuild
+  uint16_t* vl = nullptr;        // [vcap][n] candidates within rc + skin (slot<<11 | local)
+  int* vcount = nullptr;         // [n]
+  int vcap = 0;
+  int* d_rebuild = nullptr;      // [0] rebuild request, [1] rebuilds done
+  bool reuse_valid = false;      // the candidate list matches the particle order
+  bool unwrapped = false;        // positions may lie outside periodic faces (list reuse)
   // ---- adjoint buffers (adjoint.cu), null until mcfg_adjoint_run ----
   struct AdjBuffers* adj = nullptr;
   // ---- per-phase device timers ----
@@ -216,7 +232,16 @@ namespace mcfg {
 
 // launches (implemented in the .cu files)
 int build_cell_list(Handle* h);
-int compute_density(Handle* h, bool with_pressure);
+// list-reuse step pieces: a rebuild (wrap, cell list, candidate list) whose
+// kernels all return at once unless a particle has moved more than skin/2
+// (device flag), the density sweep over the candidate list, and the kick /
+// drift that leaves positions unwrapped and raises the flag
+int rebuild_if_needed(Handle* h);
+int kick_drift_reuse(Handle* h, double dt);
+int wrap_gated(Handle* h);
+int gated_cell_list(Handle* h);
+int verlet_build_gated(Handle* h);
+int compute_density(Handle* h, bool with_pressure, bool reuse = false);
 int compute_pressure(Handle* h);
 int compute_force(Handle* h, int64_t step, int fuse_mode, double dt);
 int apply_body_force(Handle* h);

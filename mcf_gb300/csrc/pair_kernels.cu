@@ -310,6 +310,205 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   }
 }
 
+// ---------------------------------------------------------------------------
+// List-reuse mode: the candidate list (gated rebuild) and the density sweep
+// over it.
+// ---------------------------------------------------------------------------
+
+// Candidates within rc + skin of every particle: k_density's FP32 scan of
+// the 27/9 neighbour cells with the larger bound, written to vl.  Returns at
+// once unless a rebuild is due.
+template <int D>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+    k_verlet_build(Consts k, const int* __restrict__ gate, const int* __restrict__ cell_start,
+                   const float4* __restrict__ off, uint16_t* __restrict__ vl,
+                   int* __restrict__ vcount, int vcap, unsigned* __restrict__ err) {
+  if (*gate == 0) return;
+  constexpr int NS = (D == 3) ? 27 : 9;
+  constexpr int CENTER = (D == 3) ? 13 : 4;
+  __shared__ NbTable tab[kWarpsPerBlock];
+  __shared__ float4 sb[kWarpsPerBlock][kStage];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = k.n;
+  for (int cell = blockIdx.x * kWarpsPerBlock + wib; cell <= k.ncell;
+       cell += gridDim.x * kWarpsPerBlock) {
+    NbTable& t = tab[wib];
+    build_table<D>(k, cell, cell_start, t);
+    const int c0 = t.start[CENTER], c1 = c0 + t.count[CENTER];
+    for (int base = c0; base < c1; base += 32) {
+      const int i = base + lane;
+      const bool active = i < c1;
+      const float4 oi = active ? off[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      int cnt = 0;
+      for (int sl = 0; sl < NS; ++sl) {
+        const int js = t.start[sl], jn = t.count[sl];
+        const float4 so = t.o[sl];
+        const float px = oi.x - so.x, py = oi.y - so.y, pz = oi.z - so.z;
+        for (int b2 = 0; b2 < jn; b2 += kStage) {
+          const int mm = min(kStage, jn - b2);
+          __syncwarp();
+          for (int q = lane; q < mm; q += 32) sb[wib][q] = off[js + b2 + q];
+          __syncwarp();
+#pragma unroll 4
+          for (int q2 = 0; q2 < mm; ++q2) {
+            const float4 oj = sb[wib][q2];
+            const float rx = px - oj.x, ry = py - oj.y;
+            float d2 = rx * rx + ry * ry;
+            if (D == 3) {
+              const float rz = pz - oj.z;
+              d2 += rz * rz;
+            }
+            const int q = b2 + q2;
+            if (active && d2 < k.rv2f && !(sl == CENTER && js + q == i)) {
+              if (cnt < vcap) vl[(size_t)cnt * n + i] = (uint16_t)((sl << kLocalBits) | q);
+              ++cnt;
+            }
+          }
+        }
+      }
+      if (active) {
+        if (cnt > vcap) atomicOr(err, kErrNeighOverflow);
+        vcount[i] = min(cnt, vcap);
+      }
+    }
+  }
+}
+
+// end of a gated rebuild: count it and lower the flag
+__global__ void k_rebuild_done(int* __restrict__ flag) {
+  if (flag[0] != 0) flag[1] += 1;
+  flag[0] = 0;
+}
+
+constexpr int kReuseTPB = 128;
+
+// Density over the candidate list, one thread per particle: the step's
+// exact pair test (FP64 path: the FP64 separation of MCF; FP32 path: the
+// FP32 test of k_density's scan, same operation order), the step's neighbour
+// list for the force sweep, the W sum and the epilogue of k_density.
+template <int D, bool FP64>
+__global__ void __launch_bounds__(kReuseTPB)
+    k_density_reuse(Consts k, const int* __restrict__ cell_start, const int* __restrict__ cell_of,
+                    const float4* __restrict__ off, const double4_32a* __restrict__ x,
+                    const double4_32a* __restrict__ v, const double* __restrict__ m,
+                    const int* __restrict__ sid, const int* __restrict__ pid,
+                    const uint16_t* __restrict__ vl, const int* __restrict__ vcount,
+                    uint16_t* __restrict__ nl, int* __restrict__ ncount, int* __restrict__ nhs,
+                    int cap, double* __restrict__ rho, double* __restrict__ pr,
+                    double4_32a* __restrict__ pc, float4* __restrict__ pcf,
+                    float4* __restrict__ vf, int with_pressure, unsigned* __restrict__ err,
+                    int* __restrict__ stats, unsigned long long* __restrict__ pairs, NN nn,
+                    CollArgs ca) {
+  constexpr int NS = (D == 3) ? 27 : 9;
+  constexpr int CENTER = (D == 3) ? 13 : 4;
+  __shared__ int s_start[NS * kReuseTPB];
+  __shared__ int s_shift[NS * kReuseTPB];
+  const int n = k.n, tid = threadIdx.x;
+  const int i = blockIdx.x * kReuseTPB + tid;
+  int my_max = 0;
+  unsigned long long my_pairs = 0;
+  if (i < n) {
+    build_lane_table<D, kReuseTPB>(k, cell_of[i], cell_start, s_start, s_shift);
+    const int li = i - s_start[CENTER * kReuseTPB + tid];
+    const int si = sid[i];
+    const bool acc_i = dyn_rho(k, si);
+    const int cnt = vcount[i];
+    int kept = 0, hs = -1;
+    double rho_i;
+    if (FP64) {
+      const double4_32a xi4 = x[i];
+      const double xi[3] = {xi4.x, xi4.y, xi4.z};
+      double sum = 0.0;
+      for (int e = 0; e < cnt; ++e) {
+        const int ent = vl[(size_t)e * n + i];
+        const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
+        const int j = s_start[sl * kReuseTPB + tid] + q;
+        const double4_32a xj4 = x[j];
+        const double xj[3] = {xj4.x, xj4.y, xj4.z};
+        double r[3];
+        const double d2 = exact_sep<D>(k, xi, xj, s_shift[sl * kReuseTPB + tid], r);
+        if (d2 >= k.rc2) continue;
+        if (hs < 0 && (sl > CENTER || (sl == CENTER && q > li))) hs = kept;
+        if (kept < cap) nl[(size_t)kept * n + i] = (uint16_t)ent;
+        ++kept;
+        if (acc_i) {
+          const double w = kernel_w<double>(k, sqrt(d2));
+          sum += (k.rhs_density_type == 1) ? w * m[j] : w;
+        }
+      }
+      rho_i = sum;
+    } else {
+      const float4 oi = off[i];
+      const bool mass = k.rhs_density_type == 1;
+      float sum = 0.0f, comp = 0.0f;
+      for (int e = 0; e < cnt; ++e) {
+        const int ent = vl[(size_t)e * n + i];
+        const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
+        const int j = s_start[sl * kReuseTPB + tid] + q;
+        const float4 oj = off[j];
+        const float sx = (float)(sl % 3 - 1) * k.csf[0];
+        const float sy = (float)((sl / 3) % 3 - 1) * k.csf[1];
+        const float sz = (D == 3) ? (float)(sl / 9 - 1) * k.csf[2] : 0.0f;
+        // the pair test as k_density's scan rounds it: (o_i - slot) - o_j
+        const float tx = (oi.x - sx) - oj.x, ty = (oi.y - sy) - oj.y;
+        float t2 = tx * tx + ty * ty;
+        if (D == 3) {
+          const float tz = (oi.z - sz) - oj.z;
+          t2 += tz * tz;
+        }
+        if (!(t2 < k.rc2f)) continue;
+        if (hs < 0 && (sl > CENTER || (sl == CENTER && q > li))) hs = kept;
+        if (kept < cap) nl[(size_t)kept * n + i] = (uint16_t)ent;
+        ++kept;
+        if (!acc_i) continue;
+        // W as k_density's second phase rounds it: (o_i - o_j) - slot
+        const float rx = (oi.x - oj.x) - sx, ry = (oi.y - oj.y) - sy;
+        float d2 = rx * rx + ry * ry;
+        if (D == 3) {
+          const float rz = (oi.z - oj.z) - sz;
+          d2 += rz * rz;
+        }
+        float w = kernel_w<float>(k, sqrtf(d2));
+        if (mass) w *= (float)m[j];
+        const float y = w - comp;
+        const float tt = sum + y;
+        comp = (tt - sum) - y;
+        sum = tt;
+      }
+      rho_i = (double)sum;
+    }
+    if (kept > cap) atomicOr(err, kErrNeighOverflow);
+    my_max = kept;
+    kept = min(kept, cap);
+    ncount[i] = kept;
+    nhs[i] = (hs < 0 || hs > kept) ? kept : hs;
+    my_pairs = (unsigned long long)kept;
+    const double mi = m[i];
+    double rho_out;
+    if (acc_i) {
+      rho_out = ((k.rhs_density_type == 1) ? k.w0 * mi : k.w0) + rho_i;
+    } else {
+      rho_out = (k.rhs_density_type == 1) ? k.init_density : k.init_density / mi;
+    }
+    rho[i] = rho_out;
+    if (!(rho_out > 0.0)) atomicOr(err, kErrZeroDensity);
+    if (with_pressure) {
+      const double4_32a vi4 =
+          (si > 0 && k.ncoll > 0) ? colloid_particle_update<D>(k, i, si, x[i], ca) : v[i];
+      write_particle_records<FP64>(k, i, rho_out, mi, pid[i], vi4, pr, pc, pcf, vf, nn);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    my_max = max(my_max, __shfl_xor_sync(0xffffffffu, my_max, o));
+    my_pairs += __shfl_xor_sync(0xffffffffu, my_pairs, o);
+  }
+  if ((tid & 31) == 0) {
+    atomicMax(&stats[1], my_max);
+    atomicAdd(pairs, my_pairs);
+  }
+}
+
 template <int D, bool FP64>
 __global__ void k_pressure(Consts k, const double* __restrict__ rho, const double* __restrict__ m,
                            const int* __restrict__ pid, const double4_32a* __restrict__ v,
@@ -347,7 +546,12 @@ __device__ __forceinline__ void force_epilogue(const Consts& k, int i, int si, c
     } else if (k.body_force_type == 2) {
       if (fabs(g[0]) > k.machine_zero) {
         const double half = k.max_phys[D - 1] * 0.5;
-        const double xl = xi[D - 1];
+        double xl = xi[D - 1];
+        // positions may sit past a periodic face between list rebuilds
+        if (k.periodic[D - 1]) {
+          if (xl < k.min_phys[D - 1]) xl = __dadd_rn(xl, k.len[D - 1]);
+          if (xl >= k.max_phys[D - 1]) xl = __dsub_rn(xl, k.len[D - 1]);
+        }
         if (xl < half)
           ax += g[0];
         else if (xl > half)
@@ -1266,7 +1470,21 @@ static int grid_for(Handle* h) {
   return g < 1 ? 1 : g;
 }
 
-int compute_density(Handle* h, bool with_pressure) {
+int verlet_build_gated(Handle* h) {
+  Consts& k = h->k;
+  const int g = grid_for(h);
+  if (k.d == 3)
+    k_verlet_build<3><<<g, kWarpsPerBlock * 32, 0, h->stream>>>(
+        k, h->d_rebuild, h->cell_start, h->off, h->vl, h->vcount, h->vcap, h->d_err);
+  else
+    k_verlet_build<2><<<g, kWarpsPerBlock * 32, 0, h->stream>>>(
+        k, h->d_rebuild, h->cell_start, h->off, h->vl, h->vcount, h->vcap, h->d_err);
+  k_rebuild_done<<<1, 1, 0, h->stream>>>(h->d_rebuild);
+  h->launches += 2;
+  return cuda_check(h, cudaGetLastError(), "candidate list launch") ? MCFG_ECUDA : MCFG_OK;
+}
+
+int compute_density(Handle* h, bool with_pressure, bool reuse) {
   Consts& k = h->k;
   cudaStream_t s = h->stream;
   if (cuda_check(h, cudaMemsetAsync(h->d_stats, 0, sizeof(int) * 4, s), "memset stats"))
@@ -1275,6 +1493,25 @@ int compute_density(Handle* h, bool with_pressure) {
     return MCFG_ECUDA;
   const int g = grid_for(h);
   const bool fp64 = h->p.precision == MCFG_PRECISION_FP64;
+  if (reuse) {
+    const int n = (int)h->n;
+    if (n == 0) return MCFG_OK;
+    const int gr = (n + kReuseTPB - 1) / kReuseTPB;
+#define LAUNCH_R(DD, PP)                                                                        \
+  k_density_reuse<DD, PP><<<gr, kReuseTPB, 0, s>>>(                                             \
+      k, h->cell_start, h->cell_of, h->off, h->x, h->v, h->m, h->sid, h->pid, h->vl, h->vcount, \
+      h->nl, h->ncount, h->nhs, h->neigh_cap, h->rho, h->pr, h->pc, h->pcf, h->vf,              \
+      with_pressure ? 1 : 0, h->d_err, h->d_stats, h->d_pairs, NN{h->ct, h->act, h->vgt, h->qq}, \
+      CollArgs{h->v, h->rxc, h->rxcf})
+    if (k.d == 3) {
+      if (fp64) LAUNCH_R(3, true); else LAUNCH_R(3, false);
+    } else {
+      if (fp64) LAUNCH_R(2, true); else LAUNCH_R(2, false);
+    }
+#undef LAUNCH_R
+    h->launches++;
+    return cuda_check(h, cudaGetLastError(), "density launch") ? MCFG_ECUDA : MCFG_OK;
+  }
 #define LAUNCH_D(DD, PP)                                                                       \
   k_density<DD, PP><<<g, kWarpsPerBlock * 32, 0, s>>>(                                          \
       k, h->cell_start, h->off, h->x, h->v, h->m, h->sid, h->pid, h->nl, h->ncount, h->nhs,    \

@@ -221,6 +221,117 @@ int colloid_drag(Handle* h, double* drag, double* torque) {
   return MCFG_OK;
 }
 
+// List-reuse form of the first half of a VV step: ct half step, kick and
+// drift as k_integrate, positions left unwrapped (the candidate list and its
+// periodic images stay valid until the next rebuild, which wraps), the FP32
+// cell offsets and wall distances refreshed against the rebuild cell, and the
+// rebuild flag raised when a particle has moved more than skin/2.
+template <int D>
+__global__ void k_kdw_reuse(Consts k, double dt, double4_32a* __restrict__ x,
+                            double4_32a* __restrict__ v, const double4_32a* __restrict__ f,
+                            const int* __restrict__ sid, double* __restrict__ ct,
+                            const double* __restrict__ act, const double4_32a* __restrict__ x_ref,
+                            const int* __restrict__ cell_of, float4* __restrict__ off,
+                            float2* __restrict__ wd, int* __restrict__ flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool far = false;
+  if (i < k.n) {
+    if (ct != nullptr) {
+#pragma unroll
+      for (int cc = 0; cc < D * D; ++cc) {
+        const size_t q = (size_t)cc * k.n + i;
+        ct[q] = __dadd_rn(ct[q], __dmul_rn(__dmul_rn(act[q], dt), 0.5));
+      }
+    }
+    const int s = sid[i];
+    double4_32a xv = x[i];
+    if (s == 0) {
+      double4_32a vv = v[i];
+      const double4_32a fv = f[i];
+      double xs[3] = {xv.x, xv.y, xv.z}, vs[3] = {vv.x, vv.y, vv.z};
+      const double fs[3] = {fv.x, fv.y, fv.z};
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        vs[a] = __dadd_rn(vs[a], __dmul_rn(__dmul_rn(0.5, fs[a]), dt));
+        xs[a] = __dadd_rn(xs[a], __dmul_rn(vs[a], dt));
+      }
+      xv = make_double4_32a(xs[0], xs[1], D == 3 ? xs[2] : 0.0, 0.0);
+      x[i] = xv;
+      v[i] = make_double4_32a(vs[0], vs[1], D == 3 ? vs[2] : 0.0, 0.0);
+    }
+    const double4_32a xr = x_ref[i];
+    const double dx = xv.x - xr.x, dy = xv.y - xr.y, dz = (D == 3) ? xv.z - xr.z : 0.0;
+    far = dx * dx + dy * dy + dz * dz > k.half_skin2;
+    // offsets to the rebuild cell's origin (k_cell_finalize's formula)
+    const int cell = cell_of[i];
+    double org[3] = {0.0, 0.0, 0.0};
+    if (cell < k.ncell) {
+      int cq = cell;
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        const int ca = cq % k.nm[a];
+        cq /= k.nm[a];
+        org[a] = k.xmin[a] + (double)ca * k.cs[a];
+      }
+    }
+    float4 of = off[i];
+    of.x = (float)(xv.x - org[0]);
+    of.y = (float)(xv.y - org[1]);
+    of.z = (D == 3) ? (float)(xv.z - org[2]) : 0.0f;
+    off[i] = of;
+    if (wd != nullptr && k.wall_axis >= 0) {
+      const double xa = k.wall_axis == 0 ? xv.x : (k.wall_axis == 1 ? xv.y : xv.z);
+      wd[i] = make_float2((float)(xa - k.min_phys[k.wall_axis]),
+                          (float)(xa - k.max_phys[k.wall_axis]));
+    }
+  }
+  if (__any_sync(0xffffffffu, far) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+// periodic wrap of every particle before a rebuild; returns at once when no
+// rebuild is due
+template <int D>
+__global__ void k_wrap_gated(Consts k, const int* __restrict__ flag, double4_32a* __restrict__ x,
+                             double4_32a* __restrict__ v, const int* __restrict__ sid) {
+  if (*flag == 0) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= k.n) return;
+  double4_32a xv = x[i], vv = v[i];
+  double xs[3] = {xv.x, xv.y, xv.z}, vs[3] = {vv.x, vv.y, vv.z};
+  const int s = sid[i];
+#pragma unroll
+  for (int a = 0; a < D; ++a) wrap_axis(k, a, s, xs[a], vs[a]);
+  x[i] = make_double4_32a(xs[0], xs[1], D == 3 ? xs[2] : 0.0, 0.0);
+  v[i] = make_double4_32a(vs[0], vs[1], D == 3 ? vs[2] : 0.0, 0.0);
+}
+
+int wrap_gated(Handle* h) {
+  const int n = (int)h->n;
+  if (n == 0) return MCFG_OK;
+  const int tb = 256, gb = (n + tb - 1) / tb;
+  if (h->k.d == 3)
+    k_wrap_gated<3><<<gb, tb, 0, h->stream>>>(h->k, h->d_rebuild, h->x, h->v, h->sid);
+  else
+    k_wrap_gated<2><<<gb, tb, 0, h->stream>>>(h->k, h->d_rebuild, h->x, h->v, h->sid);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "wrap launch") ? MCFG_ECUDA : MCFG_OK;
+}
+
+int kick_drift_reuse(Handle* h, double dt) {
+  const int n = (int)h->n;
+  if (n == 0) return MCFG_OK;
+  const int tb = 256, gb = (n + tb - 1) / tb;
+  double* ct = h->p.Newtonian ? nullptr : h->ct;
+  if (h->k.d == 3)
+    k_kdw_reuse<3><<<gb, tb, 0, h->stream>>>(h->k, dt, h->x, h->v, h->f, h->sid, ct, h->act,
+                                             h->x_ref, h->cell_of, h->off, h->wd, h->d_rebuild);
+  else
+    k_kdw_reuse<2><<<gb, tb, 0, h->stream>>>(h->k, dt, h->x, h->v, h->f, h->sid, ct, h->act,
+                                             h->x_ref, h->cell_of, h->off, h->wd, h->d_rebuild);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "kick-drift launch") ? MCFG_ECUDA : MCFG_OK;
+}
+
 static int launch_integrate(Handle* h, int flags, double dt, double lambda) {
   const int n = (int)h->n;
   if (n == 0) return MCFG_OK;
@@ -239,7 +350,12 @@ int integrate_velocity(Handle* h, double dt, double lambda) {
   return launch_integrate(h, 1, dt, lambda);
 }
 int integrate_position(Handle* h, double dt) { return launch_integrate(h, 2, dt, 0.0); }
-int adjust_particles(Handle* h) { return launch_integrate(h, 4, 0.0, 0.0); }
+int adjust_particles(Handle* h) {
+  // a wrap moves particles by a period: the candidate list's images no longer hold
+  h->reuse_valid = false;
+  h->unwrapped = false;
+  return launch_integrate(h, 4, 0.0, 0.0);
+}
 int kick_ct_half(Handle* h, double dt) {
   return launch_integrate(h, h->p.Newtonian ? 1 : 9, dt, 0.5);
 }

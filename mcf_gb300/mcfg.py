@@ -150,6 +150,8 @@ class SDPD:
             "neigh_capacity": inf.neigh_capacity,
             "kernel_launches": inf.kernel_launches,
             "device_bytes": inf.device_bytes,
+            "list_rebuilds": inf.list_rebuilds,
+            "skin": inf.skin,
         }
 
     # -- data --------------------------------------------------------------

@@ -115,6 +115,8 @@ class SDPDInfo(C.Structure):
         ("neigh_capacity", C.c_int32),
         ("kernel_launches", C.c_int64),
         ("device_bytes", C.c_int64),
+        ("list_rebuilds", C.c_int64),
+        ("skin", C.c_double),
     ]
 
 

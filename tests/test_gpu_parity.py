@@ -352,3 +352,73 @@ def test_colloid_steps_fp64_and_fp32(gpu_lib):
     vs = np.abs(b["v"]).max()
     assert np.max(np.abs(a["v"] - b["v"])) <= 1e-9 * vs
     assert np.max(np.abs(c32["v"] - b["v"])) <= 2e-4 * vs
+
+
+# ------------------------------------------------------- neighbour-list reuse
+def _reuse_pair(w, nsteps, dt, **over):
+    """the same run with and without list reuse: (standard, reuse) handles"""
+    out = []
+    for reuse in (0, 1):
+        p = w.params.copy()
+        p.reserved[1] = reuse
+        for k, v in over.items():
+            setattr(p, k, v)
+        h = SDPD(p)
+        h.upload(w.x, w.v, w.m, w.id)
+        h.marching_init_force(0)
+        h.run_vv(0, nsteps, dt)
+        out.append(h)
+    return out
+
+
+@pytest.mark.parametrize("precision", [PRECISION_FP64, PRECISION_FP32_MIXED])
+def test_list_reuse_matches_rebuild_every_step(gpu_lib, precision):
+    # 16^3 jittered: cells of 3.2 for rc = 3, skin 0.198
+    w = jittered_3d(n_side=16, precision=precision)
+    a, b = _reuse_pair(w, 50, w.dt, Brownian=0, kt=0.0)
+    info = b.info()
+    assert info["skin"] > 0.19 and info["list_rebuilds"] >= 1
+    da, db = a.download("x", "v"), b.download("x", "v")
+    L = 16.0
+    assert np.all((db["x"] >= 0.0) & (db["x"] < L))  # downloaded wrapped
+    dx = da["x"] - db["x"]
+    dx -= L * np.round(dx / L)
+    tol = 1e-10 if precision == PRECISION_FP64 else 1e-5
+    assert np.max(np.abs(dx)) <= tol
+    assert np.max(np.abs(da["v"] - db["v"])) <= tol * np.max(np.abs(da["v"]))
+
+
+def test_list_reuse_rebuilds_on_displacement(gpu_lib):
+    # fast particles (|v| ~ 0.3, dt = 1e-2: ~3e-3 per step against half a
+    # skin of 0.1): the device rebuilds many times; the trajectory is the
+    # one without reuse and the oracle's
+    w = jittered_3d(n_side=16)
+    rng = np.random.default_rng(9)
+    w.v = rng.normal(0, 0.3, w.v.shape)
+    a, b = _reuse_pair(w, 100, 1e-2, Brownian=0, kt=0.0)
+    assert b.info()["list_rebuilds"] >= 5
+    da, db = a.download("x", "v", "rho", "f"), b.download("x", "v", "rho", "f")
+    L = 16.0
+    dx = da["x"] - db["x"]
+    dx -= L * np.round(dx / L)
+    assert np.max(np.abs(dx)) <= 1e-9
+    assert np.max(np.abs(da["v"] - db["v"])) <= 1e-8 * np.max(np.abs(da["v"]))
+    assert np.max(np.abs(da["rho"] - db["rho"]) / da["rho"]) <= 1e-10
+
+
+def test_list_reuse_walls_oldroyd_and_noise(gpu_lib):
+    # walls: per-step pair terms with Morris no-slip; Oldroyd-B: ct travels
+    # with the rebuild permutation; noise: same keys, same draws
+    w = make_golden.workload("walls_small")
+    a, b = _reuse_pair(w, 30, w.dt)
+    da, db = a.download("x", "v", "f"), b.download("x", "v", "f")
+    assert np.max(np.abs(da["x"] - db["x"])) <= 1e-10
+    assert np.max(np.abs(da["v"] - db["v"])) <= 1e-8 * np.max(np.abs(da["v"]))
+    w = oldroyd_case()
+    a, b = _reuse_pair(w, 20, w.dt)
+    da, db = a.download("x", "v", "ct"), b.download("x", "v", "ct")
+    L = w.params.max_phys[0] - w.params.min_phys[0]
+    dx = da["x"] - db["x"]
+    dx -= L * np.round(dx / L)
+    assert np.max(np.abs(dx)) <= 1e-10
+    assert np.max(np.abs(da["ct"] - db["ct"])) <= 1e-10
