@@ -22,6 +22,7 @@
 //
 // Reference: particles_compute_density.F90:369-867, particles_compute_
 // interaction.F90:609-900, pp_interaction*.inc, rhs_force_ff_Newtonian*.F90.
+#include <algorithm>
 #include <type_traits>
 
 #include "mcfg_internal.cuh"
@@ -611,198 +612,192 @@ __device__ __forceinline__ void nn_epilogue(const Consts& k, const NN& nn, int i
 // FP64 force sweep
 // ---------------------------------------------------------------------------
 template <int D, bool NNW>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
-    k_force64(Consts k, const int* __restrict__ cell_start, const uint16_t* __restrict__ nl,
+__global__ void __launch_bounds__(kReuseTPB)
+    k_force64(Consts k, const int* __restrict__ cell_start, const int* __restrict__ cell_of,
+              const uint16_t* __restrict__ nl,
               const int* __restrict__ ncount, const double4_32a* __restrict__ x,
               const double4_32a* __restrict__ v, const double4_32a* __restrict__ pc,
               const int* __restrict__ sid, const int* __restrict__ pid,
               double4_32a* __restrict__ f, double* __restrict__ st, int fuse_mode, double dt,
               double4_32a* __restrict__ v_out, uint32_t step, double inv_sqdt,
               unsigned* __restrict__ err, NN nn, CollArgs ca) {
-  constexpr int CENTER = (D == 3) ? 13 : 4;
+  constexpr int NS = (D == 3) ? 27 : 9;
   constexpr int D2 = D * D;
   using T = double;
-  __shared__ NbTable tab[kWarpsPerBlock];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ int s_start[NS * kReuseTPB];
+  __shared__ int s_shift[NS * kReuseTPB];
   const int n = k.n;
   const bool noise = k.noise != 0;
-  for (int cell = blockIdx.x * kWarpsPerBlock + wib; cell <= k.ncell;
-       cell += gridDim.x * kWarpsPerBlock) {
-    NbTable& t = tab[wib];
-    build_table<D>(k, cell, cell_start, t);
-    const int c0 = t.start[CENTER], c1 = c0 + t.count[CENTER];
-    for (int base = c0; base < c1; base += 32) {
-      const int i = base + lane;
-      if (i >= c1) continue;
-      const int si = sid[i];
-      const int pidi = pid[i];
-      const double4_32a xi4 = x[i];
-      const double xi[3] = {xi4.x, xi4.y, xi4.z};
-      const double4_32a v4i = v[i];
-      const double4_32a ci = pc[i];
-      constexpr bool nnw = NNW;  // Oldroyd-B terms compiled only when used
-      const double* qq = (const double*)nn.qq;
-      T qi[1 + D2], L[D2];
+  const int i = blockIdx.x * kReuseTPB + threadIdx.x;
+  if (i >= n) return;
+  build_lane_table<D, kReuseTPB>(k, cell_of[i], cell_start, s_start, s_shift);
+  const int si = sid[i];
+  const int pidi = pid[i];
+  const double4_32a xi4 = x[i];
+  const double xi[3] = {xi4.x, xi4.y, xi4.z};
+  const double4_32a v4i = v[i];
+  const double4_32a ci = pc[i];
+  constexpr bool nnw = NNW;  // Oldroyd-B terms compiled only when used
+  const double* qq = (const double*)nn.qq;
+  T qi[1 + D2], L[D2];
 #pragma unroll
-      for (int cc = 0; cc < D2; ++cc) L[cc] = 0;
-      if (nnw) {
+  for (int cc = 0; cc < D2; ++cc) L[cc] = 0;
+  if (nnw) {
 #pragma unroll
-        for (int cc = 0; cc <= D2; ++cc) qi[cc] = qq[(size_t)cc * n + i];
+    for (int cc = 0; cc <= D2; ++cc) qi[cc] = qq[(size_t)cc * n + i];
+  }
+  T acc[3] = {0, 0, 0};
+  T sacc[9];
+#pragma unroll
+  for (int a = 0; a < 9; ++a) sacc[a] = 0;
+  const int cnt = ncount[i];
+  for (int e = 0; e < cnt; ++e) {
+    const int ent = nl[(size_t)e * n + i];
+    const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
+    const int j = s_start[sl * kReuseTPB + threadIdx.x] + q;
+    const int sj = sid[j];
+    // pp_interaction.inc:63-223: w-w and c-w never interact, c-c only
+    // between different colloids with pp_interact_cc
+    if (si != 0 && sj != 0 && !(si > 0 && sj > 0 && si != sj && k.pp_cc)) continue;
+    const double4_32a xj4 = x[j];
+    const double xj[3] = {xj4.x, xj4.y, xj4.z};
+    T r[3];
+    const double d2 = exact_sep<D>(k, xi, xj, s_shift[sl * kReuseTPB + threadIdx.x], r);
+    const T inv_d = rsqrt(d2);
+    const T d = d2 * inv_d;
+    const double4_32a v4 = v[j];
+    T vi[3] = {v4i.x, v4i.y, v4i.z};
+    T vj[3] = {v4.x, v4.y, v4.z};
+    const double4_32a cj = pc[j];
+    T Ai = ci.x, Aj = cj.x, Bi = ci.y, Bj = cj.y;
+    T qj[1 + D2], qie[1 + D2];
+    if (nnw) {
+#pragma unroll
+      for (int cc = 0; cc <= D2; ++cc) {
+        qj[cc] = qq[(size_t)cc * n + j];
+        qie[cc] = qi[cc];
       }
-      T acc[3] = {0, 0, 0};
-      T sacc[9];
+    }
+    if (si < 0 || sj < 0) {
+      // fluid-wall pair: wall particle takes the Morris no-slip velocity
+      // and the fluid pressure (pp_interaction_fw.inc / _wf.inc); in the
+      // Oldroyd-B model also the fluid density and pressure tensor
+      const int sw = (sj < 0) ? sj : si;
+      const int axis = (-sw - 1) >> 1;
+      const double xin = axis == 0 ? xi[0] : axis == 1 ? xi[1] : xi[2];
+      const double xjn = axis == 0 ? xj[0] : axis == 1 ? xj[1] : xj[2];
+      T vw[3];
+      if (sj < 0) {
+        wall_noslip<T, D>(k, xin, xjn, vi, sj, vw);
 #pragma unroll
-      for (int a = 0; a < 9; ++a) sacc[a] = 0;
-      const int cnt = ncount[i];
-      for (int e = 0; e < cnt; ++e) {
-        const int ent = nl[(size_t)e * n + i];
-        const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
-        const int j = t.start[sl] + q;
-        const int sj = sid[j];
-        // pp_interaction.inc:63-223: w-w and c-w never interact, c-c only
-        // between different colloids with pp_interact_cc
-        if (si != 0 && sj != 0 && !(si > 0 && sj > 0 && si != sj && k.pp_cc)) continue;
-        const double4_32a xj4 = x[j];
-        const double xj[3] = {xj4.x, xj4.y, xj4.z};
-        T r[3];
-        const double d2 = exact_sep<D>(k, xi, xj, t.shift[sl], r);
-        const T inv_d = rsqrt(d2);
-        const T d = d2 * inv_d;
-        const double4_32a v4 = v[j];
-        T vi[3] = {v4i.x, v4i.y, v4i.z};
-        T vj[3] = {v4.x, v4.y, v4.z};
-        const double4_32a cj = pc[j];
-        T Ai = ci.x, Aj = cj.x, Bi = ci.y, Bj = cj.y;
-        T qj[1 + D2], qie[1 + D2];
+        for (int a = 0; a < D; ++a) vj[a] = vw[a];
         if (nnw) {
+          Aj = Ai;
+          Bj = Bi;
 #pragma unroll
-          for (int cc = 0; cc <= D2; ++cc) {
-            qj[cc] = qq[(size_t)cc * n + j];
-            qie[cc] = qi[cc];
-          }
+          for (int cc = 0; cc <= D2; ++cc) qj[cc] = qi[cc];
+        } else {
+          Aj = boundary_A<T>(k.rhs_force_type, ci.w, cj.y);
         }
-        if (si < 0 || sj < 0) {
-          // fluid-wall pair: wall particle takes the Morris no-slip velocity
-          // and the fluid pressure (pp_interaction_fw.inc / _wf.inc); in the
-          // Oldroyd-B model also the fluid density and pressure tensor
-          const int sw = (sj < 0) ? sj : si;
-          const int axis = (-sw - 1) >> 1;
-          const double xin = axis == 0 ? xi[0] : axis == 1 ? xi[1] : xi[2];
-          const double xjn = axis == 0 ? xj[0] : axis == 1 ? xj[1] : xj[2];
+      } else {
+        wall_noslip<T, D>(k, xjn, xin, vj, si, vw);
+#pragma unroll
+        for (int a = 0; a < D; ++a) vi[a] = vw[a];
+        if (nnw) {
+          Ai = Aj;
+          Bi = Bj;
+#pragma unroll
+          for (int cc = 0; cc <= D2; ++cc) qie[cc] = qj[cc];
+        } else {
+          Ai = boundary_A<T>(k.rhs_force_type, cj.w, ci.y);
+        }
+      }
+    } else if ((si > 0) != (sj > 0)) {
+      // fluid-colloid pair (pp_interaction_fc.inc / _cf.inc): the
+      // boundary particle takes the Morris no-slip velocity and the
+      // fluid pressure (Oldroyd-B: also its density and pressure tensor)
+      if (sj > 0) {
+        if (k.coll_noslip == 2) {
+          const double4_32a rc4 = ca.rxc[j];
+          const T rxc_[3] = {rc4.x, rc4.y, rc4.z};
           T vw[3];
-          if (sj < 0) {
-            wall_noslip<T, D>(k, xin, xjn, vi, sj, vw);
+          colloid_noslip<T, D>(k, sj - 1, rxc_, r, vi, vw);
 #pragma unroll
-            for (int a = 0; a < D; ++a) vj[a] = vw[a];
-            if (nnw) {
-              Aj = Ai;
-              Bj = Bi;
-#pragma unroll
-              for (int cc = 0; cc <= D2; ++cc) qj[cc] = qi[cc];
-            } else {
-              Aj = boundary_A<T>(k.rhs_force_type, ci.w, cj.y);
-            }
-          } else {
-            wall_noslip<T, D>(k, xjn, xin, vj, si, vw);
-#pragma unroll
-            for (int a = 0; a < D; ++a) vi[a] = vw[a];
-            if (nnw) {
-              Ai = Aj;
-              Bi = Bj;
-#pragma unroll
-              for (int cc = 0; cc <= D2; ++cc) qie[cc] = qj[cc];
-            } else {
-              Ai = boundary_A<T>(k.rhs_force_type, cj.w, ci.y);
-            }
-          }
-        } else if ((si > 0) != (sj > 0)) {
-          // fluid-colloid pair (pp_interaction_fc.inc / _cf.inc): the
-          // boundary particle takes the Morris no-slip velocity and the
-          // fluid pressure (Oldroyd-B: also its density and pressure tensor)
-          if (sj > 0) {
-            if (k.coll_noslip == 2) {
-              const double4_32a rc4 = ca.rxc[j];
-              const T rxc_[3] = {rc4.x, rc4.y, rc4.z};
-              T vw[3];
-              colloid_noslip<T, D>(k, sj - 1, rxc_, r, vi, vw);
-#pragma unroll
-              for (int a = 0; a < D; ++a) vj[a] = vw[a];
-            }
-            if (nnw) {
-              Aj = Ai;
-              Bj = Bi;
-#pragma unroll
-              for (int cc = 0; cc <= D2; ++cc) qj[cc] = qi[cc];
-            } else {
-              Aj = boundary_A<T>(k.rhs_force_type, ci.w, cj.y);
-            }
-          } else {
-            if (k.coll_noslip == 2) {
-              const double4_32a rc4 = ca.rxc[i];
-              const T rxc_[3] = {rc4.x, rc4.y, rc4.z};
-              const T rfc[3] = {-r[0], -r[1], -r[2]};
-              T vw[3];
-              colloid_noslip<T, D>(k, si - 1, rxc_, rfc, vj, vw);
-#pragma unroll
-              for (int a = 0; a < D; ++a) vi[a] = vw[a];
-            }
-            if (nnw) {
-              Ai = Aj;
-              Bi = Bj;
-#pragma unroll
-              for (int cc = 0; cc <= D2; ++cc) qie[cc] = qj[cc];
-            } else {
-              Ai = boundary_A<T>(k.rhs_force_type, cj.w, ci.y);
-            }
-          }
+          for (int a = 0; a < D; ++a) vj[a] = vw[a];
         }
-        const T gw = kernel_gradw<T>(k, d);
-        T vij[3];
-#pragma unroll
-        for (int a = 0; a < D; ++a) vij[a] = vi[a] - vj[a];
-        float z[6];
-        if (noise) pair_draw<D>(k.rhs_force_type, k.key0, k.key1, step, pidi, pid[j], z);
-        T pa[3], si_s, sj_s;
-        pair_force<T, D>(k, r, inv_d, vij, Ai, Bi, Aj, Bj, gw, noise, z, inv_sqdt, pa);
         if (nnw) {
-          // polymer part of the pressure-tensor force,
-          // rhs_force_ff_non_Newtonian_HuAdams.F90:95-110, and the velocity
-          // gradient of pp_vgt_ip.inc
+          Aj = Ai;
+          Bj = Bi;
 #pragma unroll
-          for (int b = 0; b < D; ++b) {
-            T s_ = 0;
-#pragma unroll
-            for (int a = 0; a < D; ++a) s_ += (qie[1 + a + D * b] + qj[1 + a + D * b]) * r[a];
-            pa[b] += gw * inv_d * s_;
-          }
-          const T fac = gw * qie[0] * inv_d;
-#pragma unroll
-          for (int b = 0; b < D; ++b)
-#pragma unroll
-            for (int a = 0; a < D; ++a) L[a + D * b] += (vj[a] - vi[a]) * r[b] * fac;
+          for (int cc = 0; cc <= D2; ++cc) qj[cc] = qi[cc];
+        } else {
+          Aj = boundary_A<T>(k.rhs_force_type, ci.w, cj.y);
         }
-        pair_scales<T>(k.rhs_force_type, ci.z, cj.z, si_s, sj_s);
+      } else {
+        if (k.coll_noslip == 2) {
+          const double4_32a rc4 = ca.rxc[i];
+          const T rxc_[3] = {rc4.x, rc4.y, rc4.z};
+          const T rfc[3] = {-r[0], -r[1], -r[2]};
+          T vw[3];
+          colloid_noslip<T, D>(k, si - 1, rxc_, rfc, vj, vw);
 #pragma unroll
-        for (int a = 0; a < D; ++a) pa[a] *= si_s;
+          for (int a = 0; a < D; ++a) vi[a] = vw[a];
+        }
+        if (nnw) {
+          Ai = Aj;
+          Bi = Bj;
 #pragma unroll
-        for (int a = 0; a < D; ++a) acc[a] += pa[a];
-        if (k.stress) {
-          // pp_interaction_ff.inc:83-93: s_ab += r_a * f_b / 2
-#pragma unroll
-          for (int b = 0; b < D; ++b)
-#pragma unroll
-            for (int a = 0; a < D; ++a) sacc[b * D + a] += r[a] * pa[b] * T(0.5);
+          for (int cc = 0; cc <= D2; ++cc) qie[cc] = qj[cc];
+        } else {
+          Ai = boundary_A<T>(k.rhs_force_type, cj.w, ci.y);
         }
       }
-      if (k.stress) {
+    }
+    const T gw = kernel_gradw<T>(k, d);
+    T vij[3];
 #pragma unroll
-        for (int a = 0; a < D * D; ++a) st[(size_t)a * n + i] = sacc[a];
+    for (int a = 0; a < D; ++a) vij[a] = vi[a] - vj[a];
+    float z[6];
+    if (noise) pair_draw<D>(k.rhs_force_type, k.key0, k.key1, step, pidi, pid[j], z);
+    T pa[3], si_s, sj_s;
+    pair_force<T, D>(k, r, inv_d, vij, Ai, Bi, Aj, Bj, gw, noise, z, inv_sqdt, pa);
+    if (nnw) {
+      // polymer part of the pressure-tensor force,
+      // rhs_force_ff_non_Newtonian_HuAdams.F90:95-110, and the velocity
+      // gradient of pp_vgt_ip.inc
+#pragma unroll
+      for (int b = 0; b < D; ++b) {
+        T s_ = 0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) s_ += (qie[1 + a + D * b] + qj[1 + a + D * b]) * r[a];
+        pa[b] += gw * inv_d * s_;
       }
-      if (nnw) nn_epilogue<D>(k, nn, i, L, fuse_mode, dt);
-      force_epilogue<D>(k, i, si, xi, acc[0], acc[1], D == 3 ? acc[2] : 0.0, fuse_mode, dt, v,
-                        f, v_out, err);
+      const T fac = gw * qie[0] * inv_d;
+#pragma unroll
+      for (int b = 0; b < D; ++b)
+#pragma unroll
+        for (int a = 0; a < D; ++a) L[a + D * b] += (vj[a] - vi[a]) * r[b] * fac;
+    }
+    pair_scales<T>(k.rhs_force_type, ci.z, cj.z, si_s, sj_s);
+#pragma unroll
+    for (int a = 0; a < D; ++a) pa[a] *= si_s;
+#pragma unroll
+    for (int a = 0; a < D; ++a) acc[a] += pa[a];
+    if (k.stress) {
+      // pp_interaction_ff.inc:83-93: s_ab += r_a * f_b / 2
+#pragma unroll
+      for (int b = 0; b < D; ++b)
+#pragma unroll
+        for (int a = 0; a < D; ++a) sacc[b * D + a] += r[a] * pa[b] * T(0.5);
     }
   }
+  if (k.stress) {
+#pragma unroll
+    for (int a = 0; a < D * D; ++a) st[(size_t)a * n + i] = sacc[a];
+  }
+  if (nnw) nn_epilogue<D>(k, nn, i, L, fuse_mode, dt);
+  force_epilogue<D>(k, i, si, xi, acc[0], acc[1], D == 3 ? acc[2] : 0.0, fuse_mode, dt, v,
+                    f, v_out, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -815,12 +810,13 @@ struct JData {
 };
 
 template <int D>
-__device__ __forceinline__ JData load_j(const NbTable& t, int ent, const float4* __restrict__ off,
+__device__ __forceinline__ JData load_j(const int* __restrict__ s_start, int ent,
+                                        const float4* __restrict__ off,
                                         const float4* __restrict__ vf,
                                         const float4* __restrict__ pcf) {
   JData d;
   d.sl = ent >> kLocalBits;
-  d.j = t.start[d.sl] + (ent & (kMaxCellCount - 1));
+  d.j = s_start[d.sl * kReuseTPB + threadIdx.x] + (ent & (kMaxCellCount - 1));
   d.o = off[d.j];
   d.v = vf[d.j];
   d.c = pcf[d.j];
@@ -828,8 +824,9 @@ __device__ __forceinline__ JData load_j(const NbTable& t, int ent, const float4*
 }
 
 template <int D, bool NNW>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
-    k_force32(Consts k, const int* __restrict__ cell_start, const uint16_t* __restrict__ nl,
+__global__ void __launch_bounds__(kReuseTPB, 5)
+    k_force32(Consts k, const int* __restrict__ cell_start, const int* __restrict__ cell_of,
+              const uint16_t* __restrict__ nl,
               const int* __restrict__ ncount, const float4* __restrict__ off,
               const double4_32a* __restrict__ x, const double4_32a* __restrict__ v,
               const float4* __restrict__ pcf, const float4* __restrict__ vf,
@@ -837,223 +834,219 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
               double* __restrict__ st, int fuse_mode, double dt,
               double4_32a* __restrict__ v_out, uint32_t step, float inv_sqdt,
               unsigned* __restrict__ err, NN nn, CollArgs ca) {
-  constexpr int CENTER = (D == 3) ? 13 : 4;
+  constexpr int NS = (D == 3) ? 27 : 9;
   constexpr int D2 = D * D;
   using T = float;
-  __shared__ NbTable tab[kWarpsPerBlock];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // one thread per particle, whatever its cell: per-thread neighbour-cell
+  // tables keep every lane busy (2D cells hold ~9 particles)
+  __shared__ int s_start[NS * kReuseTPB];
+  __shared__ int s_shift[NS * kReuseTPB];
   const int n = k.n;
   const bool noise = k.noise != 0;
   const bool walls = k.wall_axis != -1;
-  for (int cell = blockIdx.x * kWarpsPerBlock + wib; cell <= k.ncell;
-       cell += gridDim.x * kWarpsPerBlock) {
-    NbTable& t = tab[wib];
-    build_table<D>(k, cell, cell_start, t);
-    const int c0 = t.start[CENTER], c1 = c0 + t.count[CENTER];
-    for (int base = c0; base < c1; base += 32) {
-      const int i = base + lane;
-      if (i >= c1) continue;
-      const float4 oi = off[i];
-      const int si = __float_as_int(oi.w);
-      const float4 v4i = vf[i];
-      const int pidi = __float_as_int(v4i.w);
-      const float4 ci = pcf[i];
-      const float2 wdi = (walls && k.wall_axis >= 0) ? wd[i] : make_float2(0.f, 0.f);
-      constexpr bool nnw = NNW;  // Oldroyd-B terms compiled only when used
-      const float* qq = (const float*)nn.qq;
-      T qi[1 + D2], L[D2];
+  const int i = blockIdx.x * kReuseTPB + threadIdx.x;
+  if (i >= n) return;
+  build_lane_table<D, kReuseTPB>(k, cell_of[i], cell_start, s_start, s_shift);
+  const float4 oi = off[i];
+  const int si = __float_as_int(oi.w);
+  const float4 v4i = vf[i];
+  const int pidi = __float_as_int(v4i.w);
+  const float4 ci = pcf[i];
+  const float2 wdi = (walls && k.wall_axis >= 0) ? wd[i] : make_float2(0.f, 0.f);
+  constexpr bool nnw = NNW;  // Oldroyd-B terms compiled only when used
+  const float* qq = (const float*)nn.qq;
+  T qi[1 + D2], L[D2];
 #pragma unroll
-      for (int cc = 0; cc < D2; ++cc) L[cc] = 0.f;
-      if (nnw) {
+  for (int cc = 0; cc < D2; ++cc) L[cc] = 0.f;
+  if (nnw) {
 #pragma unroll
-        for (int cc = 0; cc <= D2; ++cc) qi[cc] = qq[(size_t)cc * n + i];
+    for (int cc = 0; cc <= D2; ++cc) qi[cc] = qq[(size_t)cc * n + i];
+  }
+  T acc[3] = {0.f, 0.f, 0.f}, comp[3] = {0.f, 0.f, 0.f};
+  T sacc[9];
+#pragma unroll
+  for (int a = 0; a < 9; ++a) sacc[a] = 0.f;
+  const int cnt = ncount[i];
+  JData nxt;
+  int ent_n1 = 0;
+  if (cnt > 0) nxt = load_j<D>(s_start, nl[i], off, vf, pcf);
+  if (cnt > 1) ent_n1 = nl[(size_t)n + i];
+  for (int e = 0; e < cnt; ++e) {
+    const JData cur = nxt;
+    if (e + 1 < cnt) {
+      nxt = load_j<D>(s_start, ent_n1, off, vf, pcf);
+      if (e + 2 < cnt) ent_n1 = nl[(size_t)(e + 2) * n + i];
+    }
+    const int sj = __float_as_int(cur.o.w);
+    if (si != 0 && sj != 0 && !(si > 0 && sj > 0 && si != sj && k.pp_cc)) continue;
+    const int sl = cur.sl;
+    T r[3];
+    const float sx = (float)(sl % 3 - 1) * k.csf[0];
+    const float sy = (float)((sl / 3) % 3 - 1) * k.csf[1];
+    r[0] = (oi.x - cur.o.x) - sx;
+    r[1] = (oi.y - cur.o.y) - sy;
+    r[2] = (D == 3) ? (oi.z - cur.o.z) - (float)(sl / 9 - 1) * k.csf[2] : 0.f;
+    T d2 = r[0] * r[0] + r[1] * r[1];
+    if (D == 3) d2 += r[2] * r[2];
+    const T inv_d = rsqrtf(d2);
+    const T d = d2 * inv_d;
+    T vi[3] = {v4i.x, v4i.y, v4i.z};
+    T vj[3] = {cur.v.x, cur.v.y, cur.v.z};
+    T Ai = ci.x, Aj = cur.c.x, Bi = ci.y, Bj = cur.c.y;
+    T qj[1 + D2], qie[1 + D2];
+    if (nnw) {
+#pragma unroll
+      for (int cc = 0; cc <= D2; ++cc) {
+        qj[cc] = qq[(size_t)cc * n + cur.j];
+        qie[cc] = qi[cc];
       }
-      T acc[3] = {0.f, 0.f, 0.f}, comp[3] = {0.f, 0.f, 0.f};
-      T sacc[9];
+    }
+    if (si < 0 || sj < 0) {
+      // fluid-wall pair: the wall particle takes the Morris no-slip
+      // velocity and the fluid pressure (pp_interaction_fw.inc / _wf.inc),
+      // in the Oldroyd-B model also the fluid density and pressure
+      // tensor; face distances come from the FP64-rounded per-particle
+      // values (one wall axis) or from the FP64 positions (several)
+      const int sw = (sj < 0) ? sj : si;
+      const int face = -sw;
+      const bool lower = (face & 1) != 0;
+      float df, dw;
+      if (k.wall_axis >= 0) {
+        const float2 wj = wd[cur.j];
+        const float di = lower ? wdi.x : wdi.y, dj = lower ? wj.x : wj.y;
+        df = (sj < 0) ? di : dj;
+        dw = (sj < 0) ? dj : di;
+      } else {
+        const int axis = (face - 1) >> 1;
+        const double x_sur = axis == 0 ? (lower ? k.min_phys[0] : k.max_phys[0])
+                             : axis == 1 ? (lower ? k.min_phys[1] : k.max_phys[1])
+                                         : (lower ? k.min_phys[2] : k.max_phys[2]);
+        const double4_32a a4 = x[i], b4 = x[cur.j];
+        const double xa = axis == 0 ? a4.x : axis == 1 ? a4.y : a4.z;
+        const double xb = axis == 0 ? b4.x : axis == 1 ? b4.y : b4.z;
+        df = (float)(((sj < 0) ? xa : xb) - x_sur);
+        dw = (float)(((sj < 0) ? xb : xa) - x_sur);
+      }
+      T vw[3];
+      if (sj < 0) {
+        wall_noslip_dist<T, D>(k, df, dw, vi, sj, vw);
 #pragma unroll
-      for (int a = 0; a < 9; ++a) sacc[a] = 0.f;
-      const int cnt = ncount[i];
-      JData nxt;
-      int ent_n1 = 0;
-      if (cnt > 0) nxt = load_j<D>(t, nl[i], off, vf, pcf);
-      if (cnt > 1) ent_n1 = nl[(size_t)n + i];
-      for (int e = 0; e < cnt; ++e) {
-        const JData cur = nxt;
-        if (e + 1 < cnt) {
-          nxt = load_j<D>(t, ent_n1, off, vf, pcf);
-          if (e + 2 < cnt) ent_n1 = nl[(size_t)(e + 2) * n + i];
-        }
-        const int sj = __float_as_int(cur.o.w);
-        if (si != 0 && sj != 0 && !(si > 0 && sj > 0 && si != sj && k.pp_cc)) continue;
-        const int sl = cur.sl;
-        T r[3];
-        const float4 so = t.o[sl];
-        r[0] = (oi.x - cur.o.x) - so.x;
-        r[1] = (oi.y - cur.o.y) - so.y;
-        r[2] = (D == 3) ? (oi.z - cur.o.z) - so.z : 0.f;
-        T d2 = r[0] * r[0] + r[1] * r[1];
-        if (D == 3) d2 += r[2] * r[2];
-        const T inv_d = rsqrtf(d2);
-        const T d = d2 * inv_d;
-        T vi[3] = {v4i.x, v4i.y, v4i.z};
-        T vj[3] = {cur.v.x, cur.v.y, cur.v.z};
-        T Ai = ci.x, Aj = cur.c.x, Bi = ci.y, Bj = cur.c.y;
-        T qj[1 + D2], qie[1 + D2];
+        for (int a = 0; a < D; ++a) vj[a] = vw[a];
         if (nnw) {
+          Aj = Ai;
+          Bj = Bi;
 #pragma unroll
-          for (int cc = 0; cc <= D2; ++cc) {
-            qj[cc] = qq[(size_t)cc * n + cur.j];
-            qie[cc] = qi[cc];
-          }
+          for (int cc = 0; cc <= D2; ++cc) qj[cc] = qi[cc];
+        } else {
+          Aj = boundary_A<T>(k.rhs_force_type, ci.w, cur.c.y);
         }
-        if (si < 0 || sj < 0) {
-          // fluid-wall pair: the wall particle takes the Morris no-slip
-          // velocity and the fluid pressure (pp_interaction_fw.inc / _wf.inc),
-          // in the Oldroyd-B model also the fluid density and pressure
-          // tensor; face distances come from the FP64-rounded per-particle
-          // values (one wall axis) or from the FP64 positions (several)
-          const int sw = (sj < 0) ? sj : si;
-          const int face = -sw;
-          const bool lower = (face & 1) != 0;
-          float df, dw;
-          if (k.wall_axis >= 0) {
-            const float2 wj = wd[cur.j];
-            const float di = lower ? wdi.x : wdi.y, dj = lower ? wj.x : wj.y;
-            df = (sj < 0) ? di : dj;
-            dw = (sj < 0) ? dj : di;
-          } else {
-            const int axis = (face - 1) >> 1;
-            const double x_sur = axis == 0 ? (lower ? k.min_phys[0] : k.max_phys[0])
-                                 : axis == 1 ? (lower ? k.min_phys[1] : k.max_phys[1])
-                                             : (lower ? k.min_phys[2] : k.max_phys[2]);
-            const double4_32a a4 = x[i], b4 = x[cur.j];
-            const double xa = axis == 0 ? a4.x : axis == 1 ? a4.y : a4.z;
-            const double xb = axis == 0 ? b4.x : axis == 1 ? b4.y : b4.z;
-            df = (float)(((sj < 0) ? xa : xb) - x_sur);
-            dw = (float)(((sj < 0) ? xb : xa) - x_sur);
-          }
+      } else {
+        wall_noslip_dist<T, D>(k, df, dw, vj, si, vw);
+#pragma unroll
+        for (int a = 0; a < D; ++a) vi[a] = vw[a];
+        if (nnw) {
+          Ai = Aj;
+          Bi = Bj;
+#pragma unroll
+          for (int cc = 0; cc <= D2; ++cc) qie[cc] = qj[cc];
+        } else {
+          Ai = boundary_A<T>(k.rhs_force_type, cur.c.w, ci.y);
+        }
+      }
+    } else if ((si > 0) != (sj > 0)) {
+      // fluid-colloid pair (pp_interaction_fc.inc / _cf.inc)
+      if (sj > 0) {
+        if (k.coll_noslip == 2) {
+          const float4 rc4 = ca.rxcf[cur.j];
+          const T rxc_[3] = {rc4.x, rc4.y, rc4.z};
           T vw[3];
-          if (sj < 0) {
-            wall_noslip_dist<T, D>(k, df, dw, vi, sj, vw);
+          colloid_noslip<T, D>(k, sj - 1, rxc_, r, vi, vw);
 #pragma unroll
-            for (int a = 0; a < D; ++a) vj[a] = vw[a];
-            if (nnw) {
-              Aj = Ai;
-              Bj = Bi;
-#pragma unroll
-              for (int cc = 0; cc <= D2; ++cc) qj[cc] = qi[cc];
-            } else {
-              Aj = boundary_A<T>(k.rhs_force_type, ci.w, cur.c.y);
-            }
-          } else {
-            wall_noslip_dist<T, D>(k, df, dw, vj, si, vw);
-#pragma unroll
-            for (int a = 0; a < D; ++a) vi[a] = vw[a];
-            if (nnw) {
-              Ai = Aj;
-              Bi = Bj;
-#pragma unroll
-              for (int cc = 0; cc <= D2; ++cc) qie[cc] = qj[cc];
-            } else {
-              Ai = boundary_A<T>(k.rhs_force_type, cur.c.w, ci.y);
-            }
-          }
-        } else if ((si > 0) != (sj > 0)) {
-          // fluid-colloid pair (pp_interaction_fc.inc / _cf.inc)
-          if (sj > 0) {
-            if (k.coll_noslip == 2) {
-              const float4 rc4 = ca.rxcf[cur.j];
-              const T rxc_[3] = {rc4.x, rc4.y, rc4.z};
-              T vw[3];
-              colloid_noslip<T, D>(k, sj - 1, rxc_, r, vi, vw);
-#pragma unroll
-              for (int a = 0; a < D; ++a) vj[a] = vw[a];
-            }
-            if (nnw) {
-              Aj = Ai;
-              Bj = Bi;
-#pragma unroll
-              for (int cc = 0; cc <= D2; ++cc) qj[cc] = qi[cc];
-            } else {
-              Aj = boundary_A<T>(k.rhs_force_type, ci.w, cur.c.y);
-            }
-          } else {
-            if (k.coll_noslip == 2) {
-              const float4 rc4 = ca.rxcf[i];
-              const T rxc_[3] = {rc4.x, rc4.y, rc4.z};
-              const T rfc[3] = {-r[0], -r[1], -r[2]};
-              T vw[3];
-              colloid_noslip<T, D>(k, si - 1, rxc_, rfc, vj, vw);
-#pragma unroll
-              for (int a = 0; a < D; ++a) vi[a] = vw[a];
-            }
-            if (nnw) {
-              Ai = Aj;
-              Bi = Bj;
-#pragma unroll
-              for (int cc = 0; cc <= D2; ++cc) qie[cc] = qj[cc];
-            } else {
-              Ai = boundary_A<T>(k.rhs_force_type, cur.c.w, ci.y);
-            }
-          }
+          for (int a = 0; a < D; ++a) vj[a] = vw[a];
         }
-        const T gw = kernel_gradw<T>(k, d);
-        T vij[3];
-#pragma unroll
-        for (int a = 0; a < D; ++a) vij[a] = vi[a] - vj[a];
-        float z[6];
-        if (noise)
-          pair_draw<D>(k.rhs_force_type, k.key0, k.key1, step, pidi, __float_as_int(cur.v.w), z);
-        T pa[3], si_s, sj_s;
-        pair_force<T, D>(k, r, inv_d, vij, Ai, Bi, Aj, Bj, gw, noise, z, inv_sqdt, pa);
         if (nnw) {
-          // polymer pressure-tensor force and velocity gradient (FP32 pairs)
+          Aj = Ai;
+          Bj = Bi;
 #pragma unroll
-          for (int b = 0; b < D; ++b) {
-            T s_ = 0.f;
-#pragma unroll
-            for (int a = 0; a < D; ++a) s_ += (qie[1 + a + D * b] + qj[1 + a + D * b]) * r[a];
-            pa[b] += gw * inv_d * s_;
-          }
-          const T fac = gw * qie[0] * inv_d;
-#pragma unroll
-          for (int b = 0; b < D; ++b)
-#pragma unroll
-            for (int a = 0; a < D; ++a) L[a + D * b] += (vj[a] - vi[a]) * r[b] * fac;
+          for (int cc = 0; cc <= D2; ++cc) qj[cc] = qi[cc];
+        } else {
+          Aj = boundary_A<T>(k.rhs_force_type, ci.w, cur.c.y);
         }
-        pair_scales<T>(k.rhs_force_type, ci.z, cur.c.z, si_s, sj_s);
+      } else {
+        if (k.coll_noslip == 2) {
+          const float4 rc4 = ca.rxcf[i];
+          const T rxc_[3] = {rc4.x, rc4.y, rc4.z};
+          const T rfc[3] = {-r[0], -r[1], -r[2]};
+          T vw[3];
+          colloid_noslip<T, D>(k, si - 1, rxc_, rfc, vj, vw);
 #pragma unroll
-        for (int a = 0; a < D; ++a) pa[a] *= si_s;
-#pragma unroll
-        for (int a = 0; a < D; ++a) {
-          const T y = pa[a] - comp[a];
-          const T tt = acc[a] + y;
-          comp[a] = (tt - acc[a]) - y;
-          acc[a] = tt;
+          for (int a = 0; a < D; ++a) vi[a] = vw[a];
         }
-        if (k.stress) {
+        if (nnw) {
+          Ai = Aj;
+          Bi = Bj;
 #pragma unroll
-          for (int b = 0; b < D; ++b)
-#pragma unroll
-            for (int a = 0; a < D; ++a) sacc[b * D + a] += r[a] * pa[b] * 0.5f;
+          for (int cc = 0; cc <= D2; ++cc) qie[cc] = qj[cc];
+        } else {
+          Ai = boundary_A<T>(k.rhs_force_type, cur.c.w, ci.y);
         }
       }
-      if (k.stress) {
+    }
+    const T gw = kernel_gradw<T>(k, d);
+    T vij[3];
 #pragma unroll
-        for (int a = 0; a < D * D; ++a) st[(size_t)a * n + i] = (double)sacc[a];
-      }
-      const double4_32a xi4 = x[i];
-      const double xi[3] = {xi4.x, xi4.y, xi4.z};
-      if (nnw) {
-        double Ld[D2];
+    for (int a = 0; a < D; ++a) vij[a] = vi[a] - vj[a];
+    float z[6];
+    if (noise)
+      pair_draw<D>(k.rhs_force_type, k.key0, k.key1, step, pidi, __float_as_int(cur.v.w), z);
+    T pa[3], si_s, sj_s;
+    pair_force<T, D>(k, r, inv_d, vij, Ai, Bi, Aj, Bj, gw, noise, z, inv_sqdt, pa);
+    if (nnw) {
+      // polymer pressure-tensor force and velocity gradient (FP32 pairs)
 #pragma unroll
-        for (int cc = 0; cc < D2; ++cc) Ld[cc] = (double)L[cc];
-        nn_epilogue<D>(k, nn, i, Ld, fuse_mode, dt);
+      for (int b = 0; b < D; ++b) {
+        T s_ = 0.f;
+#pragma unroll
+        for (int a = 0; a < D; ++a) s_ += (qie[1 + a + D * b] + qj[1 + a + D * b]) * r[a];
+        pa[b] += gw * inv_d * s_;
       }
-      force_epilogue<D>(k, i, si, xi, (double)acc[0], (double)acc[1],
-                        D == 3 ? (double)acc[2] : 0.0, fuse_mode, dt, v, f, v_out, err);
+      const T fac = gw * qie[0] * inv_d;
+#pragma unroll
+      for (int b = 0; b < D; ++b)
+#pragma unroll
+        for (int a = 0; a < D; ++a) L[a + D * b] += (vj[a] - vi[a]) * r[b] * fac;
+    }
+    pair_scales<T>(k.rhs_force_type, ci.z, cur.c.z, si_s, sj_s);
+#pragma unroll
+    for (int a = 0; a < D; ++a) pa[a] *= si_s;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const T y = pa[a] - comp[a];
+      const T tt = acc[a] + y;
+      comp[a] = (tt - acc[a]) - y;
+      acc[a] = tt;
+    }
+    if (k.stress) {
+#pragma unroll
+      for (int b = 0; b < D; ++b)
+#pragma unroll
+        for (int a = 0; a < D; ++a) sacc[b * D + a] += r[a] * pa[b] * 0.5f;
     }
   }
+  if (k.stress) {
+#pragma unroll
+    for (int a = 0; a < D * D; ++a) st[(size_t)a * n + i] = (double)sacc[a];
+  }
+  const double4_32a xi4 = x[i];
+  const double xi[3] = {xi4.x, xi4.y, xi4.z};
+  if (nnw) {
+    double Ld[D2];
+#pragma unroll
+    for (int cc = 0; cc < D2; ++cc) Ld[cc] = (double)L[cc];
+    nn_epilogue<D>(k, nn, i, Ld, fuse_mode, dt);
+  }
+  force_epilogue<D>(k, i, si, xi, (double)acc[0], (double)acc[1],
+                    D == 3 ? (double)acc[2] : 0.0, fuse_mode, dt, v, f, v_out, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -1558,6 +1551,7 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
   const int bs = kWarpsPerBlock * 32;
   const NN nn{h->ct, h->act, h->vgt, h->qq};
   const CollArgs ca{h->v, h->rxc, h->rxcf};
+  const int gp = std::max(1, ((int)h->n + kReuseTPB - 1) / kReuseTPB);
   if (!k.stress && h->jp && fp64 && k.newtonian && k.ncoll == 0) {
     // symmetric sweep + per-particle gather: halves the FP64 pair work; the
     // FP32 path keeps the two-sided sweep, which is faster there (the
@@ -1614,7 +1608,8 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
     h->launches++;
   } else if (fp64) {
 #define LAUNCH_F64(DD, NW)                                                                      \
-  k_force64<DD, NW><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->x, h->v, h->pc,      \
+  k_force64<DD, NW><<<gp, kReuseTPB, 0, s>>>(k, h->cell_start, h->cell_of, h->nl, h->ncount,     \
+                                            h->x, h->v, h->pc,                                 \
                                      h->sid, h->pid, h->f, h->st, fuse_mode, dt, h->v2,          \
                                      (uint32_t)step, inv_sqdt, h->d_err, nn, ca)
     if (k.d == 3) {
@@ -1625,7 +1620,8 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
 #undef LAUNCH_F64
   } else {
 #define LAUNCH_F32(DD, NW)                                                                      \
-  k_force32<DD, NW><<<g, bs, 0, s>>>(k, h->cell_start, h->nl, h->ncount, h->off, h->x, h->v,    \
+  k_force32<DD, NW><<<gp, kReuseTPB, 0, s>>>(k, h->cell_start, h->cell_of, h->nl, h->ncount,     \
+                                            h->off, h->x, h->v,                                \
                                      h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2,    \
                                      (uint32_t)step, (float)inv_sqdt, h->d_err, nn, ca)
     if (k.d == 3) {
