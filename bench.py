@@ -325,9 +325,12 @@ def adjoint_cost(torch, w, T, K, local, wts):
     ta, J, g = min((adj() for _ in range(3)), key=lambda r: r[0])
     return {"workload": w.name, "n": w.n, "steps": T, "checkpoint_every": K,
             "forward_ms": 1e3 * tf, "adjoint_ms": 1e3 * ta, "adjoint_over_forward": ta / tf,
+            "reverse_over_forward": (ta - tf) / tf,
             "J": J, "dJ_deta_tau_c": [float(x) for x in g],
-            "timing": "wall clock, best of 3 after a warm-up call; adjoint includes its own "
-                      "forward pass, checkpoints and segment recomputation"}
+            "timing": "wall clock, best of 3 after a warm-up call; adjoint_over_forward is the "
+                      "whole gradient (its own forward pass with checkpoints, the segment "
+                      "recomputation and the reverse sweep) over the forward trajectory; "
+                      "reverse_over_forward leaves out the forward pass that evaluates J"}
 
 
 def fp32_accuracy(w, steps, local):

@@ -70,7 +70,7 @@ struct AdjBuffers {
   double4_32a *xb_h = nullptr, *vb_h = nullptr;  // carried adjoints (host order)
   double* cb_h = nullptr;
   double4_32a *lam = nullptr, *xbs = nullptr, *vbs = nullptr;  // per step, cell order
-  double *Lb = nullptr, *cbs = nullptr, *nbar = nullptr;
+  double *Lb = nullptr, *qb = nullptr, *cbs = nullptr, *nbar = nullptr;
   double* gp = nullptr;     // [3][n] parameter partials (host order)
   double* jpart = nullptr;  // [T][nb] block partials of w : S_t
   double* red = nullptr;    // [3][nb]
@@ -180,6 +180,7 @@ int ensure_buffers(Handle* h, int K, int T) {
   if (nnw) {
     ATRY(aalloc(h, b, &b->cb_h, d2 * N));
     ATRY(aalloc(h, b, &b->Lb, d2 * N));
+    ATRY(aalloc(h, b, &b->qb, d2 * N));
     ATRY(aalloc(h, b, &b->cbs, d2 * N));
   }
   ATRY(aalloc(h, b, &b->gp, 3 * N));
@@ -329,7 +330,8 @@ __global__ void k_adj_pre(Consts k, Tape tp, double phi, const double4_32a* __re
                           const double4_32a* __restrict__ vb_h, const double* __restrict__ cb_h,
                           double4_32a* __restrict__ lam, double4_32a* __restrict__ xbs,
                           double4_32a* __restrict__ vbs, double* __restrict__ cbs,
-                          double* __restrict__ Lb, double* __restrict__ gp) {
+                          double* __restrict__ Lb, double* __restrict__ qb,
+                          double* __restrict__ gp) {
   constexpr int D2 = D * D;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = k.n;
@@ -346,6 +348,7 @@ __global__ void k_adj_pre(Consts k, Tape tp, double phi, const double4_32a* __re
   xbs[i] = xb;
   vbs[i] = vb;
   if (NNW) {
+    const double qn = 1.0 / tp.rho[i], Bn = tp.pc[i].y;
     double cb[D2], A[D2], c[D2], L[D2];
 #pragma unroll
     for (int q = 0; q < D2; ++q) {
@@ -368,7 +371,10 @@ __global__ void k_adj_pre(Consts k, Tape tp, double phi, const double4_32a* __re
           s2 += A[j + D * a] * c[j + D * b] + A[a + D * j] * c[b + D * j];
         }
         cbs[(size_t)(a + D * b) * n + i] = cb[a + D * b] + s1 - A[a + D * b] * k.inv_tau;
-        Lb[(size_t)(a + D * b) * n + i] = s2;
+        // for the pair sweep: Lbar / n and Q = G c B, so that a pair needs
+        // only sums of its two particles' values
+        Lb[(size_t)(a + D * b) * n + i] = s2 * qn;
+        qb[(size_t)(a + D * b) * n + i] = k.G * c[a + D * b] * Bn;
         taub += A[a + D * b] * (c[a + D * b] - (a == b ? 1.0 : 0.0));
       }
     gp[(size_t)n + hi] += taub * k.inv_tau * k.inv_tau;
@@ -380,10 +386,11 @@ __global__ void k_adj_pre(Consts k, Tape tp, double phi, const double4_32a* __re
 template <int D, bool NNW>
 __global__ void __launch_bounds__(kAdjTPB)
     k_adj_force(Consts k, Tape tp, const double4_32a* __restrict__ lam,
-                const double* __restrict__ Lb, const double* __restrict__ w, double wscale,
+                const double* __restrict__ Lb, const double* __restrict__ qb,
+                const double* __restrict__ w, double wscale,
                 uint32_t step, double inv_sqdt, double4_32a* __restrict__ xbs,
                 double4_32a* __restrict__ vbs, double* __restrict__ cbs,
-                double* __restrict__ nbar, double* __restrict__ gp) {
+                double* __restrict__ nbar, double* __restrict__ gp, int split) {
   constexpr int NS = (D == 3) ? 27 : 9;
   constexpr int D2 = D * D;
   __shared__ int s_start[NS * kAdjTPB];
@@ -396,22 +403,28 @@ __global__ void __launch_bounds__(kAdjTPB)
 #pragma unroll
   for (int q = 0; q < D2; ++q) wt[q] = w[q] * wscale;
   const int tid = threadIdx.x;
-  const int i = blockIdx.x * kAdjTPB + tid;
-  if (i >= n) return;
-  build_lane_table<D, kAdjTPB>(k, tp.cell_of[i], tp.cell_start, s_start, s_shift);
-  const double4_32a xi4 = tp.x[i];
+  // `split` adjacent lanes share one particle and take every split-th
+  // neighbour entry (small systems: more threads in flight); their partial
+  // sums are combined by a fixed butterfly, so the result is deterministic
+  const int g_ = blockIdx.x * kAdjTPB + tid;
+  const int i = g_ / split, part = g_ - i * split;
+  const bool live = i < n;
+  const int il = live ? i : n - 1;
+  build_lane_table<D, kAdjTPB>(k, tp.cell_of[il], tp.cell_start, s_start, s_shift);
+  const double4_32a xi4 = tp.x[il];
   const double xi[3] = {xi4.x, xi4.y, xi4.z};
-  const double4_32a vi4 = tp.v[i];
-  const double4_32a pci = tp.pc[i];
-  const double ni = tp.rho[i];
-  const double4_32a li4 = lam[i];
-  const int pidi = tp.pid[i];
-  double ci[D2], Lbi[D2];
+  const double4_32a vi4 = tp.v[il];
+  const double4_32a pci = tp.pc[il];
+  const double ni = tp.rho[il];
+  const double4_32a li4 = lam[il];
+  const int pidi = tp.pid[il];
+  double ci[D2], Lbi[D2], Qi[D2];
   if (NNW) {
 #pragma unroll
     for (int q = 0; q < D2; ++q) {
-      ci[q] = tp.ct[(size_t)q * n + i];
-      Lbi[q] = Lb[(size_t)q * n + i];
+      ci[q] = tp.ct[(size_t)q * n + il];
+      Lbi[q] = Lb[(size_t)q * n + il];  // Lbar_i / n_i
+      Qi[q] = qb[(size_t)q * n + il];   // G c_i / n_i^2
     }
   }
   const double qi = 1.0 / ni;
@@ -419,9 +432,9 @@ __global__ void __launch_bounds__(kAdjTPB)
 #pragma unroll
   for (int q = 0; q < D2; ++q) Pbar[q] = 0.0;
   double Bbar = 0.0, Abar = 0.0, nbL = 0.0, etab = 0.0;
-  const int cnt = tp.ncount[i];
-  for (int e = 0; e < cnt; ++e) {
-    const int ent = tp.nl[(size_t)e * n + i];
+  const int cnt = live ? tp.ncount[il] : 0;
+  for (int e = part; e < cnt; e += split) {
+    const int ent = tp.nl[(size_t)e * n + il];
     const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
     const int j = s_start[sl * kAdjTPB + tid] + q;
     const double4_32a xj4 = tp.x[j];
@@ -433,8 +446,8 @@ __global__ void __launch_bounds__(kAdjTPB)
     double ev[3];
 #pragma unroll
     for (int a = 0; a < D; ++a) ev[a] = r[a] * u;
-    const double gw = kernel_gradw<double>(k, dist);
-    const double g2 = kernel_grad2w<double>(k, dist);
+    double gw, g2;
+    kernel_gradw2<double>(k, dist, gw, g2);
     const double4_32a vj4 = tp.v[j];
     const double4_32a pcj = tp.pc[j];
     const double4_32a lj4 = lam[j];
@@ -446,14 +459,19 @@ __global__ void __launch_bounds__(kAdjTPB)
     const double f_d = eta * SB * gw * u;
     // random term We = s (ca (e.g) e + cb (g - (e.g) e)), replayed from
     // the pair's keys exactly as pair_force draws it
-    double gz[3] = {0, 0, 0}, sg = 0.0, f_r = 0.0;
-    if (noise) {
+    // f_r = sqrt(-4 kT f_d)/sqrt(dt) and df_r/df_d = f_r/(2 f_d) =
+    // -2 kT/sqrt(dt) / sqrt(-4 kT f_d), from one reciprocal square root
+    double gz[3] = {0, 0, 0}, sg = 0.0, f_r = 0.0, dfr = 0.0;
+    if (noise && f_d < 0.0) {
       float z[6];
       pair_draw<D>(3, k.key0, k.key1, step, pidi, tp.pid[j], z);
 #pragma unroll
       for (int a = 0; a < D; ++a) gz[a] = (double)z[a];
       sg = (double)z[5];
-      f_r = sqrt(-4.0 * kt * f_d) * inv_sqdt;
+      const double arg = -4.0 * kt * f_d;
+      const double rs = rsqrt(arg);
+      f_r = arg * rs * inv_sqdt;
+      dfr = -2.0 * kt * rs * inv_sqdt;
     }
     const double cbn = 0.70710678118654752440;
     const double cdn = ((D == 3) ? 0.81649658092772603273 : cbn) - cbn;  // ca - cb
@@ -462,11 +480,10 @@ __global__ void __launch_bounds__(kAdjTPB)
     for (int a = 0; a < D; ++a) eg += ev[a] * gz[a];
     double P[D2], Phi[D2];
     if (NNW) {
-      const double qj = 1.0 / tp.rho[j];
 #pragma unroll
       for (int c = 0; c < D2; ++c) {
-        P[c] = G * (ci[c] * pci.y + tp.ct[(size_t)c * n + j] * pcj.y);
-        Phi[c] = Lbi[c] * qi + Lb[(size_t)c * n + j] * qj;
+        P[c] = Qi[c] + qb[(size_t)c * n + j];
+        Phi[c] = Lbi[c] + Lb[(size_t)c * n + j];
       }
     }
     const double hm = 0.5 * (pci.z + pcj.z);
@@ -494,7 +511,7 @@ __global__ void __launch_bounds__(kAdjTPB)
       gbWe += gb[a] * We[a];
       gbPr += gb[a] * Pr[a];
     }
-    const double fdb = gbv + ((noise && f_d < 0.0) ? gbWe * f_r / (2.0 * f_d) : 0.0);
+    const double fdb = gbv + gbWe * dfr;
     const double fcb = -gbe;
     double Wb = fdb * eta * SB * u + fcb * SA + u * gbPr;
     double ub = fdb * eta * SB * gw + gw * gbPr;
@@ -534,7 +551,7 @@ __global__ void __launch_bounds__(kAdjTPB)
         rb[b] += gw * u * s;
         vb[b] -= gw * u * sv;  // d/dv_i of (v_j - v_i)
       }
-      nbL -= gw * u * phi_i * qi * qi;
+      nbL -= gw * u * phi_i * qi;  // Lbi holds Lbar_i / n_i already
 #pragma unroll
       for (int b = 0; b < D; ++b)
 #pragma unroll
@@ -553,6 +570,22 @@ __global__ void __launch_bounds__(kAdjTPB)
     Abar += fcb * gw;
     etab += 0.5 * fdb * SB * gw * u;
   }
+  for (int o = 1; o < split; o <<= 1) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      xb[a] += __shfl_xor_sync(0xffffffffu, xb[a], o);
+      vb[a] += __shfl_xor_sync(0xffffffffu, vb[a], o);
+    }
+    if (NNW) {
+#pragma unroll
+      for (int q = 0; q < D2; ++q) Pbar[q] += __shfl_xor_sync(0xffffffffu, Pbar[q], o);
+    }
+    Bbar += __shfl_xor_sync(0xffffffffu, Bbar, o);
+    Abar += __shfl_xor_sync(0xffffffffu, Abar, o);
+    nbL += __shfl_xor_sync(0xffffffffu, nbL, o);
+    etab += __shfl_xor_sync(0xffffffffu, etab, o);
+  }
+  if (!live || part != 0) return;
   // per-particle chain: A = (p + G) B, B = 1/n^2, Q = G c B, p = EOS(n m)
   const double Bi = pci.y, p = pci.w, mi = 1.0 / pci.z;
   const double pbar = Abar * Bi;
@@ -597,21 +630,23 @@ __global__ void __launch_bounds__(kAdjTPB)
                   const double4_32a* __restrict__ xbs, const double4_32a* __restrict__ vbs,
                   const double* __restrict__ cbs, int drift, double dt,
                   double4_32a* __restrict__ xb_h, double4_32a* __restrict__ vb_h,
-                  double* __restrict__ cb_h) {
+                  double* __restrict__ cb_h, int split) {
   constexpr int NS = (D == 3) ? 27 : 9;
   __shared__ int s_start[NS * kAdjTPB];
   __shared__ int s_shift[NS * kAdjTPB];
   const int n = k.n;
   const int tid = threadIdx.x;
-  const int i = blockIdx.x * kAdjTPB + tid;
-  if (i >= n) return;
+  const int g_ = blockIdx.x * kAdjTPB + tid;
+  const int i0 = g_ / split, part = g_ - i0 * split;
+  const bool live = i0 < n;
+  const int i = live ? i0 : n - 1;
   build_lane_table<D, kAdjTPB>(k, tp.cell_of[i], tp.cell_start, s_start, s_shift);
   const double4_32a xi4 = tp.x[i];
   const double xi[3] = {xi4.x, xi4.y, xi4.z};
   const double nbi = nbar[i];
   double acc[3] = {0, 0, 0};
-  const int cnt = tp.ncount[i];
-  for (int e = 0; e < cnt; ++e) {
+  const int cnt = live ? tp.ncount[i] : 0;
+  for (int e = part; e < cnt; e += split) {
     const int ent = tp.nl[(size_t)e * n + i];
     const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
     const int j = s_start[sl * kAdjTPB + tid] + q;
@@ -624,6 +659,11 @@ __global__ void __launch_bounds__(kAdjTPB)
 #pragma unroll
     for (int a = 0; a < D; ++a) acc[a] += f * r[a];
   }
+  for (int o = 1; o < split; o <<= 1) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], o);
+  }
+  if (!live || part != 0) return;
   const int hi = tp.hidx[i];
   double4_32a xo = xbs[i], vo = vbs[i];
   xo.x += acc[0];
@@ -682,7 +722,12 @@ int record_tape(Handle* h, const Tape& t) {
 // right-hand side for the tape (bit-identical to mcfg_step_vv)
 int forward_step(Handle* h, int64_t step, double dt, const Tape* tape, double* jrow) {
   ATRY(kdw(h, dt));
-  ATRY(rhs(h, step, kForceBody, dt));
+  // the recomputation needs no stress (J is summed in the first pass)
+  const int stress = h->k.stress;
+  if (jrow == nullptr) h->k.stress = 0;
+  const int rc = rhs(h, step, kForceBody, dt);
+  h->k.stress = stress;
+  ATRY(rc);
   if (tape) ATRY(record_tape(h, *tape));
   if (jrow) {
     AdjBuffers* b = h->adj;
@@ -702,15 +747,19 @@ int adjoint_step(Handle* h, const Tape& tp, int64_t step, double dt, double phi,
   cudaStream_t s = h->stream;
   const double inv_sqdt = k.noise ? 1.0 / sqrt(dt) : 0.0;
   const int gp_ = std::max(1, (n + kAdjTPB - 1) / kAdjTPB);
+  // lanes per particle in the pair sweeps: small systems fill the GPU with
+  // more threads (the neighbour entries are dealt round-robin)
+  const int split = n < 150000 ? 4 : (n < 600000 ? 2 : 1);
+  const int gs_ = std::max(1, (int)(((int64_t)n * split + kAdjTPB - 1) / kAdjTPB));
 #define ADJ_LAUNCH(DD, NW)                                                                     \
   do {                                                                                         \
     k_adj_pre<DD, NW><<<grid1(n), 256, 0, s>>>(k, tp, phi, b->xb_h, b->vb_h, b->cb_h, b->lam,  \
-                                               b->xbs, b->vbs, b->cbs, b->Lb, b->gp);          \
-    k_adj_force<DD, NW><<<gp_, kAdjTPB, 0, s>>>(k, tp, b->lam, b->Lb, b->w, wscale,               \
+                                               b->xbs, b->vbs, b->cbs, b->Lb, b->qb, b->gp);   \
+    k_adj_force<DD, NW><<<gs_, kAdjTPB, 0, s>>>(k, tp, b->lam, b->Lb, b->qb, b->w, wscale,        \
                                              (uint32_t)step, inv_sqdt, b->xbs, b->vbs, b->cbs, \
-                                             b->nbar, b->gp);                                  \
-    k_adj_density<DD, NW><<<gp_, kAdjTPB, 0, s>>>(k, tp, b->nbar, b->xbs, b->vbs, b->cbs, drift,  \
-                                               dt, b->xb_h, b->vb_h, b->cb_h);                 \
+                                             b->nbar, b->gp, split);                           \
+    k_adj_density<DD, NW><<<gs_, kAdjTPB, 0, s>>>(k, tp, b->nbar, b->xbs, b->vbs, b->cbs, drift,  \
+                                               dt, b->xb_h, b->vb_h, b->cb_h, split);          \
   } while (0)
   if (k.d == 3) {
     if (k.newtonian) ADJ_LAUNCH(3, false); else ADJ_LAUNCH(3, true);

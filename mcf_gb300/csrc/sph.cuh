@@ -102,6 +102,44 @@ __device__ __forceinline__ T kernel_grad2w(const Consts& k, T r) {
   }
 }
 
+// dW/dr and d2W/dr2 together (the adjoint evaluates both per pair): the
+// same polynomials as kernel_gradw and kernel_grad2w sharing their powers
+template <typename T>
+__device__ __forceinline__ void kernel_gradw2(const Consts& k, T r, T& gw, T& g2) {
+  const T s = r * KC<T>::inv_h(k);
+  const T cgr = KC<T>::coef_grad(k);
+  if (k.kernel_type == 1) {
+    const T s3 = T(3) - s, s2 = T(2) - s, s1 = T(1) - s;
+    T a = T(0), b = T(0);
+    if (s < T(3)) {
+      const T q = s3 * s3;
+      a = T(5) * (q * q);
+      b = T(-20) * (q * s3);
+    }
+    if (s < T(2)) {
+      const T q = s2 * s2;
+      a = a - T(30) * (q * q);
+      b = b + T(120) * (q * s2);
+    }
+    if (s < T(1)) {
+      const T q = s1 * s1;
+      a = a + T(75) * (q * q);
+      b = b - T(300) * (q * s1);
+    }
+    gw = cgr * a;
+    g2 = cgr * KC<T>::inv_h(k) * b;
+  } else {
+    if (s > T(1)) {
+      gw = T(0);
+      g2 = T(0);
+      return;
+    }
+    const T om = T(1) - s;
+    gw = cgr * T(12) * s * (om * om);
+    g2 = cgr * KC<T>::inv_h(k) * T(12) * om * (T(1) - T(3) * s);
+  }
+}
+
 // Pressure, stateEquation_compute_pressure.F90:147-180 (vector forms):
 // Morris p = c^2 (rho^gamma - rho_ref), Batchelor p = p0((rho/rho_ref)^gamma - 1).
 __device__ __forceinline__ double eos_pressure(const Consts& k, double rho) {
