@@ -290,11 +290,27 @@ __device__ __forceinline__ float u01(uint32_t r) {
   return (__uint_as_float(0x3f800000u | (r >> 9)) - 1.0f) + 5.9604644775390625e-8f;
 }
 
+// -2 ln u for the Box-Muller radius: the hardware log2 (2 ulp below 1/2,
+// 2^-22 absolute in [1/2, 2]), which keeps the radius within ~4e-6 of the
+// exact one for u <= 1 - 2^-10; above, where that absolute error would
+// swamp ln u, the series -2 ln(1 - t) = 2t (1 + t/2 + t^2/3 + ...) in the
+// exact t = 1 - u (t <= 2^-10: the dropped terms are below 2^-32 of the sum).
+// The branch is taken by one lane in a thousand, so warps rarely diverge.
+__device__ __forceinline__ float neg2log(float u) {
+  if (u > 0.9990234375f) {
+    const float t = 1.0f - u;
+    return 2.0f * t * fmaf(t, fmaf(t, 0.33333334f, 0.5f), 1.0f);
+  }
+  return -1.3862943611198906f * __log2f(u);  // -2 ln 2 log2 u
+}
+
+// Box-Muller with the angle centred on [-pi, pi], where the hardware sine
+// and cosine (absolute error ~2^-21) are at their best.
 __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {
   const float u1 = u01(a), u2 = u01(b);
-  const float rad = sqrtf(-2.0f * logf(u1));
+  const float rad = sqrtf(neg2log(u1));
   float sn, cs;
-  sincospif(2.0f * u2, &sn, &cs);
+  __sincosf(6.2831853071795865f * u2 - 3.1415926535897932f, &sn, &cs);
   z0 = rad * cs;
   z1 = rad * sn;
 }

@@ -442,39 +442,57 @@ __global__ void __launch_bounds__(kReuseTPB)
       const float4 oi = off[i];
       const bool mass = k.rhs_density_type == 1;
       float sum = 0.0f, comp = 0.0f;
-      for (int e = 0; e < cnt; ++e) {
-        const int ent = vl[(size_t)e * n + i];
-        const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
-        const int j = s_start[sl * kReuseTPB + tid] + q;
-        const float4 oj = off[j];
-        const float sx = (float)(sl % 3 - 1) * k.csf[0];
-        const float sy = (float)((sl / 3) % 3 - 1) * k.csf[1];
-        const float sz = (D == 3) ? (float)(sl / 9 - 1) * k.csf[2] : 0.0f;
-        // the pair test as k_density's scan rounds it: (o_i - slot) - o_j
-        const float tx = (oi.x - sx) - oj.x, ty = (oi.y - sy) - oj.y;
-        float t2 = tx * tx + ty * ty;
-        if (D == 3) {
-          const float tz = (oi.z - sz) - oj.z;
-          t2 += tz * tz;
+      // candidates in groups of kGather: their entries, then their offsets,
+      // are loaded before any is used (the sweep waits on these gathers)
+      constexpr int kGather = 4;
+      for (int e0 = 0; e0 < cnt; e0 += kGather) {
+        int entg[kGather], jg[kGather];
+        float4 og[kGather];
+#pragma unroll
+        for (int u = 0; u < kGather; ++u)
+          entg[u] = (e0 + u < cnt) ? (int)vl[(size_t)(e0 + u) * n + i] : 0;
+#pragma unroll
+        for (int u = 0; u < kGather; ++u) {
+          jg[u] = s_start[(entg[u] >> kLocalBits) * kReuseTPB + tid] +
+                  (entg[u] & (kMaxCellCount - 1));
+          og[u] = (e0 + u < cnt) ? off[jg[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        if (!(t2 < k.rc2f)) continue;
-        if (hs < 0 && (sl > CENTER || (sl == CENTER && q > li))) hs = kept;
-        if (kept < cap) nl[(size_t)kept * n + i] = (uint16_t)ent;
-        ++kept;
-        if (!acc_i) continue;
-        // W as k_density's second phase rounds it: (o_i - o_j) - slot
-        const float rx = (oi.x - oj.x) - sx, ry = (oi.y - oj.y) - sy;
-        float d2 = rx * rx + ry * ry;
-        if (D == 3) {
-          const float rz = (oi.z - oj.z) - sz;
-          d2 += rz * rz;
+#pragma unroll
+        for (int u = 0; u < kGather; ++u) {
+          if (e0 + u >= cnt) break;
+          const int ent = entg[u];
+          const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
+          const int j = jg[u];
+          const float4 oj = og[u];
+          const float sx = (float)(sl % 3 - 1) * k.csf[0];
+          const float sy = (float)((sl / 3) % 3 - 1) * k.csf[1];
+          const float sz = (D == 3) ? (float)(sl / 9 - 1) * k.csf[2] : 0.0f;
+          // the pair test as k_density's scan rounds it: (o_i - slot) - o_j
+          const float tx = (oi.x - sx) - oj.x, ty = (oi.y - sy) - oj.y;
+          float t2 = tx * tx + ty * ty;
+          if (D == 3) {
+            const float tz = (oi.z - sz) - oj.z;
+            t2 += tz * tz;
+          }
+          if (!(t2 < k.rc2f)) continue;
+          if (hs < 0 && (sl > CENTER || (sl == CENTER && q > li))) hs = kept;
+          if (kept < cap) nl[(size_t)kept * n + i] = (uint16_t)ent;
+          ++kept;
+          if (!acc_i) continue;
+          // W as k_density's second phase rounds it: (o_i - o_j) - slot
+          const float rx = (oi.x - oj.x) - sx, ry = (oi.y - oj.y) - sy;
+          float d2 = rx * rx + ry * ry;
+          if (D == 3) {
+            const float rz = (oi.z - oj.z) - sz;
+            d2 += rz * rz;
+          }
+          float w = kernel_w<float>(k, sqrtf(d2));
+          if (mass) w *= (float)m[j];
+          const float y = w - comp;
+          const float tt = sum + y;
+          comp = (tt - sum) - y;
+          sum = tt;
         }
-        float w = kernel_w<float>(k, sqrtf(d2));
-        if (mass) w *= (float)m[j];
-        const float y = w - comp;
-        const float tt = sum + y;
-        comp = (tt - sum) - y;
-        sum = tt;
       }
       rho_i = (double)sum;
     }

@@ -189,7 +189,8 @@ static inline void box_muller(uint32_t a, uint32_t b, float* z0, float* z1) {
   const float u1 = u01(a), u2 = u01(b);
   const float lg = (float)log((double)u1);
   const float rad = sqrtf(-2.0f * lg);
-  const double th = 2.0 * MK_PI * (double)u2;
+  /* angle 2 pi u2 - pi, on [-pi, pi] */
+  const double th = 2.0 * MK_PI * (double)u2 - MK_PI;
   const float cs = (float)cos(th), sn = (float)sin(th);
   *z0 = rad * cs;
   *z1 = rad * sn;

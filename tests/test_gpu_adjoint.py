@@ -10,8 +10,10 @@ References:
     and Richardson-extrapolated steps 1e-2 / 2e-2 (eta, tau, c), see the test.
 Tolerances: without noise the adjoint matches the reference gradient to
 1e-8 relative; with the random term on, the GPU's FP32 Box-Muller normals
-(CUDA logf/sincospif) differ from the CPU's in the last bits, so the bound
-is 1e-5; against finite differences the bound is 1e-4.
+(hardware log2 / sine / cosine) are within ~6e-6 of the exact ones the CPU
+reference draws, and the trajectories they drive differ accordingly, so the
+bound is 5e-5 of the largest gradient entry; against finite differences of
+the GPU's own J the bound is 1e-4.
 The torch.autograd.Function wrapper below is test-harness only.
 """
 import numpy as np
@@ -49,7 +51,7 @@ def test_adjoint_matches_reference_gradient(gpu_lib, maker, noise):
     _, (J, g, st) = gpu_adjoint(w, ct, T, wts, K=3, state_grads=True)
     Jr, gr, sr = reference_gradient(w.params, w.x, w.v, w.m, w.id[:, 0], ct, 0, T, w.dt, wts,
                                     state_grads=True)
-    tol = 1e-5 if noise else 1e-8
+    tol = 5e-5 if noise else 1e-8
     assert abs(J - Jr) <= tol * abs(Jr)
     scale = np.abs(gr).max()
     assert np.max(np.abs(g - gr)) <= tol * scale, (g, gr)

@@ -7,7 +7,8 @@ Bars (the benchmark spec of the plain FP64 path):
     S_i = sum_j |a_ij| (net forces on near-lattice states are sums of large
     cancelling pair terms, so |a_i| itself is no scale);
   - with the random force on, the pair normals are FP32 Box-Muller values
-    (CUDA logf/sincospif on the GPU, libm on the CPU): tolerance 1e-5 * S_i;
+    (hardware log2/sine/cosine on the GPU, within ~5e-6 of the exact values
+    the CPU draws with libm): tolerance 1e-5 * S_i;
   - kT=0 trajectories over 100 steps: positions within 1e-9 of the box
     length, velocities within 1e-7 of the velocity scale.
 """
