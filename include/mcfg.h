@@ -230,6 +230,16 @@ int mcfg_step_vv(mcfg_handle* h, int64_t step, double dt);
  * the loop of marching_marching.F90:1329-1531 without I/O. */
 int mcfg_run_vv(mcfg_handle* h, int64_t step0, int32_t nsteps, double dt);
 
+/* Overwrite the positions, velocities and/or accelerations (any pointer may
+ * be NULL) of the particles of the last mcfg_upload, in host order, keeping
+ * the device's particle order and neighbour-list state: MCF's per-step
+ * drop-in hands back the arrays it received from mcfg_download (after its
+ * own changes, if any), and the next step rebuilds lists only if a particle
+ * has moved past the reuse skin.  Positions are taken in the periodic image
+ * the device holds.  The particle set (count, ids, masses) must be that of
+ * the last mcfg_upload; call mcfg_upload when it changes. */
+int mcfg_update_state(mcfg_handle* h, const double* x, const double* v, const double* f);
+
 /* Copy state back in host particle order; any pointer may be NULL.
  * x,v,f: [n*d]; rho,p: [n]; ct: [n*d*d]; s: [n*d*d] (stress_tensor). */
 int mcfg_download(mcfg_handle* h, double* x, double* v, double* rho,

@@ -328,6 +328,40 @@ __global__ void k_upload(int n, int d, const double* __restrict__ hx, const doub
   slot_of[i] = i;
 }
 
+// host-order state written into the particles' current slots; positions
+// taken in the periodic image the device holds (between list rebuilds it
+// may keep a particle up to skin/2 past a face, the host copy is wrapped)
+__global__ void k_update_state(Consts k, int n, const int* __restrict__ slot_of,
+                               const double* __restrict__ hx, const double* __restrict__ hv,
+                               const double* __restrict__ hf, double4_32a* __restrict__ x,
+                               double4_32a* __restrict__ v, double4_32a* __restrict__ f) {
+  const int hi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (hi >= n) return;
+  const int s = slot_of[hi];
+  const int d = k.d;
+  if (hx) {
+    const double4_32a xd = x[s];
+    const double cur[3] = {xd.x, xd.y, xd.z};
+    double xs[3] = {0.0, 0.0, 0.0};
+    for (int a = 0; a < d; ++a) {
+      xs[a] = hx[(size_t)hi * d + a];
+      if (k.periodic[a]) {
+        const double sh = rint((cur[a] - xs[a]) / k.len[a]);
+        if (sh != 0.0) xs[a] = xs[a] + sh * k.len[a];
+      }
+    }
+    x[s] = make_double4_32a(xs[0], xs[1], xs[2], 0.0);
+  }
+  if (hv) {
+    const double* p = hv + (size_t)hi * d;
+    v[s] = make_double4_32a(p[0], p[1], d == 3 ? p[2] : 0.0, 0.0);
+  }
+  if (hf) {
+    const double* p = hf + (size_t)hi * d;
+    f[s] = make_double4_32a(p[0], p[1], d == 3 ? p[2] : 0.0, 0.0);
+  }
+}
+
 // scatter sorted state back to host order: interleaved (d, N) layout
 __global__ void k_download(int n, int d, const int* __restrict__ hidx, const double4_32a* __restrict__ a4,
                            double* __restrict__ out) {
@@ -763,6 +797,32 @@ int mcfg_upload_force(mcfg_handle* h, const double* f) {
   return MCFG_OK;
 }
 
+int mcfg_update_state(mcfg_handle* h, const double* x, const double* v, const double* f) {
+  GUARD(h);
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  const int n = (int)h->n, d = h->p.num_dim;
+  if (n == 0) return MCFG_OK;
+  cudaStream_t s = h->stream;
+  const size_t bytes = sizeof(double) * (size_t)n * d;
+  double* dx = x ? h->up_x : nullptr;
+  double* df = f ? h->up_x + (size_t)n * 3 : nullptr;
+  double* dv = v ? h->up_v : nullptr;
+  if ((x && cuda_check(h, cudaMemcpyAsync(dx, x, bytes, cudaMemcpyHostToDevice, s), "update x")) ||
+      (v && cuda_check(h, cudaMemcpyAsync(dv, v, bytes, cudaMemcpyHostToDevice, s), "update v")) ||
+      (f && cuda_check(h, cudaMemcpyAsync(df, f, bytes, cudaMemcpyHostToDevice, s), "update f")))
+    return MCFG_ECUDA;
+  const int tb = 256, gb = (n + tb - 1) / tb;
+  k_update_state<<<gb, tb, 0, s>>>(h->k, n, h->slot_of, dx, dv, df, h->x, h->v, h->f);
+  h->launches++;
+  if (cuda_check(h, cudaGetLastError(), "update state kernel") ||
+      cuda_check(h, cudaStreamSynchronize(s), "update state sync"))
+    return MCFG_ECUDA;
+  if (f) h->have_force = true;
+  // derived per-step data (densities, lists of the stage entry points) are stale
+  h->have_list = h->have_density = h->have_pressure = false;
+  return MCFG_OK;
+}
+
 int mcfg_adjust_particles(mcfg_handle* h) {
   GUARD(h);
   if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
@@ -880,35 +940,38 @@ int mcfg_download(mcfg_handle* h, double* x, double* v, double* rho, double* p, 
   if (n == 0) return MCFG_OK;
   cudaStream_t st = h->stream;
   const int tb = 256, gb = (n + tb - 1) / tb;
-  double* stage = h->up_x;  // n*9 doubles of staging
-  auto vec_out = [&](const double4_32a* a4, double* host) -> int {
-    k_download<<<gb, tb, 0, st>>>(n, d, h->hidx, a4, stage);
+  // x, v, f, rho and p gathered into separate staging regions and copied
+  // asynchronously, one synchronisation for all of them
+  double* stage = h->up_x;  // n*9 doubles: x | v | f
+  const size_t nd = (size_t)n * d;
+  auto vec_out = [&](const double4_32a* a4, double* dst, double* host) -> int {
+    k_download<<<gb, tb, 0, st>>>(n, d, h->hidx, a4, dst);
     h->launches++;
-    if (cuda_check(h, cudaMemcpyAsync(host, stage, sizeof(double) * (size_t)n * d,
-                                      cudaMemcpyDeviceToHost, st), "download"))
-      return MCFG_ECUDA;
-    return cuda_check(h, cudaStreamSynchronize(st), "download sync") ? MCFG_ECUDA : MCFG_OK;
+    return cuda_check(h, cudaMemcpyAsync(host, dst, sizeof(double) * nd, cudaMemcpyDeviceToHost,
+                                         st), "download")
+               ? MCFG_ECUDA
+               : MCFG_OK;
   };
-  auto sca_out = [&](const double* a, double* host) -> int {
-    k_download_scalar<<<gb, tb, 0, st>>>(n, h->hidx, a, stage);
+  auto sca_out = [&](const double* a, double* dst, double* host) -> int {
+    k_download_scalar<<<gb, tb, 0, st>>>(n, h->hidx, a, dst);
     h->launches++;
-    if (cuda_check(h, cudaMemcpyAsync(host, stage, sizeof(double) * (size_t)n,
-                                      cudaMemcpyDeviceToHost, st), "download"))
-      return MCFG_ECUDA;
-    return cuda_check(h, cudaStreamSynchronize(st), "download sync") ? MCFG_ECUDA : MCFG_OK;
+    return cuda_check(h, cudaMemcpyAsync(host, dst, sizeof(double) * (size_t)n,
+                                         cudaMemcpyDeviceToHost, st), "download")
+               ? MCFG_ECUDA
+               : MCFG_OK;
   };
   if (x) {
     k_download_pos<<<gb, tb, 0, st>>>(h->k, n, h->hidx, h->x, stage);
     h->launches++;
-    if (cuda_check(h, cudaMemcpyAsync(x, stage, sizeof(double) * (size_t)n * d,
-                                      cudaMemcpyDeviceToHost, st), "download") ||
-        cuda_check(h, cudaStreamSynchronize(st), "download sync"))
+    if (cuda_check(h, cudaMemcpyAsync(x, stage, sizeof(double) * nd, cudaMemcpyDeviceToHost, st),
+                   "download"))
       return MCFG_ECUDA;
   }
-  if (v) TRY(vec_out(h->v, v));
-  if (f) TRY(vec_out(h->f, f));
-  if (rho) TRY(sca_out(h->rho, rho));
-  if (p) TRY(sca_out(h->pr, p));
+  if (v) TRY(vec_out(h->v, stage + (size_t)3 * n, v));
+  if (f) TRY(vec_out(h->f, stage + (size_t)6 * n, f));
+  if (rho) TRY(sca_out(h->rho, h->up_v, rho));
+  if (p) TRY(sca_out(h->pr, h->up_v + n, p));
+  if (cuda_check(h, cudaStreamSynchronize(st), "download sync")) return MCFG_ECUDA;
   if (ct) {
     k_download_tensor<<<gb, tb, 0, st>>>(n, d * d, h->hidx, h->ct, stage);
     h->launches++;

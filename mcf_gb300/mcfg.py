@@ -61,6 +61,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "mcfg_init_force": (C.c_int, [_h, C.c_int64]),
         "mcfg_step_vv": (C.c_int, [_h, C.c_int64, C.c_double]),
         "mcfg_run_vv": (C.c_int, [_h, C.c_int64, C.c_int32, C.c_double]),
+        "mcfg_update_state": (C.c_int, [_h, _dp, _dp, _dp]),
         "mcfg_adjoint_run": (C.c_int, [_h, C.c_int64, C.c_int32, C.c_double, C.c_int32, _dp, _dp,
                                        _dp, _dp, _dp, _dp]),
         "mcfg_download": (C.c_int, [_h, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
@@ -290,6 +291,13 @@ class SDPD:
         self._check("colloid_compute_repulsion_cc",
                     self.lib.mcfg_colloid_repulsion(self._h, _ptr(out, C.c_double)))
         return out
+
+    def update_state(self, x=None, v=None, f=None) -> None:
+        """mcfg_update_state: new x / v / f for the uploaded particles, host order"""
+        n, d = self.n, self.dim
+        arrs = [None if a is None else _as(a, np.float64, (n, d)) for a in (x, v, f)]
+        self._check("mcfg_update_state", self.lib.mcfg_update_state(
+            self._h, *(_ptr(a, C.c_double) for a in arrs)))
 
     def upload_force(self, f) -> None:
         self._f = _as(f, np.float64, (self.n, self.dim))

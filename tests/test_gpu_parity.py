@@ -423,3 +423,39 @@ def test_list_reuse_walls_oldroyd_and_noise(gpu_lib):
     dx -= L * np.round(dx / L)
     assert np.max(np.abs(dx)) <= 1e-10
     assert np.max(np.abs(da["ct"] - db["ct"])) <= 1e-10
+
+
+def test_update_state_keeps_order_and_reuse(gpu_lib):
+    # MCF's per-step drop-in: download, (modify), hand the arrays back
+    w = jittered_3d(n_side=16)
+    p = w.params.copy()
+    p.reserved[1] = 1
+    p.Brownian = 0
+    p.kt = 0.0
+    ref = SDPD(p)
+    ref.upload(w.x, w.v, w.m, w.id)
+    ref.marching_init_force(0)
+    ref.run_vv(0, 30, w.dt)
+    h = SDPD(p)
+    h.upload(w.x, w.v, w.m, w.id)
+    h.marching_init_force(0)
+    for s in range(30):
+        st = h.download("x", "v", "f")
+        h.update_state(st["x"], st["v"], st["f"])
+        h.marching_integrate_VV(s + 1, w.dt)
+    assert h.info()["list_rebuilds"] == ref.info()["list_rebuilds"] == 1
+    a, b = ref.download("x", "v"), h.download("x", "v")
+    assert np.max(np.abs(a["x"] - b["x"])) <= 1e-12 * 16
+    assert np.max(np.abs(a["v"] - b["v"])) <= 1e-10 * np.max(np.abs(a["v"]))
+    # a changed state: the same as uploading it afresh
+    st = h.download("x", "v", "f")
+    st["v"] *= 0.5
+    h.update_state(st["x"], st["v"], st["f"])
+    g = SDPD(p)
+    g.upload(st["x"], st["v"], w.m, w.id)
+    g.upload_force(st["f"])
+    h.run_vv(30, 10, w.dt)
+    g.run_vv(30, 10, w.dt)
+    a, b = g.download("x", "v"), h.download("x", "v")
+    assert np.max(np.abs(a["x"] - b["x"])) <= 1e-10
+    assert np.max(np.abs(a["v"] - b["v"])) <= 1e-8 * np.max(np.abs(a["v"]))
