@@ -257,6 +257,19 @@ int mcfg_set_colloids(mcfg_handle* h, const mcfg_colloid_params* cp,
                       const double* x, const double* v, const double* omega,
                       const double* radius);
 
+/* Move every colloid's boundary particles with it after MCF's Colloid
+ * object has integrated the rigid bodies (the O(N_c) Adams-Bashforth
+ * translation/rotation stays on the host): each particle is taken relative
+ * to the nearest image of its colloid's current centre, turned by the
+ * colloid's rotation matrix of the step (rot[9c + i + 3j] = R(i,j), MCF's
+ * coll_rot_matrix(:,:,c); NULL or rotate off: no turn), and put at the new
+ * centre x_new[c*d..] -- particles_compute_colloid_relative_position.F90 and
+ * particles_compute_colloid_absolute_position.F90 around the colloid update
+ * of marching_integrate_VV.F90:455-765.  The colloids' state becomes
+ * (x_new, v, omega).  Nothing moves unless translate or rotate is on. */
+int mcfg_move_colloids(mcfg_handle* h, const double* x_new, const double* rot,
+                       const double* v, const double* omega);
+
 /* Drag and torque of every colloid from its boundary particles' last
  * accelerations, particles_collect_colloid_interaction.F90:93-136:
  * drag[nc*d] = sum m f, torque[nc*3] = sum r x (m f). */

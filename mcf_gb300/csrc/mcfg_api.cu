@@ -991,6 +991,30 @@ int mcfg_download(mcfg_handle* h, double* x, double* v, double* rho, double* p, 
   return MCFG_OK;
 }
 
+// host copies and the device table [nc][12] (X V Omega R) of the colloids
+static int put_colloid_state(Handle* h, int nc, const double* x, const double* v,
+                             const double* omega) {
+  const int d = h->p.num_dim;
+  h->cx.assign(x, x + (size_t)nc * d);
+  h->cv.assign(v, v + (size_t)nc * d);
+  h->com.assign(omega, omega + (size_t)nc * 3);
+  std::vector<double> buf((size_t)nc * 12, 0.0);
+  for (int c = 0; c < nc; ++c) {
+    for (int a = 0; a < d; ++a) {
+      buf[(size_t)c * 12 + a] = x[(size_t)c * d + a];
+      buf[(size_t)c * 12 + 3 + a] = v[(size_t)c * d + a];
+    }
+    for (int a = 0; a < 3; ++a) buf[(size_t)c * 12 + 6 + a] = omega[(size_t)c * 3 + a];
+    buf[(size_t)c * 12 + 9] = h->crad[(size_t)c];
+  }
+  if (nc > 0 &&
+      (cuda_check(h, cudaMemcpyAsync(h->coll, buf.data(), sizeof(double) * buf.size(),
+                                     cudaMemcpyHostToDevice, h->stream), "upload colloids") ||
+       cuda_check(h, cudaStreamSynchronize(h->stream), "upload colloids")))
+    return MCFG_ECUDA;
+  return MCFG_OK;
+}
+
 int mcfg_set_colloids(mcfg_handle* h, const mcfg_colloid_params* cp, const double* x,
                       const double* v, const double* omega, const double* radius) {
   GUARD(h);
@@ -1004,28 +1028,14 @@ int mcfg_set_colloids(mcfg_handle* h, const mcfg_colloid_params* cp, const doubl
   if (cp->noslip_type < 1 || cp->noslip_type > 2)
     return set_error(h, MCFG_ENOTSUP, "colloid noslip_type must be 1 (frozen) or 2 (Morris)");
   h->cp = *cp;
-  h->cx.assign(x, x + (size_t)nc * d);
-  h->cv.assign(v, v + (size_t)nc * d);
-  h->com.assign(omega, omega + (size_t)nc * 3);
   h->crad.assign(radius, radius + nc);
-  std::vector<double> buf((size_t)nc * 12, 0.0);
-  for (int c = 0; c < nc; ++c) {
-    for (int a = 0; a < d; ++a) {
-      buf[(size_t)c * 12 + a] = x[(size_t)c * d + a];
-      buf[(size_t)c * 12 + 3 + a] = v[(size_t)c * d + a];
-    }
-    for (int a = 0; a < 3; ++a) buf[(size_t)c * 12 + 6 + a] = omega[(size_t)c * 3 + a];
-    buf[(size_t)c * 12 + 9] = radius[c];
-  }
   if (nc > 0) {
     int rc;
-    if ((rc = dalloc(h, &h->coll, buf.size())) || (rc = dalloc(h, &h->coll_out, (size_t)nc * 6)))
+    if ((rc = dalloc(h, &h->coll, (size_t)nc * 12)) ||
+        (rc = dalloc(h, &h->coll_out, (size_t)nc * 12)))
       return rc;
-    if (cuda_check(h, cudaMemcpyAsync(h->coll, buf.data(), sizeof(double) * buf.size(),
-                                      cudaMemcpyHostToDevice, h->stream), "upload colloids") ||
-        cuda_check(h, cudaStreamSynchronize(h->stream), "upload colloids"))
-      return MCFG_ECUDA;
   }
+  TRY(put_colloid_state(h, nc, x, v, omega));
   Consts& k = h->k;
   k.ncoll = nc;
   k.coll = h->coll;
@@ -1036,6 +1046,29 @@ int mcfg_set_colloids(mcfg_handle* h, const mcfg_colloid_params* cp, const doubl
   k.pp_cc = cp->pp_interact_cc;
   k.coll_dout = cp->dout;
   h->have_density = h->have_pressure = false;
+  return MCFG_OK;
+}
+
+int mcfg_move_colloids(mcfg_handle* h, const double* x_new, const double* rot, const double* v,
+                       const double* omega) {
+  GUARD(h);
+  const int nc = h->k.ncoll, d = h->p.num_dim;
+  if (nc == 0) return set_error(h, MCFG_ESTATE, "mcfg_set_colloids must come first");
+  if (!x_new || !v || !omega) return set_error(h, MCFG_EINVAL, "mcfg_move_colloids: NULL array");
+  // staging: the new centres in coll_out (nc*12 doubles), the rotations in
+  // the upload staging (nc*9 <= 3 n: every colloid owns boundary particles)
+  double* dx = h->coll_out;
+  double* dr = rot ? h->up_v : nullptr;
+  if (rot && (size_t)nc * 9 > h->up_cap * 3)
+    return set_error(h, MCFG_EINVAL, "more colloids than staging room");
+  if (cuda_check(h, cudaMemcpyAsync(dx, x_new, sizeof(double) * (size_t)nc * d,
+                                    cudaMemcpyHostToDevice, h->stream), "colloid move") ||
+      (rot && cuda_check(h, cudaMemcpyAsync(dr, rot, sizeof(double) * (size_t)nc * 9,
+                                            cudaMemcpyHostToDevice, h->stream), "colloid move")))
+    return MCFG_ECUDA;
+  TRY(colloid_move(h, dx, dr));
+  TRY(put_colloid_state(h, nc, x_new, v, omega));
+  h->have_list = h->have_density = h->have_pressure = false;
   return MCFG_OK;
 }
 

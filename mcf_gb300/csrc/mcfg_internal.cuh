@@ -259,6 +259,7 @@ int rhs(Handle* h, int64_t step, int fuse_mode, double dt);
 int kdw(Handle* h, double dt);
 void free_adjoint(Handle* h);
 int colloid_drag(Handle* h, double* drag, double* torque);
+int colloid_move(Handle* h, const double* d_xnew, const double* d_rot);
 int check_device_errors(Handle* h);
 
 // fuse_mode of compute_force

@@ -194,6 +194,67 @@ __global__ void k_colloid_drag(Consts k, const int* __restrict__ cstart,
     for (int a = 0; a < 6; ++a) out[(size_t)c * 6 + a] = acc[a];
 }
 
+// Boundary particles follow their colloid (particles_compute_colloid_
+// relative_position.F90 then _absolute_position.F90): relative to the
+// nearest image of the old centre, turned by the step's rotation matrix
+// (rot[9c + i + 3j] = R(i,j)), put at the new centre in the same periodic
+// image as before (so list reuse sees a small displacement).  One warp per
+// colloid; coll still holds the old centres.
+template <int D>
+__global__ void k_colloid_move(Consts k, const int* __restrict__ cstart,
+                               const int* __restrict__ cmem, const int* __restrict__ slot_of,
+                               const double* __restrict__ xnew, const double* __restrict__ rot,
+                               double4_32a* __restrict__ x) {
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= k.ncoll) return;
+  const double* cd = k.coll + (size_t)c * 12;
+  for (int q = cstart[c] + lane; q < cstart[c + 1]; q += 32) {
+    const int s = slot_of[cmem[q]];
+    const double4_32a xv = x[s];
+    const double xs[3] = {xv.x, xv.y, xv.z};
+    double rx[3] = {0.0, 0.0, 0.0};
+    colloid_rx<D>(k, xs, c, rx);
+    double rb[3] = {rx[0], rx[1], rx[2]};
+    if (k.coll_rotate && rot != nullptr) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        double t = 0.0;
+#pragma unroll
+        for (int b = 0; b < D; ++b)
+          t = __dadd_rn(t, __dmul_rn(rot[(size_t)c * 9 + a + 3 * b], rx[b]));
+        rb[a] = t;
+      }
+    }
+    double xo[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      // the old centre image the particle was taken against: xs - rx
+      const double img = (xs[a] - rx[a]) - cd[a];
+      double xn = __dadd_rn(rb[a], xnew[(size_t)c * D + a]);
+      if (k.periodic[a] && fabs(img) > 0.5 * k.len[a])
+        xn = __dadd_rn(xn, img > 0.0 ? k.len[a] : -k.len[a]);
+      xo[a] = xn;
+    }
+    x[s] = make_double4_32a(xo[0], xo[1], D == 3 ? xo[2] : 0.0, 0.0);
+  }
+}
+
+int colloid_move(Handle* h, const double* d_xnew, const double* d_rot) {
+  const int nc = h->k.ncoll;
+  if (nc == 0 || !(h->k.coll_translate || h->k.coll_rotate)) return MCFG_OK;
+  const int warps_per_block = 4;
+  const int g = (nc + warps_per_block - 1) / warps_per_block;
+  if (h->k.d == 3)
+    k_colloid_move<3><<<g, 32 * warps_per_block, 0, h->stream>>>(
+        h->k, h->coll_start, h->coll_mem, h->slot_of, d_xnew, d_rot, h->x);
+  else
+    k_colloid_move<2><<<g, 32 * warps_per_block, 0, h->stream>>>(
+        h->k, h->coll_start, h->coll_mem, h->slot_of, d_xnew, d_rot, h->x);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "colloid move launch") ? MCFG_ECUDA : MCFG_OK;
+}
+
 int colloid_drag(Handle* h, double* drag, double* torque) {
   const int nc = h->k.ncoll, d = h->k.d;
   if (nc == 0) return MCFG_OK;

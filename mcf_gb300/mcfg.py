@@ -76,6 +76,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "mcfg_noalloc_error": (C.c_char_p, []),
         "mcfg_set_colloids": (C.c_int, [_h, C.POINTER(ColloidParams), _dp, _dp, _dp, _dp]),
         "mcfg_colloid_drag": (C.c_int, [_h, _dp, _dp]),
+        "mcfg_move_colloids": (C.c_int, [_h, _dp, _dp, _dp, _dp]),
         "mcfg_colloid_repulsion": (C.c_int, [_h, _dp]),
     }
     for name, (res, args) in sig.items():
@@ -274,6 +275,16 @@ class SDPD:
         self._check("mcfg_set_colloids", self.lib.mcfg_set_colloids(
             self._h, C.byref(cp), _ptr(self._cx, C.c_double), _ptr(self._cv, C.c_double),
             _ptr(self._com, C.c_double), _ptr(self._crad, C.c_double)))
+
+    def move_colloids(self, x_new, rot, v, omega) -> None:
+        """mcfg_move_colloids: boundary particles follow their colloids"""
+        self._cx = _as(x_new, np.float64)
+        self._cv = _as(v, np.float64)
+        self._com = _as(omega, np.float64)
+        r = None if rot is None else _as(rot, np.float64)
+        self._check("mcfg_move_colloids", self.lib.mcfg_move_colloids(
+            self._h, _ptr(self._cx, C.c_double), _ptr(r, C.c_double),
+            _ptr(self._cv, C.c_double), _ptr(self._com, C.c_double)))
 
     def colloid_drag(self):
         """particles_collect_colloid_interaction: (drag[nc, d], torque[nc, 3])"""

@@ -802,6 +802,42 @@ int orc_set_colloids(orc_state* s, const mcfg_colloid_params* cp, const double* 
   return 0;
 }
 
+/* The boundary-particle kinematics around MCF's colloid integration
+ * (marching_integrate_VV.F90:455-765): particles_compute_colloid_relative_
+ * position.F90 takes each boundary particle relative to its colloid's
+ * nearest centre image and turns it by the colloid's rotation matrix of the
+ * step (MATMUL(R, rx), R(i,j) = rot[9c + i + 3j]); after the colloids have
+ * moved, particles_compute_colloid_absolute_position.F90 adds the new
+ * centre.  Then the colloid state is (x_new, v, omega).  Nothing moves
+ * unless the colloids translate or rotate. */
+int orc_move_colloids(orc_state* s, const double* x_new, const double* rot, const double* v,
+                      const double* omega) {
+  const int d = s->d, nc = s->cp.num_colloid;
+  if (s->cp.translate || s->cp.rotate) {
+    for (int64_t j = 0; j < s->nreal; ++j) {
+      const int c = s->sid[j] - 1;
+      if (s->sid[j] <= 0 || c >= nc) continue;
+      double ximg[3], rx[3] = {0, 0, 0}, vimg[3], rb[3] = {0, 0, 0};
+      colloid_nearest_image(s, &s->x[j * d], c, ximg, rx, vimg);
+      if (s->cp.rotate && rot) {
+        for (int a = 0; a < d; ++a) {
+          double t = 0.0;
+          for (int q = 0; q < d; ++q) t = t + rot[c * 9 + a + 3 * q] * rx[q];
+          rb[a] = t;
+        }
+      } else {
+        for (int a = 0; a < d; ++a) rb[a] = rx[a];
+      }
+      for (int a = 0; a < d; ++a) s->x[j * d + a] = rb[a] + x_new[c * d + a];
+    }
+  }
+  memcpy(s->cx, x_new, sizeof(double) * (size_t)(nc * d));
+  memcpy(s->cv, v, sizeof(double) * (size_t)(nc * d));
+  memcpy(s->com, omega, sizeof(double) * (size_t)(nc * 3));
+  s->have_list = s->have_density = s->have_pressure = 0;
+  return 0;
+}
+
 /* particles_collect_colloid_interaction.F90:93-136 */
 int orc_colloid_drag(orc_state* s, double* drag, double* torque) {
   const int d = s->d, nc = s->cp.num_colloid;

@@ -64,6 +64,8 @@ int orc_statistics(orc_state* s, double* k_energy, double* momentum,
 int orc_force_scale(const orc_state* s, double* out);
 int orc_set_colloids(orc_state* s, const mcfg_colloid_params* cp, const double* x,
                      const double* v, const double* omega, const double* radius);
+int orc_move_colloids(orc_state* s, const double* x_new, const double* rot, const double* v,
+                      const double* omega);
 int orc_colloid_drag(orc_state* s, double* drag, double* torque);
 int orc_colloid_repulsion(orc_state* s, double* force);
 /* counts: [0] reals, [1] ghosts, [2] pairs inside cut-off (last force) */

@@ -71,6 +71,7 @@ def load(rebuild: bool = True) -> C.CDLL:
         "orc_pair_we": (C.c_int, [_h, C.c_int64, C.c_int32, C.c_int32, _dp, _dp]),
         "orc_set_colloids": (C.c_int, [_h, C.POINTER(ColloidParams), _dp, _dp, _dp, _dp]),
         "orc_colloid_drag": (C.c_int, [_h, _dp, _dp]),
+        "orc_move_colloids": (C.c_int, [_h, _dp, _dp, _dp, _dp]),
         "orc_colloid_repulsion": (C.c_int, [_h, _dp]),
     }
     for name, (res, args) in sig.items():
@@ -214,6 +215,15 @@ class Oracle:
         self._check("set_colloids", self.lib.orc_set_colloids(
             self._h, C.byref(cp), _ptr(self._cx, C.c_double), _ptr(self._cv, C.c_double),
             _ptr(self._com, C.c_double), _ptr(self._crad, C.c_double)))
+
+    def move_colloids(self, x_new, rot, v, omega):
+        self._cx = np.ascontiguousarray(x_new, np.float64)
+        self._cv = np.ascontiguousarray(v, np.float64)
+        self._com = np.ascontiguousarray(omega, np.float64)
+        r = None if rot is None else np.ascontiguousarray(rot, np.float64)
+        self._check("move_colloids", self.lib.orc_move_colloids(
+            self._h, _ptr(self._cx, C.c_double), _ptr(r, C.c_double),
+            _ptr(self._cv, C.c_double), _ptr(self._com, C.c_double)))
 
     def colloid_drag(self):
         nc = self._cp.num_colloid

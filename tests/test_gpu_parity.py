@@ -459,3 +459,46 @@ def test_update_state_keeps_order_and_reuse(gpu_lib):
     a, b = g.download("x", "v"), h.download("x", "v")
     assert np.max(np.abs(a["x"] - b["x"])) <= 1e-10
     assert np.max(np.abs(a["v"] - b["v"])) <= 1e-8 * np.max(np.abs(a["v"]))
+
+
+def _rotation(axis, angle):
+    a = np.asarray(axis, float) / np.linalg.norm(axis)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) + np.sin(angle) * K + (1 - np.cos(angle)) * K @ K
+
+
+def test_colloid_move_then_steps(gpu_lib):
+    # MCF's Colloid object integrates the rigid bodies on the host; the
+    # boundary particles follow on the device (relative position, rotation,
+    # new centre), then the steps continue with the moved colloids
+    w, cs = colloid_case()
+    g, o = both(w, Brownian=0, kt=0.0)
+    for h in (g, o):
+        h.set_colloids(cs.params, cs.x, cs.v, cs.omega, cs.radius)
+        h.marching_init_force(0)
+        h.run_vv(0, 3, w.dt)
+    rng = np.random.default_rng(31)
+    nc = cs.x.shape[0]
+    x_new = cs.x + rng.uniform(-0.05, 0.05, cs.x.shape)
+    rot = np.stack([_rotation(rng.normal(size=3), 0.02) for _ in range(nc)])
+    rot_f = np.ascontiguousarray(rot.transpose(0, 2, 1)).reshape(nc, 9)  # R(i,j) at i + 3j
+    v_new = cs.v * 1.5
+    om_new = cs.omega * 0.5
+    for h in (g, o):
+        h.move_colloids(x_new, rot_f, v_new, om_new)
+    a, b = g.download("x"), o.download("x")
+    L = 24.0
+    dx = a["x"] - b["x"]
+    dx -= L * np.round(dx / L)
+    assert np.max(np.abs(dx)) <= 1e-12
+    for h in (g, o):
+        h.run_vv(3, 5, w.dt)
+    a, b = g.download("x", "v"), o.download("x", "v")
+    dx = a["x"] - b["x"]
+    dx -= L * np.round(dx / L)
+    assert np.max(np.abs(dx)) <= 1e-11
+    assert np.max(np.abs(a["v"] - b["v"])) <= 1e-9 * np.abs(b["v"]).max()
+    da, ta = g.colloid_drag()
+    db, tb = o.colloid_drag()
+    scale = np.abs(db).max() + np.abs(tb).max()
+    assert np.max(np.abs(da - db)) <= 1e-9 * scale and np.max(np.abs(ta - tb)) <= 1e-9 * scale

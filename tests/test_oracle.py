@@ -274,3 +274,27 @@ def test_pair_we_has_mcf_law_and_is_antisymmetric(dim):
     expect = (1 - 1 / dim) * np.outer(e, e) + 0.5 * (np.eye(dim) - np.outer(e, e))
     assert np.max(np.abs(ref - expect)) < 0.02
     assert np.max(np.abs(cov - expect)) < 0.04, cov
+
+
+def test_colloid_move_is_rigid():
+    # boundary particles follow a translation + rotation of their colloid:
+    # distances inside a colloid are kept, the centre moves by the shift
+    w, cs, o = _colloid_oracle(1, 2)
+    x0 = o.download("x")["x"]
+    nc = cs.x.shape[0]
+    th = 0.3
+    R = np.array([[np.cos(th), -np.sin(th), 0], [np.sin(th), np.cos(th), 0], [0, 0, 1.0]])
+    rot = np.tile(R.T.reshape(1, 9), (nc, 1))  # R(i,j) at i + 3j
+    shift = np.array([0.4, -0.2, 0.1])
+    o.move_colloids(cs.x + shift, rot, cs.v, cs.omega)
+    x1 = o.download("x")["x"]
+    L = 24.0
+    for c in range(nc):
+        m = w.id[:, 1] == c + 1
+        r0 = x0[m] - cs.x[c]
+        r0 -= L * np.round(r0 / L)
+        r1 = x1[m] - (cs.x[c] + shift)
+        r1 -= L * np.round(r1 / L)
+        assert np.allclose(r1, r0 @ R.T, atol=1e-12)
+    fl = w.id[:, 1] == 0
+    assert np.array_equal(x0[fl], x1[fl])
