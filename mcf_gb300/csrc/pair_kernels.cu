@@ -383,6 +383,16 @@ __global__ void k_rebuild_done(int* __restrict__ flag) {
 
 constexpr int kReuseTPB = 128;
 
+// FP32 offset of each stencil slot (the neighbour cell's origin minus the
+// home cell's), the same products as build_table's t.o, in a block-shared
+// table: the block's first threads fill it, then __syncthreads.
+__device__ __forceinline__ void fill_slot_offsets(const Consts& k, float4* s_slot) {
+  const int s = threadIdx.x;
+  if (s < kMaxStencil)
+    s_slot[s] = make_float4((float)(s % 3 - 1) * k.csf[0], (float)((s / 3) % 3 - 1) * k.csf[1],
+                            (float)(s / 9 - 1) * k.csf[2], 0.0f);
+}
+
 // Density over the candidate list, one thread per particle: the step's
 // exact pair test (FP64 path: the FP64 separation of MCF; FP32 path: the
 // FP32 test of k_density's scan, same operation order), the step's neighbour
@@ -404,10 +414,13 @@ __global__ void __launch_bounds__(kReuseTPB)
   constexpr int CENTER = (D == 3) ? 13 : 4;
   __shared__ int s_start[NS * kReuseTPB];
   __shared__ int s_shift[NS * kReuseTPB];
+  __shared__ float4 s_slot[kMaxStencil];
   const int n = k.n, tid = threadIdx.x;
   const int i = blockIdx.x * kReuseTPB + tid;
   int my_max = 0;
   unsigned long long my_pairs = 0;
+  fill_slot_offsets(k, s_slot);
+  __syncthreads();
   if (i < n) {
     build_lane_table<D, kReuseTPB>(k, cell_of[i], cell_start, s_start, s_shift);
     const int li = i - s_start[CENTER * kReuseTPB + tid];
@@ -464,9 +477,8 @@ __global__ void __launch_bounds__(kReuseTPB)
           const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
           const int j = jg[u];
           const float4 oj = og[u];
-          const float sx = (float)(sl % 3 - 1) * k.csf[0];
-          const float sy = (float)((sl / 3) % 3 - 1) * k.csf[1];
-          const float sz = (D == 3) ? (float)(sl / 9 - 1) * k.csf[2] : 0.0f;
+          const float4 so = s_slot[sl];
+          const float sx = so.x, sy = so.y, sz = (D == 3) ? so.z : 0.0f;
           // the pair test as k_density's scan rounds it: (o_i - slot) - o_j
           const float tx = (oi.x - sx) - oj.x, ty = (oi.y - sy) - oj.y;
           float t2 = tx * tx + ty * ty;
@@ -862,6 +874,9 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
   const int n = k.n;
   const bool noise = k.noise != 0;
   const bool walls = k.wall_axis != -1;
+  __shared__ float4 s_slot[kMaxStencil];
+  fill_slot_offsets(k, s_slot);
+  __syncthreads();
   const int i = blockIdx.x * kReuseTPB + threadIdx.x;
   if (i >= n) return;
   build_lane_table<D, kReuseTPB>(k, cell_of[i], cell_start, s_start, s_shift);
@@ -899,11 +914,10 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
     if (si != 0 && sj != 0 && !(si > 0 && sj > 0 && si != sj && k.pp_cc)) continue;
     const int sl = cur.sl;
     T r[3];
-    const float sx = (float)(sl % 3 - 1) * k.csf[0];
-    const float sy = (float)((sl / 3) % 3 - 1) * k.csf[1];
-    r[0] = (oi.x - cur.o.x) - sx;
-    r[1] = (oi.y - cur.o.y) - sy;
-    r[2] = (D == 3) ? (oi.z - cur.o.z) - (float)(sl / 9 - 1) * k.csf[2] : 0.f;
+    const float4 so = s_slot[sl];
+    r[0] = (oi.x - cur.o.x) - so.x;
+    r[1] = (oi.y - cur.o.y) - so.y;
+    r[2] = (D == 3) ? (oi.z - cur.o.z) - so.z : 0.f;
     T d2 = r[0] * r[0] + r[1] * r[1];
     if (D == 3) d2 += r[2] * r[2];
     const T inv_d = rsqrtf(d2);
