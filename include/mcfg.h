@@ -43,6 +43,7 @@ extern "C" {
  * wall_solid 9, Lees-Edwards 10 */
 #define MCFG_BC_PERIODIC 1
 #define MCFG_BC_WALL_SOLID 9
+#define MCFG_BC_LE 10
 
 #define MCFG_PRECISION_FP64 0       /* pair arithmetic in FP64              */
 #define MCFG_PRECISION_FP32_MIXED 1 /* FP32 pair arithmetic, FP64 state     */
@@ -52,7 +53,10 @@ extern "C" {
  * mcf_config/physics_config.mcf. */
 typedef struct mcfg_params {
   int32_t num_dim;            /* 2 or 3                                      */
-  int32_t bcdef[6];           /* per face x-,x+,y-,y+,z-,z+: 1 or 9          */
+  int32_t bcdef[6];           /* per face x-,x+,y-,y+,z-,z+: 1 periodic, 9
+                                 solid wall, 10 Lees-Edwards (y faces only:
+                                 planes sliding along x; x, z periodic with
+                                 min_phys_t 0; no walls or colloids)        */
   double min_phys[3];         /* fluid domain                                */
   double max_phys[3];
   double min_phys_t[3];       /* total domain incl. wall layers              */
@@ -84,7 +88,9 @@ typedef struct mcfg_params {
   double body_force[3];
   int32_t wall_noslip_type;   /* 1 frozen, 2 Morris extrapolation            */
   int32_t stress_tensor;      /* 1: accumulate per-particle stress s(d^2,N) */
-  double wall_v[6][3];        /* velocity of each solid wall face (shear_v)  */
+  double wall_v[6][3];        /* velocity of each solid-wall or Lees-Edwards
+                                 face (MCF's shear_v0; a Lees-Edwards pair
+                                 may differ only along x)                    */
   double init_density;        /* constant density of boundary particles      */
   int32_t Newtonian;          /* 1 Newtonian; 0 Oldroyd-B conformation model */
   int32_t precision;          /* MCFG_PRECISION_*                            */
@@ -148,6 +154,9 @@ typedef struct mcfg_info {
   int64_t device_bytes;   /* device memory held by the handle               */
   int64_t list_rebuilds;  /* candidate-list rebuilds so far (list reuse)    */
   double skin;            /* list-reuse skin (0: reuse off)                  */
+  double time_current;    /* MCF's time_current (advanced by dt per step)    */
+  double shear_length;    /* Lees-Edwards offset along x of the images above
+                             the y+ face at the last boundary update        */
 } mcfg_info;
 
 /* Create a handle on params->device.  Replaces the construction of MCF's
@@ -244,6 +253,25 @@ int mcfg_update_state(mcfg_handle* h, const double* x, const double* v, const do
  * x,v,f: [n*d]; rho,p: [n]; ct: [n*d*d]; s: [n*d*d] (stress_tensor). */
 int mcfg_download(mcfg_handle* h, double* x, double* v, double* rho,
                   double* p, double* f, double* ct, double* s);
+
+/* Moving boundaries, MCF's Boundary object (Class_Boundary.F90: shear_type,
+ * shear_v0 = mcfg_params.wall_v, shear_freq) and its time: shear_type[f] 2
+ * makes solid-wall face f oscillate, shear_v = wall_v[f] cos(shear_freq[f] t)
+ * (boundary_update_boundary.F90:78-98); any other value keeps
+ * shear_v = wall_v[f].  time is MCF's time_current before the next step
+ * (marching_marching.F90:330); mcfg_step_vv and mcfg_run_vv advance it by dt
+ * first, as marching_marching.F90:1393 does.  With solid walls or
+ * Lees-Edwards faces a VV step then follows marching_integrate_VV.F90:
+ * 783-806 and 1650-1675: boundary update at (time + dt, time + dt/2), wall
+ * particles drift with their velocity (particles_integrate_boundary_
+ * position.F90), and take the face's shear_v at time + dt at the end of the
+ * step (particles_set_boundary_velocity.F90).  Lees-Edwards images above the
+ * y+ face sit at x + (wall_v[3][0] - wall_v[2][0]) (time + dt) modulo L_x
+ * (ppm_bcdef_le_y.inc) with velocity + (wall_v[3][0] - wall_v[2][0])
+ * (particles_set_boundary_ghost_velocity.F90).  Without this call every
+ * shear_type is 0 and time_current starts at 0. */
+int mcfg_set_boundary_motion(mcfg_handle* h, const int32_t* shear_type /* [6] */,
+                             const double* shear_freq /* [6] */, double time);
 
 /* Colloid state for the pair terms: centres x[nc*d], velocities v[nc*d],
  * angular velocities omega[nc*3], radii radius[nc].  The colloid pair

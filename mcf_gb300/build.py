@@ -38,6 +38,10 @@ def _flags() -> list[str]:
         *ARCH,
         "-Xcompiler",
         "-fPIC",
+        # host arithmetic (boundary updates, constants) rounded as written on
+        # both x86-64 and aarch64 hosts, like the oracle
+        "-Xcompiler",
+        "-ffp-contract=off",
         "-Xptxas",
         "-warn-spills",
         "-I",

@@ -16,8 +16,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .params import (BC_PERIODIC, BC_WALL_SOLID, PRECISION_FP64, ColloidParams, SDPDParams,
-                     make_params)
+from .params import (BC_LE, BC_PERIODIC, BC_WALL_SOLID, PRECISION_FP64, ColloidParams,
+                     SDPDParams, make_params)
 
 BASE_SEED = 20261203
 
@@ -175,6 +175,52 @@ def c5_oldroyd_b_2d(n_side: int = 128, precision: int = PRECISION_FP64, seed: in
                     Newtonian=0, tau=1.0, n_p=1.0, kt_p=0.5, body_force_type=3,
                     body_force=[amplitude, 0.0, 0.0], dt=1e-3, precision=precision, seed=seed)
     return _finish(f"C5 2D {n_side}^2 Oldroyd-B", p, [1.0, 1.0], 0.0, 0.0, seed, 1e-3, 200)
+
+
+def lees_edwards(dim: int = 3, n_side: int = 24, shear_rate: float = 0.05,
+                 precision: int = PRECISION_FP64, seed: int = BASE_SEED + 6,
+                 kt: float = 0.0) -> Workload:
+    """Simple shear through Lees-Edwards y faces (bcdef 10, the planes above
+    and below slide along x at +-shear_rate L/2, boundary_update_boundary.F90
+    and ppm_bcdef_le_y.inc), periodic x (and z), dx = 1, box starting at 0:
+    C2's physics (quintic rc = 3, Hu-Adams, c = 10, eta = 1), dt = 1e-3,
+    particles jittered by 0.05 dx, velocities on the linear profile
+    v_x = shear_rate (y - L/2) plus N(0, 1e-4)."""
+    L = float(n_side)
+    box = _box(dim, 0.0, L)
+    box["bcdef"][2] = box["bcdef"][3] = BC_LE
+    wv = [[0.0] * 3 for _ in range(6)]
+    wv[2][0] = -0.5 * shear_rate * L
+    wv[3][0] = 0.5 * shear_rate * L
+    p = make_params(**box, cut_off=3.0, c=10.0, eta=1.0, kt=kt, Brownian=1 if kt > 0 else 0,
+                    body_force_type=0, dt=1e-3, precision=precision, seed=seed, wall_v=wv)
+    w = _finish(f"Lees-Edwards {dim}D {n_side}^{dim} shear {shear_rate}", p, [1.0] * dim, 0.05,
+                1e-4, seed, 1e-3, 1000)
+    w.v[:, 0] += shear_rate * (w.x[:, 1] - 0.5 * L)
+    return w
+
+
+def couette_walls(dim: int = 2, n_side: int = 32, v_top: float = 0.05,
+                  precision: int = PRECISION_FP64, seed: int = BASE_SEED + 7) -> Workload:
+    """Couette / oscillating-wall flow between solid y walls (Morris no-slip,
+    4 layers each side): the top wall moves along x at v_top (MCF's
+    shear_v0 of face y+), the bottom one rests; wall particles start with
+    their face velocity.  Periodic x (and z), dx = 1, C2's physics, dt = 1e-3.
+    mcfg_set_boundary_motion with shear_type[3] = 2 turns the top wall into
+    an oscillating one."""
+    L = float(n_side)
+    nl = wall_layers(3.0, 1.0)
+    box = _box(dim, 0.0, L, walls_axis=1, nwall_layers=nl, dx=1.0)
+    wv = [[0.0] * 3 for _ in range(6)]
+    wv[3][0] = v_top
+    p = make_params(**box, cut_off=3.0, c=10.0, eta=1.0, kt=0.0, Brownian=0,
+                    wall_noslip_type=2, wall_rho_type=0, init_density=1.0, body_force_type=0,
+                    dt=1e-3, precision=precision, seed=seed, wall_v=wv)
+    w = _finish(f"Couette {dim}D {n_side}^{dim} v_top {v_top}", p, [1.0] * dim, 0.05, 1e-4, seed,
+                1e-3, 1000)
+    top = w.id[:, 1] == -4
+    w.v[top, 0] = v_top
+    return w
 
 
 @dataclass

@@ -391,10 +391,9 @@ __global__ void __launch_bounds__(kAdjTPB)
                 uint32_t step, double inv_sqdt, double4_32a* __restrict__ xbs,
                 double4_32a* __restrict__ vbs, double* __restrict__ cbs,
                 double* __restrict__ nbar, double* __restrict__ gp, int split) {
-  constexpr int NS = (D == 3) ? 27 : 9;
   constexpr int D2 = D * D;
-  __shared__ int s_start[NS * kAdjTPB];
-  __shared__ int s_shift[NS * kAdjTPB];
+  __shared__ int s_start[kMaxStencil * kAdjTPB];
+  __shared__ int s_shift[kMaxStencil * kAdjTPB];
   const int n = k.n;
   const bool noise = k.noise != 0;
   const double eta = k.eta, kt = k.kt;
@@ -631,9 +630,8 @@ __global__ void __launch_bounds__(kAdjTPB)
                   const double* __restrict__ cbs, int drift, double dt,
                   double4_32a* __restrict__ xb_h, double4_32a* __restrict__ vb_h,
                   double* __restrict__ cb_h, int split) {
-  constexpr int NS = (D == 3) ? 27 : 9;
-  __shared__ int s_start[NS * kAdjTPB];
-  __shared__ int s_shift[NS * kAdjTPB];
+  __shared__ int s_start[kMaxStencil * kAdjTPB];
+  __shared__ int s_shift[kMaxStencil * kAdjTPB];
   const int n = k.n;
   const int tid = threadIdx.x;
   const int g_ = blockIdx.x * kAdjTPB + tid;

@@ -166,16 +166,28 @@ const char* validate_params(const mcfg_params* p) {
   if (!p->Newtonian && p->rhs_force_type != 3)
     return "the Oldroyd-B model needs rhs_force_type 3 (Hu-Adams)";
   if (!p->Newtonian && !(std::fabs(p->tau) > 1e-14)) return "tau should not be zero";
+  const bool le = p->bcdef[2] == MCFG_BC_LE || p->bcdef[3] == MCFG_BC_LE;
   for (int a = 0; a < p->num_dim; ++a) {
     const int lo = p->bcdef[2 * a], hi = p->bcdef[2 * a + 1];
-    if ((lo != MCFG_BC_PERIODIC && lo != MCFG_BC_WALL_SOLID) ||
-        (hi != MCFG_BC_PERIODIC && hi != MCFG_BC_WALL_SOLID))
-      return "bcdef: only periodic (1) and solid wall (9) faces are supported";
+    const bool le_ok = (a == 1 && lo == MCFG_BC_LE && hi == MCFG_BC_LE);
+    if (!le_ok && ((lo != MCFG_BC_PERIODIC && lo != MCFG_BC_WALL_SOLID) ||
+                   (hi != MCFG_BC_PERIODIC && hi != MCFG_BC_WALL_SOLID)))
+      return "bcdef: periodic (1) and solid wall (9) faces, Lees-Edwards (10) on both y faces";
     if ((lo == MCFG_BC_PERIODIC) != (hi == MCFG_BC_PERIODIC))
       return "bcdef: a periodic face needs a periodic opposite face";
+    if (le && a != 1) {
+      // the images' x (and z) are MODULO(x + shear_length, L): the box
+      // starts at 0 on the other axes, which are periodic
+      if (lo != MCFG_BC_PERIODIC)
+        return "Lees-Edwards y faces need periodic x (and z) faces, no solid walls";
+      if (p->min_phys_t[a] != 0.0 || p->min_phys[a] != 0.0)
+        return "Lees-Edwards: the box must start at 0 along x (and z)";
+    }
     if (!(p->max_phys_t[a] > p->min_phys_t[a])) return "max_phys_t must exceed min_phys_t";
     if (!(p->max_phys[a] > p->min_phys[a])) return "max_phys must exceed min_phys";
   }
+  if (le && p->num_dim == 3 && p->wall_v[2][2] != p->wall_v[3][2])
+    return "Lees-Edwards: the y faces may slide only along x (wall_v[2][2] == wall_v[3][2])";
   if (p->rhs_force_type == 1 && p->rhs_density_type != 1)
     return "rhs_force_type 1 (Morris) needs rhs_density_type 1 (mass density)";
   if (p->stateEquation_type == 2 && (p->rho_ref == 0.0 || p->gamma == 0.0))
@@ -220,8 +232,18 @@ void make_consts(const mcfg_params& p, Consts& k) {
   }
   k.rc2 = p.cut_off * p.cut_off;
   k.rc2f = (float)k.rc2;
+  // Lees-Edwards y faces: 3 (2D: 1) more stencil slots for the fourth x
+  // cell of the row across the face; the offsets follow the time
+  // (boundary_update)
+  k.le = (k.d >= 2 && p.bcdef[2] == MCFG_BC_LE) ? 1 : 0;
+  k.ns = (k.d == 3 ? 27 : 9) + (k.le ? (k.d == 3 ? 3 : 1) : 0);
+  k.walls = 0;
+  for (int f = 0; f < 2 * k.d; ++f)
+    if (p.bcdef[f] == MCFG_BC_WALL_SOLID) k.walls = 1;
   k.reuse = 0;
-  if (p.reserved[1] != 0) {
+  // the candidate list's images would have to follow the Lees-Edwards
+  // offset between rebuilds: list reuse stays off with Lees-Edwards faces
+  if (p.reserved[1] != 0 && !k.le) {
     double csmin = 1e300;
     for (int a = 0; a < k.d; ++a) csmin = std::min(csmin, k.cs[a]);
     const double skin = 0.99 * (csmin - p.cut_off);
@@ -278,7 +300,9 @@ void make_consts(const mcfg_params& p, Consts& k) {
     for (int a = 0; a < 3; ++a) {
       k.wall_v[f][a] = p.wall_v[f][a];
       k.wall_vf[f][a] = (float)p.wall_v[f][a];
+      k.wall_v_end[f][a] = p.wall_v[f][a];
     }
+  if (k.le) k.le_dv = p.wall_v[3][0] - p.wall_v[2][0];
   k.stress = p.stress_tensor ? 1 : 0;
   k.newtonian = p.Newtonian ? 1 : 0;
   k.G = p.n_p * p.kt_p;
@@ -563,7 +587,50 @@ int rhs_reuse(Handle* h, int64_t step, int fuse_mode, double dt) {
 }
 
 // one VV step of mcfg_step_vv / mcfg_run_vv
+// boundary_update_boundary.F90 (shear velocities of oscillating walls at
+// time_v, Lees-Edwards shear_length at time_r) into the constants the
+// kernels take by value; wall_v_end is the end-of-step update at
+// (time_r, time_r) of marching_integrate_VV.F90:1657.  Host libm cos, as
+// MCF's.
+void boundary_update(Handle* h, double time_r, double time_v) {
+  Consts& k = h->k;
+  const mcfg_params& p = h->p;
+  for (int f = 0; f < 6; ++f) {
+    // :78-98, only with walls (num_wall > 0)
+    const bool osc = k.walls && h->shear_type[f] == 2;
+    for (int a = 0; a < 3; ++a) {
+      const double v0 = p.wall_v[f][a];
+      const double vh = osc ? v0 * std::cos(h->shear_freq[f] * time_v) : v0;
+      const double ve = osc ? v0 * std::cos(h->shear_freq[f] * time_r) : v0;
+      k.wall_v[f][a] = vh;
+      k.wall_vf[f][a] = (float)vh;
+      k.wall_v_end[f][a] = ve;
+    }
+  }
+  if (k.le) {
+    // :102-122: images above the y+ face shift by (v0(y+) - v0(y-)) time_r
+    // along x; the stencil of the rows across the face follows S mod L_x
+    const double S = (p.wall_v[3][0] - p.wall_v[2][0]) * time_r;
+    k.le_S = S;
+    const double L = k.len[0];
+    double sm = std::fmod(S, L);
+    if (sm < 0.0) sm += L;
+    const double q = sm * k.rdx[0];
+    const double cu = std::ceil(q), cl = std::floor(q);
+    k.le_cu = (int)cu % k.nm[0];
+    k.le_cl = (int)cl % k.nm[0];
+    k.le_pu = cu - q;
+    k.le_pl = q - cl;
+  }
+}
+
 int vv_step(Handle* h, int64_t step, double dt) {
+  // marching_marching.F90:1393 advances time_current before the step; the
+  // step updates the boundaries at (time + dt, time + dt/2),
+  // marching_integrate_VV.F90:783-806
+  h->time_current = h->time_current + dt;
+  if (h->k.walls || h->k.le)
+    boundary_update(h, h->time_current + dt, h->time_current + 0.5 * dt);
   if (!h->k.reuse) {
     TRY(kdw(h, dt));
     return rhs(h, step, kForceBodyKick, dt);
@@ -625,13 +692,21 @@ int mcfg_create(const mcfg_params* params, mcfg_handle** out) {
   h->dt = params->dt;
   fill_consts(h);
   for (int a = 0; a < h->k.d; ++a) {
-    if (h->k.periodic[a] && h->k.nm[a] < 3) {
+    if ((h->k.periodic[a] || (h->k.le && a == 1)) && h->k.nm[a] < 3) {
       std::lock_guard<std::mutex> lk(g_create_mu);
       g_create_err = "a periodic axis needs at least 3 cells (box >= 3*1.0001*cut_off)";
       delete h;
       return MCFG_EINVAL;
     }
   }
+  if (h->k.le && h->k.nm[0] < 4) {
+    // the row across a Lees-Edwards face spans four x cells
+    std::lock_guard<std::mutex> lk(g_create_mu);
+    g_create_err = "Lees-Edwards needs at least 4 cells along x (box >= 4*1.0001*cut_off)";
+    delete h;
+    return MCFG_EINVAL;
+  }
+  boundary_update(h, h->time_current, h->time_current);
   if (cudaSetDevice(h->device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
     std::lock_guard<std::mutex> lk(g_create_mu);
@@ -685,6 +760,8 @@ int mcfg_get_info(const mcfg_handle* h, mcfg_info* info) {
         cudaStreamSynchronize(h->stream) == cudaSuccess)
       info->list_rebuilds = cntr[1];
   }
+  info->time_current = h->time_current;
+  info->shear_length = h->k.le ? h->k.le_S : 0.0;
   return MCFG_OK;
 }
 
@@ -907,9 +984,26 @@ int mcfg_integrate_position(mcfg_handle* h, double dt) {
 int mcfg_init_force(mcfg_handle* h, int64_t step) {
   GUARD(h);
   if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  // marching_marching.F90:437: boundaries at time_current
+  boundary_update(h, h->time_current, h->time_current);
   TRY(adjust_particles(h));
   TRY(rhs(h, step, kForceBody, h->dt));
   return check_device_errors(h);
+}
+
+int mcfg_set_boundary_motion(mcfg_handle* h, const int32_t* shear_type, const double* shear_freq,
+                             double time) {
+  GUARD(h);
+  if (!shear_type || !shear_freq) return set_error(h, MCFG_EINVAL, "NULL shear_type / shear_freq");
+  for (int f = 0; f < 6; ++f) {
+    if (shear_type[f] == 2 && h->p.bcdef[f] != MCFG_BC_WALL_SOLID)
+      return set_error(h, MCFG_EINVAL, "shear_type 2 (oscillating) needs a solid-wall face");
+    h->shear_type[f] = shear_type[f];
+    h->shear_freq[f] = shear_freq[f];
+  }
+  h->time_current = time;
+  boundary_update(h, time, time);
+  return MCFG_OK;
 }
 
 int mcfg_step_vv(mcfg_handle* h, int64_t step, double dt) {
@@ -1019,7 +1113,7 @@ int mcfg_set_colloids(mcfg_handle* h, const mcfg_colloid_params* cp, const doubl
                       const double* v, const double* omega, const double* radius) {
   GUARD(h);
   if (!cp || cp->num_colloid < 0) return set_error(h, MCFG_EINVAL, "bad colloid parameters");
-  const int nc = cp->num_colloid, d = h->p.num_dim;
+  const int nc = cp->num_colloid;
   if (nc > 0 && (!x || !v || !omega || !radius))
     return set_error(h, MCFG_EINVAL, "mcfg_set_colloids: NULL array");
   if (!h->have_particles) return set_error(h, MCFG_ESTATE, "upload the particles first");
@@ -1027,6 +1121,8 @@ int mcfg_set_colloids(mcfg_handle* h, const mcfg_colloid_params* cp, const doubl
     return set_error(h, MCFG_EINVAL, "a particle's sid exceeds num_colloid");
   if (cp->noslip_type < 1 || cp->noslip_type > 2)
     return set_error(h, MCFG_ENOTSUP, "colloid noslip_type must be 1 (frozen) or 2 (Morris)");
+  if (h->k.le && nc > 0)
+    return set_error(h, MCFG_ENOTSUP, "colloids with Lees-Edwards faces are not supported");
   h->cp = *cp;
   h->crad.assign(radius, radius + nc);
   if (nc > 0) {

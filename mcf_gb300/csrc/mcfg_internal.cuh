@@ -14,7 +14,13 @@
 namespace mcfg {
 
 constexpr int kWarp = 32;
-constexpr int kMaxStencil = 27;   // 3D full stencil (9 in 2D)
+constexpr int kMaxStencil = 30;   // 3D full stencil 27 (2D 9) + 3 (1) Lees-Edwards slots
+// neighbour-slot shift word: 2 bits per axis (1: image at x + L, 2: the home
+// particle's image at x + L), and the Lees-Edwards crossings: kLeUp, the
+// neighbour is a particle of the bottom row imaged above the y+ face;
+// kLeDown, the home particle is the bottom-row one imaged above
+constexpr int kLeUp = 1 << 8;
+constexpr int kLeDown = 1 << 9;
 constexpr int kLocalBits = 11;    // neighbour entry: slot<<11 | local index
 constexpr int kMaxCellCount = 1 << kLocalBits;  // particles per cell limit
 constexpr double kPi = 3.141592653589793238;    // mcf_header.F90:50
@@ -59,6 +65,21 @@ struct Consts {
   float etaf, eta_coeff, ktf;
   float wall_vf[6][3];   // FP32 copy of wall_v
   int wall_axis;         // the single solid-wall axis, -1 if none, -2 if several
+  // moving boundaries (boundary_update_boundary.F90): wall_v holds MCF's
+  // shear_v at the step's half time (the no-slip velocity), wall_v_end at its
+  // end (particles_set_boundary_velocity.F90); with solid walls, wall
+  // particles drift with their velocity and take wall_v_end after the step
+  int walls;
+  double wall_v_end[6][3];
+  // Lees-Edwards y faces (planes sliding along x): stencil of ns slots (27/9
+  // + 3/1 when le), images above the y+ face at x + le_S modulo L_x with
+  // velocity + le_dv; the crossing rows' x cells start le_cu + 1 cells left
+  // (top row) / le_cl - 1 cells right (bottom row) of the home cell, and
+  // their FP32 slot offsets are shifted by -le_pu / -le_pl cell sides
+  int le, ns;
+  double le_S, le_dv;
+  int le_cu, le_cl;
+  double le_pu, le_pl;
   // physics
   int rhs_density_type, rhs_force_type, eos_type;
   double c2, rho_ref, gamma, p0;
@@ -95,6 +116,10 @@ struct Handle {
   int cap_n = 0;           // allocated particle capacity
   int neigh_cap = 0;       // neighbour list capacity per particle
   double dt = 0.0;
+  // moving boundaries: MCF's shear_type / shear_freq per face and time_current
+  int32_t shear_type[6] = {0, 0, 0, 0, 0, 0};
+  double shear_freq[6] = {0, 0, 0, 0, 0, 0};
+  double time_current = 0.0;
   int64_t launches = 0;
   int64_t device_bytes = 0;
   int64_t num_outside = 0;
@@ -258,6 +283,10 @@ int kick_ct_half(Handle* h, double dt);
 int rhs(Handle* h, int64_t step, int fuse_mode, double dt);
 int kdw(Handle* h, double dt);
 void free_adjoint(Handle* h);
+// MCF's boundary_update_boundary(time_r, time_v) into the constants: wall
+// shear velocities at time_v (and at time_r for the end of the step),
+// Lees-Edwards offset at time_r
+void boundary_update(Handle* h, double time_r, double time_v);
 int colloid_drag(Handle* h, double* drag, double* torque);
 int colloid_move(Handle* h, const double* d_xnew, const double* d_rot);
 int check_device_errors(Handle* h);

@@ -240,6 +240,10 @@ int mcfg_density_noalloc(const mcfg_params* params, int32_t n, const double* x, 
   Consts k;
   make_consts(*params, k);
   k.n = n;
+  if (k.le) {
+    g_err = "mcfg_density_noalloc: Lees-Edwards faces are not supported here";
+    return MCFG_ENOTSUP;
+  }
   if (k.ncell > kNoAllocMaxCells) {
     char buf[160];
     snprintf(buf, sizeof buf,

@@ -163,7 +163,6 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
               double4_32a* __restrict__ pc, float4* __restrict__ pcf, float4* __restrict__ vf,
               int with_pressure, unsigned* __restrict__ err, int* __restrict__ stats,
               unsigned long long* __restrict__ pairs, NN nn, CollArgs ca) {
-  constexpr int NS = (D == 3) ? 27 : 9;
   constexpr int CENTER = (D == 3) ? 13 : 4;
   __shared__ NbTable tab[kWarpsPerBlock];
   __shared__ float4 sb[kWarpsPerBlock][kStage];
@@ -185,7 +184,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       int cnt = 0;
       // phase 1: candidate scan, offsets of each neighbour cell staged in
       // shared memory by coalesced loads, then broadcast to the lanes
-      for (int sl = 0; sl < NS; ++sl) {
+      for (int sl = 0; sl < k.ns; ++sl) {
         const int js = t.start[sl], jn = t.count[sl];
         const float4 so = t.o[sl];
         const float px = oi.x - so.x, py = oi.y - so.y, pz = oi.z - so.z;
@@ -325,7 +324,6 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
                    const float4* __restrict__ off, uint16_t* __restrict__ vl,
                    int* __restrict__ vcount, int vcap, unsigned* __restrict__ err) {
   if (*gate == 0) return;
-  constexpr int NS = (D == 3) ? 27 : 9;
   constexpr int CENTER = (D == 3) ? 13 : 4;
   __shared__ NbTable tab[kWarpsPerBlock];
   __shared__ float4 sb[kWarpsPerBlock][kStage];
@@ -341,7 +339,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       const bool active = i < c1;
       const float4 oi = active ? off[i] : make_float4(0.f, 0.f, 0.f, 0.f);
       int cnt = 0;
-      for (int sl = 0; sl < NS; ++sl) {
+      for (int sl = 0; sl < k.ns; ++sl) {
         const int js = t.start[sl], jn = t.count[sl];
         const float4 so = t.o[sl];
         const float px = oi.x - so.x, py = oi.y - so.y, pz = oi.z - so.z;
@@ -384,13 +382,23 @@ __global__ void k_rebuild_done(int* __restrict__ flag) {
 constexpr int kReuseTPB = 128;
 
 // FP32 offset of each stencil slot (the neighbour cell's origin minus the
-// home cell's), the same products as build_table's t.o, in a block-shared
-// table: the block's first threads fill it, then __syncthreads.
+// home cell's, w = Lees-Edwards velocity jump), build_table's t.o, in a
+// block-shared table of kSlotTable entries: slot s of a home cell in
+// Lees-Edwards state st at st * kMaxStencil + s.  The block's first threads
+// fill it, then __syncthreads.
+constexpr int kSlotTable = 3 * kMaxStencil;
+static_assert(kSlotTable <= kReuseTPB, "one thread per slot-table entry");
+template <int D>
 __device__ __forceinline__ void fill_slot_offsets(const Consts& k, float4* s_slot) {
-  const int s = threadIdx.x;
-  if (s < kMaxStencil)
-    s_slot[s] = make_float4((float)(s % 3 - 1) * k.csf[0], (float)((s / 3) % 3 - 1) * k.csf[1],
-                            (float)(s / 9 - 1) * k.csf[2], 0.0f);
+  const int e = threadIdx.x;
+  if (e < kSlotTable) s_slot[e] = slot_offset<D>(k, e % kMaxStencil, e / kMaxStencil);
+}
+
+// slot offsets of the Lees-Edwards row state of the home cell
+__device__ __forceinline__ const float4* slot_table(const Consts& k, const float4* s_slot,
+                                                   int cell) {
+  if (!k.le || cell >= k.ncell) return s_slot;
+  return s_slot + le_state(k, (cell / k.nm[0]) % k.nm[1]) * kMaxStencil;
 }
 
 // Density over the candidate list, one thread per particle: the step's
@@ -410,16 +418,15 @@ __global__ void __launch_bounds__(kReuseTPB)
                     float4* __restrict__ vf, int with_pressure, unsigned* __restrict__ err,
                     int* __restrict__ stats, unsigned long long* __restrict__ pairs, NN nn,
                     CollArgs ca) {
-  constexpr int NS = (D == 3) ? 27 : 9;
   constexpr int CENTER = (D == 3) ? 13 : 4;
-  __shared__ int s_start[NS * kReuseTPB];
-  __shared__ int s_shift[NS * kReuseTPB];
-  __shared__ float4 s_slot[kMaxStencil];
+  __shared__ int s_start[kMaxStencil * kReuseTPB];
+  __shared__ int s_shift[kMaxStencil * kReuseTPB];
+  __shared__ float4 s_slot[kSlotTable];
   const int n = k.n, tid = threadIdx.x;
   const int i = blockIdx.x * kReuseTPB + tid;
   int my_max = 0;
   unsigned long long my_pairs = 0;
-  fill_slot_offsets(k, s_slot);
+  fill_slot_offsets<D>(k, s_slot);
   __syncthreads();
   if (i < n) {
     build_lane_table<D, kReuseTPB>(k, cell_of[i], cell_start, s_start, s_shift);
@@ -604,6 +611,13 @@ __device__ __forceinline__ void force_epilogue(const Consts& k, int i, int si, c
       vv.x = __dadd_rn(vv.x, __dmul_rn(__dmul_rn(0.5, ax), dt));
       vv.y = __dadd_rn(vv.y, __dmul_rn(__dmul_rn(0.5, ay), dt));
       if (D == 3) vv.z = __dadd_rn(vv.z, __dmul_rn(__dmul_rn(0.5, az), dt));
+    } else if (si < 0 && k.walls) {
+      // end of the step: the face's shear velocity (moving walls)
+      double vs[3] = {vv.x, vv.y, vv.z};
+      wall_end_velocity<D>(k, si, vs);
+      vv.x = vs[0];
+      vv.y = vs[1];
+      if (D == 3) vv.z = vs[2];
     }
     v_out[i] = vv;
   }
@@ -651,11 +665,10 @@ __global__ void __launch_bounds__(kReuseTPB)
               double4_32a* __restrict__ f, double* __restrict__ st, int fuse_mode, double dt,
               double4_32a* __restrict__ v_out, uint32_t step, double inv_sqdt,
               unsigned* __restrict__ err, NN nn, CollArgs ca) {
-  constexpr int NS = (D == 3) ? 27 : 9;
   constexpr int D2 = D * D;
   using T = double;
-  __shared__ int s_start[NS * kReuseTPB];
-  __shared__ int s_shift[NS * kReuseTPB];
+  __shared__ int s_start[kMaxStencil * kReuseTPB];
+  __shared__ int s_shift[kMaxStencil * kReuseTPB];
   const int n = k.n;
   const bool noise = k.noise != 0;
   const int i = blockIdx.x * kReuseTPB + threadIdx.x;
@@ -692,12 +705,14 @@ __global__ void __launch_bounds__(kReuseTPB)
     const double4_32a xj4 = x[j];
     const double xj[3] = {xj4.x, xj4.y, xj4.z};
     T r[3];
-    const double d2 = exact_sep<D>(k, xi, xj, s_shift[sl * kReuseTPB + threadIdx.x], r);
+    const int shj = s_shift[sl * kReuseTPB + threadIdx.x];
+    const double d2 = exact_sep<D>(k, xi, xj, shj, r);
     const T inv_d = rsqrt(d2);
     const T d = d2 * inv_d;
     const double4_32a v4 = v[j];
     T vi[3] = {v4i.x, v4i.y, v4i.z};
     T vj[3] = {v4.x, v4.y, v4.z};
+    if (shj >= kLeUp) le_velocity<T>(k, shj, vi, vj);
     const double4_32a cj = pc[j];
     T Ai = ci.x, Aj = cj.x, Bi = ci.y, Bj = cj.y;
     T qj[1 + D2], qie[1 + D2];
@@ -864,22 +879,23 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
               double* __restrict__ st, int fuse_mode, double dt,
               double4_32a* __restrict__ v_out, uint32_t step, float inv_sqdt,
               unsigned* __restrict__ err, NN nn, CollArgs ca) {
-  constexpr int NS = (D == 3) ? 27 : 9;
   constexpr int D2 = D * D;
   using T = float;
   // one thread per particle, whatever its cell: per-thread neighbour-cell
   // tables keep every lane busy (2D cells hold ~9 particles)
-  __shared__ int s_start[NS * kReuseTPB];
-  __shared__ int s_shift[NS * kReuseTPB];
+  __shared__ int s_start[kMaxStencil * kReuseTPB];
+  __shared__ int s_shift[kMaxStencil * kReuseTPB];
   const int n = k.n;
   const bool noise = k.noise != 0;
   const bool walls = k.wall_axis != -1;
-  __shared__ float4 s_slot[kMaxStencil];
-  fill_slot_offsets(k, s_slot);
+  __shared__ float4 s_slot[kSlotTable];
+  fill_slot_offsets<D>(k, s_slot);
   __syncthreads();
   const int i = blockIdx.x * kReuseTPB + threadIdx.x;
   if (i >= n) return;
-  build_lane_table<D, kReuseTPB>(k, cell_of[i], cell_start, s_start, s_shift);
+  const int celli = cell_of[i];
+  build_lane_table<D, kReuseTPB>(k, celli, cell_start, s_start, s_shift);
+  const float4* slot_tab = slot_table(k, s_slot, celli);
   const float4 oi = off[i];
   const int si = __float_as_int(oi.w);
   const float4 v4i = vf[i];
@@ -914,7 +930,7 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
     if (si != 0 && sj != 0 && !(si > 0 && sj > 0 && si != sj && k.pp_cc)) continue;
     const int sl = cur.sl;
     T r[3];
-    const float4 so = s_slot[sl];
+    const float4 so = slot_tab[sl];
     r[0] = (oi.x - cur.o.x) - so.x;
     r[1] = (oi.y - cur.o.y) - so.y;
     r[2] = (D == 3) ? (oi.z - cur.o.z) - so.z : 0.f;
@@ -923,7 +939,7 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
     const T inv_d = rsqrtf(d2);
     const T d = d2 * inv_d;
     T vi[3] = {v4i.x, v4i.y, v4i.z};
-    T vj[3] = {cur.v.x, cur.v.y, cur.v.z};
+    T vj[3] = {cur.v.x + so.w, cur.v.y, cur.v.z};
     T Ai = ci.x, Aj = cur.c.x, Bi = ci.y, Bj = cur.c.y;
     T qj[1 + D2], qie[1 + D2];
     if (nnw) {
@@ -1584,7 +1600,7 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
   const NN nn{h->ct, h->act, h->vgt, h->qq};
   const CollArgs ca{h->v, h->rxc, h->rxcf};
   const int gp = std::max(1, ((int)h->n + kReuseTPB - 1) / kReuseTPB);
-  if (!k.stress && h->jp && fp64 && k.newtonian && k.ncoll == 0) {
+  if (!k.stress && h->jp && fp64 && k.newtonian && k.ncoll == 0 && !k.le) {
     // symmetric sweep + per-particle gather: halves the FP64 pair work; the
     // FP32 path keeps the two-sided sweep, which is faster there (the
     // symmetric sweep's shared-memory partner sums cap its occupancy)

@@ -6,6 +6,7 @@
 // particles_apply_body_force.F90:96-353, marching_integrate_VV.F90:303-322,
 // statistic_compute_statistic.F90:230-303.
 #include "mcfg_internal.cuh"
+#include "pair_common.cuh"
 #include "sph.cuh"
 
 namespace mcfg {
@@ -37,9 +38,36 @@ __device__ __forceinline__ void wrap_axis(const Consts& k, int a,
   }
 }
 
-// flags: 1 half kick, 2 drift, 4 wrap, 8 conformation-tensor half step.
+// particles_adjust_particles.F90:228-257, 352-381: a particle leaving
+// through a Lees-Edwards y face re-enters through the other one with the
+// other coordinates MODULO(x - shear_length, L) (x: shear_length(x, y-) =
+// -S, (x, y+) = S; z: 0) and the x velocity jump shear_v(y+/-) -
+// shear_v(y-/+).  MCF then checks no further axis for it (EXIT).
+template <int D>
+__device__ __forceinline__ bool le_wrap(const Consts& k, double* xs, double* vs) {
+  double sl;
+  if (xs[1] < k.min_phys[1]) {
+    xs[1] = __dadd_rn(xs[1], k.len[1]);
+    sl = -k.le_S;
+    vs[0] = __dadd_rn(vs[0], k.le_dv);
+  } else if (xs[1] >= k.max_phys[1]) {
+    xs[1] = __dsub_rn(xs[1], k.len[1]);
+    sl = k.le_S;
+    vs[0] = __dadd_rn(vs[0], -k.le_dv);
+  } else {
+    return false;
+  }
+  xs[0] = f_modulo(__dsub_rn(xs[0], sl), k.len[0]);
+  if (D == 3) xs[2] = f_modulo(xs[2], k.len[2]);
+  return true;
+}
+
+// flags: 1 half kick, 2 drift, 4 wrap, 8 conformation-tensor half step,
+// 16 end of a VV step (wall particles take their face's velocity).
 // The arithmetic is rounded exactly like MCF's: v + (lambda*f)*dt,
-// x + v*dt, ct + act*dt*lambda (no fused multiply-add).
+// x + v*dt, ct + act*dt*lambda (no fused multiply-add).  With solid walls
+// the drift also moves wall particles with their velocity
+// (particles_integrate_boundary_position.F90, marching_integrate_VV.F90:797).
 template <int D>
 __global__ void k_integrate(Consts k, int flags, double dt, double lambda,
                             double4_32a* __restrict__ x, double4_32a* __restrict__ v,
@@ -69,10 +97,22 @@ __global__ void k_integrate(Consts k, int flags, double dt, double lambda,
 #pragma unroll
       for (int a = 0; a < D; ++a) xs[a] = __dadd_rn(xs[a], __dmul_rn(vs[a], dt));
     }
+  } else if (s < 0 && k.walls) {
+    if (flags & 2) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) xs[a] = __dadd_rn(xs[a], __dmul_rn(vs[a], dt));
+    }
+    if (flags & 16) wall_end_velocity<D>(k, s, vs);
   }
   if (flags & 4) {
 #pragma unroll
-    for (int a = 0; a < D; ++a) wrap_axis(k, a, s, xs[a], vs[a]);
+    for (int a = 0; a < D; ++a) {
+      if (a == 1 && k.le) {
+        if (s >= 0 && le_wrap<D>(k, xs, vs)) break;
+      } else {
+        wrap_axis(k, a, s, xs[a], vs[a]);
+      }
+    }
   }
   x[i] = make_double4_32a(xs[0], xs[1], D == 3 ? xs[2] : 0.0, 0.0);
   v[i] = make_double4_32a(vs[0], vs[1], D == 3 ? vs[2] : 0.0, 0.0);
@@ -319,6 +359,13 @@ __global__ void k_kdw_reuse(Consts k, double dt, double4_32a* __restrict__ x,
       xv = make_double4_32a(xs[0], xs[1], D == 3 ? xs[2] : 0.0, 0.0);
       x[i] = xv;
       v[i] = make_double4_32a(vs[0], vs[1], D == 3 ? vs[2] : 0.0, 0.0);
+    } else if (s < 0 && k.walls) {
+      // wall particles drift with their velocity
+      const double4_32a vv = v[i];
+      xv.x = __dadd_rn(xv.x, __dmul_rn(vv.x, dt));
+      xv.y = __dadd_rn(xv.y, __dmul_rn(vv.y, dt));
+      if (D == 3) xv.z = __dadd_rn(xv.z, __dmul_rn(vv.z, dt));
+      x[i] = xv;
     }
     const double4_32a xr = x_ref[i];
     const double dx = xv.x - xr.x, dy = xv.y - xr.y, dz = (D == 3) ? xv.z - xr.z : 0.0;
@@ -418,7 +465,7 @@ int adjust_particles(Handle* h) {
   return launch_integrate(h, 4, 0.0, 0.0);
 }
 int kick_ct_half(Handle* h, double dt) {
-  return launch_integrate(h, h->p.Newtonian ? 1 : 9, dt, 0.5);
+  return launch_integrate(h, (h->p.Newtonian ? 1 : 9) | 16, dt, 0.5);
 }
 int kick_drift_wrap(Handle* h, double dt) {
   return launch_integrate(h, h->p.Newtonian ? 7 : 15, dt, 0.5);

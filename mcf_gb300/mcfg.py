@@ -78,6 +78,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "mcfg_colloid_drag": (C.c_int, [_h, _dp, _dp]),
         "mcfg_move_colloids": (C.c_int, [_h, _dp, _dp, _dp, _dp]),
         "mcfg_colloid_repulsion": (C.c_int, [_h, _dp]),
+        "mcfg_set_boundary_motion": (C.c_int, [_h, C.POINTER(C.c_int32), _dp, C.c_double]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -154,7 +155,18 @@ class SDPD:
             "device_bytes": inf.device_bytes,
             "list_rebuilds": inf.list_rebuilds,
             "skin": inf.skin,
+            "time_current": inf.time_current,
+            "shear_length": inf.shear_length,
         }
+
+    def set_boundary_motion(self, shear_type, shear_freq, time: float = 0.0) -> None:
+        """MCF's Boundary shear_type / shear_freq per face (2 = oscillating
+        solid wall) and time_current (mcfg_set_boundary_motion)."""
+        st = np.ascontiguousarray(shear_type, dtype=np.int32).reshape(6)
+        sf = np.ascontiguousarray(shear_freq, dtype=np.float64).reshape(6)
+        self._check("mcfg_set_boundary_motion",
+                    self.lib.mcfg_set_boundary_motion(self._h, st.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                      _ptr(sf, C.c_double), float(time)))
 
     # -- data --------------------------------------------------------------
     def upload(self, x, v, m, id_, ct=None) -> None:

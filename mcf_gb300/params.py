@@ -34,6 +34,7 @@ STATUS_NAMES = {
 
 BC_PERIODIC = 1
 BC_WALL_SOLID = 9
+BC_LE = 10  # Lees-Edwards (y faces, sliding along x)
 PRECISION_FP64 = 0
 PRECISION_FP32_MIXED = 1
 
@@ -117,6 +118,8 @@ class SDPDInfo(C.Structure):
         ("device_bytes", C.c_int64),
         ("list_rebuilds", C.c_int64),
         ("skin", C.c_double),
+        ("time_current", C.c_double),
+        ("shear_length", C.c_double),
     ]
 
 

@@ -57,6 +57,15 @@ struct orc_state {
   /* colloids (Class_Colloid): centre, velocity, angular velocity, radius */
   mcfg_colloid_params cp;
   double *cx, *cv, *com, *crad;
+  /* moving boundaries (Class_Boundary.F90): shear_type, shear_freq, the
+   * current shear_v per face, Lees-Edwards shear_length along x of the y+
+   * face (the y- face's is its negative), time_current */
+  int walls, le;
+  int32_t shear_type[6];
+  double shear_freq[6];
+  double shear_v[6][3];
+  double le_S;
+  double time_current;
   double timers[4];
   char err[256];
 };
@@ -248,6 +257,8 @@ orc_state* orc_create(const mcfg_params* p, char* err, int errlen) {
     msg = "the Oldroyd-B model needs rhs_force_type 3 (Hu-Adams)";
   else if (!p->Newtonian && !(fabs(p->tau) > 1e-14))
     msg = "tau should not be zero";
+  else if ((p->bcdef[2] == MCFG_BC_LE) != (p->bcdef[3] == MCFG_BC_LE))
+    msg = "Lees-Edwards faces come in pairs";
   if (msg) {
     if (err) snprintf(err, (size_t)errlen, "%s", msg);
     return NULL;
@@ -267,8 +278,47 @@ orc_state* orc_create(const mcfg_params* p, char* err, int errlen) {
     s->len[i] = p->max_phys_t[i] - p->min_phys_t[i];
     s->periodic[i] = (p->bcdef[2 * i] == MCFG_BC_PERIODIC);
   }
+  /* boundary_set_bcdef (boundary_set.F90): num_shear counts wall and
+   * Lees-Edwards faces; shear_v starts at shear_v0 (boundary_set_shear_v0) */
+  for (int f = 0; f < 2 * s->d; ++f) {
+    if (p->bcdef[f] == MCFG_BC_WALL_SOLID) s->walls = 1;
+    if (p->bcdef[f] == MCFG_BC_LE) s->le = 1;
+  }
+  memcpy(s->shear_v, p->wall_v, sizeof s->shear_v);
   s->nthreads = 1;
   return s;
+}
+
+/* boundary_update_boundary.F90:78-122: oscillating solid walls
+ * shear_v = shear_v0 cos(shear_freq time_v) (with walls), Lees-Edwards
+ * shear_length = (shear_v0(y+) - shear_v0(y-)) time_r along x */
+static void boundary_update(orc_state* s, double time_r, double time_v) {
+  for (int f = 0; f < 6; ++f)
+    if (s->walls && s->shear_type[f] == 2)
+      for (int a = 0; a < 3; ++a)
+        s->shear_v[f][a] = s->p.wall_v[f][a] * cos(s->shear_freq[f] * time_v);
+  if (s->le) s->le_S = (s->p.wall_v[3][0] - s->p.wall_v[2][0]) * time_r;
+}
+
+int orc_set_boundary_motion(orc_state* s, const int32_t* shear_type, const double* shear_freq,
+                            double time) {
+  for (int f = 0; f < 6; ++f) {
+    s->shear_type[f] = shear_type[f];
+    s->shear_freq[f] = shear_freq[f];
+  }
+  s->time_current = time;
+  boundary_update(s, time, time);
+  return 0;
+}
+
+double orc_time(const orc_state* s) { return s->time_current; }
+
+/* gfortran's MODULO for reals (p > 0): fmod, plus p for a negative
+ * remainder */
+static double f_modulo(double a, double p) {
+  double r = fmod(a, p);
+  if (r < 0.0) r = r + p;
+  return r;
 }
 
 static void free_arrays(orc_state* s) {
@@ -355,6 +405,32 @@ int orc_adjust_particles(orc_state* s) {
   for (int64_t j = 0; j < s->nreal; ++j) {
     for (int i = 0; i < d; ++i) {
       double* xi = &s->x[j * d + i];
+      if (s->p.bcdef[2 * i] == MCFG_BC_LE) {
+        /* particles_adjust_particles.F90:228-257, 352-381: through the
+         * lower face x(i) + length, the others MODULO(x(k) -
+         * shear_length(k, 2i-1), length(k)), v(k) + shear_v(k, 2i) -
+         * shear_v(k, 2i-1); the upper face alike; then no further axis
+         * (EXIT).  shear_length(x, y-) = -S, (x, y+) = S, 0 along z. */
+        if (s->sid[j] < 0) continue;
+        int face = 0;
+        if (*xi < mn[i])
+          face = 1;
+        else if (*xi >= mx[i])
+          face = 2;
+        if (face == 0) continue;
+        const double lk = mx[i] - mn[i];
+        *xi = (face == 1) ? *xi + lk : *xi - lk;
+        for (int k = 0; k < d; ++k) {
+          if (k == i) continue;
+          const double sl = (k == 0) ? (face == 1 ? -s->le_S : s->le_S) : 0.0;
+          const double lenk = mx[k] - mn[k];
+          s->x[j * d + k] = f_modulo(s->x[j * d + k] - sl, lenk);
+          const double jump = (face == 1) ? s->shear_v[2 * i + 1][k] - s->shear_v[2 * i][k]
+                                          : s->shear_v[2 * i][k] - s->shear_v[2 * i + 1][k];
+          s->v[j * d + k] = s->v[j * d + k] + jump;
+        }
+        break;
+      }
       if (*xi < mn[i]) {
         if (s->p.bcdef[2 * i] == MCFG_BC_PERIODIC) {
           *xi = *xi + s->len[i];
@@ -402,6 +478,42 @@ static void copy_particle(orc_state* s, int64_t to, int64_t from) {
 static void ghost_get(orc_state* s) {
   const int d = s->d;
   s->nall = s->nreal;
+  if (s->le) {
+    /* ppm_bcdef_le_y.inc (before the periodic images,
+     * ppm_map_part_ghost_get.F90:776-800): a particle with y in
+     * [min, min + ghostsize) gets an image at y + len, other coordinates
+     * MODULO(x + shear_length(x, y+), len); without symmetry also
+     * (max - ghostsize, max] at y - len with shear_length(x, y-) */
+    const double ymin = s->p.min_phys[1], ymax = s->p.max_phys[1];
+    const double ly = ymax - ymin;
+    const int64_t nnow = s->nall;
+    for (int64_t i = 0; i < nnow; ++i) {
+      const double yv = s->x[i * d + 1];
+      if (yv >= ymin && yv < ymin + s->gs) {
+        ensure_cap(s, s->nall + 1);
+        copy_particle(s, s->nall, i);
+        double* xg = &s->x[s->nall * d];
+        xg[1] = yv + ly;
+        xg[0] = f_modulo(xg[0] + s->le_S, s->p.max_phys[0] - s->p.min_phys[0]);
+        if (d == 3) xg[2] = f_modulo(xg[2] + 0.0, s->p.max_phys[2] - s->p.min_phys[2]);
+        s->nall++;
+      }
+    }
+    if (!s->p.symmetry) {
+      for (int64_t i = 0; i < nnow; ++i) {
+        const double yv = s->x[i * d + 1];
+        if (yv > ymax - s->gs && yv <= ymax) {
+          ensure_cap(s, s->nall + 1);
+          copy_particle(s, s->nall, i);
+          double* xg = &s->x[s->nall * d];
+          xg[1] = yv - ly;
+          xg[0] = f_modulo(xg[0] - s->le_S, s->p.max_phys[0] - s->p.min_phys[0]);
+          if (d == 3) xg[2] = f_modulo(xg[2] + 0.0, s->p.max_phys[2] - s->p.min_phys[2]);
+          s->nall++;
+        }
+      }
+    }
+  }
   for (int dim = 0; dim < d; ++dim) {
     if (!s->periodic[dim]) continue;
     const double xminf = s->p.min_phys_t[dim], xmini = xminf + s->gs;
@@ -440,6 +552,18 @@ static void ghost_refresh(orc_state* s) {
     s->pr[g] = s->pr[o];
     memcpy(&s->v[g * d], &s->v[o * d], sizeof(double) * (size_t)d);
     memcpy(&s->ct[g * d2], &s->ct[o * d2], sizeof(double) * (size_t)d2);
+    if (s->le) {
+      /* particles_set_boundary_ghost_velocity.F90: a ghost beyond a
+       * Lees-Edwards face moves with the face velocity difference */
+      const double yg = s->x[g * d + 1];
+      for (int k = 0; k < d; ++k) {
+        if (k == 1) continue;
+        if (yg < s->p.min_phys[1])
+          s->v[g * d + k] = s->v[g * d + k] + (s->shear_v[2][k] - s->shear_v[3][k]);
+        else if (yg >= s->p.max_phys[1])
+          s->v[g * d + k] = s->v[g * d + k] + (s->shear_v[3][k] - s->shear_v[2][k]);
+      }
+    }
   }
 }
 
@@ -1155,7 +1279,7 @@ static void wall_noslip(const orc_state* s, const double* xf, const double* xw,
                         const double* vf, double* vw, int32_t sid_w) {
   const int d = s->d;
   const int index_w = sid_w < 0 ? -sid_w : sid_w;
-  const double* sv = s->p.wall_v[index_w - 1];
+  const double* sv = s->shear_v[index_w - 1];
   if (s->p.wall_noslip_type <= 1) {
     for (int a = 0; a < d; ++a) vw[a] = sv[a];
     return;
@@ -1444,20 +1568,34 @@ static int rhs(orc_state* s, int64_t step) {
   return rc;
 }
 
-/* marching_marching.F90:528-911 (initial right-hand side) */
+/* marching_marching.F90:528-911 (initial right-hand side), boundaries
+ * updated at time_current first (:437) */
 int orc_init_force(orc_state* s, int64_t step) {
+  if (s->walls || s->le) boundary_update(s, s->time_current, s->time_current);
   int rc = orc_adjust_particles(s);
   if (rc) return rc;
   return rhs(s, step);
 }
 
-/* marching_integrate_VV.F90:303-1620 */
+/* marching_integrate_VV.F90:303-1620; time_current advanced first
+ * (marching_marching.F90:1393) */
 int orc_step_vv(orc_state* s, int64_t step, double dt) {
   set_dt(s, dt);
+  s->time_current = s->time_current + dt;
+  const double time = s->time_current;
+  const int d = s->d;
   double t0 = now_s();
   orc_integrate_velocity(s, dt, 0.5);
   orc_integrate_position(s, dt);
   if (!s->p.Newtonian) integrate_ct(s, dt, 0.5); /* marching_integrate_VV.F90:413 */
+  if (s->walls || s->le) {
+    /* :783-806: boundary update, wall particles x + v dt
+     * (particles_integrate_boundary_position.F90) */
+    boundary_update(s, time + dt, time + 0.5 * dt);
+    for (int64_t j = 0; j < s->nreal; ++j)
+      if (s->sid[j] < 0)
+        for (int a = 0; a < d; ++a) s->x[j * d + a] = s->x[j * d + a] + s->v[j * d + a] * dt;
+  }
   orc_adjust_particles(s);
   s->timers[3] += now_s() - t0;
   int rc = rhs(s, step);
@@ -1465,6 +1603,16 @@ int orc_step_vv(orc_state* s, int64_t step, double dt) {
   t0 = now_s();
   if (!s->p.Newtonian) integrate_ct(s, dt, 0.5); /* :1511 */
   orc_integrate_velocity(s, dt, 0.5);
+  if (s->walls || s->le) {
+    /* :1650-1675: boundary update at the end of the step, wall particles
+     * take their face's shear_v (particles_set_boundary_velocity.F90) */
+    boundary_update(s, time + dt, time + dt);
+    for (int64_t j = 0; j < s->nreal; ++j)
+      if (s->sid[j] < 0) {
+        const int f = -s->sid[j] - 1;
+        for (int a = 0; a < d; ++a) s->v[j * d + a] = s->shear_v[f][a];
+      }
+  }
   s->timers[3] += now_s() - t0;
   return 0;
 }

@@ -54,6 +54,11 @@ int orc_integrate_position(orc_state* s, double dt);
 int orc_init_force(orc_state* s, int64_t step);
 int orc_step_vv(orc_state* s, int64_t step, double dt);
 int orc_run_vv(orc_state* s, int64_t step0, int32_t nsteps, double dt);
+/* moving boundaries: shear_type[6] (2 = oscillating solid wall),
+ * shear_freq[6], MCF's time_current (advanced by dt at every step) */
+int orc_set_boundary_motion(orc_state* s, const int32_t* shear_type, const double* shear_freq,
+                            double time);
+double orc_time(const orc_state* s);
 int orc_download(orc_state* s, double* x, double* v, double* rho, double* p,
                  double* f, double* ct, double* s_out);
 int orc_statistics(orc_state* s, double* k_energy, double* momentum,

@@ -54,6 +54,8 @@ def load(rebuild: bool = True) -> C.CDLL:
         "orc_init_force": (C.c_int, [_h, C.c_int64]),
         "orc_step_vv": (C.c_int, [_h, C.c_int64, C.c_double]),
         "orc_run_vv": (C.c_int, [_h, C.c_int64, C.c_int32, C.c_double]),
+        "orc_set_boundary_motion": (C.c_int, [_h, C.POINTER(C.c_int32), _dp, C.c_double]),
+        "orc_time": (C.c_double, [_h]),
         "orc_download": (C.c_int, [_h, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
         "orc_statistics": (C.c_int, [_h, _dp, _dp, _dp]),
         "orc_counts": (C.c_int, [_h, C.POINTER(C.c_int64)]),
@@ -191,6 +193,17 @@ class Oracle:
 
     def run_vv(self, step0, nsteps, dt):
         self._check("run_vv", self.lib.orc_run_vv(self._h, int(step0), int(nsteps), float(dt)))
+
+    def set_boundary_motion(self, shear_type, shear_freq, time: float = 0.0):
+        st = np.ascontiguousarray(shear_type, dtype=np.int32).reshape(6)
+        sf = np.ascontiguousarray(shear_freq, dtype=np.float64).reshape(6)
+        self._check("orc_set_boundary_motion",
+                    self.lib.orc_set_boundary_motion(self._h, _ptr(st, C.c_int32),
+                                                     _ptr(sf, C.c_double), float(time)))
+
+    @property
+    def time(self) -> float:
+        return float(self.lib.orc_time(self._h))
 
     def statistic_compute_statistic(self):
         ke = C.c_double()
