@@ -42,14 +42,6 @@ __device__ __forceinline__ void slot_dirs(int s, int st, int* o) {
   }
 }
 
-template <int D>
-__device__ __forceinline__ bool slot_crosses(int s, int st) {
-  if (st == 0) return false;
-  int o[3];
-  slot_dirs<D>(s, st, o);
-  return o[1] == ((st == 1) ? 1 : -1);
-}
-
 // Neighbour cell of home cell c (coordinates) in slot s, -1 if none, and
 // the slot's shift word.  Periodic axes wrap with an image bit; across a
 // Lees-Edwards face the x cells of the row are those of the images' x
