@@ -22,7 +22,9 @@ steps and the same step with MCF's cell list rebuilt every step;
 path on the same workload.  `e2e` is the same metric through the C-ABI with host
 buffers: every step hands x, v, f over from pinned host memory
 (mcfg_update_state), runs mcfg_step_vv and downloads x, v, f (masses and
-ids go over once, before the timed steps).  `cpu_baseline` is the CPU restatement
+ids go over once, before the timed steps).  `output_write` times MCF's
+particle output file of the workload written through mcfg_write_particles
+(E16.8 text formatted on the device).  `cpu_baseline` is the CPU restatement
 of MCF's path (the oracle; MCF itself cannot be built here) on the host
 cores.  With --impl reference only that CPU path is timed.
 
@@ -71,6 +73,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-list-reuse", action="store_true")
+    ap.add_argument("--no-output", action="store_true")
     ap.add_argument("--accuracy-steps", type=int, default=200)
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     return ap.parse_args()
@@ -524,6 +527,24 @@ def run_ours(args, ws, rank, local):
                "d2h_bytes_per_step": int(n * 3 * 8 * 3), "steps": ke,
                "path": "mcfg_update_state(x, v, f) + mcfg_step_vv + mcfg_download(x, v, f) per "
                        "step from pinned host buffers (masses and ids uploaded once before)"}
+    output = None
+    if rank == 0 and not args.no_output:
+        # MCF's particle output file of the whole workload, formatted on the
+        # device (E16.8, io_write_particles.F90), copied once, written once
+        import shutil
+        tmpd = tempfile.mkdtemp(prefix="mcfg_out_")
+        try:
+            path = os.path.join(tmpd, "mcf_particles00000001.out")
+            sd.write_particles(path)  # buffers allocated on the first call
+            t0 = time.perf_counter()
+            sd.write_particles(path)
+            tw = time.perf_counter() - t0
+            nbytes = os.path.getsize(path)
+        finally:
+            shutil.rmtree(tmpd, ignore_errors=True)
+        output = {"particles": int(w.n), "bytes": int(nbytes), "seconds": tw,
+                  "path": "mcfg_write_particles: device E16.8 formatting, one device-to-host "
+                          "copy, one fwrite (to a temporary file)"}
     adjoint = None
     if not args.no_adjoint:
         w5 = configs.c5_oldroyd_b_2d()
@@ -550,7 +571,7 @@ def run_ours(args, ws, rank, local):
                    "neighbour_capacity": info["neigh_capacity"], "max_neigh": info["max_neigh"],
                    "pairs_per_step": info["num_pairs"], "list_reuse": list_reuse},
         "roofline": roof, "fp64": fp64, "fp32_error_vs_fp64": err, "e2e": e2e,
-        "adjoint": adjoint,
+        "adjoint": adjoint, "output_write": output,
         "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
         "pair_interactions_per_s": info["num_pairs"] * args.steps * ws / tmax,
     }

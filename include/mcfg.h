@@ -254,6 +254,18 @@ int mcfg_update_state(mcfg_handle* h, const double* x, const double* v, const do
 int mcfg_download(mcfg_handle* h, double* x, double* v, double* rho,
                   double* p, double* f, double* ct, double* s);
 
+/* MCF's particle files, formatted on the device in host order and written
+ * to path in one host write.  kind 0: the particle output of
+ * io_write_particles.F90:225-403 (name it as MCF does,
+ * TRIM(output_particles_file)//I8.8 step//'.out'); kind 1: the restart file
+ * of io_write_restart_particles.F90:100-215 (the particle count first,
+ * list-directed).  One record per particle, format (<ncol>E16.8): x(d) v(d)
+ * rho m pid sid, and with flags & 1 (kind 0, stress_tensor on) the stress
+ * components s(2) s(3) of MCF's __IO_PARTICLES_STRESS_TOTAL build.  E16.8
+ * digits are the correctly rounded decimal values (ties to even), exact for
+ * magnitudes in [1e-18, 1e30). */
+int mcfg_write_particles(mcfg_handle* h, const char* path, int32_t kind, int32_t flags);
+
 /* Moving boundaries, MCF's Boundary object (Class_Boundary.F90: shear_type,
  * shear_v0 = mcfg_params.wall_v, shear_freq) and its time: shear_type[f] 2
  * makes solid-wall face f oscillate, shear_v = wall_v[f] cos(shear_freq[f] t)

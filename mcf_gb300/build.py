@@ -19,7 +19,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libmcfg.so"
-SOURCES = ["mcfg_api.cu", "cell_list.cu", "pair_kernels.cu", "update.cu", "noalloc.cu", "adjoint.cu"]
+SOURCES = ["mcfg_api.cu", "cell_list.cu", "pair_kernels.cu", "update.cu", "noalloc.cu", "adjoint.cu",
+           "output.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -107,6 +107,11 @@ int dalloc(Handle* h, T** p, size_t count) {
 
 void free_all(Handle* h) {
   free_adjoint(h);
+  if (h->out_dev) cudaFree(h->out_dev);
+  if (h->out_host) cudaFreeHost(h->out_host);
+  h->out_dev = nullptr;
+  h->out_host = nullptr;
+  h->out_cap = 0;
   for (void* p : {(void*)h->x_ref, (void*)h->vl, (void*)h->vcount, (void*)h->d_rebuild})
     if (p) cudaFree(p);
   h->x_ref = nullptr;
@@ -989,6 +994,15 @@ int mcfg_init_force(mcfg_handle* h, int64_t step) {
   TRY(adjust_particles(h));
   TRY(rhs(h, step, kForceBody, h->dt));
   return check_device_errors(h);
+}
+
+int mcfg_write_particles(mcfg_handle* h, const char* path, int32_t kind, int32_t flags) {
+  GUARD(h);
+  if (!path) return set_error(h, MCFG_EINVAL, "NULL path");
+  if (kind != 0 && kind != 1) return set_error(h, MCFG_EINVAL, "kind must be 0 (output) or 1 (restart)");
+  if (kind == 1 && (flags & 1)) return set_error(h, MCFG_EINVAL, "the restart file has no stress");
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  return write_particle_file(h, path, kind, flags);
 }
 
 int mcfg_set_boundary_motion(mcfg_handle* h, const int32_t* shear_type, const double* shear_freq,

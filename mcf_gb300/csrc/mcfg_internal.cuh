@@ -198,6 +198,10 @@ struct Handle {
   int* d_rebuild = nullptr;      // [0] rebuild request, [1] rebuilds done
   bool reuse_valid = false;      // the candidate list matches the particle order
   bool unwrapped = false;        // positions may lie outside periodic faces (list reuse)
+  // ---- particle-file text (output.cu), grow-only, null until the first write ----
+  char* out_dev = nullptr;
+  char* out_host = nullptr;  // pinned
+  size_t out_cap = 0;
   // ---- adjoint buffers (adjoint.cu), null until mcfg_adjoint_run ----
   struct AdjBuffers* adj = nullptr;
   // ---- per-phase device timers ----
@@ -287,6 +291,9 @@ void free_adjoint(Handle* h);
 // shear velocities at time_v (and at time_r for the end of the step),
 // Lees-Edwards offset at time_r
 void boundary_update(Handle* h, double time_r, double time_v);
+// MCF's particle output (kind 0) or restart (kind 1) file formatted on the
+// device; flags & 1 adds the stress columns s(2), s(3)
+int write_particle_file(Handle* h, const char* path, int kind, int flags);
 int colloid_drag(Handle* h, double* drag, double* torque);
 int colloid_move(Handle* h, const double* d_xnew, const double* d_rot);
 int check_device_errors(Handle* h);

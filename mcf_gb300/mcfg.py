@@ -79,6 +79,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "mcfg_move_colloids": (C.c_int, [_h, _dp, _dp, _dp, _dp]),
         "mcfg_colloid_repulsion": (C.c_int, [_h, _dp]),
         "mcfg_set_boundary_motion": (C.c_int, [_h, C.POINTER(C.c_int32), _dp, C.c_double]),
+        "mcfg_write_particles": (C.c_int, [_h, C.c_char_p, C.c_int32, C.c_int32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -158,6 +159,14 @@ class SDPD:
             "time_current": inf.time_current,
             "shear_length": inf.shear_length,
         }
+
+    def write_particles(self, path, kind: int = 0, stress: bool = False) -> None:
+        """MCF's particle output (kind 0, io_write_particles) or restart
+        (kind 1, io_write_restart_particles) file, formatted on the device
+        (mcfg_write_particles)."""
+        self._check("mcfg_write_particles",
+                    self.lib.mcfg_write_particles(self._h, str(path).encode(), int(kind),
+                                                  1 if stress else 0))
 
     def set_boundary_motion(self, shear_type, shear_freq, time: float = 0.0) -> None:
         """MCF's Boundary shear_type / shear_freq per face (2 = oscillating

@@ -1,0 +1,54 @@
+"""CPU restatement of MCF's particle-file text.  TEST INFRASTRUCTURE ONLY:
+the checker of the device formatter (mcfg_write_particles); the product
+never imports it.
+
+MCF writes its particle output (io_write_particles.F90:225-403) and restart
+files (io_write_restart_particles.F90:100-215) with ppm_io in ASCII mode:
+WRITE(unit, '(<ncol>E16.8)') of the (ncol, N) array, one record per
+particle; the restart file first writes the particle count list-directed
+(ppm_io_write_ascii.F90: WRITE(unit, *)).  E16.8 with the default scale
+factor prints [-]0.d1...d8 followed by E+ee, or +eee when the exponent
+exceeds 99, right-justified in 16 columns; the eight digits here are
+Python's correctly rounded ones (ties to even), the C library's %.7E.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def e16_8(x: float) -> str:
+    x = float(x)
+    if math.isnan(x):
+        return "NaN".rjust(16)
+    if math.isinf(x):
+        return ("-Infinity" if x < 0 else "Infinity").rjust(16)
+    neg = math.copysign(1.0, x) < 0
+    ax = abs(x)
+    if ax == 0.0:
+        digits, e = "00000000", 0
+    else:
+        mant, ex = f"{ax:.7e}".split("e")
+        digits = mant.replace(".", "")
+        e = int(ex) + 1
+    body = ("-" if neg else "") + "0." + digits
+    if abs(e) <= 99:
+        body += "E" + ("-" if e < 0 else "+") + f"{abs(e):02d}"
+    else:
+        body += ("-" if e < 0 else "+") + f"{abs(e):03d}"
+    return body.rjust(16)
+
+
+def particle_rows(x, v, rho, m, ids, s=None) -> str:
+    """x(d) v(d) rho m pid sid [s(2) s(3)] per particle, (ncol E16.8)."""
+    cols = [np.asarray(x, float), np.asarray(v, float), np.asarray(rho, float)[:, None],
+            np.asarray(m, float)[:, None], np.asarray(ids, float)]
+    if s is not None:
+        cols.append(np.asarray(s, float)[:, 1:3])
+    table = np.concatenate(cols, axis=1)
+    return "".join("".join(e16_8(val) for val in row) + "\n" for row in table)
+
+
+def restart_text(x, v, rho, m, ids) -> str:
+    return f"{x.shape[0]:12d}\n" + particle_rows(x, v, rho, m, ids)
