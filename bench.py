@@ -20,9 +20,10 @@ them exactly (config.list_reuse gives the skin, the rebuilds inside the timed
 steps and the same step with MCF's cell list rebuilt every step;
 --no-list-reuse times that mode as the headline).  `fp64` is the plain FP64
 path on the same workload.  `e2e` is the same metric through the C-ABI with host
-buffers: every step hands x, v, f over from pinned host memory
-(mcfg_update_state), runs mcfg_step_vv and downloads x, v, f (masses and
-ids go over once, before the timed steps).  `output_write` times MCF's
+buffers: every step is one mcfg_step_vv_host call that hands x, v over from
+pinned host memory, runs the step and copies x, v back (the positions' copy
+overlapping the sweeps on a second stream); masses, ids and the initial
+forces go over once, before the timed steps.  `output_write` times MCF's
 particle output file of the workload written through mcfg_write_particles
 (E16.8 text formatted on the device).  `cpu_baseline` is the CPU restatement
 of MCF's path (the oracle; MCF itself cannot be built here) on the host
@@ -499,18 +500,15 @@ def run_ours(args, ws, rank, local):
         dp = C.POINTER(C.c_double)
 
         def step_e2e(s):
-            # MCF's per-step drop-in: hand the state over, step, read it back
-            rc = sd.lib.mcfg_update_state(sd._h, hx.ctypes.data_as(dp), hv.ctypes.data_as(dp),
-                                          hf.ctypes.data_as(dp))
-            if rc == 0:
-                rc = sd.lib.mcfg_step_vv(sd._h, s, w.dt)
-            if rc == 0:
-                rc = sd.lib.mcfg_download(sd._h, hx.ctypes.data_as(dp), hv.ctypes.data_as(dp),
-                                          None, None, hf.ctypes.data_as(dp), None, None)
+            # MCF's per-step drop-in, one call: x, v over, the step, x, v back
+            # (the positions' copy back overlaps the sweeps on a second stream)
+            rc = sd.lib.mcfg_step_vv_host(sd._h, s, w.dt, hx.ctypes.data_as(dp),
+                                          hv.ctypes.data_as(dp))
             if rc != 0:
                 raise RuntimeError(sd.lib.mcfg_last_error(sd._h).decode())
 
-        # the particle set (masses, ids) goes over once; every step carries x, v, f
+        # the particle set (masses, ids) and the initial forces go over once;
+        # every step carries x, v both ways, the forces stay on the device
         sd.upload(hx, hv, hm, hid)
         sd.upload_force(hf)
         for q in range(2):
@@ -523,10 +521,11 @@ def run_ours(args, ws, rank, local):
         torch.cuda.synchronize()
         te = max_over_ranks(time.perf_counter() - t0, ws)
         e2e = {"value": aggregate_throughput(w.n_fluid * ke, te, ws), "unit": UNIT,
-               "h2d_bytes_per_step": int(n * 3 * 8 * 3),
-               "d2h_bytes_per_step": int(n * 3 * 8 * 3), "steps": ke,
-               "path": "mcfg_update_state(x, v, f) + mcfg_step_vv + mcfg_download(x, v, f) per "
-                       "step from pinned host buffers (masses and ids uploaded once before)"}
+               "h2d_bytes_per_step": int(n * 3 * 8 * 2),
+               "d2h_bytes_per_step": int(n * 3 * 8 * 2), "steps": ke,
+               "path": "mcfg_step_vv_host(x, v) per step with pinned host buffers: x, v to the "
+                       "device, the step, x, v back (masses, ids and the initial forces uploaded "
+                       "once before; the forces stay on the device between steps)"}
     output = None
     if rank == 0 and not args.no_output:
         # MCF's particle output file of the whole workload, formatted on the

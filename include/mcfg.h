@@ -239,6 +239,17 @@ int mcfg_step_vv(mcfg_handle* h, int64_t step, double dt);
  * the loop of marching_marching.F90:1329-1531 without I/O. */
 int mcfg_run_vv(mcfg_handle* h, int64_t step0, int32_t nsteps, double dt);
 
+/* One VV step with the state in the caller's host arrays, MCF's per-step
+ * drop-in in one call: x, v [n*d] (pinned memory for full speed) go over,
+ * the step runs (as mcfg_step_vv), and x, v of the new state come back into
+ * the same arrays.  Equivalent to mcfg_update_state(h, x, v, NULL) +
+ * mcfg_step_vv + mcfg_download(h, x, v, ...), but the positions' copy back
+ * runs on a second stream, overlapping the density and force sweeps (the
+ * positions are final once the step's list phase is done).  The forces stay
+ * on the device between steps (MCF does not change them between steps;
+ * mcfg_download returns them on output steps). */
+int mcfg_step_vv_host(mcfg_handle* h, int64_t step, double dt, double* x, double* v);
+
 /* Overwrite the positions, velocities and/or accelerations (any pointer may
  * be NULL) of the particles of the last mcfg_upload, in host order, keeping
  * the device's particle order and neighbour-list state: MCF's per-step

@@ -545,6 +545,7 @@ int rhs(Handle* h, int64_t step, int fuse_mode, double dt) {
     TRY(build_cell_list(h));
   }
   h->have_list = true;
+  if (h->io_x_out) TRY(download_x_async(h));
   {
     PhaseScope ps(h, kPhaseDensity);
     TRY(compute_density(h, true));
@@ -578,6 +579,7 @@ int rhs_reuse(Handle* h, int64_t step, int fuse_mode, double dt) {
     h->reuse_valid = true;
   }
   h->have_list = false;  // stage entry points rebuild MCF's list themselves
+  if (h->io_x_out) TRY(download_x_async(h));
   {
     PhaseScope ps(h, kPhaseDensity);
     TRY(compute_density(h, true, true));
@@ -592,6 +594,22 @@ int rhs_reuse(Handle* h, int64_t step, int fuse_mode, double dt) {
 }
 
 // one VV step of mcfg_step_vv / mcfg_run_vv
+int download_x_async(Handle* h) {
+  const int n = (int)h->n, d = h->p.num_dim;
+  double* stage = h->up_x;  // x | v | (x in) regions of n*3 doubles
+  const int tb = 256, gb = (n + tb - 1) / tb;
+  k_download_pos<<<gb, tb, 0, h->stream>>>(h->k, n, h->hidx, h->x, stage);
+  h->launches++;
+  if (cuda_check(h, cudaGetLastError(), "x out kernel") ||
+      cuda_check(h, cudaEventRecord(h->ev_x, h->stream), "x out event") ||
+      cuda_check(h, cudaStreamWaitEvent(h->copy_stream, h->ev_x, 0), "x out wait") ||
+      cuda_check(h, cudaMemcpyAsync(h->io_x_out, stage, sizeof(double) * (size_t)n * d,
+                                    cudaMemcpyDeviceToHost, h->copy_stream),
+                 "x out"))
+    return MCFG_ECUDA;
+  return MCFG_OK;
+}
+
 // boundary_update_boundary.F90 (shear velocities of oscillating walls at
 // time_v, Lees-Edwards shear_length at time_r) into the constants the
 // kernels take by value; wall_v_end is the end-of-step update at
@@ -734,6 +752,11 @@ int mcfg_destroy(mcfg_handle* h) {
   }
   h->ev_pool.clear();
   free_all(h);
+  if (h->copy_stream) {
+    cudaStreamSynchronize(h->copy_stream);
+    cudaStreamDestroy(h->copy_stream);
+  }
+  if (h->ev_x) cudaEventDestroy(h->ev_x);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return MCFG_OK;
@@ -1026,6 +1049,51 @@ int mcfg_step_vv(mcfg_handle* h, int64_t step, double dt) {
   if (!(dt > 0.0)) return set_error(h, MCFG_EINVAL, "dt must be positive");
   h->dt = dt;
   TRY(vv_step(h, step, dt));
+  return check_device_errors(h);
+}
+
+int mcfg_step_vv_host(mcfg_handle* h, int64_t step, double dt, double* x, double* v) {
+  GUARD(h);
+  if (!h->have_force) return set_error(h, MCFG_ESTATE, "mcfg_init_force must come first");
+  if (!(dt > 0.0)) return set_error(h, MCFG_EINVAL, "dt must be positive");
+  if (!x || !v) return set_error(h, MCFG_EINVAL, "NULL x or v");
+  const int n = (int)h->n, d = h->p.num_dim;
+  if (n == 0) return mcfg_step_vv(h, step, dt);
+  if (!h->copy_stream &&
+      (cuda_check(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking),
+                  "copy stream") ||
+       cuda_check(h, cudaEventCreateWithFlags(&h->ev_x, cudaEventDisableTiming), "copy event")))
+    return MCFG_ECUDA;
+  cudaStream_t s = h->stream;
+  const size_t bytes = sizeof(double) * (size_t)n * d;
+  // the step's inputs: x, v into their particles' current slots
+  if (cuda_check(h, cudaMemcpyAsync(h->up_x + (size_t)n * 6, x, bytes, cudaMemcpyHostToDevice, s),
+                 "x in") ||
+      cuda_check(h, cudaMemcpyAsync(h->up_v, v, bytes, cudaMemcpyHostToDevice, s), "v in"))
+    return MCFG_ECUDA;
+  const int tb = 256, gb = (n + tb - 1) / tb;
+  k_update_state<<<gb, tb, 0, s>>>(h->k, n, h->slot_of, h->up_x + (size_t)n * 6, h->up_v, nullptr,
+                                   h->x, h->v, h->f);
+  h->launches++;
+  if (cuda_check(h, cudaGetLastError(), "update state kernel")) return MCFG_ECUDA;
+  h->have_list = h->have_density = h->have_pressure = false;
+  h->dt = dt;
+  // the step; its list phase starts the positions' copy back (copy stream)
+  h->io_x_out = x;
+  const int rc = vv_step(h, step, dt);
+  h->io_x_out = nullptr;
+  if (rc != MCFG_OK) {
+    cudaStreamSynchronize(h->copy_stream);
+    return rc;
+  }
+  // the step's velocities after the second kick
+  double* stage_v = h->up_x + (size_t)n * 3;
+  k_download<<<gb, tb, 0, s>>>(n, d, h->hidx, h->v, stage_v);
+  h->launches++;
+  if (cuda_check(h, cudaMemcpyAsync(v, stage_v, bytes, cudaMemcpyDeviceToHost, s), "v out") ||
+      cuda_check(h, cudaStreamSynchronize(s), "step sync") ||
+      cuda_check(h, cudaStreamSynchronize(h->copy_stream), "x out sync"))
+    return MCFG_ECUDA;
   return check_device_errors(h);
 }
 

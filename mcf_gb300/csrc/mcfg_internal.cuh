@@ -108,6 +108,12 @@ struct Handle {
   Consts k{};
   int device = 0;
   cudaStream_t stream = nullptr;
+  // mcfg_step_vv_host: a copy stream for the positions' device-to-host copy
+  // (overlapping the density and force sweeps), its event, and the host
+  // array it fills (null outside that call)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_x = nullptr;
+  double* io_x_out = nullptr;
   std::string err;
   bool have_particles = false, have_list = false, have_density = false,
        have_pressure = false, have_force = false;
@@ -291,6 +297,10 @@ void free_adjoint(Handle* h);
 // shear velocities at time_v (and at time_r for the end of the step),
 // Lees-Edwards offset at time_r
 void boundary_update(Handle* h, double time_r, double time_v);
+// inside mcfg_step_vv_host, once the step's list phase has fixed the
+// positions: gather them to host order and copy them to h->io_x_out on the
+// copy stream while the sweeps run
+int download_x_async(Handle* h);
 // MCF's particle output (kind 0) or restart (kind 1) file formatted on the
 // device; flags & 1 adds the stress columns s(2), s(3)
 int write_particle_file(Handle* h, const char* path, int kind, int flags);

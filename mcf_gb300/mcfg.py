@@ -61,6 +61,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "mcfg_init_force": (C.c_int, [_h, C.c_int64]),
         "mcfg_step_vv": (C.c_int, [_h, C.c_int64, C.c_double]),
         "mcfg_run_vv": (C.c_int, [_h, C.c_int64, C.c_int32, C.c_double]),
+        "mcfg_step_vv_host": (C.c_int, [_h, C.c_int64, C.c_double, _dp, _dp]),
         "mcfg_update_state": (C.c_int, [_h, _dp, _dp, _dp]),
         "mcfg_adjoint_run": (C.c_int, [_h, C.c_int64, C.c_int32, C.c_double, C.c_int32, _dp, _dp,
                                        _dp, _dp, _dp, _dp]),
@@ -249,6 +250,16 @@ class SDPD:
 
     def marching_integrate_VV(self, step: int, dt: float) -> None:
         self._check("marching_integrate_VV", self.lib.mcfg_step_vv(self._h, int(step), float(dt)))
+
+    def step_vv_host(self, step: int, dt: float, x: np.ndarray, v: np.ndarray) -> None:
+        """mcfg_step_vv_host: x, v (float64, C-contiguous [n, d]) in, the new
+        state written back into them."""
+        for a in (x, v):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.shape != (self.n, self.dim):
+                raise ValueError("x, v must be C-contiguous float64 [n, d]")
+        self._check("mcfg_step_vv_host",
+                    self.lib.mcfg_step_vv_host(self._h, int(step), float(dt),
+                                               _ptr(x, C.c_double), _ptr(v, C.c_double)))
 
     def run_vv(self, step0: int, nsteps: int, dt: float) -> None:
         self._check("marching_marching", self.lib.mcfg_run_vv(self._h, int(step0), int(nsteps), float(dt)))

@@ -502,3 +502,32 @@ def test_colloid_move_then_steps(gpu_lib):
     db, tb = o.colloid_drag()
     scale = np.abs(db).max() + np.abs(tb).max()
     assert np.max(np.abs(da - db)) <= 1e-9 * scale and np.max(np.abs(ta - tb)) <= 1e-9 * scale
+
+
+def test_step_vv_host_equals_update_step_download(gpu_lib):
+    # the fused host-array step (inputs over, step, positions back on a
+    # second stream, velocities back) against the three calls it replaces,
+    # with and without list reuse, over steps that rebuild the list
+    for reuse in (0, 1):
+        w = jittered_3d(n_side=14)
+        w.params.reserved[1] = reuse
+        outs = []
+        for mode in ("fused", "calls"):
+            g = SDPD(w.params)
+            g.upload(w.x, w.v, w.m, w.id)
+            g.marching_init_force(0)
+            st = g.download("x", "v")
+            x = np.ascontiguousarray(st["x"])
+            v = np.ascontiguousarray(st["v"])
+            for s in range(1, 8):
+                if mode == "fused":
+                    g.step_vv_host(s, w.dt, x, v)
+                else:
+                    g.update_state(x=x, v=v)
+                    g.marching_integrate_VV(s, w.dt)
+                    r = g.download("x", "v")
+                    x, v = np.ascontiguousarray(r["x"]), np.ascontiguousarray(r["v"])
+                v = v * 1.0  # the host owns its arrays between steps
+            outs.append((x.copy(), v.copy()))
+        assert np.array_equal(outs[0][0], outs[1][0])
+        assert np.array_equal(outs[0][1], outs[1][1])
