@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(kAdjTPB)
     double gz[3] = {0, 0, 0}, sg = 0.0, f_r = 0.0, dfr = 0.0;
     if (noise && f_d < 0.0) {
       float z[6];
-      pair_draw<D>(3, k.key0, k.key1, step, pidi, tp.pid[j], z);
+      pair_draw<D>(3, k.rk, step, pidi, tp.pid[j], z);
 #pragma unroll
       for (int a = 0; a < D; ++a) gz[a] = (double)z[a];
       sg = (double)z[5];

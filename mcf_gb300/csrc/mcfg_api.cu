@@ -315,6 +315,10 @@ void make_consts(const mcfg_params& p, Consts& k) {
   k.inv_tau = p.Newtonian ? 0.0 : 1.0 / p.tau;
   k.key0 = (uint32_t)p.seed;
   k.key1 = (uint32_t)(p.seed >> 32);
+  for (int r = 0; r < 10; ++r) {
+    k.rk[2 * r] = k.key0 + (uint32_t)r * 0x9E3779B9u;
+    k.rk[2 * r + 1] = k.key1 + (uint32_t)r * 0xBB67AE85u;
+  }
   k.body_force_type = p.body_force_type;
   for (int a = 0; a < 3; ++a) k.body_force[a] = p.body_force[a];
 }

@@ -98,6 +98,8 @@ struct Consts {
   int newtonian;
   double G, tau, inv_tau;  // G = n_p kt_p
   uint32_t key0, key1;   // Philox key (seed)
+  uint32_t rk[20];       // its round keys (key + r * Weyl increment), taken
+                         // from the parameter bank by the unrolled rounds
   int body_force_type;
   double body_force[3];
   double machine_zero;
@@ -317,7 +319,9 @@ enum { kForceOnly = 0, kForceBody = 1, kForceBodyKick = 2 };
 
 // Philox4x32-10, Salmon et al., SC'11 ("Parallel random numbers: as easy as
 // 1, 2, 3"): multipliers and Weyl key increments of the published algorithm.
-__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+// rk: the 10 round keys, rk[2r] = k0 + r * 0x9E3779B9, rk[2r+1] = k1 + r *
+// 0xBB67AE85 (Consts::rk, expanded once per configuration).
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, const uint32_t* rk) {
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
     // one 32x32 -> 64-bit product per word (low and high halves together)
@@ -325,9 +329,7 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1
     const uint64_t p1 = (uint64_t)0xCD9E8D57u * c.z;
     const uint32_t lo0 = (uint32_t)p0, hi0 = (uint32_t)(p0 >> 32);
     const uint32_t lo1 = (uint32_t)p1, hi1 = (uint32_t)(p1 >> 32);
-    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
-    k0 += 0x9E3779B9u;
-    k1 += 0xBB67AE85u;
+    c = make_uint4(hi1 ^ c.y ^ rk[2 * r], lo1, hi0 ^ c.w ^ rk[2 * r + 1], lo0);
   }
   return c;
 }
@@ -367,17 +369,17 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, fl
 // 2D z[0..2]; the counter is (min pid, max pid, step, call) so the draw is
 // the same from both particles of the pair.
 template <int D>
-__device__ __forceinline__ void pair_normals(uint32_t k0, uint32_t k1, uint32_t step,
+__device__ __forceinline__ void pair_normals(const uint32_t* rk, uint32_t step,
                                              int pa, int pb, float* z) {
   const uint32_t a = (uint32_t)min(pa, pb), b = (uint32_t)max(pa, pb);
-  uint4 r = philox4x32_10(make_uint4(a, b, step, 0u), k0, k1);
+  uint4 r = philox4x32_10(make_uint4(a, b, step, 0u), rk);
   float t0, t1;
   box_muller(r.x, r.y, z[0], z[1]);
   box_muller(r.z, r.w, t0, t1);
   z[2] = t0;
   if (D == 3) {
     z[3] = t1;
-    r = philox4x32_10(make_uint4(a, b, step, 1u), k0, k1);
+    r = philox4x32_10(make_uint4(a, b, step, 1u), rk);
     box_muller(r.x, r.y, z[4], z[5]);
   }
 }
@@ -390,14 +392,14 @@ __device__ __forceinline__ void pair_normals(uint32_t k0, uint32_t k1, uint32_t 
 //     otherwise (orients We so that the pair's two sides are opposite);
 //   type 4 (angular): one normal.
 template <int D>
-__device__ __forceinline__ void pair_draw(int type, uint32_t k0, uint32_t k1, uint32_t step,
+__device__ __forceinline__ void pair_draw(int type, const uint32_t* rk, uint32_t step,
                                           int pa, int pb, float* z) {
   if (type == 2) {
-    pair_normals<D>(k0, k1, step, pa, pb, z);
+    pair_normals<D>(rk, step, pa, pb, z);
     return;
   }
   const uint32_t a = (uint32_t)min(pa, pb), b = (uint32_t)max(pa, pb);
-  const uint4 r = philox4x32_10(make_uint4(a, b, step, 0u), k0, k1);
+  const uint4 r = philox4x32_10(make_uint4(a, b, step, 0u), rk);
   box_muller(r.x, r.y, z[0], z[1]);
   if (type == 3) {
     if (D == 3) {

@@ -803,7 +803,7 @@ __global__ void __launch_bounds__(kReuseTPB)
 #pragma unroll
     for (int a = 0; a < D; ++a) vij[a] = vi[a] - vj[a];
     float z[6];
-    if (noise) pair_draw<D>(k.rhs_force_type, k.key0, k.key1, step, pidi, pid[j], z);
+    if (noise) pair_draw<D>(k.rhs_force_type, k.rk, step, pidi, pid[j], z);
     T pa[3], si_s, sj_s;
     pair_force<T, D>(k, r, inv_d, vij, Ai, Bi, Aj, Bj, gw, noise, z, inv_sqdt, pa);
     if (nnw) {
@@ -1046,7 +1046,7 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
     for (int a = 0; a < D; ++a) vij[a] = vi[a] - vj[a];
     float z[6];
     if (noise)
-      pair_draw<D>(k.rhs_force_type, k.key0, k.key1, step, pidi, __float_as_int(cur.v.w), z);
+      pair_draw<D>(k.rhs_force_type, k.rk, step, pidi, __float_as_int(cur.v.w), z);
     T pa[3], si_s, sj_s;
     pair_force<T, D>(k, r, inv_d, vij, Ai, Bi, Aj, Bj, gw, noise, z, inv_sqdt, pa);
     if (nnw) {
@@ -1349,7 +1349,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 #pragma unroll
             for (int a = 0; a < D; ++a) vij[a] = vi[a] - vj[a];
             float z[6];
-            if (noise) pair_draw<D>(k.rhs_force_type, k.key0, k.key1, step, pidi, pidj, z);
+            if (noise) pair_draw<D>(k.rhs_force_type, k.rk, step, pidi, pidj, z);
             T g[3], s_i, s_j;
             pair_force<T, D>(k, rr, inv_d, vij, Ai, Bi, Aj, Bj, gw, noise, z, inv_sqdt, g);
             pair_scales<T>(k.rhs_force_type, Ci, Cj, s_i, s_j);
