@@ -19,7 +19,17 @@ from mcf_gb300 import configs  # noqa: E402
 from mcf_gb300.params import make_params  # noqa: E402
 from oracle.oracle import Oracle  # noqa: E402
 
-CASES = ("c1_small", "c2_small", "walls_small")
+CASES = ("c1_small", "c2_small", "walls_small", "le_small", "couette_osc_small")
+
+# boundary motion of a case: (shear_type[6], shear_freq[6], time_current)
+MOTION = {
+    "le_small": ((0,) * 6, (0.0,) * 6, 2.7),
+    "couette_osc_small": ((0, 0, 0, 2, 0, 0), (0.0, 0.0, 0.0, 2 * np.pi / 0.02, 0.0, 0.0), 0.013),
+}
+
+
+def motion(name: str):
+    return MOTION.get(name)
 
 
 def workload(name: str) -> configs.Workload:
@@ -37,12 +47,25 @@ def workload(name: str) -> configs.Workload:
         fl = w.id[:, 1] == 0
         w.v[fl] = rng.normal(0, 1e-2, (int(fl.sum()), 3))
         return w
+    if name == "le_small":
+        w = configs.lees_edwards(dim=3, n_side=14, shear_rate=0.3)
+        rng = np.random.default_rng(13)
+        w.x = np.mod(w.x + rng.uniform(-0.3, 0.3, w.x.shape), 14.0)
+        return w
+    if name == "couette_osc_small":
+        w = configs.couette_walls(dim=2, n_side=16, v_top=0.1)
+        rng = np.random.default_rng(14)
+        fl = w.id[:, 1] == 0
+        w.v[fl] = rng.normal(0, 1e-2, (int(fl.sum()), 2))
+        return w
     raise KeyError(name)
 
 
 def compute(name: str) -> dict:
     w = workload(name)
     o = Oracle(w.params)
+    if motion(name):
+        o.set_boundary_motion(*motion(name))
     o.upload(w.x, w.v, w.m, w.id)
     o.marching_init_force(0)
     ncd, cs, lp = o.technique_build_list()

@@ -144,6 +144,8 @@ def test_fp64_golden_fixtures(gpu_lib):
     for name, fx in make_golden.load_all().items():
         w = make_golden.workload(name)
         g = SDPD(w.params)
+        if make_golden.motion(name):
+            g.set_boundary_motion(*make_golden.motion(name))
         g.upload(w.x, w.v, w.m, w.id)
         g.marching_init_force(0)
         d = g.download("rho", "f")
@@ -151,6 +153,16 @@ def test_fp64_golden_fixtures(gpu_lib):
         noise = bool(w.params.Brownian and w.params.kt > 0)
         tol = 1e-5 if noise else 1e-9
         assert np.all(np.abs(d["f"] - fx["f0"]) <= tol * (np.abs(fx["f0"]).max() + 1.0))
+        # five VV steps from there (kT = 0 cases)
+        if not noise:
+            g.run_vv(0, 5, w.dt)
+            d5 = g.download("x", "v")
+            L = np.asarray(w.params.max_phys_t)[: w.params.num_dim] - \
+                np.asarray(w.params.min_phys_t)[: w.params.num_dim]
+            dx = np.abs(d5["x"] - fx["x5"])
+            dx = np.minimum(dx, L - dx)
+            assert dx.max() <= 1e-10 * L.max(), name
+            assert np.abs(d5["v"] - fx["v5"]).max() <= 1e-8 * (np.abs(fx["v5"]).max() + 1e-3), name
 
 
 def test_stress_tensor_and_statistics(gpu_lib):
