@@ -807,6 +807,7 @@ extern "C" int mcfg_adjoint_run(mcfg_handle* h, int64_t step0, int32_t nsteps, d
                                 int32_t checkpoint_every, const double* w, double* J,
                                 double* dJ_dparams, double* dJ_dx0, double* dJ_dv0,
                                 double* dJ_dct0) {
+  if (h) h->graph_gen++;
   if (!h) return MCFG_EINVAL;
   if (cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice")) return MCFG_ECUDA;
   if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");

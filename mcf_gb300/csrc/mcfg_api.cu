@@ -107,6 +107,10 @@ int dalloc(Handle* h, T** p, size_t count) {
 
 void free_all(Handle* h) {
   free_adjoint(h);
+  destroy_graphs(h);
+  h->graph_gen++;
+  if (h->d_step) cudaFree(h->d_step);
+  h->d_step = nullptr;
   if (h->out_dev) cudaFree(h->out_dev);
   if (h->out_host) cudaFreeHost(h->out_host);
   h->out_dev = nullptr;
@@ -673,6 +677,82 @@ int vv_step(Handle* h, int64_t step, double dt) {
   return rhs_reuse(h, step, kForceBodyKick, dt);
 }
 
+__global__ void k_step_set(int64_t* __restrict__ d_step, int64_t value) { *d_step = value; }
+__global__ void k_step_advance(int64_t* __restrict__ d_step) { *d_step += 1; }
+
+void destroy_graphs(Handle* h) {
+  for (auto& g : h->graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = Handle::GraphSlot{};
+  }
+}
+
+// run_vv may replay captured steps: list reuse (the rebuild is decided on the
+// device), a candidate list in place, no profiling, and constants that do
+// not change from step to step (no oscillating walls; Lees-Edwards runs
+// without list reuse anyway)
+static bool graph_eligible(const Handle* h) {
+  if (!h->k.reuse || !h->reuse_valid || h->profiling || h->graph_off || h->k.le) return false;
+  if (h->k.walls)
+    for (int f = 0; f < 6; ++f)
+      if (h->shear_type[f] == 2) return false;
+  return true;
+}
+
+// the graph of two list-reuse VV steps for the handle's current state
+// (captured on first use and whenever constants, buffers or dt change)
+static Handle::GraphSlot* graph_for(Handle* h, double dt) {
+  for (auto& g : h->graphs)
+    if (g.exec && g.gen == h->graph_gen && g.dt == dt && g.v == (const void*)h->v) return &g;
+  if (!h->d_step && cudaMalloc(&h->d_step, sizeof(int64_t)) != cudaSuccess) {
+    cudaGetLastError();
+    h->graph_off = true;
+    return nullptr;
+  }
+  Handle::GraphSlot* slot = &h->graphs[0];
+  for (auto& g : h->graphs)
+    if (!g.exec || g.gen != h->graph_gen || g.dt != dt) {
+      slot = &g;
+      break;
+    }
+  if (slot->exec) cudaGraphExecDestroy(slot->exec);
+  *slot = Handle::GraphSlot{};
+  const void* v0 = h->v;
+  const int64_t launches0 = h->launches;
+  const double t0 = h->time_current;
+  cudaGraph_t graph = nullptr;
+  bool ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  if (ok) {
+    h->graph_capturing = true;
+    for (int q = 0; q < 2 && ok; ++q) {
+      ok = kick_drift_reuse(h, dt) == MCFG_OK && rhs_reuse(h, 0, kForceBodyKick, dt) == MCFG_OK;
+      k_step_advance<<<1, 1, 0, h->stream>>>(h->d_step);
+    }
+    h->graph_capturing = false;
+    const bool ended = cudaStreamEndCapture(h->stream, &graph) == cudaSuccess;
+    ok = ok && ended && graph != nullptr &&
+         cudaGraphInstantiate(&slot->exec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+  }
+  h->time_current = t0;  // capture ran no step
+  const int64_t captured = h->launches - launches0;
+  h->launches = launches0;
+  if (!ok || h->v != v0) {
+    // fall back to plain launches for this handle; the capture ran nothing
+    cudaGetLastError();
+    if (slot->exec) cudaGraphExecDestroy(slot->exec);
+    *slot = Handle::GraphSlot{};
+    h->graph_off = true;
+    h->err.clear();
+    return nullptr;
+  }
+  slot->gen = h->graph_gen;
+  slot->dt = dt;
+  slot->v = v0;
+  slot->launches = captured + 2;
+  return slot;
+}
+
 }  // namespace mcfg
 
 namespace {
@@ -800,6 +880,7 @@ int mcfg_get_info(const mcfg_handle* h, mcfg_info* info) {
 int mcfg_upload(mcfg_handle* h, int64_t n, const double* x, const double* v, const double* m,
                 const int32_t* id, const double* ct) {
   GUARD(h);
+  h->graph_gen++;
   if (n < 0 || (n > 0 && (!x || !v || !m || !id)))
     return set_error(h, MCFG_EINVAL, "mcfg_upload: NULL array");
   if (ct && h->p.Newtonian) return set_error(h, MCFG_EINVAL, "conformation tensor of a Newtonian run");
@@ -1035,6 +1116,7 @@ int mcfg_write_particles(mcfg_handle* h, const char* path, int32_t kind, int32_t
 int mcfg_set_boundary_motion(mcfg_handle* h, const int32_t* shear_type, const double* shear_freq,
                              double time) {
   GUARD(h);
+  h->graph_gen++;
   if (!shear_type || !shear_freq) return set_error(h, MCFG_EINVAL, "NULL shear_type / shear_freq");
   for (int f = 0; f < 6; ++f) {
     if (shear_type[f] == 2 && h->p.bcdef[f] != MCFG_BC_WALL_SOLID)
@@ -1106,7 +1188,25 @@ int mcfg_run_vv(mcfg_handle* h, int64_t step0, int32_t nsteps, double dt) {
   if (!h->have_force) return set_error(h, MCFG_ESTATE, "mcfg_init_force must come first");
   if (!(dt > 0.0)) return set_error(h, MCFG_EINVAL, "dt must be positive");
   h->dt = dt;
-  for (int32_t q = 1; q <= nsteps; ++q) TRY(vv_step(h, step0 + q, dt));
+  int32_t q = 1;
+  while (q <= nsteps) {
+    Handle::GraphSlot* g = (nsteps - q >= 1 && graph_eligible(h)) ? graph_for(h, dt) : nullptr;
+    if (!g) {
+      TRY(vv_step(h, step0 + q, dt));
+      ++q;
+      continue;
+    }
+    // pairs of steps from the graph: the device counter carries the step
+    k_step_set<<<1, 1, 0, h->stream>>>(h->d_step, step0 + q);
+    h->launches++;
+    h->unwrapped = true;
+    for (; nsteps - q >= 1; q += 2) {
+      if (cuda_check(h, cudaGraphLaunch(g->exec, h->stream), "graph launch")) return MCFG_ECUDA;
+      h->launches += g->launches;
+      h->time_current = h->time_current + dt;
+      h->time_current = h->time_current + dt;
+    }
+  }
   return check_device_errors(h);
 }
 
@@ -1198,6 +1298,7 @@ static int put_colloid_state(Handle* h, int nc, const double* x, const double* v
 int mcfg_set_colloids(mcfg_handle* h, const mcfg_colloid_params* cp, const double* x,
                       const double* v, const double* omega, const double* radius) {
   GUARD(h);
+  h->graph_gen++;
   if (!cp || cp->num_colloid < 0) return set_error(h, MCFG_EINVAL, "bad colloid parameters");
   const int nc = cp->num_colloid;
   if (nc > 0 && (!x || !v || !omega || !radius))
@@ -1234,6 +1335,7 @@ int mcfg_set_colloids(mcfg_handle* h, const mcfg_colloid_params* cp, const doubl
 int mcfg_move_colloids(mcfg_handle* h, const double* x_new, const double* rot, const double* v,
                        const double* omega) {
   GUARD(h);
+  h->graph_gen++;
   const int nc = h->k.ncoll, d = h->p.num_dim;
   if (nc == 0) return set_error(h, MCFG_ESTATE, "mcfg_set_colloids must come first");
   if (!x_new || !v || !omega) return set_error(h, MCFG_EINVAL, "mcfg_move_colloids: NULL array");

@@ -206,6 +206,24 @@ struct Handle {
   int* d_rebuild = nullptr;      // [0] rebuild request, [1] rebuilds done
   bool reuse_valid = false;      // the candidate list matches the particle order
   bool unwrapped = false;        // positions may lie outside periodic faces (list reuse)
+  // ---- CUDA graph of two list-reuse VV steps (mcfg_run_vv) ----
+  // The step is launch-bound below ~50k particles (14 launches a step); run_vv
+  // replays a captured pair of steps instead (two: the fused second kick
+  // swaps v and v2, so two steps bring the buffers back).  The force sweeps
+  // of the captured steps read the Philox step from d_step, which a one-thread
+  // kernel advances after every step.  A graph is reused while the handle's
+  // constants and buffers are those it captured (graph_gen, v).
+  int64_t* d_step = nullptr;
+  bool graph_capturing = false;
+  bool graph_off = false;        // capture failed once: plain launches from then on
+  uint64_t graph_gen = 1;        // bumped whenever constants or buffers change
+  struct GraphSlot {
+    cudaGraphExec_t exec = nullptr;
+    uint64_t gen = 0;
+    double dt = 0.0;
+    const void* v = nullptr;
+    int64_t launches = 0;
+  } graphs[2];
   // ---- particle-file text (output.cu), grow-only, null until the first write ----
   char* out_dev = nullptr;
   char* out_host = nullptr;  // pinned
@@ -303,6 +321,8 @@ void boundary_update(Handle* h, double time_r, double time_v);
 // positions: gather them to host order and copy them to h->io_x_out on the
 // copy stream while the sweeps run
 int download_x_async(Handle* h);
+// release the captured step graphs (buffers or constants changed)
+void destroy_graphs(Handle* h);
 // MCF's particle output (kind 0) or restart (kind 1) file formatted on the
 // device; flags & 1 adds the stress columns s(2), s(3)
 int write_particle_file(Handle* h, const char* path, int kind, int flags);

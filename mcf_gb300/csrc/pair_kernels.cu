@@ -663,10 +663,14 @@ __global__ void __launch_bounds__(kReuseTPB)
               const double4_32a* __restrict__ v, const double4_32a* __restrict__ pc,
               const int* __restrict__ sid, const int* __restrict__ pid,
               double4_32a* __restrict__ f, double* __restrict__ st, int fuse_mode, double dt,
-              double4_32a* __restrict__ v_out, uint32_t step, double inv_sqdt,
+              double4_32a* __restrict__ v_out, uint32_t step_arg,
+              const int64_t* __restrict__ step_ptr, double inv_sqdt,
               unsigned* __restrict__ err, NN nn, CollArgs ca) {
   constexpr int D2 = D * D;
   using T = double;
+  // the Philox counter's step: the argument, or the device step counter
+  // when the sweep runs inside a captured graph
+  const uint32_t step = step_ptr ? (uint32_t)*step_ptr : step_arg;
   __shared__ int s_start[kMaxStencil * kReuseTPB];
   __shared__ int s_shift[kMaxStencil * kReuseTPB];
   const int n = k.n;
@@ -877,10 +881,12 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
               const float4* __restrict__ pcf, const float4* __restrict__ vf,
               const float2* __restrict__ wd, double4_32a* __restrict__ f,
               double* __restrict__ st, int fuse_mode, double dt,
-              double4_32a* __restrict__ v_out, uint32_t step, float inv_sqdt,
+              double4_32a* __restrict__ v_out, uint32_t step_arg,
+              const int64_t* __restrict__ step_ptr, float inv_sqdt,
               unsigned* __restrict__ err, NN nn, CollArgs ca) {
   constexpr int D2 = D * D;
   using T = float;
+  const uint32_t step = step_ptr ? (uint32_t)*step_ptr : step_arg;
   // one thread per particle, whatever its cell: per-thread neighbour-cell
   // tables keep every lane busy (2D cells hold ~9 particles)
   __shared__ int s_start[kMaxStencil * kReuseTPB];
@@ -1145,7 +1151,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
                 const float4* __restrict__ pcf, const float4* __restrict__ vf,
                 const float2* __restrict__ wd, const int* __restrict__ sid,
                 const int* __restrict__ pid, typename SymT<FP64>::T* __restrict__ jp,
-                uint32_t step, typename SymT<FP64>::T inv_sqdt) {
+                uint32_t step_arg, const int64_t* __restrict__ step_ptr,
+                typename SymT<FP64>::T inv_sqdt) {
+  // the Philox counter's step: the argument, or the device step counter
+  // when the sweep runs inside a captured graph
+  const uint32_t step = step_ptr ? (uint32_t)*step_ptr : step_arg;
   using T = typename SymT<FP64>::T;
   constexpr int CC = SymT<FP64>::CC;
   constexpr int CENTER = (D == 3) ? 13 : 4;
@@ -1600,6 +1610,7 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
   const NN nn{h->ct, h->act, h->vgt, h->qq};
   const CollArgs ca{h->v, h->rxc, h->rxcf};
   const int gp = std::max(1, ((int)h->n + kReuseTPB - 1) / kReuseTPB);
+  const int64_t* step_ptr = h->graph_capturing ? h->d_step : nullptr;
   if (!k.stress && h->jp && fp64 && k.newtonian && k.ncoll == 0 && !k.le) {
     // symmetric sweep + per-particle gather: halves the FP64 pair work; the
     // FP32 path keeps the two-sided sweep, which is faster there (the
@@ -1623,14 +1634,14 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
       if (k.d == 3) {
         k_force_sym<3, true><<<g, bs, kWarpsPerBlock * sym_warp_bytes<3, true>(), s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
                                               h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
-                                              h->pid, jp, (uint32_t)step, inv_sqdt);
+                                              h->pid, jp, (uint32_t)step, step_ptr, inv_sqdt);
         if (n > 0)
           k_force_gather<3, true><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid, h->f,
                                                       fuse_mode, dt, h->v2, h->d_err);
       } else {
         k_force_sym<2, true><<<g, bs, kWarpsPerBlock * sym_warp_bytes<2, true>(), s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
                                               h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
-                                              h->pid, jp, (uint32_t)step, inv_sqdt);
+                                              h->pid, jp, (uint32_t)step, step_ptr, inv_sqdt);
         if (n > 0)
           k_force_gather<2, true><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid, h->f,
                                                       fuse_mode, dt, h->v2, h->d_err);
@@ -1640,14 +1651,16 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
       if (k.d == 3) {
         k_force_sym<3, false><<<g, bs, kWarpsPerBlock * sym_warp_bytes<3, false>(), s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
                                                h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
-                                               h->pid, jp, (uint32_t)step, (float)inv_sqdt);
+                                               h->pid, jp, (uint32_t)step, step_ptr,
+                                               (float)inv_sqdt);
         if (n > 0)
           k_force_gather<3, false><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid,
                                                        h->f, fuse_mode, dt, h->v2, h->d_err);
       } else {
         k_force_sym<2, false><<<g, bs, kWarpsPerBlock * sym_warp_bytes<2, false>(), s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
                                                h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
-                                               h->pid, jp, (uint32_t)step, (float)inv_sqdt);
+                                               h->pid, jp, (uint32_t)step, step_ptr,
+                                               (float)inv_sqdt);
         if (n > 0)
           k_force_gather<2, false><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid,
                                                        h->f, fuse_mode, dt, h->v2, h->d_err);
@@ -1659,7 +1672,7 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
   k_force64<DD, NW><<<gp, kReuseTPB, 0, s>>>(k, h->cell_start, h->cell_of, h->nl, h->ncount,     \
                                             h->x, h->v, h->pc,                                 \
                                      h->sid, h->pid, h->f, h->st, fuse_mode, dt, h->v2,          \
-                                     (uint32_t)step, inv_sqdt, h->d_err, nn, ca)
+                                     (uint32_t)step, step_ptr, inv_sqdt, h->d_err, nn, ca)
     if (k.d == 3) {
       if (k.newtonian) LAUNCH_F64(3, false); else LAUNCH_F64(3, true);
     } else {
@@ -1671,7 +1684,7 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
   k_force32<DD, NW><<<gp, kReuseTPB, 0, s>>>(k, h->cell_start, h->cell_of, h->nl, h->ncount,     \
                                             h->off, h->x, h->v,                                \
                                      h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2,    \
-                                     (uint32_t)step, (float)inv_sqdt, h->d_err, nn, ca)
+                                     (uint32_t)step, step_ptr, (float)inv_sqdt, h->d_err, nn, ca)
     if (k.d == 3) {
       if (k.newtonian) LAUNCH_F32(3, false); else LAUNCH_F32(3, true);
     } else {

@@ -543,3 +543,35 @@ def test_step_vv_host_equals_update_step_download(gpu_lib):
             outs.append((x.copy(), v.copy()))
         assert np.array_equal(outs[0][0], outs[1][0])
         assert np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_run_vv_graph_replay_equals_step_vv(gpu_lib):
+    # with list reuse mcfg_run_vv replays a captured pair of steps (the
+    # Philox step from the device counter), mcfg_step_vv launches every
+    # step: bit-identical, also across device-side rebuilds and odd counts
+    fast = jittered_3d(n_side=12)
+    fast.v = np.random.default_rng(9).normal(0, 0.3, fast.v.shape)
+    cases = [(jittered_3d(n_side=12), 1e-4), (make_golden.workload("walls_small"), None),
+             (fast, 1e-2)]
+    for w, dt in cases:
+        dt = dt or w.dt
+        outs = []
+        for mode in ("run", "step"):
+            p = w.params.copy()
+            p.reserved[1] = 1
+            p.precision = PRECISION_FP32_MIXED
+            p.Brownian, p.kt = 1, 1e-4
+            g = SDPD(p)
+            g.upload(w.x, w.v, w.m, w.id)
+            g.marching_init_force(0)
+            if mode == "run":
+                g.run_vv(0, 9, dt)
+                g.run_vv(9, 6, dt)
+            else:
+                for s in range(1, 16):
+                    g.marching_integrate_VV(s, dt)
+            outs.append((g.download("x", "v", "f"), g.info()))
+        for k in ("x", "v", "f"):
+            assert np.array_equal(outs[0][0][k], outs[1][0][k]), k
+        assert outs[0][1]["list_rebuilds"] == outs[1][1]["list_rebuilds"]
+        assert outs[0][1]["time_current"] == outs[1][1]["time_current"]
