@@ -380,6 +380,8 @@ __global__ void k_rebuild_done(int* __restrict__ flag) {
 }
 
 constexpr int kReuseTPB = 128;
+// below this many particles the FP32 force sweep runs 4 lanes per particle
+constexpr int64_t kSplitBelow = 50000;
 
 // FP32 offset of each stencil slot (the neighbour cell's origin minus the
 // home cell's, w = Lees-Edwards velocity jump), build_table's t.o, in a
@@ -405,7 +407,7 @@ __device__ __forceinline__ const float4* slot_table(const Consts& k, const float
 // exact pair test (FP64 path: the FP64 separation of MCF; FP32 path: the
 // FP32 test of k_density's scan, same operation order), the step's neighbour
 // list for the force sweep, the W sum and the epilogue of k_density.
-template <int D, bool FP64>
+template <int D, bool FP64, int S>
 __global__ void __launch_bounds__(kReuseTPB)
     k_density_reuse(Consts k, const int* __restrict__ cell_start, const int* __restrict__ cell_of,
                     const float4* __restrict__ off, const double4_32a* __restrict__ x,
@@ -423,19 +425,25 @@ __global__ void __launch_bounds__(kReuseTPB)
   __shared__ int s_shift[kMaxStencil * kReuseTPB];
   __shared__ float4 s_slot[kSlotTable];
   const int n = k.n, tid = threadIdx.x;
-  const int i = blockIdx.x * kReuseTPB + tid;
+  // S lanes per particle in the FP32 path for small systems (as k_force32):
+  // lane l tests candidates l, l + S, ...; the step's list keeps candidate
+  // order (positions from the group's ballot) and the W sums are added in
+  // lane order
+  const int gt = blockIdx.x * kReuseTPB + tid;
+  const int i = gt / S, lane_s = gt % S;
   int my_max = 0;
   unsigned long long my_pairs = 0;
   fill_slot_offsets<D>(k, s_slot);
   __syncthreads();
+  int kept = 0, hs = -1, si = 0;
+  bool acc_i = false;
+  double rho_i = 0.0;
   if (i < n) {
     build_lane_table<D, kReuseTPB>(k, cell_of[i], cell_start, s_start, s_shift);
     const int li = i - s_start[CENTER * kReuseTPB + tid];
-    const int si = sid[i];
-    const bool acc_i = dyn_rho(k, si);
+    si = sid[i];
+    acc_i = dyn_rho(k, si);
     const int cnt = vcount[i];
-    int kept = 0, hs = -1;
-    double rho_i;
     if (FP64) {
       const double4_32a xi4 = x[i];
       const double xi[3] = {xi4.x, xi4.y, xi4.z};
@@ -458,6 +466,62 @@ __global__ void __launch_bounds__(kReuseTPB)
         }
       }
       rho_i = sum;
+    } else if (S > 1) {
+      const float4 oi = off[i];
+      const bool mass = k.rhs_density_type == 1;
+      float sum = 0.0f, comp = 0.0f;
+      const int base = (tid & 31) & ~(S - 1);
+      const unsigned gmask = ((1u << S) - 1u) << base;
+      for (int e0 = 0; e0 < cnt; e0 += S) {
+        const int e = e0 + lane_s;
+        bool in = false, fwd = false;
+        int ent = 0;
+        float rx = 0.f, ry = 0.f, rz = 0.f;
+        int j = 0;
+        if (e < cnt) {
+          ent = vl[(size_t)e * n + i];
+          const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
+          j = s_start[sl * kReuseTPB + tid] + q;
+          const float4 oj = off[j];
+          const float4 so = s_slot[sl];
+          const float sx = so.x, sy = so.y, sz = (D == 3) ? so.z : 0.0f;
+          // the pair test as k_density's scan rounds it: (o_i - slot) - o_j
+          const float tx = (oi.x - sx) - oj.x, ty = (oi.y - sy) - oj.y;
+          float t2 = tx * tx + ty * ty;
+          if (D == 3) {
+            const float tz = (oi.z - sz) - oj.z;
+            t2 += tz * tz;
+          }
+          in = t2 < k.rc2f;
+          fwd = in && (sl > CENTER || (sl == CENTER && q > li));
+          rx = (oi.x - oj.x) - sx;
+          ry = (oi.y - oj.y) - sy;
+          rz = (D == 3) ? (oi.z - oj.z) - sz : 0.f;
+        }
+        const unsigned bal = __ballot_sync(gmask, in) >> base;
+        const unsigned fb = __ballot_sync(gmask, fwd) >> base;
+        if (hs < 0 && fb) hs = kept + __popc(bal & ((1u << (__ffs(fb) - 1)) - 1u));
+        if (in) {
+          const int pos = kept + __popc(bal & ((1u << lane_s) - 1u));
+          if (pos < cap) nl[(size_t)pos * n + i] = (uint16_t)ent;
+          if (acc_i) {
+            // W as k_density's second phase rounds it: (o_i - o_j) - slot
+            float d2 = rx * rx + ry * ry;
+            if (D == 3) d2 += rz * rz;
+            float w = kernel_w<float>(k, sqrtf(d2));
+            if (mass) w *= (float)m[j];
+            const float y = w - comp;
+            const float tt = sum + y;
+            comp = (tt - sum) - y;
+            sum = tt;
+          }
+        }
+        kept += __popc(bal);
+      }
+      const float part = sum - comp;
+      float tot = part;
+      for (int q = 1; q < S; ++q) tot += __shfl_sync(gmask, part, base + q);
+      rho_i = (double)tot;
     } else {
       const float4 oi = off[i];
       const bool mass = k.rhs_density_type == 1;
@@ -515,6 +579,8 @@ __global__ void __launch_bounds__(kReuseTPB)
       }
       rho_i = (double)sum;
     }
+  }
+  if (i < n && lane_s == 0) {
     if (kept > cap) atomicOr(err, kErrNeighOverflow);
     my_max = kept;
     kept = min(kept, cap);
@@ -872,7 +938,11 @@ __device__ __forceinline__ JData load_j(const int* __restrict__ s_start, int ent
   return d;
 }
 
-template <int D, bool NNW>
+// S lanes per particle (1, or 4 for small systems, where one thread per
+// particle leaves most of the GPU idle and each thread's serial pair loop
+// sets the time): lane l takes list entries l, l + S, ...; the lanes' sums
+// are added in lane order by the first lane, which runs the epilogue.
+template <int D, bool NNW, int S>
 __global__ void __launch_bounds__(kReuseTPB, 5)
     k_force32(Consts k, const int* __restrict__ cell_start, const int* __restrict__ cell_of,
               const uint16_t* __restrict__ nl,
@@ -897,8 +967,9 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
   __shared__ float4 s_slot[kSlotTable];
   fill_slot_offsets<D>(k, s_slot);
   __syncthreads();
-  const int i = blockIdx.x * kReuseTPB + threadIdx.x;
-  if (i >= n) return;
+  const int gt = blockIdx.x * kReuseTPB + threadIdx.x;
+  const int i = gt / S, lane_s = gt % S;
+  if (i >= n) return;  // the S lanes of a particle leave together
   const int celli = cell_of[i];
   build_lane_table<D, kReuseTPB>(k, celli, cell_start, s_start, s_shift);
   const float4* slot_tab = slot_table(k, s_slot, celli);
@@ -924,13 +995,13 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
   const int cnt = ncount[i];
   JData nxt;
   int ent_n1 = 0;
-  if (cnt > 0) nxt = load_j<D>(s_start, nl[i], off, vf, pcf);
-  if (cnt > 1) ent_n1 = nl[(size_t)n + i];
-  for (int e = 0; e < cnt; ++e) {
+  if (lane_s < cnt) nxt = load_j<D>(s_start, nl[(size_t)lane_s * n + i], off, vf, pcf);
+  if (lane_s + S < cnt) ent_n1 = nl[(size_t)(lane_s + S) * n + i];
+  for (int e = lane_s; e < cnt; e += S) {
     const JData cur = nxt;
-    if (e + 1 < cnt) {
+    if (e + S < cnt) {
       nxt = load_j<D>(s_start, ent_n1, off, vf, pcf);
-      if (e + 2 < cnt) ent_n1 = nl[(size_t)(e + 2) * n + i];
+      if (e + 2 * S < cnt) ent_n1 = nl[(size_t)(e + 2 * S) * n + i];
     }
     const int sj = __float_as_int(cur.o.w);
     if (si != 0 && sj != 0 && !(si > 0 && sj > 0 && si != sj && k.pp_cc)) continue;
@@ -1086,6 +1157,38 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
 #pragma unroll
         for (int a = 0; a < D; ++a) sacc[b * D + a] += r[a] * pa[b] * 0.5f;
     }
+  }
+  if (S > 1) {
+    // the lanes' sums, added in lane order by lane 0 of the group
+    const unsigned gmask = ((1u << S) - 1u) << ((threadIdx.x & 31) & ~(S - 1));
+    const int base = (threadIdx.x & 31) & ~(S - 1);
+    T part[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) part[a] = acc[a] - comp[a];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      T tot = part[a];
+      for (int q = 1; q < S; ++q) tot += __shfl_sync(gmask, part[a], base + q);
+      acc[a] = tot;
+      comp[a] = 0.f;
+    }
+    if (nnw) {
+#pragma unroll
+      for (int cc = 0; cc < D2; ++cc) {
+        T tot = L[cc];
+        for (int q = 1; q < S; ++q) tot += __shfl_sync(gmask, L[cc], base + q);
+        L[cc] = tot;
+      }
+    }
+    if (k.stress) {
+#pragma unroll
+      for (int a = 0; a < 9; ++a) {
+        T tot = sacc[a];
+        for (int q = 1; q < S; ++q) tot += __shfl_sync(gmask, sacc[a], base + q);
+        sacc[a] = tot;
+      }
+    }
+    if (lane_s != 0) return;
   }
   if (k.stress) {
 #pragma unroll
@@ -1548,16 +1651,23 @@ int compute_density(Handle* h, bool with_pressure, bool reuse) {
     const int n = (int)h->n;
     if (n == 0) return MCFG_OK;
     const int gr = (n + kReuseTPB - 1) / kReuseTPB;
-#define LAUNCH_R(DD, PP)                                                                        \
-  k_density_reuse<DD, PP><<<gr, kReuseTPB, 0, s>>>(                                             \
+#define LAUNCH_R(DD, PP, SS, G)                                                                 \
+  k_density_reuse<DD, PP, SS><<<G, kReuseTPB, 0, s>>>(                                          \
       k, h->cell_start, h->cell_of, h->off, h->x, h->v, h->m, h->sid, h->pid, h->vl, h->vcount, \
       h->nl, h->ncount, h->nhs, h->neigh_cap, h->rho, h->pr, h->pc, h->pcf, h->vf,              \
       with_pressure ? 1 : 0, h->d_err, h->d_stats, h->d_pairs, NN{h->ct, h->act, h->vgt, h->qq}, \
       CollArgs{h->v, h->rxc, h->rxcf})
+    // small systems: 4 lanes per particle in the FP32 path
+    const bool split = !fp64 && n < kSplitBelow;
+    const int gr4 = (int)(((int64_t)n * 4 + kReuseTPB - 1) / kReuseTPB);
     if (k.d == 3) {
-      if (fp64) LAUNCH_R(3, true); else LAUNCH_R(3, false);
+      if (fp64) LAUNCH_R(3, true, 1, gr);
+      else if (split) LAUNCH_R(3, false, 4, gr4);
+      else LAUNCH_R(3, false, 1, gr);
     } else {
-      if (fp64) LAUNCH_R(2, true); else LAUNCH_R(2, false);
+      if (fp64) LAUNCH_R(2, true, 1, gr);
+      else if (split) LAUNCH_R(2, false, 4, gr4);
+      else LAUNCH_R(2, false, 1, gr);
     }
 #undef LAUNCH_R
     h->launches++;
@@ -1611,6 +1721,9 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
   const CollArgs ca{h->v, h->rxc, h->rxcf};
   const int gp = std::max(1, ((int)h->n + kReuseTPB - 1) / kReuseTPB);
   const int64_t* step_ptr = h->graph_capturing ? h->d_step : nullptr;
+  // small systems: 4 lanes per particle in the FP32 sweep
+  const bool split = h->n < kSplitBelow;
+  const int gp4 = std::max(1, (int)((h->n * 4 + kReuseTPB - 1) / kReuseTPB));
   if (!k.stress && h->jp && fp64 && k.newtonian && k.ncoll == 0 && !k.le) {
     // symmetric sweep + per-particle gather: halves the FP64 pair work; the
     // FP32 path keeps the two-sided sweep, which is faster there (the
@@ -1681,10 +1794,18 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
 #undef LAUNCH_F64
   } else {
 #define LAUNCH_F32(DD, NW)                                                                      \
-  k_force32<DD, NW><<<gp, kReuseTPB, 0, s>>>(k, h->cell_start, h->cell_of, h->nl, h->ncount,     \
-                                            h->off, h->x, h->v,                                \
-                                     h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2,    \
-                                     (uint32_t)step, step_ptr, (float)inv_sqdt, h->d_err, nn, ca)
+  do {                                                                                           \
+    if (split)                                                                                   \
+      k_force32<DD, NW, 4><<<gp4, kReuseTPB, 0, s>>>(                                            \
+          k, h->cell_start, h->cell_of, h->nl, h->ncount, h->off, h->x, h->v, h->pcf, h->vf,     \
+          h->wd, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step, step_ptr, (float)inv_sqdt,   \
+          h->d_err, nn, ca);                                                                     \
+    else                                                                                         \
+      k_force32<DD, NW, 1><<<gp, kReuseTPB, 0, s>>>(                                             \
+          k, h->cell_start, h->cell_of, h->nl, h->ncount, h->off, h->x, h->v, h->pcf, h->vf,     \
+          h->wd, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step, step_ptr, (float)inv_sqdt,   \
+          h->d_err, nn, ca);                                                                     \
+  } while (0)
     if (k.d == 3) {
       if (k.newtonian) LAUNCH_F32(3, false); else LAUNCH_F32(3, true);
     } else {
