@@ -507,12 +507,11 @@ int ensure_capacity(Handle* h, int64_t n64) {
     }
     if (h->p.stress_tensor) {
       if ((rc = dalloc(h, &h->st, cap * (size_t)(d * d)))) return rc;
-    } else {
-      // symmetric force partial sums: (forward slots + owner) x 3 planes
+    } else if (h->p.precision == MCFG_PRECISION_FP64) {
+      // symmetric FP64 force partial sums: (forward slots + owner) x 3 planes
       const size_t planes = (size_t)((d == 3 ? 14 : 5) + 1) * 3;
-      const size_t elt = (h->p.precision == MCFG_PRECISION_FP64) ? 8 : 4;
-      char* pj = nullptr;
-      if ((rc = dalloc(h, &pj, cap * planes * elt))) return rc;
+      double* pj = nullptr;
+      if ((rc = dalloc(h, &pj, cap * planes))) return rc;
       h->jp = pj;
     }
     if ((rc = dalloc(h, &h->up_x, cap * 9)) || (rc = dalloc(h, &h->up_v, cap * 3)) ||

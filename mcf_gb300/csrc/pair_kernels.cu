@@ -1736,48 +1736,23 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
                            kWarpsPerBlock * sym_warp_bytes<3, true>());
       cudaFuncSetAttribute(k_force_sym<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kWarpsPerBlock * sym_warp_bytes<2, true>());
-      cudaFuncSetAttribute(k_force_sym<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kWarpsPerBlock * sym_warp_bytes<3, false>());
-      cudaFuncSetAttribute(k_force_sym<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kWarpsPerBlock * sym_warp_bytes<2, false>());
       attr_set = true;
     }
-    if (fp64) {
-      double* jp = (double*)h->jp;
-      if (k.d == 3) {
-        k_force_sym<3, true><<<g, bs, kWarpsPerBlock * sym_warp_bytes<3, true>(), s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
-                                              h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
-                                              h->pid, jp, (uint32_t)step, step_ptr, inv_sqdt);
-        if (n > 0)
-          k_force_gather<3, true><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid, h->f,
-                                                      fuse_mode, dt, h->v2, h->d_err);
-      } else {
-        k_force_sym<2, true><<<g, bs, kWarpsPerBlock * sym_warp_bytes<2, true>(), s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
-                                              h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
-                                              h->pid, jp, (uint32_t)step, step_ptr, inv_sqdt);
-        if (n > 0)
-          k_force_gather<2, true><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid, h->f,
-                                                      fuse_mode, dt, h->v2, h->d_err);
-      }
+    double* jp = (double*)h->jp;
+    if (k.d == 3) {
+      k_force_sym<3, true><<<g, bs, kWarpsPerBlock * sym_warp_bytes<3, true>(), s>>>(
+          k, h->cell_start, h->nl, h->ncount, h->nhs, h->off, h->x, h->v, h->pc, h->pcf, h->vf,
+          h->wd, h->sid, h->pid, jp, (uint32_t)step, step_ptr, inv_sqdt);
+      if (n > 0)
+        k_force_gather<3, true><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid, h->f,
+                                                    fuse_mode, dt, h->v2, h->d_err);
     } else {
-      float* jp = (float*)h->jp;
-      if (k.d == 3) {
-        k_force_sym<3, false><<<g, bs, kWarpsPerBlock * sym_warp_bytes<3, false>(), s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
-                                               h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
-                                               h->pid, jp, (uint32_t)step, step_ptr,
-                                               (float)inv_sqdt);
-        if (n > 0)
-          k_force_gather<3, false><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid,
-                                                       h->f, fuse_mode, dt, h->v2, h->d_err);
-      } else {
-        k_force_sym<2, false><<<g, bs, kWarpsPerBlock * sym_warp_bytes<2, false>(), s>>>(k, h->cell_start, h->nl, h->ncount, h->nhs, h->off,
-                                               h->x, h->v, h->pc, h->pcf, h->vf, h->wd, h->sid,
-                                               h->pid, jp, (uint32_t)step, step_ptr,
-                                               (float)inv_sqdt);
-        if (n > 0)
-          k_force_gather<2, false><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid,
-                                                       h->f, fuse_mode, dt, h->v2, h->d_err);
-      }
+      k_force_sym<2, true><<<g, bs, kWarpsPerBlock * sym_warp_bytes<2, true>(), s>>>(
+          k, h->cell_start, h->nl, h->ncount, h->nhs, h->off, h->x, h->v, h->pc, h->pcf, h->vf,
+          h->wd, h->sid, h->pid, jp, (uint32_t)step, step_ptr, inv_sqdt);
+      if (n > 0)
+        k_force_gather<2, true><<<gbn, 256, 0, s>>>(k, h->cell_of, jp, h->x, h->v, h->sid, h->f,
+                                                    fuse_mode, dt, h->v2, h->d_err);
     }
     h->launches++;
   } else if (fp64) {
