@@ -277,6 +277,16 @@ int mcfg_download(mcfg_handle* h, double* x, double* v, double* rho,
  * magnitudes in [1e-18, 1e30). */
 int mcfg_write_particles(mcfg_handle* h, const char* path, int32_t kind, int32_t flags);
 
+/* One line of MCF's statistic file, io_write_statistic.F90:131-257,
+ * appended to path (created when absent; io_open.F90:188-211 appends to an
+ * existing file on a restarted run): format (I9,<1+num_data>E16.8) of step,
+ * time, kinetic energy, momentum(1:d) and, with stress_tensor on, the
+ * stress sums s(2) s(3) -- the global sums mcfg_statistics returns.  The
+ * optional columns of runs with flow_v_fixed, dynamic_density_ref or
+ * p_energy are not written (those features are not on this path).  A step
+ * outside I9's range prints nine asterisks, as Fortran does. */
+int mcfg_write_statistic(mcfg_handle* h, const char* path, int64_t step, double time);
+
 /* Moving boundaries, MCF's Boundary object (Class_Boundary.F90: shear_type,
  * shear_v0 = mcfg_params.wall_v, shear_freq) and its time: shear_type[f] 2
  * makes solid-wall face f oscillate, shear_v = wall_v[f] cos(shear_freq[f] t)

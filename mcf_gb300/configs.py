@@ -223,6 +223,27 @@ def couette_walls(dim: int = 2, n_side: int = 32, v_top: float = 0.05,
     return w
 
 
+def poiseuille_channel(dim: int = 2, n_side: int = 20, force: float = 0.01,
+                       precision: int = PRECISION_FP64, seed: int = BASE_SEED + 8) -> Workload:
+    """Transient plane Poiseuille flow: fluid at rest on the dx = 1 lattice
+    between solid y walls (Morris no-slip, 4 constant-density layers each
+    side, the channel y in [0, n_side]), periodic x (and z), driven by a
+    uniform body force g_x = force (body_force_type 1); c = 10, eta = 1
+    (nu = 1 at rho = 1), kT = 0, dt = 0.01 (the viscous limit
+    0.125 dx^2 / nu is 0.125)."""
+    L = float(n_side)
+    nl = wall_layers(3.0, 1.0)
+    box = _box(dim, 0.0, L, walls_axis=1, nwall_layers=nl, dx=1.0)
+    p = make_params(**box, cut_off=3.0, c=10.0, eta=1.0, kt=0.0, Brownian=0,
+                    body_force_type=1, body_force=[force, 0.0, 0.0], dt=0.01,
+                    wall_noslip_type=2, wall_rho_type=0, init_density=1.0,
+                    precision=precision, seed=seed)
+    w = _finish(f"Poiseuille channel {dim}D {n_side}^{dim} g {force}", p, [1.0] * dim, 0.0, 0.0,
+                seed, 0.01, 10000)
+    w.v[:] = 0.0
+    return w
+
+
 @dataclass
 class ColloidSet:
     params: ColloidParams

@@ -1112,6 +1112,13 @@ int mcfg_write_particles(mcfg_handle* h, const char* path, int32_t kind, int32_t
   return write_particle_file(h, path, kind, flags);
 }
 
+int mcfg_write_statistic(mcfg_handle* h, const char* path, int64_t step, double time) {
+  GUARD(h);
+  if (!path) return set_error(h, MCFG_EINVAL, "NULL path");
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  return write_statistic_line(h, path, step, time);
+}
+
 int mcfg_set_boundary_motion(mcfg_handle* h, const int32_t* shear_type, const double* shear_freq,
                              double time) {
   GUARD(h);

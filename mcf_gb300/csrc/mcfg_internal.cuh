@@ -326,6 +326,7 @@ void destroy_graphs(Handle* h);
 // MCF's particle output (kind 0) or restart (kind 1) file formatted on the
 // device; flags & 1 adds the stress columns s(2), s(3)
 int write_particle_file(Handle* h, const char* path, int kind, int flags);
+int write_statistic_line(Handle* h, const char* path, int64_t step, double time);
 int colloid_drag(Handle* h, double* drag, double* torque);
 int colloid_move(Handle* h, const double* d_xnew, const double* d_rot);
 int check_device_errors(Handle* h);

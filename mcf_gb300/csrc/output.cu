@@ -20,6 +20,8 @@
 // boundary can differ).
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
+#include <string>
 
 #include "mcfg_internal.cuh"
 
@@ -270,6 +272,69 @@ int write_particle_file(Handle* h, const char* path, int kind, int flags) {
   if (ok && bytes > 0) ok = std::fwrite(h->out_host, 1, bytes, f) == bytes;
   ok = (std::fclose(f) == 0) && ok;
   if (!ok) return set_error(h, MCFG_EINVAL, std::string("write failed: ") + path);
+  return MCFG_OK;
+}
+
+// Fortran E16.8 on the host, for the few values of a statistic line: the C
+// library's %.7E prints the same eight correctly rounded digits (ties to
+// even) as d.dddddddE+xx, one decimal exponent below E16.8's 0.dddddddd.
+static void host_e16_8(double x, std::string& line) {
+  char t[48];
+  std::string body;
+  if (std::isnan(x)) {
+    body = "NaN";
+  } else if (std::isinf(x)) {
+    body = x < 0 ? "-Infinity" : "Infinity";
+  } else {
+    const double ax = std::fabs(x);
+    std::string digits = "00000000";
+    int e = 0;
+    if (ax != 0.0) {
+      std::snprintf(t, sizeof t, "%.7E", ax);
+      digits[0] = t[0];
+      for (int i = 0; i < 7; ++i) digits[1 + i] = t[2 + i];
+      e = std::atoi(t + 10) + 1;
+    }
+    if (std::signbit(x)) body += '-';
+    body += "0.";
+    body += digits;
+    const int ae = e < 0 ? -e : e;
+    if (ae <= 99)
+      std::snprintf(t, sizeof t, "E%c%02d", e < 0 ? '-' : '+', ae);
+    else
+      std::snprintf(t, sizeof t, "%c%03d", e < 0 ? '-' : '+', ae);
+    body += t;
+  }
+  if (body.size() < 16) line.append(16 - body.size(), ' ');
+  line += body;
+}
+
+int write_statistic_line(Handle* h, const char* path, int64_t step, double time) {
+  const int d = h->p.num_dim;
+  double ke = 0.0, mom[3] = {0.0, 0.0, 0.0}, st[9] = {0.0};
+  const int rc = statistics(h, &ke, mom, st);
+  if (rc != MCFG_OK) return rc;
+  std::string line;
+  if (step >= -99999999 && step <= 999999999) {
+    char t[16];
+    std::snprintf(t, sizeof t, "%9lld", (long long)step);
+    line = t;
+  } else {
+    line = "*********";
+  }
+  host_e16_8(time, line);
+  host_e16_8(ke, line);
+  for (int a = 0; a < d; ++a) host_e16_8(mom[a], line);
+  if (h->p.stress_tensor) {
+    host_e16_8(st[1], line);
+    host_e16_8(st[2], line);
+  }
+  line += '\n';
+  FILE* f = std::fopen(path, "ab");
+  if (!f) return set_error(h, MCFG_EINVAL, std::string("cannot open ") + path);
+  const bool ok = std::fwrite(line.data(), 1, line.size(), f) == line.size();
+  if (!((std::fclose(f) == 0) && ok))
+    return set_error(h, MCFG_EINVAL, std::string("write failed: ") + path);
   return MCFG_OK;
 }
 

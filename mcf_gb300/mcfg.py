@@ -81,6 +81,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "mcfg_colloid_repulsion": (C.c_int, [_h, _dp]),
         "mcfg_set_boundary_motion": (C.c_int, [_h, C.POINTER(C.c_int32), _dp, C.c_double]),
         "mcfg_write_particles": (C.c_int, [_h, C.c_char_p, C.c_int32, C.c_int32]),
+        "mcfg_write_statistic": (C.c_int, [_h, C.c_char_p, C.c_int64, C.c_double]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -168,6 +169,14 @@ class SDPD:
         self._check("mcfg_write_particles",
                     self.lib.mcfg_write_particles(self._h, str(path).encode(), int(kind),
                                                   1 if stress else 0))
+
+    def write_statistic(self, path, step: int, time: float) -> None:
+        """Append one line of MCF's statistic file (io_write_statistic):
+        step, time, kinetic energy, momentum and, with stress_tensor, the
+        stress sums s(2) s(3) (mcfg_write_statistic)."""
+        self._check("mcfg_write_statistic",
+                    self.lib.mcfg_write_statistic(self._h, str(path).encode(), int(step),
+                                                  float(time)))
 
     def set_boundary_motion(self, shear_type, shear_freq, time: float = 0.0) -> None:
         """MCF's Boundary shear_type / shear_freq per face (2 = oscillating

@@ -1,4 +1,4 @@
-"""CPU restatement of MCF's particle-file text.  TEST INFRASTRUCTURE ONLY:
+"""CPU restatement of MCF's particle-file and statistic-line text.  TEST INFRASTRUCTURE ONLY:
 the checker of the device formatter (mcfg_write_particles); the product
 never imports it.
 
@@ -6,7 +6,10 @@ MCF writes its particle output (io_write_particles.F90:225-403) and restart
 files (io_write_restart_particles.F90:100-215) with ppm_io in ASCII mode:
 WRITE(unit, '(<ncol>E16.8)') of the (ncol, N) array, one record per
 particle; the restart file first writes the particle count list-directed
-(ppm_io_write_ascii.F90: WRITE(unit, *)).  E16.8 with the default scale
+(ppm_io_write_ascii.F90: WRITE(unit, *)).  The statistic file gets one
+line per write, (I9,<n>E16.8) of step, time, kinetic energy, momentum and
+the stress sums s(2) s(3), trailing blanks trimmed
+(io_write_statistic.F90:131-257).  E16.8 with the default scale
 factor prints [-]0.d1...d8 followed by E+ee, or +eee when the exponent
 exceeds 99, right-justified in 16 columns; the eight digits here are
 Python's correctly rounded ones (ties to even), the C library's %.7E.
@@ -52,3 +55,19 @@ def particle_rows(x, v, rho, m, ids, s=None) -> str:
 
 def restart_text(x, v, rho, m, ids) -> str:
     return f"{x.shape[0]:12d}\n" + particle_rows(x, v, rho, m, ids)
+
+
+def i9(step: int) -> str:
+    """Fortran I9: right-justified in 9 columns, asterisks when it does not fit."""
+    t = str(int(step))
+    return t.rjust(9) if len(t) <= 9 else "*" * 9
+
+
+def statistic_line(step, time, k_energy, momentum, stress=None) -> str:
+    """io_write_statistic.F90:131-257 without the optional flow_v_fixed,
+    dynamic_density_ref and p_energy columns; stress is the d*d sum
+    (column-major) when stress_tensor is on."""
+    vals = [time, k_energy, *list(momentum)]
+    if stress is not None:
+        vals += [stress[1], stress[2]]
+    return (i9(step) + "".join(e16_8(v) for v in vals)).rstrip() + "\n"

@@ -4,12 +4,13 @@ byte: the particle output with and without the stress columns and the
 restart file of a stepped workload, and E16.8 of values chosen to be hard
 (decimal ties, powers of ten and their neighbours, carries into the next
 decade, signed zero, subnormals, exponents past 99, random magnitudes
-1e-17 .. 1e29)."""
+1e-17 .. 1e29); the statistic line (mcfg_write_statistic) against the
+restatement fed with the same global sums."""
 import numpy as np
 import pytest
 
 from mcf_gb300 import SDPD, configs
-from oracle.mcf_format import particle_rows, restart_text
+from oracle.mcf_format import particle_rows, restart_text, statistic_line
 
 pytestmark = pytest.mark.gpu
 
@@ -67,3 +68,22 @@ def test_hard_values_2d_and_3d(gpu_lib, tmp_path):
         assert len(got) == len(ref) == n
         bad = [(i, a, b) for i, (a, b) in enumerate(zip(got, ref)) if a != b]
         assert not bad, bad[:3]
+
+
+@pytest.mark.parametrize("stress", [False, True])
+def test_statistic_lines_appended(gpu_lib, tmp_path, stress):
+    w = configs.c5_oldroyd_b_2d(n_side=40) if not stress else configs.c2_fluctuating_3d(n_side=12)
+    w.params.stress_tensor = 1 if stress else 0
+    g = SDPD(w.params)
+    g.upload(w.x, w.v, w.m, w.id)
+    g.marching_init_force(0)
+    path = tmp_path / "mcf_statistic.dat"
+    ref = ""
+    for s0 in (0, 5, 10):
+        if s0:
+            g.run_vv(s0 - 5, 5, w.dt)
+        ke, mom, st = g.statistic_compute_statistic()
+        g.write_statistic(path, s0, s0 * w.dt)
+        ref += statistic_line(s0, s0 * w.dt, ke, mom[: w.x.shape[1]], st if stress else None)
+    assert path.read_text() == ref
+    assert path.read_text().count("\n") == 3

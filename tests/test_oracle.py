@@ -142,6 +142,33 @@ def test_walls_channel_setup():
     assert np.allclose(rho[fl], rho[fl][0], rtol=1e-9)
 
 
+def test_transient_poiseuille_against_series():
+    # MCF's own validation case (the series of poiseuille_theoretical_2d.perl):
+    # 2D channel of 20 dx, from rest under g_x = 0.01, profile at t = 40
+    # (0.1 L^2 / nu).  Against the series with the no-slip planes at the
+    # domain faces the profile is within 5% of u_max; what is left is a
+    # uniform slip: with the planes 0.2 dx outside the faces it is within
+    # 0.3% of u_max.
+    from oracle.analytic import poiseuille_transient
+    w = configs.poiseuille_channel(dim=2, n_side=20)
+    o = Oracle(w.params)
+    o.upload(w.x, w.v, w.m, w.id)
+    o.marching_init_force(0)
+    o.run_vv(0, 4000, w.dt)
+    d = o.download("x", "v")
+    fl = w.id[:, 1] == 0
+    y, vx = d["x"][fl, 1], d["v"][fl, 0]
+    L, t = 20.0, 4000 * w.dt
+    ua = poiseuille_transient(y, t, 0.01, 1.0, L)
+    assert np.max(np.abs(vx - ua)) / ua.max() < 0.05
+    ub = poiseuille_transient(y + 0.2, t, 0.01, 1.0, L + 0.4)
+    assert np.max(np.abs(vx - ub)) / ub.max() < 3e-3
+    rows = np.floor(y).astype(int)  # laminar: one velocity per lattice row, mirror-symmetric
+    prof = np.array([vx[rows == r].mean() for r in range(20)])
+    assert max(np.ptp(vx[rows == r]) for r in range(20)) < 1e-9 * ub.max()
+    assert np.allclose(prof, prof[::-1], rtol=0, atol=1e-9 * ub.max())
+
+
 def test_golden_fixtures_regression():
     from tests.golden import make_golden
 
