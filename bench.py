@@ -25,7 +25,10 @@ pinned host memory, runs the step and copies x, v back (the positions' copy
 overlapping the sweeps on a second stream); masses, ids and the initial
 forces go over once, before the timed steps.  `output_write` times MCF's
 particle output file of the workload written through mcfg_write_particles
-(E16.8 text formatted on the device).  `cpu_baseline` is the CPU restatement
+(E16.8 text formatted on the device).  `lees_edwards` times a sheared box
+of the same size (y faces sliding along x, bcdef 10) with the cell list
+rebuilt every step and with the candidate list kept across steps.
+`cpu_baseline` is the CPU restatement
 of MCF's path (the oracle; MCF itself cannot be built here) on the host
 cores.  With --impl reference only that CPU path is timed.
 
@@ -75,6 +78,7 @@ def parse():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-list-reuse", action="store_true")
     ap.add_argument("--no-output", action="store_true")
+    ap.add_argument("--no-lees-edwards", action="store_true")
     ap.add_argument("--accuracy-steps", type=int, default=200)
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     return ap.parse_args()
@@ -544,6 +548,32 @@ def run_ours(args, ws, rank, local):
         output = {"particles": int(w.n), "bytes": int(nbytes), "seconds": tw,
                   "path": "mcfg_write_particles: device E16.8 formatting, one device-to-host "
                           "copy, one fwrite (to a temporary file)"}
+    # Lees-Edwards shear (y faces sliding along x) on the same box: MCF's
+    # cell list rebuilt every step, and the candidate list kept while the
+    # images across the faces move less than the skin
+    lees_edwards = None
+    if not args.no_lees_edwards:
+        kle = max(3, min(args.steps, 50))
+        lees_edwards = {"workload": f"Lees-Edwards 3D {args.n_side}^3 FP32-mixed, shear rate 0.05, "
+                                    "kT 1e-4, dt 1e-3", "steps": kle}
+        for name, ru in (("rebuild_every_step", 0), ("list_reuse", 1)):
+            wl = configs.lees_edwards(dim=3, n_side=args.n_side, shear_rate=0.05,
+                                      precision=PRECISION_FP32_MIXED, kt=1e-4)
+            wl.params.device = local
+            wl.params.reserved[1] = ru
+            sl = SDPD(wl.params)
+            sl.upload(wl.x, wl.v, wl.m, wl.id)
+            sl.marching_init_force(0)
+            sl.run_vv(0, args.warmup, wl.dt)
+            rb0 = sl.info()["list_rebuilds"]
+            tl, _ = timed_run(sl, torch, kle, args.warmup, wl.dt, ws)
+            tl = max_over_ranks(tl, ws)
+            lees_edwards[name] = {"value": aggregate_throughput(wl.n * kle, tl, ws), "unit": UNIT,
+                                  "ms_per_step": 1e3 * tl / kle}
+            if ru:
+                lees_edwards[name]["rebuilds_in_timed_steps"] = sl.info()["list_rebuilds"] - rb0
+                lees_edwards[name]["skin"] = sl.info()["skin"]
+            del sl
     adjoint = None
     if not args.no_adjoint:
         w5 = configs.c5_oldroyd_b_2d()
@@ -570,7 +600,7 @@ def run_ours(args, ws, rank, local):
                    "neighbour_capacity": info["neigh_capacity"], "max_neigh": info["max_neigh"],
                    "pairs_per_step": info["num_pairs"], "list_reuse": list_reuse},
         "roofline": roof, "fp64": fp64, "fp32_error_vs_fp64": err, "e2e": e2e,
-        "adjoint": adjoint, "output_write": output,
+        "adjoint": adjoint, "output_write": output, "lees_edwards": lees_edwards,
         "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
         "pair_interactions_per_s": info["num_pairs"] * args.steps * ws / tmax,
     }

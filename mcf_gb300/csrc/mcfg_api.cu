@@ -250,15 +250,15 @@ void make_consts(const mcfg_params& p, Consts& k) {
   for (int f = 0; f < 2 * k.d; ++f)
     if (p.bcdef[f] == MCFG_BC_WALL_SOLID) k.walls = 1;
   k.reuse = 0;
-  // the candidate list's images would have to follow the Lees-Edwards
-  // offset between rebuilds: list reuse stays off with Lees-Edwards faces
-  if (p.reserved[1] != 0 && !k.le) {
+  k.le_dS = 0.0;
+  if (p.reserved[1] != 0) {
     double csmin = 1e300;
     for (int a = 0; a < k.d; ++a) csmin = std::min(csmin, k.cs[a]);
     const double skin = 0.99 * (csmin - p.cut_off);
     if (skin > 0.0) {
       k.reuse = 1;
       k.half_skin2 = 0.25 * skin * skin;
+      k.half_skin_le2 = k.half_skin2;
       const double rv = p.cut_off + skin;
       k.rv2f = (float)(rv * rv * (1.0 + 1e-4));
     }
@@ -331,7 +331,10 @@ void make_consts(const mcfg_params& p, Consts& k) {
 
 namespace {
 
-void fill_consts(Handle* h) { make_consts(h->p, h->k); }
+void fill_consts(Handle* h) {
+  make_consts(h->p, h->k);
+  h->le_skin = h->k.reuse ? 2.0 * std::sqrt(h->k.half_skin2) : 0.0;
+}
 
 // conformation tensor: host (d*d, N) interleaved -> device [c][n]; identity
 // when no host array is given (particles_init_partial_inter.F90:145-148)
@@ -639,19 +642,41 @@ void boundary_update(Handle* h, double time_r, double time_v) {
   }
   if (k.le) {
     // :102-122: images above the y+ face shift by (v0(y+) - v0(y-)) time_r
-    // along x; the stencil of the rows across the face follows S mod L_x
+    // along x
     const double S = (p.wall_v[3][0] - p.wall_v[2][0]) * time_r;
     k.le_S = S;
-    const double L = k.len[0];
-    double sm = std::fmod(S, L);
-    if (sm < 0.0) sm += L;
-    const double q = sm * k.rdx[0];
-    const double cu = std::ceil(q), cl = std::floor(q);
-    k.le_cu = (int)cu % k.nm[0];
-    k.le_cl = (int)cl % k.nm[0];
-    k.le_pu = cu - q;
-    k.le_pl = q - cl;
+    // the stencil of the rows across the face follows S mod L_x; with a
+    // candidate list in place it keeps the rebuild's cells while the images
+    // have moved less than the skin (past that the list is dropped)
+    const double dS = S - h->le_S_ref;
+    if (k.reuse && h->reuse_valid && std::fabs(dS) < h->le_skin) {
+      k.le_dS = dS;
+      const double m = 0.5 * (h->le_skin - std::fabs(dS));
+      k.half_skin_le2 = m * m;
+    } else {
+      le_map(h);
+      h->reuse_valid = false;
+    }
   }
+}
+
+// the cells of the Lees-Edwards crossing rows for the current shift, which
+// becomes the reference of the next candidate list
+void le_map(Handle* h) {
+  Consts& k = h->k;
+  const double S = k.le_S;
+  const double L = k.len[0];
+  double sm = std::fmod(S, L);
+  if (sm < 0.0) sm += L;
+  const double q = sm * k.rdx[0];
+  const double cu = std::ceil(q), cl = std::floor(q);
+  k.le_cu = (int)cu % k.nm[0];
+  k.le_cl = (int)cl % k.nm[0];
+  k.le_pu = cu - q;
+  k.le_pl = q - cl;
+  k.le_dS = 0.0;
+  k.half_skin_le2 = k.half_skin2;
+  h->le_S_ref = S;
 }
 
 int vv_step(Handle* h, int64_t step, double dt) {
@@ -669,6 +694,17 @@ int vv_step(Handle* h, int64_t step, double dt) {
     PhaseScope ps(h, kPhaseUpdate);
     h->unwrapped = true;
     TRY(kick_drift_reuse(h, dt));
+    if (h->k.le) {
+      // a rebuild in this step takes the crossing rows' cells of the
+      // current shift: the host reads the device's decision
+      int flag = 0;
+      if (cuda_check(h, cudaMemcpyAsync(&flag, h->d_rebuild, sizeof(int), cudaMemcpyDeviceToHost,
+                                        h->stream),
+                     "rebuild flag") ||
+          cuda_check(h, cudaStreamSynchronize(h->stream), "rebuild flag sync"))
+        return MCFG_ECUDA;
+      if (flag != 0) le_map(h);
+    }
   } else {
     // no candidate list yet: MCF's kick-drift-wrap; the rebuild follows
     TRY(kdw(h, dt));

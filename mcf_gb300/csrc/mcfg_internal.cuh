@@ -75,11 +75,18 @@ struct Consts {
   // + 3/1 when le), images above the y+ face at x + le_S modulo L_x with
   // velocity + le_dv; the crossing rows' x cells start le_cu + 1 cells left
   // (top row) / le_cl - 1 cells right (bottom row) of the home cell, and
-  // their FP32 slot offsets are shifted by -le_pu / -le_pl cell sides
+  // their FP32 slot offsets are shifted by -le_pu / -le_pl cell sides.
+  // With list reuse the crossing rows' cells stay those of the shift at the
+  // last rebuild (le_cu .. le_pl computed from it) and le_dS = le_S minus
+  // that shift moves the images of their slot offsets (0 otherwise); home
+  // particles of the crossing rows then rebuild at a displacement of
+  // (skin - |le_dS|) / 2, half_skin_le2 its square.
   int le, ns;
   double le_S, le_dv;
   int le_cu, le_cl;
   double le_pu, le_pl;
+  double le_dS;
+  double half_skin_le2;
   // physics
   int rhs_density_type, rhs_force_type, eos_type;
   double c2, rho_ref, gamma, p0;
@@ -128,6 +135,8 @@ struct Handle {
   int32_t shear_type[6] = {0, 0, 0, 0, 0, 0};
   double shear_freq[6] = {0, 0, 0, 0, 0, 0};
   double time_current = 0.0;
+  // Lees-Edwards with list reuse: the shift of the last rebuild and the skin
+  double le_S_ref = 0.0, le_skin = 0.0;
   int64_t launches = 0;
   int64_t device_bytes = 0;
   int64_t num_outside = 0;
@@ -326,6 +335,7 @@ void destroy_graphs(Handle* h);
 // MCF's particle output (kind 0) or restart (kind 1) file formatted on the
 // device; flags & 1 adds the stress columns s(2), s(3)
 int write_particle_file(Handle* h, const char* path, int kind, int flags);
+void le_map(Handle* h);
 int write_statistic_line(Handle* h, const char* path, int64_t step, double time);
 int colloid_drag(Handle* h, double* drag, double* torque);
 int colloid_move(Handle* h, const double* d_xnew, const double* d_rot);

@@ -87,13 +87,18 @@ __device__ __forceinline__ int slot_cell(const Consts& k, const int* c, int s, i
 // neighbour cell's origin (its image's, across a Lees-Edwards face) minus
 // the home cell's; w = the x-velocity jump added to the neighbour (+dv for
 // an image above, -dv when the home particle is the one imaged above).
+// Between list rebuilds the images have moved by le_dS since the cells of
+// the row were chosen: + le_dS for the neighbour's image above, - le_dS
+// when it is the home particle's (0 without list reuse, leaving the
+// offset unchanged).
 template <int D>
 __device__ __forceinline__ float4 slot_offset(const Consts& k, int s, int st) {
   int o[3];
   slot_dirs<D>(s, st, o);
   float ox = (float)o[0] * k.csf[0], w = 0.0f;
   if (st != 0 && o[1] == ((st == 1) ? 1 : -1)) {
-    ox = (float)(((double)o[0] - ((st == 1) ? k.le_pu : k.le_pl)) * k.cs[0]);
+    const double base = __dmul_rn((double)o[0] - ((st == 1) ? k.le_pu : k.le_pl), k.cs[0]);
+    ox = (float)__dadd_rn(base, (st == 1) ? k.le_dS : -k.le_dS);
     w = (float)((st == 1) ? k.le_dv : -k.le_dv);
   }
   return make_float4(ox, (float)o[1] * k.csf[1], D == 3 ? (float)o[2] * k.csf[2] : 0.0f, w);

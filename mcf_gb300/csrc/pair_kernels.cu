@@ -439,7 +439,9 @@ __global__ void __launch_bounds__(kReuseTPB)
   bool acc_i = false;
   double rho_i = 0.0;
   if (i < n) {
-    build_lane_table<D, kReuseTPB>(k, cell_of[i], cell_start, s_start, s_shift);
+    const int celli = cell_of[i];
+    build_lane_table<D, kReuseTPB>(k, celli, cell_start, s_start, s_shift);
+    const float4* slot_tab = slot_table(k, s_slot, celli);
     const int li = i - s_start[CENTER * kReuseTPB + tid];
     si = sid[i];
     acc_i = dyn_rho(k, si);
@@ -483,7 +485,7 @@ __global__ void __launch_bounds__(kReuseTPB)
           const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
           j = s_start[sl * kReuseTPB + tid] + q;
           const float4 oj = off[j];
-          const float4 so = s_slot[sl];
+          const float4 so = slot_tab[sl];
           const float sx = so.x, sy = so.y, sz = (D == 3) ? so.z : 0.0f;
           // the pair test as k_density's scan rounds it: (o_i - slot) - o_j
           const float tx = (oi.x - sx) - oj.x, ty = (oi.y - sy) - oj.y;
@@ -548,7 +550,7 @@ __global__ void __launch_bounds__(kReuseTPB)
           const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
           const int j = jg[u];
           const float4 oj = og[u];
-          const float4 so = s_slot[sl];
+          const float4 so = slot_tab[sl];
           const float sx = so.x, sy = so.y, sz = (D == 3) ? so.z : 0.0f;
           // the pair test as k_density's scan rounds it: (o_i - slot) - o_j
           const float tx = (oi.x - sx) - oj.x, ty = (oi.y - sy) - oj.y;

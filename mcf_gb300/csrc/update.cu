@@ -326,7 +326,8 @@ int colloid_drag(Handle* h, double* drag, double* torque) {
 // drift as k_integrate, positions left unwrapped (the candidate list and its
 // periodic images stay valid until the next rebuild, which wraps), the FP32
 // cell offsets and wall distances refreshed against the rebuild cell, and the
-// rebuild flag raised when a particle has moved more than skin/2.
+// rebuild flag raised when a particle has moved more than skin/2 (less in
+// the rows along Lees-Edwards faces) or leaves through a Lees-Edwards face.
 template <int D>
 __global__ void k_kdw_reuse(Consts k, double dt, double4_32a* __restrict__ x,
                             double4_32a* __restrict__ v, const double4_32a* __restrict__ f,
@@ -369,10 +370,10 @@ __global__ void k_kdw_reuse(Consts k, double dt, double4_32a* __restrict__ x,
     }
     const double4_32a xr = x_ref[i];
     const double dx = xv.x - xr.x, dy = xv.y - xr.y, dz = (D == 3) ? xv.z - xr.z : 0.0;
-    far = dx * dx + dy * dy + dz * dz > k.half_skin2;
     // offsets to the rebuild cell's origin (k_cell_finalize's formula)
     const int cell = cell_of[i];
     double org[3] = {0.0, 0.0, 0.0};
+    int cy = -1;
     if (cell < k.ncell) {
       int cq = cell;
 #pragma unroll
@@ -380,8 +381,16 @@ __global__ void k_kdw_reuse(Consts k, double dt, double4_32a* __restrict__ x,
         const int ca = cq % k.nm[a];
         cq /= k.nm[a];
         org[a] = k.xmin[a] + (double)ca * k.cs[a];
+        if (a == 1) cy = ca;
       }
     }
+    // a home particle of a Lees-Edwards crossing row has its pairs across
+    // the face, whose images have moved by le_dS since the rebuild; a fluid
+    // particle leaving through a y face re-enters at the rebuild (its
+    // shift and velocity jump are applied there, in this step, as MCF does)
+    const bool le_row = k.le && (cy == 0 || cy == k.nm[1] - 1);
+    far = dx * dx + dy * dy + dz * dz > (le_row ? k.half_skin_le2 : k.half_skin2);
+    if (k.le && s >= 0 && (xv.y < k.min_phys[1] || xv.y >= k.max_phys[1])) far = true;
     float4 of = off[i];
     of.x = (float)(xv.x - org[0]);
     of.y = (float)(xv.y - org[1]);
@@ -396,8 +405,9 @@ __global__ void k_kdw_reuse(Consts k, double dt, double4_32a* __restrict__ x,
   if (__any_sync(0xffffffffu, far) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
 }
 
-// periodic wrap of every particle before a rebuild; returns at once when no
-// rebuild is due
+// periodic wrap of every particle before a rebuild (Lees-Edwards re-entry
+// through the y faces as k_integrate's); returns at once when no rebuild is
+// due
 template <int D>
 __global__ void k_wrap_gated(Consts k, const int* __restrict__ flag, double4_32a* __restrict__ x,
                              double4_32a* __restrict__ v, const int* __restrict__ sid) {
@@ -408,7 +418,13 @@ __global__ void k_wrap_gated(Consts k, const int* __restrict__ flag, double4_32a
   double xs[3] = {xv.x, xv.y, xv.z}, vs[3] = {vv.x, vv.y, vv.z};
   const int s = sid[i];
 #pragma unroll
-  for (int a = 0; a < D; ++a) wrap_axis(k, a, s, xs[a], vs[a]);
+  for (int a = 0; a < D; ++a) {
+    if (a == 1 && k.le) {
+      if (s >= 0 && le_wrap<D>(k, xs, vs)) break;
+    } else {
+      wrap_axis(k, a, s, xs[a], vs[a]);
+    }
+  }
   x[i] = make_double4_32a(xs[0], xs[1], D == 3 ? xs[2] : 0.0, 0.0);
   v[i] = make_double4_32a(vs[0], vs[1], D == 3 ? vs[2] : 0.0, 0.0);
 }

@@ -2,7 +2,9 @@
 oracle: Lees-Edwards y faces (sheared images, crossing with shifted x and
 velocity) and moving / oscillating solid walls.
 
-Bars as for the fixed boundaries: FP64 density within 1e-12 relative and
+With the candidate list kept across steps (list reuse) the same bars hold
+against the oracle over 300 steps with rebuilds in between.  Bars as for
+the fixed boundaries: FP64 density within 1e-12 relative and
 acceleration within 1e-12 of the per-particle scale S_i = sum_j |a_ij| at a
 shear offset that is not a whole number of cells; kT = 0 trajectories of
 100 steps within 1e-9 of the box (positions) and 1e-7 of the velocity
@@ -134,8 +136,9 @@ def test_le_and_walls_fp32_run_vv_equals_step_vv(gpu_lib):
             assert np.array_equal(outs[0][k], outs[1][k])
 
 
+@pytest.mark.parametrize("reuse", [0, 1])
 @pytest.mark.parametrize("precision", [PRECISION_FP64, PRECISION_FP32_MIXED])
-def test_le_shear_viscosity(gpu_lib, precision):
+def test_le_shear_viscosity(gpu_lib, precision, reuse):
     # steady simple shear on the linear profile: the flux of x momentum
     # across y planes, sum_pairs r_y f_x / V -> -eta * rate (m = 1), averaged
     # over 400 steps.  (SDPD's viscous pair force is along v_ij, not r_ij,
@@ -145,6 +148,7 @@ def test_le_shear_viscosity(gpu_lib, precision):
     w = configs.lees_edwards(dim=3, n_side=16, shear_rate=rate, precision=precision)
     p = w.params
     p.stress_tensor = 1
+    p.reserved[1] = reuse
     g = SDPD(p)
     g.set_boundary_motion((0,) * 6, (0.0,) * 6, 0.0)
     g.upload(w.x, w.v, w.m, w.id)
@@ -165,6 +169,59 @@ def test_le_shear_viscosity(gpu_lib, precision):
     prof = np.array([r["v"][bins == b, 0].mean() for b in range(8)])
     ref = rate * (2.0 * np.arange(8) + 1.0 - 8.0)
     assert np.max(np.abs(prof - ref)) < 0.1 * rate * 8.0
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_le_list_reuse_fp64_trajectory(gpu_lib, dim):
+    # candidate list kept across steps: the crossing rows keep the cells of
+    # the rebuild's shift while the images move (0.007-0.01 a step against
+    # skins of 0.33-0.50), rebuilds come from the shift, from displacement
+    # and from particles re-entering through a y face
+    w = sheared(dim, 14 if dim == 3 else 20, rate=0.5)
+    g, o = pair(w, 3.7)
+    p = w.params.copy()
+    p.reserved[1] = 1
+    g = SDPD(p)
+    g.set_boundary_motion((0,) * 6, (0.0,) * 6, 3.7)
+    g.upload(w.x, w.v, w.m, w.id)
+    g.marching_init_force(0)
+    o.marching_init_force(0)
+    for s in range(1, 301):
+        g.marching_integrate_VV(s, w.dt)
+        o.marching_integrate_VV(s, w.dt)
+    info = g.info()
+    assert info["skin"] > 0.3 and 4 <= info["list_rebuilds"] <= 150
+    a = g.download("x", "v", "rho")
+    b = o.download("x", "v", "rho")
+    L = float(w.params.max_phys[0])
+    d = np.abs(a["x"] - b["x"])
+    d = np.minimum(d, L - d)
+    assert d.max() <= 1e-9 * L
+    assert np.abs(a["v"] - b["v"]).max() <= 1e-7 * np.abs(b["v"]).max()
+    assert np.max(np.abs(a["rho"] - b["rho"]) / b["rho"]) <= 1e-10
+    assert np.all((a["x"] >= 0.0) & (a["x"] < L))
+
+
+def test_le_list_reuse_fp32_matches_rebuild_every_step(gpu_lib):
+    w = sheared(3, 14, rate=0.5)
+    outs = []
+    for reuse in (0, 1):
+        p = w.params.copy()
+        p.precision = PRECISION_FP32_MIXED
+        p.reserved[1] = reuse
+        g = SDPD(p)
+        g.set_boundary_motion((0,) * 6, (0.0,) * 6, 2.5)
+        g.upload(w.x, w.v, w.m, w.id)
+        g.marching_init_force(0)
+        g.run_vv(0, 200, w.dt)
+        outs.append((g.download("x", "v"), g.info()))
+    assert outs[1][1]["list_rebuilds"] >= 2
+    L = float(w.params.max_phys[0])
+    d = np.abs(outs[0][0]["x"] - outs[1][0]["x"])
+    d = np.minimum(d, L - d)
+    assert d.max() <= 1e-6 * L
+    vs = np.abs(outs[0][0]["v"]).max()
+    assert np.abs(outs[0][0]["v"] - outs[1][0]["v"]).max() <= 1e-5 * vs
 
 
 def test_le_rejects_what_it_does_not_support(gpu_lib):
