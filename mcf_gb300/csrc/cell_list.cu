@@ -324,6 +324,7 @@ static int cell_list_launches(Handle* h, const int* gate) {
 
 int build_cell_list(Handle* h) {
   h->reuse_valid = false;  // the particle order changes under any candidate list
+  if (h->k.le) le_map(h);  // the crossing rows' cells of the current shift
   if (h->unwrapped) {      // after list-reuse steps: MCF's wrap first
     const int rc = adjust_particles(h);
     if (rc) return rc;

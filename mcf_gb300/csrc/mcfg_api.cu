@@ -334,6 +334,8 @@ namespace {
 void fill_consts(Handle* h) {
   make_consts(h->p, h->k);
   h->le_skin = h->k.reuse ? 2.0 * std::sqrt(h->k.half_skin2) : 0.0;
+  h->le_reach = h->p.cut_off + h->le_skin;
+  h->k.le_y0 = 0.5 * (h->k.min_phys[1] + h->k.max_phys[1]);
 }
 
 // conformation tensor: host (d*d, N) interleaved -> device [c][n]; identity
@@ -645,13 +647,20 @@ void boundary_update(Handle* h, double time_r, double time_v) {
     // along x
     const double S = (p.wall_v[3][0] - p.wall_v[2][0]) * time_r;
     k.le_S = S;
-    // the stencil of the rows across the face follows S mod L_x; with a
-    // candidate list in place it keeps the rebuild's cells while the images
-    // have moved less than the skin (past that the list is dropped)
+    // the stencil of the rows across the face follows S mod L_x.  With a
+    // candidate list in place the rows keep the rebuild's cells and the
+    // images move by dS.  Measured from the shear the faces impose (x
+    // velocity dv (y - y0) / L_y, which carries a particle's image across a
+    // face with the particle), a pair's separation changes by the two
+    // particles' displacements from that flow plus the flow's own change
+    // over the pair, at most |dS| (rc + skin) / L_y: the list holds while
+    // twice the largest displacement stays below skin minus that (past it
+    // the list is dropped)
     const double dS = S - h->le_S_ref;
-    if (k.reuse && h->reuse_valid && std::fabs(dS) < h->le_skin) {
+    const double m = 0.5 * (h->le_skin - std::fabs(dS) * h->le_reach / k.len[1]);
+    if (k.reuse && h->reuse_valid && m > 0.0) {
       k.le_dS = dS;
-      const double m = 0.5 * (h->le_skin - std::fabs(dS));
+      k.le_aff = dS / k.len[1];
       k.half_skin_le2 = m * m;
     } else {
       le_map(h);
@@ -675,6 +684,7 @@ void le_map(Handle* h) {
   k.le_pu = cu - q;
   k.le_pl = q - cl;
   k.le_dS = 0.0;
+  k.le_aff = 0.0;
   k.half_skin_le2 = k.half_skin2;
   h->le_S_ref = S;
 }

@@ -78,14 +78,15 @@ struct Consts {
   // their FP32 slot offsets are shifted by -le_pu / -le_pl cell sides.
   // With list reuse the crossing rows' cells stay those of the shift at the
   // last rebuild (le_cu .. le_pl computed from it) and le_dS = le_S minus
-  // that shift moves the images of their slot offsets (0 otherwise); home
-  // particles of the crossing rows then rebuild at a displacement of
-  // (skin - |le_dS|) / 2, half_skin_le2 its square.
+  // that shift moves the images of their slot offsets (0 otherwise).  The
+  // rebuild test then measures displacements against the shear the faces
+  // impose: x - x_ref - le_aff (y_ref - le_y0), le_aff = le_dS / L_y,
+  // against a bound whose square is half_skin_le2.
   int le, ns;
   double le_S, le_dv;
   int le_cu, le_cl;
   double le_pu, le_pl;
-  double le_dS;
+  double le_dS, le_aff, le_y0;
   double half_skin_le2;
   // physics
   int rhs_density_type, rhs_force_type, eos_type;
@@ -135,8 +136,9 @@ struct Handle {
   int32_t shear_type[6] = {0, 0, 0, 0, 0, 0};
   double shear_freq[6] = {0, 0, 0, 0, 0, 0};
   double time_current = 0.0;
-  // Lees-Edwards with list reuse: the shift of the last rebuild and the skin
-  double le_S_ref = 0.0, le_skin = 0.0;
+  // Lees-Edwards with list reuse: the shift of the last rebuild, the skin
+  // and the candidate radius rc + skin
+  double le_S_ref = 0.0, le_skin = 0.0, le_reach = 0.0;
   int64_t launches = 0;
   int64_t device_bytes = 0;
   int64_t num_outside = 0;

@@ -326,8 +326,9 @@ int colloid_drag(Handle* h, double* drag, double* torque) {
 // drift as k_integrate, positions left unwrapped (the candidate list and its
 // periodic images stay valid until the next rebuild, which wraps), the FP32
 // cell offsets and wall distances refreshed against the rebuild cell, and the
-// rebuild flag raised when a particle has moved more than skin/2 (less in
-// the rows along Lees-Edwards faces) or leaves through a Lees-Edwards face.
+// rebuild flag raised when a particle has moved more than skin/2 (with
+// Lees-Edwards faces: from the imposed shear, by more than the bound the
+// host derives) or leaves through a Lees-Edwards face.
 template <int D>
 __global__ void k_kdw_reuse(Consts k, double dt, double4_32a* __restrict__ x,
                             double4_32a* __restrict__ v, const double4_32a* __restrict__ f,
@@ -373,7 +374,6 @@ __global__ void k_kdw_reuse(Consts k, double dt, double4_32a* __restrict__ x,
     // offsets to the rebuild cell's origin (k_cell_finalize's formula)
     const int cell = cell_of[i];
     double org[3] = {0.0, 0.0, 0.0};
-    int cy = -1;
     if (cell < k.ncell) {
       int cq = cell;
 #pragma unroll
@@ -381,16 +381,20 @@ __global__ void k_kdw_reuse(Consts k, double dt, double4_32a* __restrict__ x,
         const int ca = cq % k.nm[a];
         cq /= k.nm[a];
         org[a] = k.xmin[a] + (double)ca * k.cs[a];
-        if (a == 1) cy = ca;
       }
     }
-    // a home particle of a Lees-Edwards crossing row has its pairs across
-    // the face, whose images have moved by le_dS since the rebuild; a fluid
-    // particle leaving through a y face re-enters at the rebuild (its
-    // shift and velocity jump are applied there, in this step, as MCF does)
-    const bool le_row = k.le && (cy == 0 || cy == k.nm[1] - 1);
-    far = dx * dx + dy * dy + dz * dz > (le_row ? k.half_skin_le2 : k.half_skin2);
-    if (k.le && s >= 0 && (xv.y < k.min_phys[1] || xv.y >= k.max_phys[1])) far = true;
+    if (k.le) {
+      // Lees-Edwards: the displacement from the shear the faces impose
+      // (which moves the images across the faces with their particles); a
+      // fluid particle leaving through a y face re-enters at the rebuild
+      // (its shift and velocity jump are applied there, in this step, as
+      // MCF does)
+      const double px = dx - k.le_aff * (xr.y - k.le_y0);
+      far = px * px + dy * dy + dz * dz > k.half_skin_le2;
+      if (s >= 0 && (xv.y < k.min_phys[1] || xv.y >= k.max_phys[1])) far = true;
+    } else {
+      far = dx * dx + dy * dy + dz * dz > k.half_skin2;
+    }
     float4 of = off[i];
     of.x = (float)(xv.x - org[0]);
     of.y = (float)(xv.y - org[1]);

@@ -174,10 +174,12 @@ def test_le_shear_viscosity(gpu_lib, precision, reuse):
 @pytest.mark.parametrize("dim", [2, 3])
 def test_le_list_reuse_fp64_trajectory(gpu_lib, dim):
     # candidate list kept across steps: the crossing rows keep the cells of
-    # the rebuild's shift while the images move (0.007-0.01 a step against
-    # skins of 0.33-0.50), rebuilds come from the shift, from displacement
-    # and from particles re-entering through a y face
+    # the rebuild's shift while the images move (0.007-0.01 a step, past a
+    # whole cell between rebuilds), rebuilds come from displacements off the
+    # imposed shear and from particles re-entering through a y face (y
+    # velocities of 0.2 carry dozens of them across)
     w = sheared(dim, 14 if dim == 3 else 20, rate=0.5)
+    w.v[:, 1] += np.random.default_rng(5).normal(0.0, 0.2, w.v.shape[0])
     g, o = pair(w, 3.7)
     p = w.params.copy()
     p.reserved[1] = 1
@@ -190,7 +192,7 @@ def test_le_list_reuse_fp64_trajectory(gpu_lib, dim):
         g.marching_integrate_VV(s, w.dt)
         o.marching_integrate_VV(s, w.dt)
     info = g.info()
-    assert info["skin"] > 0.3 and 4 <= info["list_rebuilds"] <= 150
+    assert info["skin"] > 0.3 and 3 <= info["list_rebuilds"] <= 150
     a = g.download("x", "v", "rho")
     b = o.download("x", "v", "rho")
     L = float(w.params.max_phys[0])
@@ -204,6 +206,7 @@ def test_le_list_reuse_fp64_trajectory(gpu_lib, dim):
 
 def test_le_list_reuse_fp32_matches_rebuild_every_step(gpu_lib):
     w = sheared(3, 14, rate=0.5)
+    w.v[:, 1] += np.random.default_rng(6).normal(0.0, 0.2, w.v.shape[0])
     outs = []
     for reuse in (0, 1):
         p = w.params.copy()
