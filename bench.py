@@ -274,7 +274,7 @@ def timed_run(sd, torch, nsteps, step0, dt, ws):
     return e0.elapsed_time(e1) / 1e3, launches
 
 
-def roofline_for(sd, torch, w, prec_idx, peaks, step0):
+def roofline_for(sd, torch, w, prec_idx, peaks, step0, clock_mhz=None):
     sd.set_profiling(2)
     sd.set_profiling(1)
     sd.run_vv(step0, 5, w.dt)
@@ -290,15 +290,30 @@ def roofline_for(sd, torch, w, prec_idx, peaks, step0):
     # DRAM bytes per particle of this kernel from the committed ncu summary
     # (a smaller case of the same workload, scaled by the particles)
     traffic = None
+    issue = None
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
-        per = json.loads(tf.read_text()).get("fp64" if prec_idx else "fp32", {}).get(top)
+        prof = json.loads(tf.read_text())
+        per = prof.get("fp64" if prec_idx else "fp32", {}).get(top)
         if per:
             traffic = per * w.n
+        # the pair sweeps are bound by instruction issue, not HBM: warp
+        # instructions per particle of the same ncu capture over this
+        # launch's time, against 4 warp instructions per clock per SM at
+        # the clock sampled during the timed steps
+        wi = prof.get("warp_instructions_per_particle", {}).get(
+            "fp64" if prec_idx else "fp32", {}).get(top)
+        if wi and clock_mhz:
+            sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+            ach = wi * w.n / (avg_ms / 1e3)
+            pk = 4.0 * sms * clock_mhz * 1e6
+            issue = {"achieved": ach, "peak": pk, "unit": "warp instructions/s", "frac": ach / pk,
+                     "warp_instructions_per_launch": wi * w.n, "sms": sms,
+                     "clock_mhz": clock_mhz}
     return {"kernel_phase": top, "bound": "hbm", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": (achieved / peak) if peak else None, "traffic": traffic,
             "avg_ms": avg_ms, "algo_bytes_per_launch": algo,
-            "peak_source": peaks.get("source"), "phase_share": share}
+            "peak_source": peaks.get("source"), "phase_share": share, "issue": issue}
 
 
 def adjoint_cost(torch, w, T, K, local, wts):
@@ -440,7 +455,8 @@ def run_ours(args, ws, rank, local):
     if reuse:
         list_reuse = {"skin": info["skin"], "rebuilds_in_timed_steps": info["list_rebuilds"] - r0,
                       "rebuilds_total": info["list_rebuilds"]}
-    roof = roofline_for(sd, torch, w, 0, peaks, args.warmup + args.steps)
+    roof = roofline_for(sd, torch, w, 0, peaks, args.warmup + args.steps,
+                        clocks.get("sm_mhz") if clocks else None)
     # the same FP32-mixed step with MCF's cell list rebuilt every step
     every_step = None
     if reuse:
