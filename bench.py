@@ -28,6 +28,9 @@ particle output file of the workload written through mcfg_write_particles
 (E16.8 text formatted on the device).  `lees_edwards` times a sheared box
 of the same size (y faces sliding along x, bcdef 10) with the cell list
 rebuilt every step and with the candidate list kept across steps.
+`mcf_scalability_deck` runs the physics of MCF's own 1M-particle
+scalability input (cut-off 4 dx, Batchelor equation of state, Hu-Adams
+angular force) read from an MCF deck by mcf_config.load_mcf_deck.
 `cpu_baseline` is the CPU restatement
 of MCF's path (the oracle; MCF itself cannot be built here) on the host
 cores.  With --impl reference only that CPU path is timed.
@@ -79,6 +82,7 @@ def parse():
     ap.add_argument("--no-list-reuse", action="store_true")
     ap.add_argument("--no-output", action="store_true")
     ap.add_argument("--no-lees-edwards", action="store_true")
+    ap.add_argument("--no-mcf-deck", action="store_true")
     ap.add_argument("--accuracy-steps", type=int, default=200)
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     return ap.parse_args()
@@ -590,6 +594,37 @@ def run_ours(args, ws, rank, local):
                 lees_edwards[name]["rebuilds_in_timed_steps"] = sl.info()["list_rebuilds"] - rb0
                 lees_edwards[name]["skin"] = sl.info()["skin"]
             del sl
+    # MCF's own 1M-particle scalability deck (cut-off 4 dx, Batchelor
+    # equation of state, Hu-Adams angular force), read through
+    # mcf_config.load_mcf_deck from a deck written in MCF's format
+    mcf_deck = None
+    if not args.no_mcf_deck:
+        from mcf_gb300.configs import write_mcf_scalability_deck
+        from mcf_gb300.mcf_config import load_mcf_deck
+
+        tmpd = tempfile.mkdtemp(prefix="mcfg_deck_")
+        try:
+            deck = load_mcf_deck(write_mcf_scalability_deck(tmpd, n_side=args.n_side),
+                                 precision=PRECISION_FP32_MIXED, list_reuse=True)
+        finally:
+            import shutil
+            shutil.rmtree(tmpd, ignore_errors=True)
+        wd_ = deck.workload
+        wd_.params.device = local
+        sk = SDPD(wd_.params)
+        sk.upload(wd_.x, wd_.v, wd_.m, wd_.id)
+        sk.marching_init_force(0)
+        sk.run_vv(0, args.warmup, deck.dt)
+        kd = max(3, min(args.steps, 100))
+        td, _ = timed_run(sk, torch, kd, args.warmup, deck.dt, ws)
+        td = max_over_ranks(td, ws)
+        inf = sk.info()
+        mcf_deck = {"workload": f"MCF scalability deck {args.n_side}^3 (rc 4 dx, Batchelor gamma 7, "
+                                "Hu-Adams angular), FP32-mixed with list reuse",
+                    "value": aggregate_throughput(wd_.n * kd, td, ws), "unit": UNIT,
+                    "ms_per_step": 1e3 * td / kd, "steps": kd, "dt": deck.dt,
+                    "max_neigh": inf["max_neigh"], "pairs_per_step": inf["num_pairs"]}
+        del sk
     adjoint = None
     if not args.no_adjoint:
         w5 = configs.c5_oldroyd_b_2d()
@@ -617,6 +652,7 @@ def run_ours(args, ws, rank, local):
                    "pairs_per_step": info["num_pairs"], "list_reuse": list_reuse},
         "roofline": roof, "fp64": fp64, "fp32_error_vs_fp64": err, "e2e": e2e,
         "adjoint": adjoint, "output_write": output, "lees_edwards": lees_edwards,
+        "mcf_scalability_deck": mcf_deck,
         "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
         "pair_interactions_per_s": info["num_pairs"] * args.steps * ws / tmax,
     }

@@ -244,6 +244,37 @@ def poiseuille_channel(dim: int = 2, n_side: int = 20, force: float = 0.01,
     return w
 
 
+def write_mcf_scalability_deck(folder, n_side: int = 100, box: float | None = None):
+    """Write, in MCF's deck format, the physics of MCF's 1M-particle
+    scalability input (mcf_config_test_SupMuc/ctrl.mcf and
+    physics_config.mcf): 3D periodic cube of n_side^3 lattice sites, dx =
+    0.1 (box 10 at 100^3), cut-off 0.4 = 4 dx, quintic kernel, number
+    density, Batchelor equation of state (c = 84.6, rho = 1, rho_ref = 0.9,
+    gamma = 7), Hu-Adams angular force (rhs_force_type 4, eta = 8.46,
+    eta_coef = 4), no noise, no body force, 2000 steps, dt from MCF's
+    criteria (the viscous one, 2.63e-4).  Returns the folder."""
+    from pathlib import Path
+    f = Path(folder)
+    f.mkdir(parents=True, exist_ok=True)
+    L = box if box is not None else 0.1 * n_side
+    ctrl = {"job_name": "ppm_mcf_scalability", "mcf_physics_config_file": "physics_config.mcf",
+            "relax_run": "F", "read_external": "F", "kernel_type": 1, "symmetry": "T",
+            "rhs_density_type": 2, "dynamic_density_ref": "F", "stateEquation_type": 2,
+            "Newtonian": "T", "Brownian": "F", "random_seed": -1, "rhs_force_type": 4,
+            "pp_interact_cc": "F", "p_energy": "F", "flow_v_fixed": "F", "integrate_type": 2,
+            "adaptive_dt": 0}
+    phys = {"num_species": 1, "num_dim": 3, "min_phys": "0.0, 0.0, 0.0",
+            "max_phys": f"{L!r}, {L!r}, {L!r}", "lattice": 1,
+            "num_part": f"{n_side}, {n_side}, {n_side}", "cut_off": 0.4, "dt": -1.0,
+            "step_start": 0, "step_end": 2000, "rho": 1.0, "eta": 8.46, "eta_coef": 4.0,
+            "kt": 0.0, "c": 84.6, "rho_ref": 0.9, "gamma": 7.0, "body_force_type": 0,
+            "body_force": "0.0, 0.0, 0.0", "num_colloid": 0, "bcdef": "1,1,1,1,1,1",
+            "shear_type": "1,1,1,1,1,1", "wall_rho_type": 0, "wall_noslip": 2}
+    (f / "ctrl.mcf").write_text("".join(f"{k} = {v}\n" for k, v in ctrl.items()))
+    (f / "physics_config.mcf").write_text("".join(f"{k} = {v}\n" for k, v in phys.items()))
+    return f
+
+
 @dataclass
 class ColloidSet:
     params: ColloidParams
