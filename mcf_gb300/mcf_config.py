@@ -22,8 +22,12 @@ does:
   ones dropped), masses rho * dx(1) * ... * dx(d) in that order
   (particles_compute_mass.F90:363-450), pids 1..N.
 
+With read_external the particles come from the io deck's
+read_particles_file instead (io_read_particles.F90; MCF's restart files
+and those mcfg_write_particles writes).
+
 What this path does not cover is rejected with the key that asks for it
-(relaxation runs, external particle files, other lattices, the
+(relaxation runs, other lattices, the
 eigen-dynamics conformation model, adaptive time steps, dynamic reference
 density, non-spherical colloids), and the decks' output settings
 (io_config.mcf) are left to the caller.
@@ -113,10 +117,26 @@ def _get(d, key, default=None):
     return v[0] if v else default
 
 
+def read_particles_file(path, dim: int):
+    """MCF's particle input / restart file (io_read_particles.F90): the
+    particle count list-directed, then per particle x(d) v(d) rho m pid sid
+    list-directed (the restart file mcfg_write_particles writes with kind
+    1).  Returns x, v, rho, m, id as MCF lays them out."""
+    lines = Path(path).read_text().splitlines()
+    head = [t for t in lines if t.strip()]
+    n = int(_items(head[0])[0])
+    rows = [[_float(t) for t in _items(line)] for line in head[1:1 + n]]
+    if len(rows) != n or any(len(r) < 2 * dim + 4 for r in rows):
+        raise ValueError(f"{path}: expected {n} records of {2 * dim + 4} values")
+    a = np.array([r[:2 * dim + 4] for r in rows], dtype=np.float64).reshape(n, 2 * dim + 4)
+    ids = np.rint(a[:, 2 * dim + 2:2 * dim + 4]).astype(np.int32)
+    return a[:, :dim].copy(), a[:, dim:2 * dim].copy(), a[:, 2 * dim].copy(), \
+        a[:, 2 * dim + 1].copy(), ids
+
+
 def _unsupported(ctrl, phys):
     checks = [
         ("RELAX_RUN", ctrl, lambda v: _logical(v), "relaxation runs"),
-        ("READ_EXTERNAL", ctrl, lambda v: _logical(v), "particles from an external file"),
         ("DYNAMIC_DENSITY_REF", ctrl, lambda v: _logical(v), "a dynamic reference density"),
         ("FLOW_V_FIXED", ctrl, lambda v: _logical(v), "a fixed mean flow velocity"),
         ("P_ENERGY", ctrl, lambda v: _logical(v), "the potential-energy statistic"),
@@ -294,7 +314,17 @@ def load_mcf_deck(path, precision: int = PRECISION_FP64, list_reuse: bool = Fals
         mass = mass * dx[a]
     m = np.full(n, mass)
     ids = np.stack([np.arange(1, n + 1, dtype=np.int32), sid], axis=1).astype(np.int32)
+    v = np.zeros((n, dim))
+    if _logical(_get(ctrl, "READ_EXTERNAL", "F")):
+        # mcf.F90:701-734: the particles come from read_particles_file of
+        # the io deck (a restart file), the rest of the set-up stays
+        io_name = _get(ctrl, "MCF_IO_CONFIG_FILE", "io_config.mcf")
+        io_path = ctrl_path.parent / io_name
+        io = parse_mcf_file(io_path) if io_path.exists() else {}
+        fname = _get(io, "READ_PARTICLES_FILE", "mcf_restart_particles.dat")
+        x, v, _, m, ids = read_particles_file(ctrl_path.parent / fname, dim)
+        n = x.shape[0]
     name = _get(ctrl, "JOB_NAME", ctrl_path.parent.name)
-    wl = Workload(f"MCF deck {name}", params, x, np.zeros((n, dim)), m, ids, dt, n_steps)
+    wl = Workload(f"MCF deck {name}", params, x, v, m, ids, dt, n_steps)
     return McfDeck(name=name, workload=wl, dt=dt, n_steps=n_steps, step_start=step_start, h=h,
                    dx=dx, colloids=colloids, shear_type=shear_type, shear_freq=shear_freq)

@@ -2,17 +2,19 @@
 the readers' rules (key = value lines, # comments, case-insensitive keys,
 list-directed values, colloid keys once per colloid), MCF's set-up
 arithmetic (dx, wall layers, time step, masses, shear velocities) on decks
-written here, and -- where the reference tree is present -- its two sample
-decks (the 2D flow around a cylinder and the 1M-particle 3D scalability
-deck), read exactly as MCF sets them up."""
+written here, particles read from a restart file (read_external), and --
+where the reference tree is present -- its two sample decks (the 2D flow
+around a cylinder and the 1M-particle 3D scalability deck), read exactly as
+MCF sets them up."""
 import math
 from pathlib import Path
 
 import numpy as np
 import pytest
 
-from mcf_gb300.mcf_config import load_mcf_deck, parse_mcf_file
+from mcf_gb300.mcf_config import load_mcf_deck, parse_mcf_file, read_particles_file
 from mcf_gb300.params import BC_WALL_SOLID
+from oracle.mcf_format import e16_8, restart_text
 
 REF = Path("/root/reference/mcf")
 
@@ -87,8 +89,8 @@ def test_shear_v_3d_order(tmp_path):
     assert got == [[0, 1, 2], [0, 3, 4], [5, 0, 6], [7, 0, 8], [9, 10, 0], [11, 12, 0]]
 
 
-@pytest.mark.parametrize("key,val", [("relax_run", "T"), ("read_external", ".true."),
-                                     ("integrate_type", 1)])
+@pytest.mark.parametrize("key,val", [("relax_run", ".true."), ("integrate_type", 1),
+                                     ("adaptive_dt", 1)])
 def test_unsupported_ctrl_keys_are_named(tmp_path, key, val):
     ctrl = dict(CTRL)
     ctrl[key] = val
@@ -135,3 +137,26 @@ def test_reference_sample_decks():
     h = 0.4 / 3
     assert big.dt == 0.125 * h * h * 1.0 / 8.46
     assert q.reserved[0] >= 300  # rc = 4 dx: ~268 neighbours per particle
+
+
+def test_read_external_restart_file(tmp_path):
+    # a run's restart text (MCF's E16.8 records) read back as the particles
+    # of a deck with read_external: the values of the text, the same ids
+    first = load_mcf_deck(write_deck(tmp_path / "a", CTRL, channel_phys()))
+    w = first.workload
+    rng = np.random.default_rng(3)
+    v = rng.normal(0.0, 1e-2, w.x.shape)
+    rho = rng.uniform(0.9, 1.1, w.n) * 400.0
+    folder = tmp_path / "b"
+    ctrl = dict(CTRL, read_external="T", mcf_io_config_file="io.mcf")
+    write_deck(folder, ctrl, channel_phys())
+    (folder / "io.mcf").write_text("read_particles_file = restart_in.dat\n")
+    (folder / "restart_in.dat").write_text(restart_text(w.x, v, rho, w.m, w.id))
+    deck = load_mcf_deck(folder)
+    r = deck.workload
+    assert r.n == w.n and np.array_equal(r.id, w.id)
+    as_text = np.vectorize(lambda q: float(e16_8(q)))
+    assert np.array_equal(r.x, as_text(w.x)) and np.array_equal(r.v, as_text(v))
+    assert np.array_equal(r.m, as_text(w.m))
+    x2, v2, rho2, m2, id2 = read_particles_file(folder / "restart_in.dat", 2)
+    assert np.array_equal(rho2, as_text(rho))
