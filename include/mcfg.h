@@ -36,7 +36,7 @@ extern "C" {
 #define MCFG_EPHYS -6      /* physics check failed (zero mass/density, NaN)   */
 #define MCFG_ENODEV -7     /* no CUDA device / kernels not loadable           */
 #define MCFG_ETIMEOUT -8   /* a bounded device wait gave up                   */
-#define MCFG_ENOTSUP -9    /* option not supported by this build              */
+#define MCFG_ENOTSUP -9    /* option not supported by the library            */
 
 /* ---- enumerations (values are MCF's own) -------------------------------- */
 /* boundary types, PPM ppm_param.h: periodic 1, symmetry 3, wall_sym 7,
@@ -106,7 +106,10 @@ typedef struct mcfg_params {
    *   (skin = 0.99 x (smallest cell side - cut_off), so the cell stencil of
    *   the rebuild holds every pair) and re-tested exactly every step; the
    *   rebuild -- wrap, MCF's cell list, candidate list -- happens on the
-   *   device when a particle has moved more than skin/2 since the last one.
+   *   device when a particle has moved more than skin/2 since the last one
+   *   (with Lees-Edwards faces: displacements measured from the shear the
+   *   faces impose, against skin/2 less the shear's change over rc + skin,
+   *   and at every re-entry through a y face).
    *   The pair set of every step is the same as without reuse; positions
    *   may sit up to skin/2 past a periodic face between rebuilds (mcfg_download
    *   returns them wrapped).  Widen the skin with cell_factor.

@@ -1,5 +1,5 @@
 """CPU restatement of MCF's particle-file and statistic-line text.  TEST INFRASTRUCTURE ONLY:
-the checker of the device formatter (mcfg_write_particles); the product
+the tests compare the device formatter (mcfg_write_particles) with it; the product
 never imports it.
 
 MCF writes its particle output (io_write_particles.F90:225-403) and restart

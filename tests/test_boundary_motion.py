@@ -1,4 +1,4 @@
-"""Moving boundaries in the CPU oracle (the checker of the CUDA path):
+"""Moving boundaries in the CPU oracle (what the CUDA path is compared with):
 
   - Lees-Edwards y faces: images above the y+ face at x + shear_length
     modulo L_x (ppm_bcdef_le_y.inc), their velocity + the face velocity

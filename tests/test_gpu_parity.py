@@ -1,6 +1,6 @@
 """GPU parity tests: the CUDA path through the C-ABI against the CPU oracle.
 
-Bars (the benchmark spec of the plain FP64 path):
+Bars of the plain FP64 path:
   - cell lists bit-exact (per real cell, sorted host indices, PPM order);
   - per-step density within 1e-12 relative;
   - per-step acceleration within 1e-12 of the per-particle scale
