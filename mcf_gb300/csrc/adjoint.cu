@@ -63,6 +63,12 @@ struct Ckpt {
 struct AdjBuffers {
   int n = 0, d = 0, nnw = 0, K = 0, T = 0, ncell = 0, neigh = 0, nb = 0;
   std::vector<Tape> tape;  // K slots + 1 for the initial right-hand side
+  // a second set of tapes when memory allows: segment s - 1 is recomputed
+  // into one set while the reverse sweep of segment s reads the other, on
+  // its own stream (rs); ev_fill / ev_read order the two sets' reuse
+  std::vector<Tape> tape2;
+  cudaStream_t rs = nullptr;
+  cudaEvent_t ev_fill[2] = {nullptr, nullptr}, ev_read[2] = {nullptr, nullptr};
   std::vector<Ckpt> ck;    // segment starts 0, K, 2K, ...
   Ckpt last{};             // state after the last step
   double* m_h = nullptr;
@@ -80,6 +86,13 @@ struct AdjBuffers {
 
 void free_adjoint(Handle* h) {
   if (!h->adj) return;
+  AdjBuffers* b = h->adj;
+  if (b->rs) cudaStreamSynchronize(b->rs);
+  for (int q = 0; q < 2; ++q) {
+    if (b->ev_fill[q]) cudaEventDestroy(b->ev_fill[q]);
+    if (b->ev_read[q]) cudaEventDestroy(b->ev_read[q]);
+  }
+  if (b->rs) cudaStreamDestroy(b->rs);
   for (void* p : h->adj->allocs) cudaFree(p);
   delete h->adj;
   h->adj = nullptr;
@@ -143,25 +156,47 @@ int ensure_buffers(Handle* h, int K, int T) {
   int nb = (n + kAdjRedThreads - 1) / kAdjRedThreads;
   b->nb = std::max(1, std::min(nb, 1024));
   const size_t N = (size_t)n, d2 = (size_t)d * d;
-  b->tape.resize((size_t)K + 1);
-  for (Tape& t : b->tape) {
-    t = Tape{};
-    ATRY(aalloc(h, b, &t.x, N));
-    ATRY(aalloc(h, b, &t.v, N));
-    ATRY(aalloc(h, b, &t.pc, N));
-    ATRY(aalloc(h, b, &t.rho, N));
-    ATRY(aalloc(h, b, &t.pid, N));
-    ATRY(aalloc(h, b, &t.hidx, N));
-    ATRY(aalloc(h, b, &t.ncount, N));
-    ATRY(aalloc(h, b, &t.cell_of, N));
-    ATRY(aalloc(h, b, &t.cell_start, (size_t)ncell + 2));
-    ATRY(aalloc(h, b, &t.nl, (size_t)neigh * N));
-    if (nnw) {
-      ATRY(aalloc(h, b, &t.ct, d2 * N));
-      ATRY(aalloc(h, b, &t.vgt, d2 * N));
+  auto alloc_tapes = [&](std::vector<Tape>& set) -> int {
+    set.resize((size_t)K + 1);
+    for (Tape& t : set) {
+      t = Tape{};
+      ATRY(aalloc(h, b, &t.x, N));
+      ATRY(aalloc(h, b, &t.v, N));
+      ATRY(aalloc(h, b, &t.pc, N));
+      ATRY(aalloc(h, b, &t.rho, N));
+      ATRY(aalloc(h, b, &t.pid, N));
+      ATRY(aalloc(h, b, &t.hidx, N));
+      ATRY(aalloc(h, b, &t.ncount, N));
+      ATRY(aalloc(h, b, &t.cell_of, N));
+      ATRY(aalloc(h, b, &t.cell_start, (size_t)ncell + 2));
+      ATRY(aalloc(h, b, &t.nl, (size_t)neigh * N));
+      if (nnw) {
+        ATRY(aalloc(h, b, &t.ct, d2 * N));
+        ATRY(aalloc(h, b, &t.vgt, d2 * N));
+      }
     }
-  }
+    return MCFG_OK;
+  };
+  ATRY(alloc_tapes(b->tape));
   const int nseg = (T + K - 1) / K;
+  if (nseg > 1) {
+    // the second tape set, if it leaves a quarter of the device free
+    const size_t set_bytes =
+        (size_t)(K + 1) * (N * (3 * sizeof(double4_32a) + sizeof(double) + 4 * sizeof(int) +
+                                neigh * sizeof(uint16_t) + (nnw ? 2 * d2 * sizeof(double) : 0)) +
+                           sizeof(int) * ((size_t)ncell + 2));
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && free_b > set_bytes + total_b / 4 &&
+        cudaStreamCreateWithFlags(&b->rs, cudaStreamNonBlocking) == cudaSuccess) {
+      bool ok = true;
+      for (int q = 0; q < 2 && ok; ++q)
+        ok = cudaEventCreateWithFlags(&b->ev_fill[q], cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&b->ev_read[q], cudaEventDisableTiming) == cudaSuccess;
+      if (!ok) return set_error(h, MCFG_ECUDA, "adjoint stream events");
+      ATRY(alloc_tapes(b->tape2));
+    }
+    cudaGetLastError();
+  }
   b->ck.resize((size_t)nseg);
   for (int s = 0; s < nseg; ++s) ATRY(alloc_ckpt(h, b, b->ck[(size_t)s], s > 0));
   ATRY(alloc_ckpt(h, b, b->last, true));
@@ -737,12 +772,10 @@ int forward_step(Handle* h, int64_t step, double dt, const Tape* tape, double* j
 }
 
 int adjoint_step(Handle* h, const Tape& tp, int64_t step, double dt, double phi, int drift,
-                 double wscale) {
-  PhaseScope ps(h, kPhaseOther);
+                 double wscale, cudaStream_t s) {
   AdjBuffers* b = h->adj;
   const Consts& k = h->k;
   const int n = (int)h->n;
-  cudaStream_t s = h->stream;
   const double inv_sqdt = k.noise ? 1.0 / sqrt(dt) : 0.0;
   const int gp_ = std::max(1, (n + kAdjTPB - 1) / kAdjTPB);
   // lanes per particle in the pair sweeps: small systems fill the GPU with
@@ -861,21 +894,60 @@ extern "C" int mcfg_adjoint_run(mcfg_handle* h, int64_t step0, int32_t nsteps, d
       cuda_check(h, cudaMemsetAsync(b->cb_h, 0, sizeof(double) * (size_t)d2 * n, s), "zero"))
     return MCFG_ECUDA;
   const double wscale = 1.0 / (double)T;
-  for (int sg = nseg - 1; sg >= 0; --sg) {
+  // segment sg recomputed from its checkpoint into a tape set
+  auto recompute = [&](int sg, std::vector<Tape>& set) -> int {
     const int k0 = sg * K, k1 = std::min(k0 + K, T);
-    if (sg < nseg - 1) {
-      ATRY(restore_ckpt(h, b->ck[(size_t)sg]));
-      if (sg == 0) {
-        ATRY(rhs(h, step0, kForceBody, dt));
-        ATRY(record_tape(h, b->tape[(size_t)K]));
-      }
-      for (int t = k0 + 1; t <= k1; ++t)
-        ATRY(forward_step(h, step0 + t, dt, &b->tape[(size_t)(t - k0 - 1)], nullptr));
+    ATRY(restore_ckpt(h, b->ck[(size_t)sg]));
+    if (sg == 0) {
+      ATRY(rhs(h, step0, kForceBody, dt));
+      ATRY(record_tape(h, set[(size_t)K]));
     }
+    for (int t = k0 + 1; t <= k1; ++t)
+      ATRY(forward_step(h, step0 + t, dt, &set[(size_t)(t - k0 - 1)], nullptr));
+    return MCFG_OK;
+  };
+  // segment sg walked backwards from a tape set
+  auto reverse = [&](int sg, std::vector<Tape>& set, cudaStream_t st) -> int {
+    const int k0 = sg * K, k1 = std::min(k0 + K, T);
     for (int t = k1; t > k0; --t)
-      ATRY(adjoint_step(h, b->tape[(size_t)(t - k0 - 1)], step0 + t, dt,
-                        t == T ? 0.5 * dt : dt, 1, wscale));
-    if (sg == 0) ATRY(adjoint_step(h, b->tape[(size_t)K], step0, dt, 0.5 * dt, 0, 0.0));
+      ATRY(adjoint_step(h, set[(size_t)(t - k0 - 1)], step0 + t, dt, t == T ? 0.5 * dt : dt, 1,
+                        wscale, st));
+    if (sg == 0) ATRY(adjoint_step(h, set[(size_t)K], step0, dt, 0.5 * dt, 0, 0.0, st));
+    return MCFG_OK;
+  };
+  if (b->tape2.empty()) {
+    for (int sg = nseg - 1; sg >= 0; --sg) {
+      if (sg < nseg - 1) ATRY(recompute(sg, b->tape));
+      ATRY(reverse(sg, b->tape, s));
+    }
+  } else {
+    // two tape sets: while segment sg is walked back on rs from one set,
+    // segment sg - 1 is recomputed on the handle's stream into the other
+    // (the reverse sweep reads only tapes and adjoint buffers, so the two
+    // streams share no data but the tape sets; the arithmetic and its order
+    // are those of the sequential sweep)
+    std::vector<Tape>* sets[2] = {&b->tape, &b->tape2};
+    int cur = 0;  // the first pass taped the last segment into set 0
+    if (cuda_check(h, cudaEventRecord(b->ev_fill[0], s), "tape event")) return MCFG_ECUDA;
+    for (int sg = nseg - 1; sg >= 0; --sg) {
+      if (sg > 0) {
+        // set cur ^ 1 was last read by the reverse of segment sg + 1
+        if (cuda_check(h, cudaStreamWaitEvent(s, b->ev_read[cur ^ 1], 0), "tape wait"))
+          return MCFG_ECUDA;
+        ATRY(recompute(sg - 1, *sets[cur ^ 1]));
+        if (cuda_check(h, cudaEventRecord(b->ev_fill[cur ^ 1], s), "tape event"))
+          return MCFG_ECUDA;
+      }
+      if (cuda_check(h, cudaStreamWaitEvent(b->rs, b->ev_fill[cur], 0), "tape wait"))
+        return MCFG_ECUDA;
+      ATRY(reverse(sg, *sets[cur], b->rs));
+      if (cuda_check(h, cudaEventRecord(b->ev_read[cur], b->rs), "tape event"))
+        return MCFG_ECUDA;
+      cur ^= 1;
+    }
+    // the outputs below read the adjoint buffers on the handle's stream
+    if (cuda_check(h, cudaStreamWaitEvent(s, b->ev_read[cur ^ 1], 0), "reverse wait"))
+      return MCFG_ECUDA;
   }
   ATRY(restore_ckpt(h, b->last));
   h->have_list = false;
