@@ -21,6 +21,9 @@ from oracle.oracle import Oracle  # noqa: E402
 
 CASES = ("c1_small", "c2_small", "walls_small", "le_small", "couette_osc_small")
 
+# steps after which a case's state is dumped
+STEPS = {"c1_small": (1, 5, 10, 100), "c2_small": (1, 5, 10, 100)}
+
 # boundary motion of a case: (shear_type[6], shear_freq[6], time_current)
 MOTION = {
     "le_small": ((0,) * 6, (0.0,) * 6, 2.7),
@@ -72,9 +75,15 @@ def compute(name: str) -> dict:
     out = {"num_cell_dim": ncd, "cell_start": cs, "lpdx": lp}
     d0 = o.download("rho", "p", "f")
     out.update({"rho0": d0["rho"], "p0": d0["p"], "f0": d0["f"]})
-    o.run_vv(0, 5, w.dt)
-    d1 = o.download("x", "v", "rho", "f")
-    out.update({"x5": d1["x"], "v5": d1["v"], "rho5": d1["rho"], "f5": d1["f"]})
+    # per-stage dumps after steps 1, 5, 10 and 100 for the two base
+    # workloads (C1, C2), after step 5 for the others
+    marks = STEPS.get(name, (5,))
+    done = 0
+    for t in marks:
+        o.run_vv(done, t - done, w.dt)
+        done = t
+        d1 = o.download("x", "v", "rho", "f")
+        out.update({f"x{t}": d1["x"], f"v{t}": d1["v"], f"rho{t}": d1["rho"], f"f{t}": d1["f"]})
     return out
 
 

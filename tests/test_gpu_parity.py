@@ -153,16 +153,27 @@ def test_fp64_golden_fixtures(gpu_lib):
         noise = bool(w.params.Brownian and w.params.kt > 0)
         tol = 1e-5 if noise else 1e-9
         assert np.all(np.abs(d["f"] - fx["f0"]) <= tol * (np.abs(fx["f0"]).max() + 1.0))
-        # five VV steps from there (kT = 0 cases)
-        if not noise:
-            g.run_vv(0, 5, w.dt)
-            d5 = g.download("x", "v")
-            L = np.asarray(w.params.max_phys_t)[: w.params.num_dim] - \
-                np.asarray(w.params.min_phys_t)[: w.params.num_dim]
-            dx = np.abs(d5["x"] - fx["x5"])
+        # the dumped steps (1, 5, 10, 100 for C1 and C2; 5 for the others).
+        # With the random force the GPU's FP32 normals differ from the
+        # CPU's in the last bits: measured 5e-7 of the velocity scale and
+        # 8e-12 of the box after 100 C2 steps, against 7e-15 and 1e-16
+        # without it (C1)
+        L = np.asarray(w.params.max_phys_t)[: w.params.num_dim] - \
+            np.asarray(w.params.min_phys_t)[: w.params.num_dim]
+        bx, bv, br, bf = (1e-9, 1e-5, 1e-9, 1e-5) if noise else (1e-10, 1e-8, 1e-12, 1e-10)
+        done = 0
+        for t in make_golden.STEPS.get(name, (5,)):
+            g.run_vv(done, t - done, w.dt)
+            done = t
+            dt_ = g.download("x", "v", "rho", "f")
+            dx = np.abs(dt_["x"] - fx[f"x{t}"])
             dx = np.minimum(dx, L - dx)
-            assert dx.max() <= 1e-10 * L.max(), name
-            assert np.abs(d5["v"] - fx["v5"]).max() <= 1e-8 * (np.abs(fx["v5"]).max() + 1e-3), name
+            assert dx.max() <= bx * L.max(), (name, t)
+            assert np.abs(dt_["v"] - fx[f"v{t}"]).max() <= \
+                bv * (np.abs(fx[f"v{t}"]).max() + 1e-3), (name, t)
+            assert np.max(np.abs(dt_["rho"] - fx[f"rho{t}"]) / fx[f"rho{t}"]) <= br, (name, t)
+            assert np.abs(dt_["f"] - fx[f"f{t}"]).max() <= \
+                bf * (np.abs(fx[f"f{t}"]).max() + 1.0), (name, t)
 
 
 def test_stress_tensor_and_statistics(gpu_lib):
