@@ -99,8 +99,9 @@ typedef struct mcfg_params {
   double kt_p;                /* polymer kT (G = n_p*kt_p)                   */
   uint64_t seed;              /* Philox key for the Wiener increments        */
   int32_t device;             /* CUDA device ordinal                         */
-  /* reserved[0]: neighbour-list capacity per particle (0: 256 in 3D, 96 in
-   *   2D).
+  /* reserved[0]: neighbour-list capacity per particle (0: from the first
+   *   upload's mean number density, 1.3 x the particles within the cut-off
+   *   + 16, at least 256 in 3D and 96 in 2D).
    * reserved[1]: non-zero enables neighbour-list reuse in mcfg_step_vv /
    *   mcfg_run_vv: the candidates within rc + skin are listed at a rebuild
    *   (skin = 0.99 x (smallest cell side - cut_off), so the cell stencil of

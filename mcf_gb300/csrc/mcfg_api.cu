@@ -457,7 +457,20 @@ int ensure_capacity(Handle* h, int64_t n64) {
   if (n > h->cap_n || !h->x) {
     free_all(h);
     const size_t cap = (size_t)(n > 0 ? n : 1);
-    int neigh = h->p.reserved[0] > 0 ? h->p.reserved[0] : (d == 3 ? 256 : 96);
+    int neigh = h->p.reserved[0];
+    if (neigh <= 0) {
+      // room for the neighbourhood at the uploaded mean number density
+      // (pi rc^2 or 4/3 pi rc^3 of it, plus 30% and 16 for compression and
+      // disorder), at least 96 in 2D and 256 in 3D: cut-offs of 4-5 lattice
+      // spacings, as MCF's own decks use, need more than the default
+      double vol = 1.0;
+      for (int a = 0; a < d; ++a) vol *= h->p.max_phys_t[a] - h->p.min_phys_t[a];
+      const double rc = h->p.cut_off;
+      const double reach = (d == 3) ? 4.0 / 3.0 * M_PI * rc * rc * rc : M_PI * rc * rc;
+      const double est = vol > 0.0 ? (double)n / vol * reach : 0.0;
+      neigh = std::max(d == 3 ? 256 : 96, (int)std::ceil(1.3 * est + 16.0));
+      neigh = std::min((neigh + 7) / 8 * 8, 4096);
+    }
     h->neigh_cap = neigh;
     const int nbins = h->k.ncell + 1;
     const int ntiles = (nbins + 4095) / 4096 + 1;

@@ -97,6 +97,23 @@ def test_scalability_deck_physics_fp64(gpu_lib, tmp_path):
     check_trajectory(g, o, 2.0)
 
 
+def test_default_capacity_fits_the_deck_cut_off(gpu_lib, tmp_path):
+    # without an explicit capacity the library sizes the lists from the
+    # upload's number density: rc = 4 dx in 3D needs ~270 entries
+    deck = load_mcf_deck(write_mcf_scalability_deck(tmp_path / "cap", n_side=20))
+    w = deck.workload
+    rng = np.random.default_rng(14)  # off the lattice: some particles see > 256
+    w.x = np.mod(w.x + rng.uniform(-0.02, 0.02, w.x.shape), 2.0)
+    p = w.params.copy()
+    p.reserved[0] = 0
+    g = SDPD(p)
+    g.upload(w.x, w.v, w.m, w.id)
+    g.marching_init_force(0)
+    g.run_vv(0, 3, deck.dt)
+    info = g.info()
+    assert info["neigh_capacity"] >= 300 and info["max_neigh"] > 256
+
+
 def test_scalability_deck_physics_fp32(gpu_lib, tmp_path):
     deck = load_mcf_deck(write_mcf_scalability_deck(tmp_path / "supermuc32", n_side=20))
     w = deck.workload
