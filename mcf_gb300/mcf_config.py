@@ -117,6 +117,13 @@ def _get(d, key, default=None):
     return v[0] if v else default
 
 
+def _need(d, key, path):
+    v = d.get(key)
+    if not v:
+        raise ValueError(f"{path}: {key} is required")
+    return v[0]
+
+
 def read_particles_file(path, dim: int):
     """MCF's particle input / restart file (io_read_particles.F90): the
     particle count list-directed, then per particle x(d) v(d) rho m pid sid
@@ -168,10 +175,13 @@ def load_mcf_deck(path, precision: int = PRECISION_FP64, list_reuse: bool = Fals
         raise ValueError(f"NUM_DIM = {dim}: this path runs 2D and 3D")
     nspec = int(_get(phys, "NUM_SPECIES", "1"))
     ncoll = int(_get(phys, "NUM_COLLOID", "0")) if nspec > 1 else 0
-    mn = _floats(_get(phys, "MIN_PHYS"), dim)
-    mx = _floats(_get(phys, "MAX_PHYS"), dim)
-    npart = _ints(_get(phys, "NUM_PART"), dim)
-    rc = _float(_get(phys, "CUT_OFF"))
+    phys_path = ctrl_path.parent / phys_name
+    mn = _floats(_need(phys, "MIN_PHYS", phys_path), dim)
+    mx = _floats(_need(phys, "MAX_PHYS", phys_path), dim)
+    npart = _ints(_need(phys, "NUM_PART", phys_path), dim)
+    rc = _float(_need(phys, "CUT_OFF", phys_path))
+    if len(mn) < dim or len(mx) < dim or len(npart) < dim:
+        raise ValueError(f"{phys_path}: MIN_PHYS, MAX_PHYS and NUM_PART need {dim} values")
     kernel_type = int(_get(ctrl, "KERNEL_TYPE", "1"))
     h = rc / 3.0 if kernel_type == 1 else rc  # kernel_new.F90:41-63
     dx = [(mx[a] - mn[a]) / npart[a] for a in range(dim)]

@@ -160,3 +160,10 @@ def test_read_external_restart_file(tmp_path):
     assert np.array_equal(r.m, as_text(w.m))
     x2, v2, rho2, m2, id2 = read_particles_file(folder / "restart_in.dat", 2)
     assert np.array_equal(rho2, as_text(rho))
+
+
+def test_missing_required_key_is_named(tmp_path):
+    phys = channel_phys()
+    del phys["cut_off"]
+    with pytest.raises(ValueError, match="CUT_OFF is required"):
+        load_mcf_deck(write_deck(tmp_path / "m", CTRL, phys))
