@@ -80,8 +80,9 @@ def test_le_fp64_trajectory(gpu_lib, dim):
     assert g.info()["time_current"] == o.time
 
 
-def test_le_fp32_mixed_force(gpu_lib):
-    w = sheared(3, 16, amp=0.05)
+@pytest.mark.parametrize("dim", [2, 3])
+def test_le_fp32_mixed_force(gpu_lib, dim):
+    w = sheared(dim, 16 if dim == 3 else 24, amp=0.05)
     g, o = pair(w, 7.3, precision=PRECISION_FP32_MIXED)
     g.marching_init_force(0)
     o.marching_init_force(0)

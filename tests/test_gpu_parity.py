@@ -288,6 +288,18 @@ def test_fp32_mixed_force_forms_kernels_eos(gpu_lib, ftype, ktype, eos, dim):
     assert np.max(np.abs(a["f"] - b["f"]) / scale) < 1e-4
 
 
+@pytest.mark.parametrize("ftype", [2, 3, 4])
+def test_fp32_mixed_random_force(gpu_lib, ftype):
+    # the same Philox draws in the FP32-mixed path: within 1e-4 of the scale
+    w = jittered_3d(amp=0.05)
+    g, o = both(w, precision=PRECISION_FP32_MIXED, rhs_force_type=ftype, Brownian=1, kt=1e-3)
+    g.marching_init_force(23)
+    o.marching_init_force(23)
+    a = g.download("f")["f"]
+    b = o.download("f")["f"]
+    assert np.max(np.abs(a - b) / o.force_scale()[:, None]) < 1e-4
+
+
 # ----------------------------------------------------------- error handling
 def test_neighbour_overflow_is_reported(gpu_lib):
     from mcf_gb300 import MCFGError
