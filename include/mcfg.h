@@ -254,6 +254,15 @@ int mcfg_run_vv(mcfg_handle* h, int64_t step0, int32_t nsteps, double dt);
  * mcfg_download returns them on output steps). */
 int mcfg_step_vv_host(mcfg_handle* h, int64_t step, double dt, double* x, double* v);
 
+/* Page-lock a caller's host array (cudaHostRegister) so that the copies of
+ * mcfg_step_vv_host, mcfg_update_state and mcfg_download run at full DMA
+ * speed: MCF's x and v are ordinary Fortran arrays; registering them once
+ * after allocation gives the speed of pinned buffers.  Unregister before
+ * the array is freed (or reallocated by MCF).  ptr must not already be
+ * registered; bytes > 0. */
+int mcfg_host_register(mcfg_handle* h, void* ptr, int64_t bytes);
+int mcfg_host_unregister(mcfg_handle* h, void* ptr);
+
 /* Overwrite the positions, velocities and/or accelerations (any pointer may
  * be NULL) of the particles of the last mcfg_upload, in host order, keeping
  * the device's particle order and neighbour-list state: MCF's per-step

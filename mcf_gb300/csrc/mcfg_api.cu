@@ -1171,6 +1171,22 @@ int mcfg_write_particles(mcfg_handle* h, const char* path, int32_t kind, int32_t
   return write_particle_file(h, path, kind, flags);
 }
 
+int mcfg_host_register(mcfg_handle* h, void* ptr, int64_t bytes) {
+  GUARD(h);
+  if (!ptr || bytes <= 0) return set_error(h, MCFG_EINVAL, "host_register: NULL pointer or size");
+  if (cuda_check(h, cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault),
+                 "cudaHostRegister"))
+    return MCFG_ECUDA;
+  return MCFG_OK;
+}
+
+int mcfg_host_unregister(mcfg_handle* h, void* ptr) {
+  GUARD(h);
+  if (!ptr) return set_error(h, MCFG_EINVAL, "host_unregister: NULL pointer");
+  if (cuda_check(h, cudaHostUnregister(ptr), "cudaHostUnregister")) return MCFG_ECUDA;
+  return MCFG_OK;
+}
+
 int mcfg_write_statistic(mcfg_handle* h, const char* path, int64_t step, double time) {
   GUARD(h);
   if (!path) return set_error(h, MCFG_EINVAL, "NULL path");

@@ -82,6 +82,8 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "mcfg_set_boundary_motion": (C.c_int, [_h, C.POINTER(C.c_int32), _dp, C.c_double]),
         "mcfg_write_particles": (C.c_int, [_h, C.c_char_p, C.c_int32, C.c_int32]),
         "mcfg_write_statistic": (C.c_int, [_h, C.c_char_p, C.c_int64, C.c_double]),
+        "mcfg_host_register": (C.c_int, [_h, C.c_void_p, C.c_int64]),
+        "mcfg_host_unregister": (C.c_int, [_h, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -169,6 +171,17 @@ class SDPD:
         self._check("mcfg_write_particles",
                     self.lib.mcfg_write_particles(self._h, str(path).encode(), int(kind),
                                                   1 if stress else 0))
+
+    def host_register(self, a: np.ndarray) -> None:
+        """Page-lock a C-contiguous host array for full-speed copies
+        (mcfg_host_register); unregister it before it is freed."""
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("host_register needs a C-contiguous array")
+        self._check("mcfg_host_register",
+                    self.lib.mcfg_host_register(self._h, a.ctypes.data, a.nbytes))
+
+    def host_unregister(self, a: np.ndarray) -> None:
+        self._check("mcfg_host_unregister", self.lib.mcfg_host_unregister(self._h, a.ctypes.data))
 
     def write_statistic(self, path, step: int, time: float) -> None:
         """Append one line of MCF's statistic file (io_write_statistic):

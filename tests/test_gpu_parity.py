@@ -591,6 +591,34 @@ def test_step_vv_host_equals_update_step_download(gpu_lib):
         assert np.array_equal(outs[0][1], outs[1][1])
 
 
+def test_host_registered_arrays_step_alike(gpu_lib):
+    # MCF's ordinary host arrays page-locked with mcfg_host_register: the
+    # same steps as with plain arrays, bit for bit; unregistering leaves
+    # them usable
+    w = jittered_3d(n_side=14)
+    w.params.reserved[1] = 1
+    outs = []
+    for reg in (False, True):
+        g = SDPD(w.params)
+        g.upload(w.x, w.v, w.m, w.id)
+        g.marching_init_force(0)
+        st = g.download("x", "v")
+        x = np.ascontiguousarray(st["x"])
+        v = np.ascontiguousarray(st["v"])
+        if reg:
+            g.host_register(x)
+            g.host_register(v)
+        for s in range(1, 6):
+            g.step_vv_host(s, w.dt, x, v)
+        if reg:
+            g.host_unregister(x)
+            g.host_unregister(v)
+        outs.append((x.copy(), v.copy()))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    with pytest.raises(Exception):
+        g.host_unregister(x)  # no longer registered
+
+
 def test_run_vv_graph_replay_equals_step_vv(gpu_lib):
     # with list reuse mcfg_run_vv replays a captured pair of steps (the
     # Philox step from the device counter), mcfg_step_vv launches every
