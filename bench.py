@@ -21,7 +21,8 @@ steps and the same step with MCF's cell list rebuilt every step;
 --no-list-reuse times that mode as the headline).  `fp64` is the plain FP64
 path on the same workload.  `e2e` is the same metric through the C-ABI with host
 buffers: every step is one mcfg_step_vv_host call that hands x, v over from
-pinned host memory, runs the step and copies x, v back (the positions' copy
+the caller's arrays (page-locked once with mcfg_host_register, as MCF's own
+x, v would be), runs the step and copies x, v back (the positions' copy
 overlapping the sweeps on a second stream); masses, ids and the initial
 forces go over once, before the timed steps.  `output_write` times MCF's
 particle output file of the workload written through mcfg_write_particles
@@ -511,12 +512,13 @@ def run_ours(args, ws, rank, local):
     e2e = None
     if not args.no_e2e:
         n, d = w.n, 3
-        pin = lambda shape, dt_: torch.empty(shape, dtype=dt_, pin_memory=True).numpy()  # noqa
-        hx, hv, hf = pin((n, d), torch.float64), pin((n, d), torch.float64), pin((n, d), torch.float64)
-        hm, hid = pin((n,), torch.float64), pin((n, 2), torch.int32)
+        # the caller's ordinary host arrays (as MCF's x, v are), page-locked
+        # once through the library's mcfg_host_register
         st = sd.download("x", "v", "f")
-        hx[:], hv[:], hf[:] = st["x"], st["v"], st["f"]
-        hm[:], hid[:] = w.m, w.id
+        hx, hv, hf = (np.ascontiguousarray(st[k]) for k in ("x", "v", "f"))
+        hm, hid = np.ascontiguousarray(w.m), np.ascontiguousarray(w.id)
+        sd.host_register(hx)
+        sd.host_register(hv)
         ke = max(3, min(args.steps, 20))
         step = args.warmup + args.steps + 10
 
@@ -544,12 +546,15 @@ def run_ours(args, ws, rank, local):
             step_e2e(step + 2 + q)
         torch.cuda.synchronize()
         te = max_over_ranks(time.perf_counter() - t0, ws)
+        sd.host_unregister(hx)
+        sd.host_unregister(hv)
         e2e = {"value": aggregate_throughput(w.n_fluid * ke, te, ws), "unit": UNIT,
                "h2d_bytes_per_step": int(n * 3 * 8 * 2),
                "d2h_bytes_per_step": int(n * 3 * 8 * 2), "steps": ke,
-               "path": "mcfg_step_vv_host(x, v) per step with pinned host buffers: x, v to the "
-                       "device, the step, x, v back (masses, ids and the initial forces uploaded "
-                       "once before; the forces stay on the device between steps)"}
+               "path": "mcfg_step_vv_host(x, v) per step on the caller's numpy arrays, "
+                       "page-locked once with mcfg_host_register: x, v to the device, the step, "
+                       "x, v back (masses, ids and the initial forces uploaded once before; the "
+                       "forces stay on the device between steps)"}
     output = None
     if rank == 0 and not args.no_output:
         # MCF's particle output file of the whole workload, formatted on the
