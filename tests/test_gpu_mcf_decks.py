@@ -1,9 +1,11 @@
 """MCF input decks run through the C-ABI against the CPU oracle: the
 physics of MCF's 1M-particle scalability deck on a 20^3 box (cut-off 4 dx,
 ~270 neighbours a particle, Batchelor equation of state with gamma = 7,
-Hu-Adams angular force) and of its 2D flow-around-a-cylinder deck (one
-fixed colloid, cut-off 4.8 dx, Batchelor, Hu-Adams), both read by
-mcf_config.load_mcf_deck from deck files written here.
+Hu-Adams angular force), of its 2D flow-around-a-cylinder deck (one
+fixed colloid, cut-off 4.8 dx, Batchelor, Hu-Adams) and of a channel with
+solid walls and two moving spheres (wall, colloid and fluid pair terms in
+one sweep), all read by mcf_config.load_mcf_deck from deck files written
+here.
 
 Bars as for the other workloads: FP64 density within 1e-12 relative and
 acceleration within 1e-12 of the per-particle scale sum_j |a_ij|; kT = 0
@@ -138,3 +140,41 @@ def test_cylinder_deck_fp64(gpu_lib, tmp_path):
     da, ta = g.colloid_drag()
     db, tb = o.colloid_drag()
     assert np.max(np.abs(da - db)) <= 1e-10 * np.max(np.abs(db))
+
+
+def test_walls_and_colloids_together_fp64(gpu_lib, tmp_path):
+    # a deck with solid y walls and two translating, rotating spheres in the
+    # channel: wall-fluid, colloid-fluid and colloid-wall pair terms in one
+    # sweep, against the oracle
+    folder = tmp_path / "wc"
+    folder.mkdir()
+    (folder / "ctrl.mcf").write_text(
+        "mcf_physics_config_file = physics_config.mcf\nkernel_type = 1\nsymmetry = T\n"
+        "rhs_density_type = 2\nstateEquation_type = 1\nNewtonian = T\nBrownian = F\n"
+        "rhs_force_type = 3\nstress_tensor = F\nintegrate_type = 2\n")
+    (folder / "physics_config.mcf").write_text(
+        "num_species = 2\nnum_dim = 3\nmin_phys = 0, 0, 0\nmax_phys = 16, 16, 16\n"
+        "lattice = 1\nnum_part = 16, 16, 16\ncut_off = 3.0\ndt = 1e-3\nstep_end = 20\n"
+        "rho = 1.0\neta = 1.0\nc = 10.0\nrho_ref = 1.0\ngamma = 1.0\nkt = 0.0\n"
+        "body_force_type = 1\nbody_force = 0.05, 0, 0\nbcdef = 1, 1, 9, 9, 1, 1\n"
+        "wall_rho_type = 0\nwall_noslip = 2\nnum_colloid = 2\ncoll_translate = T\n"
+        "coll_rotate = T\ncoll_noslip = 2\n"
+        "coll_shape = 2\ncoll_radius = 3.2, 0\ncoll_x = 4.3, 5.1, 8.2\n"
+        "coll_v = 0.01, 0, 0\ncoll_omega = 0, 0, 0.02\n"
+        "coll_shape = 2\ncoll_radius = 2.6, 0\ncoll_x = 11.7, 10.4, 7.9\n"
+        "coll_v = -0.01, 0.005, 0\ncoll_omega = 0.01, 0, 0\n")
+    deck = load_mcf_deck(folder)
+    sid = deck.workload.id[:, 1]
+    assert (sid == 1).sum() > 0 and (sid == 2).sum() > 0 and (sid < 0).sum() == 16 * 16 * 8
+    w = deck.workload
+    w.v = np.random.default_rng(15).normal(0.0, 1e-2, w.v.shape) * (sid == 0)[:, None]
+    g, o = both(deck)
+    check_rhs(g, o)
+    for s in range(1, 21):
+        g.marching_integrate_VV(s, deck.dt)
+        o.marching_integrate_VV(s, deck.dt)
+    check_trajectory(g, o, 16.0)
+    da, ta = g.colloid_drag()
+    db, tb = o.colloid_drag()
+    assert np.max(np.abs(da - db)) <= 1e-10 * np.max(np.abs(db))
+    assert np.max(np.abs(ta - tb)) <= 1e-10 * np.max(np.abs(tb))
