@@ -1732,14 +1732,13 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
     // symmetric sweep's shared-memory partner sums cap its occupancy)
     const int n = (int)h->n;
     const int gbn = (n + 255) / 256;
-    static bool attr_set = false;
-    if (!attr_set) {
+    // the attribute is per device: set it for the handle's (a host call)
+    if (k.d == 3)
       cudaFuncSetAttribute(k_force_sym<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kWarpsPerBlock * sym_warp_bytes<3, true>());
+    else
       cudaFuncSetAttribute(k_force_sym<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kWarpsPerBlock * sym_warp_bytes<2, true>());
-      attr_set = true;
-    }
     double* jp = (double*)h->jp;
     if (k.d == 3) {
       k_force_sym<3, true><<<g, bs, kWarpsPerBlock * sym_warp_bytes<3, true>(), s>>>(
