@@ -25,6 +25,10 @@ int cuda_check(Handle* h, cudaError_t e, const char* what) {
   char buf[256];
   snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
   h->err = buf;
+  // consume the thread's last-error state: a failed call that leaves the
+  // context usable (a bad argument, an unregistered pointer) must not fail
+  // the next launch check of this or another handle
+  cudaGetLastError();
   return MCFG_ECUDA;
 }
 
