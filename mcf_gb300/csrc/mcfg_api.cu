@@ -1178,7 +1178,7 @@ int mcfg_write_particles(mcfg_handle* h, const char* path, int32_t kind, int32_t
 int mcfg_host_register(mcfg_handle* h, void* ptr, int64_t bytes) {
   GUARD(h);
   if (!ptr || bytes <= 0) return set_error(h, MCFG_EINVAL, "host_register: NULL pointer or size");
-  if (cuda_check(h, cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault),
+  if (cuda_check(h, cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterPortable),
                  "cudaHostRegister"))
     return MCFG_ECUDA;
   return MCFG_OK;

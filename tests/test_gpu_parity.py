@@ -617,6 +617,7 @@ def test_host_registered_arrays_step_alike(gpu_lib):
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
     with pytest.raises(Exception):
         g.host_unregister(x)  # no longer registered
+    g.step_vv_host(6, w.dt, x, v)  # the failed call leaves the handle usable
 
 
 def test_run_vv_graph_replay_equals_step_vv(gpu_lib):
