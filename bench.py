@@ -201,10 +201,44 @@ def cpu_baseline(w, steps: int, threads: int | None = None) -> dict:
     t0 = time.perf_counter()
     o.run_vv(0, steps, w.dt)
     dt = time.perf_counter() - t0
-    return {"value": w.n_fluid * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{w.name}: {steps} full VV steps of all {w.n} particles "
-                      f"({w.n_fluid} fluid), OpenMP full-stencil loops, {dt:.1f} s",
-            "seconds_per_step": dt / steps}
+    out = {"value": w.n_fluid * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{w.name}: {steps} full VV steps of all {w.n} particles "
+                     f"({w.n_fluid} fluid), OpenMP full-stencil loops, {dt:.1f} s",
+           "seconds_per_step": dt / steps, "cpu_model": cpu_model()}
+    if threads > 1:
+        # one core, MCF's symmetric loops: the work of one MCF MPI rank,
+        # on a 40^3 sub-box of the same workload (one step, a few seconds)
+        from mcf_gb300 import configs
+        ws_ = configs.c3_poiseuille_3d(n_side=40)
+        o1 = Oracle(ws_.params, threads=1)
+        o1.upload(ws_.x, ws_.v, ws_.m, ws_.id)
+        o1.marching_init_force(0)
+        t0 = time.perf_counter()
+        o1.run_vv(0, 1, ws_.dt)
+        t1 = time.perf_counter() - t0
+        out["single_core"] = {"value": ws_.n_fluid / t1, "unit": UNIT, "cores": 1,
+                              "sample": f"1 full VV step of the 40^3 + walls sub-box "
+                                        f"({ws_.n} particles), symmetric loops, {t1:.1f} s"}
+    return out
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (Linux /proc/cpuinfo; Arm hosts may only
+    name the implementer and part), with the core count."""
+    name = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            k = line.split(":", 1)[0].strip().lower()
+            if k in ("model name", "cpu model", "hardware") and not name:
+                name = line.split(":", 1)[1].strip()
+            elif k == "cpu part" and not name:
+                part = line.split(":", 1)[1].strip()
+                name = {"0xd4f": "Arm Neoverse V2", "0xd40": "Arm Neoverse V1",
+                        "0xd0c": "Arm Neoverse N1"}.get(part, "Arm cpu part " + part)
+    except OSError:
+        pass
+    import platform
+    return f"{name or platform.processor() or platform.machine()} ({os.cpu_count()} cores)"
 
 
 def run_reference(args, ws, rank):
