@@ -45,10 +45,6 @@ from .configs import Workload, lattice, wall_sid
 from .params import (BC_LE, BC_PERIODIC, BC_WALL_SOLID, PRECISION_FP64, ColloidParams,
                      SDPDParams, make_params)
 
-# colloid keys that MCF reads once per colloid, in order
-_PER_COLLOID = ("COLL_SHAPE", "COLL_RADIUS", "COLL_FREQ", "COLL_M", "COLL_MMI", "COLL_X",
-                "COLL_V", "COLL_ROT_VECTOR", "COLL_THETA", "COLL_OMEGA")
-
 
 def parse_mcf_file(path) -> dict[str, list[str]]:
     """`key = value` lines of an MCF config file: upper-case keys, each with

@@ -16,7 +16,6 @@ HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
 
 from mcf_gb300 import configs  # noqa: E402
-from mcf_gb300.params import make_params  # noqa: E402
 from oracle.oracle import Oracle  # noqa: E402
 
 CASES = ("c1_small", "c2_small", "walls_small", "le_small", "couette_osc_small")
