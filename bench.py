@@ -551,12 +551,16 @@ def run_ours(args, ws, rank, local):
         st = sd.download("x", "v", "f")
         hx, hv, hf = (np.ascontiguousarray(st[k]) for k in ("x", "v", "f"))
         hm, hid = np.ascontiguousarray(w.m), np.ascontiguousarray(w.id)
-        registered = True
-        try:
-            sd.host_register(hx)
-            sd.host_register(hv)
-        except Exception:  # page-locking refused: the same steps on pageable arrays
-            registered = False
+        # each array is unregistered only if its own registration succeeded;
+        # page-locking refused: the same steps on pageable arrays
+        locked = []
+        for a in (hx, hv):
+            try:
+                sd.host_register(a)
+                locked.append(a)
+            except Exception:
+                break
+        registered = len(locked) == 2
         ke = max(3, min(args.steps, 20))
         step = args.warmup + args.steps + 10
 
@@ -577,16 +581,17 @@ def run_ours(args, ws, rank, local):
         sd.upload_force(hf)
         for q in range(2):
             step_e2e(step + q)
-        barrier(ws)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for q in range(ke):
-            step_e2e(step + 2 + q)
-        torch.cuda.synchronize()
-        te = max_over_ranks(time.perf_counter() - t0, ws)
-        if registered:
-            sd.host_unregister(hx)
-            sd.host_unregister(hv)
+        try:
+            barrier(ws)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for q in range(ke):
+                step_e2e(step + 2 + q)
+            torch.cuda.synchronize()
+            te = max_over_ranks(time.perf_counter() - t0, ws)
+        finally:
+            for a in locked:
+                sd.host_unregister(a)
         e2e = {"value": aggregate_throughput(w.n_fluid * ke, te, ws), "unit": UNIT,
                "h2d_bytes_per_step": int(n * 3 * 8 * 2),
                "d2h_bytes_per_step": int(n * 3 * 8 * 2), "steps": ke,

@@ -411,17 +411,27 @@ int mcfg_get_phase_times(mcfg_handle* h, double* ms, int64_t* counts);
  * variant of mcfg_compute_density.  x [n*d], m [n], id [n*2] and the output
  * rho [n] are DEVICE pointers owned by the caller, laid out like the host
  * arrays of mcfg_upload; stream is a cudaStream_t (NULL = default stream)
- * and the call is asynchronous on it.  Nothing is allocated: the cell list
- * lives in a fixed array inside the library (about 1.3 MB, held on every GPU
- * that loads the library until the process exits), so n <= 65,536 and the
- * mesh may have at most 65,536 real cells; larger inputs return MCFG_EINVAL.
- * The first call on a device looks up that array's device address (with the
- * device current); make that first call before any stream capture.  All
- * calls share the array: calls whose GPU work overlaps race, so serialise
- * them.  Errors: mcfg_noalloc_error(). */
-int mcfg_density_noalloc(const mcfg_params* params, int32_t n, const double* x,
-                         const double* m, const int32_t* id, double* rho,
+ * and the call is asynchronous on it.  Species rules as mcfg_compute_density:
+ * fluid sums over its pairs, walls when params->wall_rho_type is 1, colloid
+ * boundary particles (sid > 0) when coll_rho_type is 1 (the rho_type of
+ * mcfg_colloid_params; 0 = constant init_density); the others get the
+ * constant density.  Sums run in a fixed order (host index order inside
+ * each cell): repeated calls give identical bits.  Nothing is allocated: the
+ * cell list lives in a fixed array inside the library (about 1.3 MB, held on
+ * every GPU that loads the library until the process exits), so
+ * n <= 65,536 and the mesh may have at most 65,536 real cells; larger inputs
+ * return MCFG_EINVAL.  The first call on a device looks up that array's
+ * device address (with the device current); make that first call before
+ * any stream capture.  The caller's current device is the same after the
+ * call.  All calls share the array: calls whose GPU work overlaps race, so
+ * serialise them.  Errors: mcfg_noalloc_error(). */
+int mcfg_density_noalloc(const mcfg_params* params, int32_t coll_rho_type, int32_t n,
+                         const double* x, const double* m, const int32_t* id, double* rho,
                          void* stream);
+/* Status of the last mcfg_density_noalloc on device: waits for stream and
+ * sets *flags to 0, or to 1 when a density came out <= 0 or NaN (the handle
+ * path's MCFG_EPHYS condition).  Allocates nothing. */
+int mcfg_noalloc_status(int32_t device, void* stream, int32_t* flags);
 const char* mcfg_noalloc_error(void);
 
 #ifdef __cplusplus

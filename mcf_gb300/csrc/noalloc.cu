@@ -10,14 +10,19 @@
 //
 // Limits: at most kNoAllocMaxParticles particles and kNoAllocMaxCells real
 // cells per call.  Every call uses the same array and it keeps the previous
-// call's contents, so the per-cell counters are cleared at the start of each
-// call, and calls whose GPU work overlaps (different streams, or different
-// host threads on one device) race on it: serialise them.
+// call's contents, so the per-cell counters and the status word are cleared
+// at the start of each call, and calls whose GPU work overlaps (different
+// streams, or different host threads on one device) race on it: serialise
+// them.
 //
 // The sweep is the density of particles_compute_density.F90:369-867 (same
 // PPM box index, same FP64 pair separation and cut-off test, same species
-// rules) computed with a plain cell-list gather; it is a variant of the
-// handle-based mcfg_compute_density and agrees with it to rounding.
+// rules: fluid always sums, walls with wall_rho_type 1 and colloid boundary
+// particles with a dynamic colloid density) computed with a plain cell-list
+// gather.  Each cell's particles are visited in host index order, as in
+// PPM's stable cell list, so the sums have a fixed order and repeated calls
+// give identical bits; the result agrees with mcfg_compute_density to
+// rounding.
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -32,9 +37,13 @@ using namespace mcfg;
 
 constexpr int kNoAllocMaxParticles = 1 << 16;  // 65,536
 constexpr int kNoAllocMaxCells = 1 << 16;      // 65,536 real cells
-// layout in int32 words: key[P] | rank[P] | order[P] | cnt[C+1] | start[C+2]
+// layout in int32 words:
+//   key[P] | rank[P] | order[P] | cnt[C+1] | status | start[C+2]
+// rank[] is reused for the host-index order of each cell after the scatter;
+// status (cleared with the counters) collects kNaZeroDensity
 constexpr size_t kScratchWords =
-    3 * (size_t)kNoAllocMaxParticles + 2 * (size_t)kNoAllocMaxCells + 3;
+    3 * (size_t)kNoAllocMaxParticles + 2 * (size_t)kNoAllocMaxCells + 4;
+constexpr int kNaZeroDensity = 1;  // a density came out <= 0 (or NaN)
 
 static __device__ __align__(256) int g_noalloc_scratch[kScratchWords];
 
@@ -42,6 +51,28 @@ std::mutex g_mu;
 constexpr int kMaxDevices = 64;
 int* g_scratch_dev[kMaxDevices] = {};  // device address per device ordinal
 std::string g_err = "no error";
+
+// A failed CUDA call also leaves the error as the thread's last error; take
+// it off so that a later, unrelated launch check does not report it again.
+int cuda_fail(const char* what, cudaError_t e) {
+  (void)cudaGetLastError();
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return MCFG_ECUDA;
+}
+
+// Puts the caller's current device back when the call returns.
+struct DeviceRestore {
+  int prev = -1;
+  DeviceRestore() {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      (void)cudaGetLastError();
+      prev = -1;
+    }
+  }
+  ~DeviceRestore() {
+    if (prev >= 0 && cudaSetDevice(prev) != cudaSuccess) (void)cudaGetLastError();
+  }
+};
 
 // The array's name is a host-side stand-in in host code: its device address
 // is looked up once per device, with that device current.
@@ -53,8 +84,9 @@ int scratch_address(int dev, int** out) {
   if (!g_scratch_dev[dev]) {
     int* ptr = nullptr;
     cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess || ptr == nullptr) {
-      g_err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+    if (e != cudaSuccess) return cuda_fail("cudaGetSymbolAddress", e);
+    if (ptr == nullptr) {
+      g_err = "cudaGetSymbolAddress returned no address";
       return MCFG_ECUDA;
     }
     g_scratch_dev[dev] = ptr;
@@ -132,18 +164,40 @@ __global__ void k_na_scatter(int n, const int* __restrict__ key, const int* __re
   order[start[key[p]] + rank[p]] = p;
 }
 
+// The scatter's slot order inside a cell follows the atomics of k_na_count
+// and changes from call to call.  One warp per cell writes the cell's
+// particles to sorted[] in host index order (PPM's stable order): an entry's
+// place is the number of the cell's entries with a smaller index (indices
+// are distinct).
+__global__ void k_na_order(int ncell, const int* __restrict__ start,
+                           const int* __restrict__ order, int* __restrict__ sorted) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= ncell) return;
+  const int s0 = start[warp], len = start[warp + 1] - s0;
+  for (int t = lane; t < len; t += 32) {
+    const int me = order[s0 + t];
+    int below = 0;
+    for (int u = 0; u < len; ++u) below += order[s0 + u] < me;
+    sorted[s0 + below] = me;
+  }
+}
+
 template <int D>
 __global__ void k_na_density(Consts k, int n, const double* __restrict__ x,
                              const double* __restrict__ m, const int* __restrict__ id,
                              const int* __restrict__ key, const int* __restrict__ start,
-                             const int* __restrict__ order, double* __restrict__ rho) {
+                             const int* __restrict__ order, double* __restrict__ rho,
+                             int* __restrict__ status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int si = id[2 * i + 1];
-  const bool acc_i = (si == 0) || (si < 0 && k.wall_rho_type == 1);
+  const bool acc_i = dyn_rho(k, si);
   const double mi = m[i];
   if (!acc_i) {
-    rho[i] = (k.rhs_density_type == 1) ? k.init_density : k.init_density / mi;
+    const double r0 = (k.rhs_density_type == 1) ? k.init_density : k.init_density / mi;
+    rho[i] = r0;
+    if (!(r0 > 0.0)) atomicOr(status, kNaZeroDensity);
     return;
   }
   double xi[3] = {0.0, 0.0, 0.0};
@@ -210,15 +264,34 @@ __global__ void k_na_density(Consts k, int n, const double* __restrict__ x,
       }
     }
   }
-  rho[i] = ((k.rhs_density_type == 1) ? k.w0 * mi : k.w0) + sum;
+  const double r = ((k.rhs_density_type == 1) ? k.w0 * mi : k.w0) + sum;
+  rho[i] = r;
+  if (!(r > 0.0)) atomicOr(status, kNaZeroDensity);
+}
+
+// the scratch words of one call
+struct NaScratch {
+  int *key, *rank, *order, *cnt, *status, *start;
+};
+
+NaScratch na_layout(int* base) {
+  NaScratch t;
+  t.key = base;
+  t.rank = t.key + kNoAllocMaxParticles;
+  t.order = t.rank + kNoAllocMaxParticles;
+  t.cnt = t.order + kNoAllocMaxParticles;
+  t.status = t.cnt + (kNoAllocMaxCells + 1);
+  t.start = t.status + 1;
+  return t;
 }
 
 }  // namespace
 
 extern "C" {
 
-int mcfg_density_noalloc(const mcfg_params* params, int32_t n, const double* x, const double* m,
-                         const int32_t* id, double* rho, void* stream) {
+int mcfg_density_noalloc(const mcfg_params* params, int32_t coll_rho_type, int32_t n,
+                         const double* x, const double* m, const int32_t* id, double* rho,
+                         void* stream) {
   std::lock_guard<std::mutex> lk(g_mu);
   const char* msg = validate_params(params);
   if (msg) {
@@ -233,6 +306,10 @@ int mcfg_density_noalloc(const mcfg_params* params, int32_t n, const double* x, 
     g_err = buf;
     return MCFG_EINVAL;
   }
+  if (coll_rho_type != 0 && coll_rho_type != 1) {
+    g_err = "mcfg_density_noalloc: coll_rho_type must be 0 (constant) or 1 (dynamic)";
+    return MCFG_EINVAL;
+  }
   if (n > 0 && (!x || !m || !id || !rho)) {
     g_err = "mcfg_density_noalloc: NULL array";
     return MCFG_EINVAL;
@@ -240,6 +317,7 @@ int mcfg_density_noalloc(const mcfg_params* params, int32_t n, const double* x, 
   Consts k;
   make_consts(*params, k);
   k.n = n;
+  k.coll_rho_type = coll_rho_type;
   if (k.le) {
     g_err = "mcfg_density_noalloc: Lees-Edwards faces are not supported here";
     return MCFG_ENOTSUP;
@@ -257,43 +335,67 @@ int mcfg_density_noalloc(const mcfg_params* params, int32_t n, const double* x, 
       g_err = "a periodic axis needs at least 3 cells (box >= 3*1.0001*cut_off)";
       return MCFG_EINVAL;
     }
-  if (cudaSetDevice(params->device) != cudaSuccess) {
-    g_err = "cudaSetDevice failed";
+  DeviceRestore restore;
+  cudaError_t e = cudaSetDevice(params->device);
+  if (e != cudaSuccess) {
+    cuda_fail("cudaSetDevice", e);
     return MCFG_ENODEV;
   }
-  int* scratch = nullptr;
-  int rc = scratch_address(params->device, &scratch);
+  int* base = nullptr;
+  int rc = scratch_address(params->device, &base);
   if (rc) return rc;
-  if (n == 0) return MCFG_OK;
-  int* key = scratch;
-  int* rank = key + kNoAllocMaxParticles;
-  int* order = rank + kNoAllocMaxParticles;
-  int* cnt = order + kNoAllocMaxParticles;
-  int* start = cnt + (kNoAllocMaxCells + 1);
+  const NaScratch t = na_layout(base);
   cudaStream_t s = (cudaStream_t)stream;
   const int nbins = k.ncell + 1;
-  // the counters keep the previous call's values: clear them
-  cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)nbins, s);
-  if (e != cudaSuccess) {
-    g_err = std::string("cudaMemsetAsync: ") + cudaGetErrorString(e);
-    return MCFG_ECUDA;
-  }
+  // the counters and the status word after them keep the previous call's
+  // values: clear both
+  e = cudaMemsetAsync(t.cnt, 0, sizeof(int) * ((size_t)kNoAllocMaxCells + 2), s);
+  if (e != cudaSuccess) return cuda_fail("cudaMemsetAsync", e);
+  if (n == 0) return MCFG_OK;
   const int tb = 256, gb = (n + tb - 1) / tb;
   if (k.d == 3)
-    k_na_count<3><<<gb, tb, 0, s>>>(k, n, x, key, rank, cnt);
+    k_na_count<3><<<gb, tb, 0, s>>>(k, n, x, t.key, t.rank, t.cnt);
   else
-    k_na_count<2><<<gb, tb, 0, s>>>(k, n, x, key, rank, cnt);
-  k_na_scan<<<1, 1024, 0, s>>>(cnt, nbins, start);
-  k_na_scatter<<<gb, tb, 0, s>>>(n, key, rank, start, order);
+    k_na_count<2><<<gb, tb, 0, s>>>(k, n, x, t.key, t.rank, t.cnt);
+  k_na_scan<<<1, 1024, 0, s>>>(t.cnt, nbins, t.start);
+  k_na_scatter<<<gb, tb, 0, s>>>(n, t.key, t.rank, t.start, t.order);
+  // host-index order inside each real cell, into rank[] (free after the
+  // scatter); particles outside the mesh take no part in any sum
+  const int gcell = (int)(((int64_t)k.ncell * 32 + tb - 1) / tb);
+  k_na_order<<<gcell, tb, 0, s>>>(k.ncell, t.start, t.order, t.rank);
   if (k.d == 3)
-    k_na_density<3><<<gb, tb, 0, s>>>(k, n, x, m, id, key, start, order, rho);
+    k_na_density<3><<<gb, tb, 0, s>>>(k, n, x, m, id, t.key, t.start, t.rank, rho, t.status);
   else
-    k_na_density<2><<<gb, tb, 0, s>>>(k, n, x, m, id, key, start, order, rho);
+    k_na_density<2><<<gb, tb, 0, s>>>(k, n, x, m, id, t.key, t.start, t.rank, rho, t.status);
   e = cudaGetLastError();
-  if (e != cudaSuccess) {
-    g_err = std::string("mcfg_density_noalloc launch: ") + cudaGetErrorString(e);
-    return MCFG_ECUDA;
+  if (e != cudaSuccess) return cuda_fail("mcfg_density_noalloc launch", e);
+  return MCFG_OK;
+}
+
+int mcfg_noalloc_status(int32_t device, void* stream, int32_t* flags) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!flags) {
+    g_err = "mcfg_noalloc_status: NULL flags";
+    return MCFG_EINVAL;
   }
+  *flags = 0;
+  DeviceRestore restore;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    cuda_fail("cudaSetDevice", e);
+    return MCFG_ENODEV;
+  }
+  int* base = nullptr;
+  int rc = scratch_address(device, &base);
+  if (rc) return rc;
+  const NaScratch t = na_layout(base);
+  cudaStream_t s = (cudaStream_t)stream;
+  int32_t word = 0;
+  e = cudaMemcpyAsync(&word, t.status, sizeof word, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail("cudaMemcpyAsync", e);
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail("cudaStreamSynchronize", e);
+  *flags = word;
   return MCFG_OK;
 }
 

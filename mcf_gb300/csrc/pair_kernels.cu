@@ -39,12 +39,6 @@ struct NN {
   void* qq;          // 1/n and G*ct/n^2, [1+d*d][n] in the path's type
 };
 
-__device__ __forceinline__ bool dyn_rho(const Consts& k, int sid) {
-  if (sid == 0) return true;
-  if (sid < 0) return k.wall_rho_type == 1;
-  return k.coll_rho_type == 1;
-}
-
 // colloid arrays handed to the sweeps
 struct CollArgs {
   double4_32a* v;      // state velocity (boundary particles get the rigid one)

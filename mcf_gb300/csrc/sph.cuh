@@ -5,6 +5,16 @@
 
 namespace mcfg {
 
+// Does a particle of species sid sum its density over its pairs?  Fluid
+// always; walls with wall_rho_type 1 and colloid boundary particles with
+// coll_rho_type 1 (dynamic); the others keep init_density
+// (particles_compute_density.F90:700-771, :812-815).
+__device__ __forceinline__ bool dyn_rho(const Consts& k, int sid) {
+  if (sid == 0) return true;
+  if (sid < 0) return k.wall_rho_type == 1;
+  return k.coll_rho_type == 1;
+}
+
 template <typename T>
 struct KC;  // kernel and pair constants in T
 template <>

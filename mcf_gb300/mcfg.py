@@ -72,8 +72,10 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "mcfg_get_stream": (C.c_void_p, [_h]),
         "mcfg_set_profiling": (C.c_int, [_h, C.c_int]),
         "mcfg_get_phase_times": (C.c_int, [_h, _dp, C.POINTER(C.c_int64)]),
-        "mcfg_density_noalloc": (C.c_int, [C.POINTER(SDPDParams), C.c_int32, C.c_void_p,
-                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+        "mcfg_density_noalloc": (C.c_int, [C.POINTER(SDPDParams), C.c_int32, C.c_int32,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_void_p]),
+        "mcfg_noalloc_status": (C.c_int, [C.c_int32, C.c_void_p, C.POINTER(C.c_int32)]),
         "mcfg_noalloc_error": (C.c_char_p, []),
         "mcfg_set_colloids": (C.c_int, [_h, C.POINTER(ColloidParams), _dp, _dp, _dp, _dp]),
         "mcfg_colloid_drag": (C.c_int, [_h, _dp, _dp]),

@@ -5,8 +5,10 @@ arithmetic (dx, wall layers, time step, masses, shear velocities) on decks
 written here, particles read from a restart file (read_external), and --
 where the reference tree is present -- its two sample decks (the 2D flow
 around a cylinder and the 1M-particle 3D scalability deck), read exactly as
-MCF sets them up."""
+MCF sets them up (MCF_REFERENCE_DIR names the reference's mcf/ folder;
+those tests skip when it is unset)."""
 import math
+import os
 from pathlib import Path
 
 import numpy as np
@@ -16,7 +18,8 @@ from mcf_gb300.mcf_config import load_mcf_deck, parse_mcf_file, read_particles_f
 from mcf_gb300.params import BC_WALL_SOLID
 from oracle.mcf_format import e16_8, restart_text
 
-REF = Path("/root/reference/mcf")
+_REF_ENV = os.environ.get("MCF_REFERENCE_DIR", "")
+REF = Path(_REF_ENV) if _REF_ENV else None
 
 
 def write_deck(folder: Path, ctrl: dict, phys: dict, extra_phys: str = "") -> Path:
@@ -118,7 +121,8 @@ def test_colloid_keys_per_colloid(tmp_path):
         assert np.all(dist[sid == 0] > r) and not np.any(dist <= r - 1.05 * 0.15)
 
 
-@pytest.mark.skipif(not REF.exists(), reason="reference tree not present")
+@pytest.mark.skipif(REF is None or not REF.exists(),
+                    reason="MCF_REFERENCE_DIR unset or not a directory")
 def test_reference_sample_decks():
     cyl = load_mcf_deck(REF / "mcf_config")
     p = cyl.params
