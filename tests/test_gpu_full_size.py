@@ -1,0 +1,150 @@
+"""FP64 GPU path against the oracle at the sizes of the five workloads.
+
+The other parity tests run on 12^3-24^3 boxes; these run the workloads at
+their own sizes through the C-ABI, with the oracle's OpenMP loops (MCF's
+full-stencil loop mode, symmetry = F, over all host cores) as the checker:
+
+  - C2, 64^3 = 262,144 particles, jittered lattice: cell lists bit-exact,
+    one right-hand side at 1e-12 (density relative, acceleration of the
+    per-particle scale sum_j |a_ij|), one with the random force at 1e-5 of
+    the scale (FP32 Box-Muller normals, as in the small-box tests), then 10
+    kT = 0 steps: positions within 1e-9 of the box, velocities within 1e-7
+    of the velocity scale (the bars of the 100-step C1 trajectory);
+  - C3, 100^3 fluid + 80,000 wall particles: cell lists bit-exact, one
+    right-hand side at 1e-12, 5 kT = 0 steps at the trajectory bars;
+  - C4, 96^3 lattice with 200 rigid spheres (moving, turning): one
+    right-hand side at 1e-12, the boundary particles' rigid velocities, and
+    drag and torque of every colloid within 1e-10 of the largest
+    (particles_compute_interaction.F90:609-900,
+    particles_collect_colloid_interaction.F90:93-136);
+  - C5, 128^2 Oldroyd-B: 10 kT = 0 steps, positions, velocities and the
+    conformation tensor at the bars of the small Oldroyd-B test.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from mcf_gb300 import SDPD, configs
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+THREADS = max(1, os.cpu_count() or 1)
+
+
+def pair(w, **over):
+    p = w.params.copy()
+    for k, v in over.items():
+        setattr(p, k, v)
+    g = SDPD(p)
+    g.upload(w.x, w.v, w.m, w.id)
+    o = Oracle(p, threads=THREADS)
+    o.upload(w.x, w.v, w.m, w.id)
+    return g, o
+
+
+def lists_equal(g, o):
+    g.particles_adjust_particles()
+    o.particles_adjust_particles()
+    ga = g.technique_build_list()
+    oa = o.technique_build_list()
+    for a, b in zip(ga, oa):
+        assert np.array_equal(a, b)
+
+
+def rhs_close(g, o, step=0, tol=1e-12):
+    g.marching_init_force(step)
+    o.marching_init_force(step)
+    a = g.download("rho", "f")
+    b = o.download("rho", "f")
+    assert np.all(np.abs(a["rho"] - b["rho"]) <= 1e-12 * np.abs(b["rho"]))
+    scale = o.force_scale()[:, None] + np.abs(b["f"])
+    err = np.abs(a["f"] - b["f"])
+    assert np.all(err <= tol * scale), float(np.max(err / scale))
+    return a, b
+
+
+def trajectory_close(g, o, nsteps, dt, box, tol_x=1e-9, tol_v=1e-7, extra=()):
+    g.run_vv(0, nsteps, dt)
+    o.run_vv(0, nsteps, dt)
+    a = g.download("x", "v", *extra)
+    b = o.download("x", "v", *extra)
+    assert np.max(np.abs(a["x"] - b["x"])) <= tol_x * box
+    vs = np.abs(b["v"]).max()
+    assert vs > 0
+    assert np.max(np.abs(a["v"] - b["v"])) <= tol_v * vs
+    return a, b
+
+
+def c2_case():
+    w = configs.c2_fluctuating_3d()  # lattice with 0.05 dx uniform jitter
+    rng = np.random.default_rng(64)
+    w.v = rng.normal(0.0, 1e-3, w.v.shape)
+    return w
+
+
+def test_c2_64cubed_lists_rhs_and_10_steps(gpu_lib):
+    w = c2_case()
+    g, o = pair(w, Brownian=0, kt=0.0)
+    lists_equal(g, o)
+    rhs_close(g, o)
+    trajectory_close(g, o, 10, w.dt, 64.0)
+
+
+def test_c2_64cubed_rhs_with_random_force(gpu_lib):
+    w = c2_case()
+    g, o = pair(w)  # kT = 1e-3, Hu-Adams noise
+    assert w.params.Brownian == 1 and w.params.kt > 0
+    rhs_close(g, o, step=11, tol=1e-5)
+
+
+def test_c3_100cubed_walls_lists_rhs_and_5_steps(gpu_lib):
+    w = configs.c3_poiseuille_3d()
+    assert w.n == 1_080_000 and w.n_fluid == 1_000_000
+    rng = np.random.default_rng(100)
+    fl = w.id[:, 1] == 0
+    w.x[fl] += rng.uniform(-0.05, 0.05, (int(fl.sum()), 3))
+    w.v[fl] = rng.normal(0.0, 1e-3, (int(fl.sum()), 3))
+    g, o = pair(w, Brownian=0, kt=0.0)
+    lists_equal(g, o)
+    rhs_close(g, o)
+    trajectory_close(g, o, 5, w.dt, 100.0)
+
+
+def test_c4_96cubed_200_colloids_rhs_drag_torque(gpu_lib):
+    w, cs = configs.c4_colloids(v_scale=0.05, omega_scale=0.02)
+    assert cs.x.shape[0] == 200
+    rng = np.random.default_rng(96)
+    fl = w.id[:, 1] == 0
+    w.x[fl] += rng.uniform(-0.05, 0.05, (int(fl.sum()), 3))
+    w.v[fl] = rng.normal(0.0, 1e-3, (int(fl.sum()), 3))
+    g, o = pair(w, Brownian=0, kt=0.0)
+    for h in (g, o):
+        h.set_colloids(cs.params, cs.x, cs.v, cs.omega, cs.radius)
+    rhs_close(g, o)
+    bp = w.id[:, 1] > 0
+    va = g.download("v")["v"]
+    vb = o.download("v")["v"]
+    assert np.allclose(va[bp], vb[bp], rtol=0, atol=1e-14)
+    da, ta = g.colloid_drag()
+    db, tb = o.colloid_drag()
+    scale = np.abs(db).max() + np.abs(tb).max()
+    assert scale > 0
+    assert np.max(np.abs(da - db)) <= 1e-10 * scale
+    assert np.max(np.abs(ta - tb)) <= 1e-10 * scale
+
+
+def test_c5_128squared_oldroyd_b_10_steps(gpu_lib):
+    w = configs.c5_oldroyd_b_2d()
+    assert w.n == 16384
+    rng = np.random.default_rng(128)
+    w.x = w.x + rng.uniform(-0.05, 0.05, w.x.shape)
+    g, o = pair(w, Brownian=0, kt=0.0)
+    ct0 = np.tile(np.array([1.0, 0.0, 0.0, 1.0]), (w.n, 1))
+    for h in (g, o):
+        h.upload(w.x, w.v, w.m, w.id, ct0)
+    rhs_close(g, o)
+    a, b = trajectory_close(g, o, 10, w.dt, 128.0, tol_x=1e-12, tol_v=1e-10, extra=("ct",))
+    assert np.max(np.abs(a["ct"] - b["ct"])) <= 1e-12
+    assert np.max(np.abs(b["ct"] - ct0)) > 1e-8  # the tensor has moved
