@@ -344,6 +344,69 @@ int mcfg_set_colloids(mcfg_handle* h, const mcfg_colloid_params* cp,
 int mcfg_move_colloids(mcfg_handle* h, const double* x_new, const double* rot,
                        const double* v, const double* omega);
 
+/* Rigid-body dynamics of the colloids on the device: the Colloid object's
+ * explicit Adams-Bashforth update (integrate_colloid_type 1-2) of
+ * marching_integrate_VV.F90:455-765, run inside every mcfg_step_vv /
+ * mcfg_run_vv / mcfg_step_vv_host step once this call has been made, so a
+ * step needs no host round trip for the colloids.  Per step: the fluid's
+ * drag and torque on each colloid from its boundary particles
+ * (particles_collect_colloid_interaction.F90:93-136), then per sub-step
+ * (dt / sub_time_step): rotation vector from the angular-velocity history
+ * (colloid_compute_rotation_vector.F90), rotation matrix
+ * (tool_rotation_matrix.F90), accumulated orientation
+ * (colloid_compute_accumulation_matrix.F90), angular velocity
+ * (colloid_integrate_rotate_velocity.F90), centre and velocity
+ * (colloid_integrate_translate_position/_velocity.F90, AB orders 1-5 ramping
+ * up from the first step after step_start), colloid-colloid repulsion at
+ * the new centres (colloid_compute_interaction.F90 with
+ * colloid_compute_repulsion_cc.F90, nearest image, partners in index
+ * order), body force (colloid_apply_body_force.F90), accelerations
+ * (colloid_compute_translate/rotate_acceleration.F90; spheres and disks),
+ * periodic wrap or wall clamp of the centres (colloid_adjust_colloid.F90),
+ * and the boundary particles moved with their colloid (relative position
+ * turned by the rotation, put at the new centre).  mcfg_init_force then also
+ * computes the initial accelerations, as marching_marching.F90:995-1110.
+ * Histories use MCF's layouts: v_hist(d, nc, AB), omega_hist(3, nc, AB),
+ * f_hist(d, nc, AB), alpha_hist(3, nc, AB) (level 1 first, column-major),
+ * acc_matrix(3, 3, nc), theta(3, nc); NULL gives MCF's start: level 1 of
+ * v / omega from mcfg_set_colloids and zeros elsewhere, zero accelerations,
+ * the identity orientation, zero angles.  mass[nc], mmi[nc*3] (moments of
+ * inertia, particles_compute_mass.F90: spheres 0.4 m a^2, disks
+ * 0.5 m a^2 in mmi(3)).  Call after mcfg_set_colloids; colloid-wall
+ * repulsion and lubrication are not supported (MCFG_ENOTSUP). */
+typedef struct mcfg_colloid_dynamics {
+  int32_t integrate_AB;    /* Adams-Bashforth order 1..5 (Colloid%integrate_AB) */
+  int32_t sub_time_step;   /* colloid sub-steps per fluid step, >= 1          */
+  int64_t step_start;      /* MCF's step_start                                 */
+  int32_t body_force_type; /* 0 none, 1 constant body_force per unit mass     */
+  int32_t reserved0;       /* must be 0                                        */
+  double body_force[3];
+} mcfg_colloid_dynamics;
+
+int mcfg_set_colloid_dynamics(mcfg_handle* h, const mcfg_colloid_dynamics* cd,
+                              const double* mass, const double* mmi, const double* v_hist,
+                              const double* omega_hist, const double* f_hist,
+                              const double* alpha_hist, const double* acc_matrix,
+                              const double* theta);
+
+/* The colloid part of one VV step alone (what mcfg_step_vv runs for the
+ * colloids after the fluid's half kick and drift, marching_integrate_VV.F90:
+ * 455-765), for stage-by-stage use and comparison; step is the step number
+ * of the VV step it belongs to. */
+int mcfg_colloid_integrate(mcfg_handle* h, int64_t step, double dt);
+
+/* Colloid state after the last step (any pointer may be NULL), layouts as
+ * mcfg_set_colloid_dynamics: x[nc*d], histories, drag[nc*d] (fluid +
+ * repulsion + body force, what the last translate acceleration divided by
+ * the mass), torque[nc*3], rot_matrix[nc*9] of the last sub-step,
+ * acc_matrix[nc*9], acc_vector[nc*4] (axis, angle from acc_matrix as
+ * tool_rotation_vector.F90 computes them, for MCF's colloid output),
+ * theta[nc*3]. */
+int mcfg_get_colloid_state(mcfg_handle* h, double* x, double* v_hist, double* omega_hist,
+                           double* f_hist, double* alpha_hist, double* drag, double* torque,
+                           double* rot_matrix, double* acc_matrix, double* acc_vector,
+                           double* theta);
+
 /* Drag and torque of every colloid from its boundary particles' last
  * accelerations, particles_collect_colloid_interaction.F90:93-136:
  * drag[nc*d] = sum m f, torque[nc*3] = sum r x (m f). */

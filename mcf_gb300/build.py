@@ -20,7 +20,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libmcfg.so"
 SOURCES = ["mcfg_api.cu", "cell_list.cu", "pair_kernels.cu", "update.cu", "noalloc.cu", "adjoint.cu",
-           "output.cu"]
+           "output.cu", "colloid.cu", "sweep32.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -56,7 +56,7 @@ def _flags() -> list[str]:
 # The adjoint replays the pair normals (FP32 Box-Muller), so it is compiled
 # with the same flags to draw the same bits.
 _PAIR_FLAGS = ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
-EXTRA = {"pair_kernels.cu": _PAIR_FLAGS, "adjoint.cu": _PAIR_FLAGS}
+EXTRA = {"pair_kernels.cu": _PAIR_FLAGS, "adjoint.cu": _PAIR_FLAGS, "sweep32.cu": _PAIR_FLAGS}
 
 
 def _compile(src: str, verbose: bool) -> Path:

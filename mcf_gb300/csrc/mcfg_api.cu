@@ -120,10 +120,13 @@ void free_all(Handle* h) {
   h->out_dev = nullptr;
   h->out_host = nullptr;
   h->out_cap = 0;
-  for (void* p : {(void*)h->x_ref, (void*)h->vl, (void*)h->vcount, (void*)h->d_rebuild})
+  for (void* p : {(void*)h->x_ref, (void*)h->vl, (void*)h->vcount, (void*)h->d_rebuild,
+                  (void*)h->vmask})
     if (p) cudaFree(p);
   h->x_ref = nullptr;
   h->vl = nullptr;
+  h->vmask = nullptr;
+  h->masked = false;
   h->vcount = h->d_rebuild = nullptr;
   h->vcap = 0;
   h->reuse_valid = false;
@@ -133,7 +136,7 @@ void free_all(Handle* h) {
                   h->ncount, h->nhs, h->jp, h->pc, h->pcf, h->vf, h->wd, h->red, h->d_err, h->d_stats, h->d_pairs,
                   h->up_x, h->up_v, h->up_m, h->up_id, h->ct, h->act, h->vgt, h->ct2,
                   h->act2, h->qq, h->coll, h->coll_start, h->coll_mem, h->slot_of, h->rxc,
-                  h->rxcf, h->coll_out};
+                  h->rxcf, h->coll_out, h->crec, h->cxnew};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   h->x = h->v = h->f = h->x2 = h->v2 = h->f2 = nullptr;
@@ -145,6 +148,9 @@ void free_all(Handle* h) {
   h->ct = h->act = h->vgt = h->ct2 = h->act2 = nullptr;
   h->qq = nullptr;
   h->coll = h->coll_out = nullptr;
+  h->crec = h->cxnew = nullptr;
+  h->cdyn = false;
+  h->coll_host_stale = false;
   h->coll_start = h->coll_mem = h->slot_of = nullptr;
   h->rxc = nullptr;
   h->rxcf = nullptr;
@@ -505,6 +511,9 @@ int ensure_capacity(Handle* h, int64_t n64) {
       if ((rc = dalloc(h, &h->x_ref, cap)) || (rc = dalloc(h, &h->vl, cap * (size_t)h->vcap)) ||
           (rc = dalloc(h, &h->vcount, cap)) || (rc = dalloc(h, &h->d_rebuild, 2)))
         return rc;
+      if (h->p.precision != MCFG_PRECISION_FP64 &&
+          (rc = dalloc(h, &h->vmask, cap * (size_t)((h->vcap + 31) / 32))))
+        return rc;
       if (cuda_check(h, cudaMemsetAsync(h->d_rebuild, 0, 2 * sizeof(int), h->stream),
                      "memset rebuild"))
         return MCFG_ECUDA;
@@ -713,6 +722,13 @@ int vv_step(Handle* h, int64_t step, double dt) {
   h->time_current = h->time_current + dt;
   if (h->k.walls || h->k.le)
     boundary_update(h, h->time_current + dt, h->time_current + 0.5 * dt);
+  // the colloids' rigid-body update (marching_integrate_VV.F90:455-765); it
+  // touches only colloid boundary particles, so running it before the
+  // fluid's half kick and drift gives MCF's state
+  if (h->cdyn) {
+    PhaseScope ps(h, kPhaseUpdate);
+    TRY(colloid_section(h, step, dt));
+  }
   if (!h->k.reuse) {
     TRY(kdw(h, dt));
     return rhs(h, step, kForceBodyKick, dt);
@@ -787,7 +803,8 @@ static Handle::GraphSlot* graph_for(Handle* h, double dt) {
   if (ok) {
     h->graph_capturing = true;
     for (int q = 0; q < 2 && ok; ++q) {
-      ok = kick_drift_reuse(h, dt) == MCFG_OK && rhs_reuse(h, 0, kForceBodyKick, dt) == MCFG_OK;
+      ok = (!h->cdyn || colloid_section(h, 0, dt) == MCFG_OK) &&
+           kick_drift_reuse(h, dt) == MCFG_OK && rhs_reuse(h, 0, kForceBodyKick, dt) == MCFG_OK;
       k_step_advance<<<1, 1, 0, h->stream>>>(h->d_step);
     }
     h->graph_capturing = false;
@@ -1163,6 +1180,7 @@ int mcfg_init_force(mcfg_handle* h, int64_t step) {
   boundary_update(h, h->time_current, h->time_current);
   TRY(adjust_particles(h));
   TRY(rhs(h, step, kForceBody, h->dt));
+  if (h->cdyn) TRY(colloid_initial(h));  // marching_marching.F90:995-1110
   return check_device_errors(h);
 }
 
@@ -1396,6 +1414,8 @@ int mcfg_set_colloids(mcfg_handle* h, const mcfg_colloid_params* cp, const doubl
   if (h->k.le && nc > 0)
     return set_error(h, MCFG_ENOTSUP, "colloids with Lees-Edwards faces are not supported");
   h->cp = *cp;
+  h->cdyn = false;  // new colloids: mcfg_set_colloid_dynamics again to integrate them
+  h->coll_host_stale = false;
   h->crad.assign(radius, radius + nc);
   if (nc > 0) {
     int rc;
@@ -1424,6 +1444,10 @@ int mcfg_move_colloids(mcfg_handle* h, const double* x_new, const double* rot, c
   const int nc = h->k.ncoll, d = h->p.num_dim;
   if (nc == 0) return set_error(h, MCFG_ESTATE, "mcfg_set_colloids must come first");
   if (!x_new || !v || !omega) return set_error(h, MCFG_EINVAL, "mcfg_move_colloids: NULL array");
+  if (h->cdyn)
+    return set_error(h, MCFG_ESTATE,
+                     "mcfg_move_colloids: the colloids are integrated on the device "
+                     "(mcfg_set_colloid_dynamics); call mcfg_set_colloids to hand them back");
   // staging: the new centres in coll_out (nc*12 doubles), the rotations in
   // the upload staging (nc*9 <= 3 n: every colloid owns boundary particles)
   double* dx = h->coll_out;
@@ -1441,6 +1465,144 @@ int mcfg_move_colloids(mcfg_handle* h, const double* x_new, const double* rot, c
   return MCFG_OK;
 }
 
+int mcfg_set_colloid_dynamics(mcfg_handle* h, const mcfg_colloid_dynamics* cd,
+                              const double* mass, const double* mmi, const double* v_hist,
+                              const double* omega_hist, const double* f_hist,
+                              const double* alpha_hist, const double* acc_matrix,
+                              const double* theta) {
+  GUARD(h);
+  h->graph_gen++;
+  const int nc = h->k.ncoll, d = h->p.num_dim;
+  if (nc == 0) return set_error(h, MCFG_ESTATE, "mcfg_set_colloids must come first");
+  if (!cd || !mass || !mmi) return set_error(h, MCFG_EINVAL, "mcfg_set_colloid_dynamics: NULL");
+  if (cd->integrate_AB < 1 || cd->integrate_AB > 5)
+    return set_error(h, MCFG_EINVAL, "integrate_AB must be 1..5");
+  if (cd->sub_time_step < 1) return set_error(h, MCFG_EINVAL, "sub_time_step must be >= 1");
+  if (cd->body_force_type != 0 && cd->body_force_type != 1)
+    return set_error(h, MCFG_ENOTSUP, "colloid body_force_type must be 0 or 1");
+  if (cd->reserved0 != 0) return set_error(h, MCFG_EINVAL, "reserved0 must be 0");
+  for (int c = 0; c < nc; ++c) {
+    if (!(mass[c] > 0.0)) return set_error(h, MCFG_EPHYS, "colloid mass must be positive");
+    for (int a = 0; a < 3; ++a)
+      if (h->cp.rotate && (d == 3 || a == 2) && !(mmi[(size_t)c * 3 + a] > 0.0))
+        return set_error(h, MCFG_EPHYS, "colloid moment of inertia must be positive");
+  }
+  const int AB = cd->integrate_AB;
+  TRY(colloid_sync_host(h));
+  // the device record, laid out as colloid.cu's kRec* offsets
+  std::vector<double> rec((size_t)nc * kCollRec, 0.0);
+  for (int c = 0; c < nc; ++c) {
+    double* r = &rec[(size_t)c * kCollRec];
+    r[0] = mass[c];
+    for (int a = 0; a < 3; ++a) r[1 + a] = mmi[(size_t)c * 3 + a];
+    for (int a = 0; a < 3; ++a) r[4 + a] = theta ? theta[(size_t)c * 3 + a] : 0.0;
+    for (int q = 0; q < 9; ++q) {
+      r[13 + q] = (q % 4 == 0) ? 1.0 : 0.0;
+      r[22 + q] = acc_matrix ? acc_matrix[(size_t)c * 9 + q] : r[13 + q];
+    }
+    for (int l = 0; l < AB; ++l)
+      for (int a = 0; a < 3; ++a) {
+        const size_t iv = ((size_t)l * nc + c) * d + a, i3 = ((size_t)l * nc + c) * 3 + a;
+        double vv = 0.0, ff = 0.0;
+        if (a < d) {
+          vv = v_hist ? v_hist[iv] : (l == 0 ? h->cv[(size_t)c * d + a] : 0.0);
+          ff = f_hist ? f_hist[iv] : 0.0;
+        }
+        r[31 + 3 * l + a] = vv;
+        r[46 + 3 * l + a] = omega_hist ? omega_hist[i3] : (l == 0 ? h->com[(size_t)c * 3 + a] : 0.0);
+        r[61 + 3 * l + a] = ff;
+        r[76 + 3 * l + a] = alpha_hist ? alpha_hist[i3] : 0.0;
+      }
+  }
+  int rc;
+  if ((rc = dalloc(h, &h->crec, rec.size())) || (rc = dalloc(h, &h->cxnew, (size_t)nc * 3)))
+    return rc;
+  if (cuda_check(h, cudaMemcpyAsync(h->crec, rec.data(), sizeof(double) * rec.size(),
+                                    cudaMemcpyHostToDevice, h->stream), "colloid dynamics"))
+    return MCFG_ECUDA;
+  // level 1 of the histories is the colloids' velocity in the table the
+  // sweeps read
+  std::vector<double> v1((size_t)nc * d), w1((size_t)nc * 3);
+  for (int c = 0; c < nc; ++c) {
+    for (int a = 0; a < d; ++a) v1[(size_t)c * d + a] = rec[(size_t)c * kCollRec + 31 + a];
+    for (int a = 0; a < 3; ++a) w1[(size_t)c * 3 + a] = rec[(size_t)c * kCollRec + 46 + a];
+  }
+  std::vector<double> x0(h->cx);
+  TRY(put_colloid_state(h, nc, x0.data(), v1.data(), w1.data()));
+  h->cdp = *cd;
+  h->cdyn = true;
+  return MCFG_OK;
+}
+
+int mcfg_colloid_integrate(mcfg_handle* h, int64_t step, double dt) {
+  GUARD(h);
+  if (!h->cdyn) return set_error(h, MCFG_ESTATE, "mcfg_set_colloid_dynamics must come first");
+  if (!h->have_force) return set_error(h, MCFG_ESTATE, "no force computed yet");
+  if (step - h->cdp.step_start < 1)
+    return set_error(h, MCFG_EINVAL, "step must follow step_start (Adams-Bashforth order >= 1)");
+  h->graph_gen++;
+  TRY(colloid_section(h, step, dt));
+  h->have_list = h->have_density = h->have_pressure = false;
+  h->reuse_valid = false;
+  return check_device_errors(h);
+}
+
+int mcfg_get_colloid_state(mcfg_handle* h, double* x, double* v_hist, double* omega_hist,
+                           double* f_hist, double* alpha_hist, double* drag, double* torque,
+                           double* rot_matrix, double* acc_matrix, double* acc_vector,
+                           double* theta) {
+  GUARD(h);
+  const int nc = h->k.ncoll, d = h->p.num_dim;
+  if (nc == 0) return set_error(h, MCFG_ESTATE, "no colloids");
+  TRY(colloid_sync_host(h));
+  if (x) std::copy(h->cx.begin(), h->cx.end(), x);
+  if (!h->cdyn) {
+    if (v_hist || omega_hist || f_hist || alpha_hist || drag || torque || rot_matrix ||
+        acc_matrix || acc_vector || theta)
+      return set_error(h, MCFG_ESTATE, "no device dynamics (mcfg_set_colloid_dynamics)");
+    return MCFG_OK;
+  }
+  const int AB = h->cdp.integrate_AB;
+  std::vector<double> rec((size_t)nc * kCollRec);
+  if (cuda_check(h, cudaMemcpyAsync(rec.data(), h->crec, sizeof(double) * rec.size(),
+                                    cudaMemcpyDeviceToHost, h->stream), "colloid record") ||
+      cuda_check(h, cudaStreamSynchronize(h->stream), "colloid record"))
+    return MCFG_ECUDA;
+  for (int c = 0; c < nc; ++c) {
+    const double* r = &rec[(size_t)c * kCollRec];
+    for (int l = 0; l < AB; ++l)
+      for (int a = 0; a < 3; ++a) {
+        const size_t iv = ((size_t)l * nc + c) * d + a, i3 = ((size_t)l * nc + c) * 3 + a;
+        if (a < d && v_hist) v_hist[iv] = r[31 + 3 * l + a];
+        if (a < d && f_hist) f_hist[iv] = r[61 + 3 * l + a];
+        if (omega_hist) omega_hist[i3] = r[46 + 3 * l + a];
+        if (alpha_hist) alpha_hist[i3] = r[76 + 3 * l + a];
+      }
+    for (int a = 0; a < 3; ++a) {
+      if (a < d && drag) drag[(size_t)c * d + a] = r[7 + a];
+      if (torque) torque[(size_t)c * 3 + a] = r[10 + a];
+      if (theta) theta[(size_t)c * 3 + a] = r[4 + a];
+    }
+    for (int q = 0; q < 9; ++q) {
+      if (rot_matrix) rot_matrix[(size_t)c * 9 + q] = r[13 + q];
+      if (acc_matrix) acc_matrix[(size_t)c * 9 + q] = r[22 + q];
+    }
+    if (acc_vector) {
+      // tool_rotation_vector.F90 on the accumulated matrix (as MCF's
+      // colloid_compute_accumulation_vector, which divides by sin(phi)
+      // also when phi is 0)
+      const double* am = r + 22;
+      const double phi = std::acos((am[0] + am[4] + am[8] - 1.0) / 2.0);
+      double* av = acc_vector + (size_t)c * 4;
+      av[0] = (am[2 + 3 * 1] - am[1 + 3 * 2]) / (2.0 * std::sin(phi));
+      av[1] = (am[0 + 3 * 2] - am[2 + 3 * 0]) / (2.0 * std::sin(phi));
+      av[2] = (am[1 + 3 * 0] - am[0 + 3 * 1]) / (2.0 * std::sin(phi));
+      av[3] = phi;
+    }
+  }
+  return MCFG_OK;
+}
+
 int mcfg_colloid_drag(mcfg_handle* h, double* drag, double* torque) {
   GUARD(h);
   if (!h->have_force) return set_error(h, MCFG_ESTATE, "no force computed yet");
@@ -1450,6 +1612,7 @@ int mcfg_colloid_drag(mcfg_handle* h, double* drag, double* torque) {
 int mcfg_colloid_repulsion(mcfg_handle* h, double* force) {
   GUARD(h);
   if (!force) return set_error(h, MCFG_EINVAL, "NULL output");
+  TRY(colloid_sync_host(h));
   const int nc = h->k.ncoll, d = h->p.num_dim;
   const mcfg_colloid_params& cp = h->cp;
   for (int q = 0; q < nc * d; ++q) force[q] = 0.0;
@@ -1483,9 +1646,11 @@ int mcfg_colloid_repulsion(mcfg_handle* h, double* force) {
         F = F0 / hn * std::exp(-gap / hn) / (1.0 - std::exp(-gap / hn)) -
             F0 / hn * std::exp(-5.0) / (1.0 - std::exp(-5.0));
       }
+      // colloid_compute_repulsion_cc.F90:155-156: R12 / r, then F times it
       for (int a = 0; a < d; ++a) {
-        force[(size_t)i * d + a] += F * R12[a] / r;
-        force[(size_t)j * d + a] -= F * R12[a] / r;
+        const double fij = F * (R12[a] / r);
+        force[(size_t)i * d + a] += fij;
+        force[(size_t)j * d + a] -= fij;
       }
     }
   return MCFG_OK;

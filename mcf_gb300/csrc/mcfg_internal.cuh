@@ -174,6 +174,12 @@ struct Handle {
   double4_32a* rxc = nullptr;  // FP64 path: boundary particle minus its colloid image centre
   float4* rxcf = nullptr;      // FP32 path: same in FP32
   double* coll_out = nullptr;  // [nc][6] drag + torque
+  // rigid-body dynamics of the colloids on the device (colloid.cu)
+  bool cdyn = false;             // mcfg_set_colloid_dynamics was called
+  mcfg_colloid_dynamics cdp{};
+  double* crec = nullptr;        // [nc][kCollRec] masses, histories, matrices
+  double* cxnew = nullptr;       // [nc][3] centres after a sub-step
+  bool coll_host_stale = false;  // cx/cv/com behind the device table
   // double buffers for the permutation
   double4_32a *x2 = nullptr, *v2 = nullptr, *f2 = nullptr;
   double* m2 = nullptr;
@@ -211,7 +217,11 @@ struct Handle {
   size_t up_cap = 0;
   // ---- neighbour-list reuse ----
   double4_32a* x_ref = nullptr;  // positions at the last rebuild
-  uint16_t* vl = nullptr;        // [vcap][n] candidates within rc + skin (slot<<11 | local)
+  uint16_t* vl = nullptr;        // [vcap][n] candidates within rc + skin (slot<<11 | local);
+                                 // FP32 handles: fluid-fluid pairs from row 0 up, the
+                                 // others from row vcap-1 down (sweep32.cu)
+  uint32_t* vmask = nullptr;     // FP32: [vcap/32][n] the step's pairs among the candidates
+  bool masked = false;           // the last density sweep wrote vmask (force_mask follows)
   int* vcount = nullptr;         // [n]
   int vcap = 0;
   int* d_rebuild = nullptr;      // [0] rebuild request, [1] rebuilds done
@@ -310,6 +320,9 @@ int verlet_build_gated(Handle* h);
 int compute_density(Handle* h, bool with_pressure, bool reuse = false);
 int compute_pressure(Handle* h);
 int compute_force(Handle* h, int64_t step, int fuse_mode, double dt);
+// FP32-mixed sweeps over the candidate list with a per-step pair mask
+int density_mask(Handle* h, bool with_pressure);
+int force_mask(Handle* h, int64_t step, int fuse_mode, double dt);
 int apply_body_force(Handle* h);
 int integrate_velocity(Handle* h, double dt, double lambda);
 int integrate_position(Handle* h, double dt);
@@ -342,6 +355,15 @@ int write_statistic_line(Handle* h, const char* path, int64_t step, double time)
 int colloid_drag(Handle* h, double* drag, double* torque);
 int colloid_move(Handle* h, const double* d_xnew, const double* d_rot);
 int check_device_errors(Handle* h);
+
+// the colloid part of a VV step, the initial colloid accelerations, the
+// drag/torque sums into coll_out, host copies of the colloid table
+int colloid_section(Handle* h, int64_t step, double dt);
+int colloid_initial(Handle* h);
+int colloid_drag_launch(Handle* h);
+int colloid_sync_host(Handle* h);
+// doubles per colloid of the device record of the dynamics (colloid.cu)
+constexpr int kCollRec = 96;
 
 // fuse_mode of compute_force
 enum { kForceOnly = 0, kForceBody = 1, kForceBodyKick = 2 };

@@ -237,7 +237,7 @@ namespace mcfg {
 // thread t lives at s * TPB + t (conflict-free).  Same slots, starts and
 // periodic image bits as build_table, so the neighbour-list entries
 // slot<<11 | local index decode the same way.
-template <int D, int TPB>
+template <int D, int TPB, bool SHIFT = true>
 __device__ __forceinline__ void build_lane_table(const Consts& k, int cell,
                                                  const int* __restrict__ cell_start,
                                                  int* __restrict__ s_start,
@@ -248,7 +248,7 @@ __device__ __forceinline__ void build_lane_table(const Consts& k, int cell,
   if (cell == k.ncell) {
     for (int s = 0; s < k.ns; ++s) {
       s_start[s * TPB + t] = (s == CENTER) ? cell_start[cell] : 0;
-      s_shift[s * TPB + t] = 0;
+      if (SHIFT) s_shift[s * TPB + t] = 0;
     }
     return;
   }
@@ -260,13 +260,13 @@ __device__ __forceinline__ void build_lane_table(const Consts& k, int cell,
     int sh;
     const int nc = slot_cell<D>(k, c, s, st, sh);
     s_start[s * TPB + t] = (nc >= 0) ? cell_start[nc] : 0;
-    s_shift[s * TPB + t] = sh;
+    if (SHIFT) s_shift[s * TPB + t] = sh;
   }
   for (int s = NS0; s < k.ns; ++s) {
     int sh;
     const int nc = slot_cell<D>(k, c, s, st, sh);
     s_start[s * TPB + t] = (nc >= 0) ? cell_start[nc] : 0;
-    s_shift[s * TPB + t] = sh;
+    if (SHIFT) s_shift[s * TPB + t] = sh;
   }
 }
 

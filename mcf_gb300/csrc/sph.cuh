@@ -19,6 +19,11 @@ template <typename T>
 struct KC;  // kernel and pair constants in T
 template <>
 struct KC<double> {
+  // the kernel's argument s = r / h as MCF divides it
+  // (kernel_kernel_quintic_spline.F90:69,177): near the cut-off W and W'
+  // amplify a rounding difference of s by 4-5 s / (3 - s), so the FP64 path
+  // keeps MCF's division
+  __device__ static double arg(const Consts& k, double r) { return r / k.h; }
   __device__ static double inv_h(const Consts& k) { return k.inv_h; }
   __device__ static double coef(const Consts& k) { return k.coef; }
   __device__ static double coef_grad(const Consts& k) { return k.coef_grad; }
@@ -28,6 +33,7 @@ struct KC<double> {
 };
 template <>
 struct KC<float> {
+  __device__ static float arg(const Consts& k, float r) { return r * k.inv_hf; }
   __device__ static float inv_h(const Consts& k) { return k.inv_hf; }
   __device__ static float coef(const Consts& k) { return k.coeff; }
   __device__ static float coef_grad(const Consts& k) { return k.coef_gradf; }
@@ -40,7 +46,7 @@ struct KC<float> {
 // - 6(2-s)^5 + 15(1-s)^5] piecewise) and kernel_kernel_Lucy.F90:68-78.
 template <typename T>
 __device__ __forceinline__ T kernel_w(const Consts& k, T r) {
-  const T s = r * KC<T>::inv_h(k);
+  const T s = KC<T>::arg(k, r);
   if (k.kernel_type == 1) {
     const T s3 = T(3) - s, s2 = T(2) - s, s1 = T(1) - s;
     T a3 = s3 * s3;
@@ -68,7 +74,7 @@ __device__ __forceinline__ T kernel_w(const Consts& k, T r) {
 // dW/dr: kernel_kernel_quintic_spline.F90:177-215, kernel_kernel_Lucy.F90:155-168
 template <typename T>
 __device__ __forceinline__ T kernel_gradw(const Consts& k, T r) {
-  const T s = r * KC<T>::inv_h(k);
+  const T s = KC<T>::arg(k, r);
   if (k.kernel_type == 1) {
     const T s3 = T(3) - s, s2 = T(2) - s, s1 = T(1) - s;
     T g = T(0);

@@ -295,7 +295,8 @@ int colloid_move(Handle* h, const double* d_xnew, const double* d_rot) {
   return cuda_check(h, cudaGetLastError(), "colloid move launch") ? MCFG_ECUDA : MCFG_OK;
 }
 
-int colloid_drag(Handle* h, double* drag, double* torque) {
+// the drag and torque sums of every colloid into coll_out [nc][6]
+int colloid_drag_launch(Handle* h) {
   const int nc = h->k.ncoll, d = h->k.d;
   if (nc == 0) return MCFG_OK;
   const int warps_per_block = 4;
@@ -307,6 +308,14 @@ int colloid_drag(Handle* h, double* drag, double* torque) {
     k_colloid_drag<2><<<g, 32 * warps_per_block, 0, h->stream>>>(
         h->k, h->coll_start, h->coll_mem, h->slot_of, h->x, h->f, h->m, h->coll_out);
   h->launches++;
+  return cuda_check(h, cudaGetLastError(), "colloid drag launch") ? MCFG_ECUDA : MCFG_OK;
+}
+
+int colloid_drag(Handle* h, double* drag, double* torque) {
+  const int nc = h->k.ncoll, d = h->k.d;
+  if (nc == 0) return MCFG_OK;
+  int rc = colloid_drag_launch(h);
+  if (rc) return rc;
   std::vector<double> buf((size_t)nc * 6);
   if (cuda_check(h, cudaMemcpyAsync(buf.data(), h->coll_out, sizeof(double) * buf.size(),
                                     cudaMemcpyDeviceToHost, h->stream),

@@ -14,7 +14,7 @@ from pathlib import Path
 
 import numpy as np
 
-from .params import STATUS_NAMES, ColloidParams, SDPDInfo, SDPDParams
+from .params import STATUS_NAMES, ColloidDynamics, ColloidParams, SDPDInfo, SDPDParams
 
 _LIB = None
 LIB_PATH = Path(__file__).resolve().parent / "libmcfg.so"
@@ -81,6 +81,11 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "mcfg_colloid_drag": (C.c_int, [_h, _dp, _dp]),
         "mcfg_move_colloids": (C.c_int, [_h, _dp, _dp, _dp, _dp]),
         "mcfg_colloid_repulsion": (C.c_int, [_h, _dp]),
+        "mcfg_set_colloid_dynamics": (C.c_int, [_h, C.POINTER(ColloidDynamics), _dp, _dp, _dp,
+                                                _dp, _dp, _dp, _dp, _dp]),
+        "mcfg_colloid_integrate": (C.c_int, [_h, C.c_int64, C.c_double]),
+        "mcfg_get_colloid_state": (C.c_int, [_h, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                             _dp, _dp]),
         "mcfg_set_boundary_motion": (C.c_int, [_h, C.POINTER(C.c_int32), _dp, C.c_double]),
         "mcfg_write_particles": (C.c_int, [_h, C.c_char_p, C.c_int32, C.c_int32]),
         "mcfg_write_statistic": (C.c_int, [_h, C.c_char_p, C.c_int64, C.c_double]),
@@ -357,6 +362,36 @@ class SDPD:
         out = np.zeros((self._cp.num_colloid, self.dim))
         self._check("colloid_compute_repulsion_cc",
                     self.lib.mcfg_colloid_repulsion(self._h, _ptr(out, C.c_double)))
+        return out
+
+    def set_colloid_dynamics(self, cd: ColloidDynamics, mass, mmi, v_hist=None, omega_hist=None,
+                             f_hist=None, alpha_hist=None, acc_matrix=None, theta=None) -> None:
+        """mcfg_set_colloid_dynamics: integrate the colloids on the device"""
+        self._cd = cd
+        self._cdyn = [None if a is None else _as(a, np.float64)
+                      for a in (mass, mmi, v_hist, omega_hist, f_hist, alpha_hist, acc_matrix,
+                                theta)]
+        self._check("mcfg_set_colloid_dynamics", self.lib.mcfg_set_colloid_dynamics(
+            self._h, C.byref(cd), *[_ptr(a, C.c_double) for a in self._cdyn]))
+
+    def colloid_integrate(self, step: int, dt: float) -> None:
+        """mcfg_colloid_integrate: the colloid part of one VV step"""
+        self._check("mcfg_colloid_integrate",
+                    self.lib.mcfg_colloid_integrate(self._h, int(step), float(dt)))
+
+    def colloid_state(self) -> dict:
+        """mcfg_get_colloid_state: x[nc, d], histories [AB, nc, d|3], drag, torque,
+        rot / acc matrices [nc, 9] (column-major), acc_vector [nc, 4], theta"""
+        nc, d, ab = self._cp.num_colloid, self.dim, self._cd.integrate_AB
+        out = {"x": np.zeros((nc, d)), "v": np.zeros((ab, nc, d)), "omega": np.zeros((ab, nc, 3)),
+               "f": np.zeros((ab, nc, d)), "alpha": np.zeros((ab, nc, 3)),
+               "drag": np.zeros((nc, d)), "torque": np.zeros((nc, 3)),
+               "rot": np.zeros((nc, 9)), "acc": np.zeros((nc, 9)),
+               "acc_vector": np.zeros((nc, 4)), "theta": np.zeros((nc, 3))}
+        keys = ["x", "v", "omega", "f", "alpha", "drag", "torque", "rot", "acc", "acc_vector",
+                "theta"]
+        self._check("mcfg_get_colloid_state", self.lib.mcfg_get_colloid_state(
+            self._h, *[_ptr(out[k], C.c_double) for k in keys]))
         return out
 
     def update_state(self, x=None, v=None, f=None) -> None:

@@ -105,6 +105,20 @@ class ColloidParams(C.Structure):
     ]
 
 
+class ColloidDynamics(C.Structure):
+    """mcfg_colloid_dynamics: the Colloid object's rigid-body integration
+    settings (Adams-Bashforth order, sub-steps, step_start, body force)."""
+
+    _fields_ = [
+        ("integrate_AB", C.c_int32),
+        ("sub_time_step", C.c_int32),
+        ("step_start", C.c_int64),
+        ("body_force_type", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("body_force", C.c_double * 3),
+    ]
+
+
 class SDPDInfo(C.Structure):
     _fields_ = [
         ("num_part", C.c_int64),

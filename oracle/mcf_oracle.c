@@ -57,6 +57,14 @@ struct orc_state {
   /* colloids (Class_Colloid): centre, velocity, angular velocity, radius */
   mcfg_colloid_params cp;
   double *cx, *cv, *com, *crad;
+  /* rigid-body dynamics of the colloids (Class_Colloid.F90), on when cdyn:
+   * mass, moments of inertia mmi(3,num), the Adams-Bashforth histories
+   * v(d,num,AB), omega(3,num,AB), f(d,num,AB), alpha(3,num,AB) (level 1
+   * first), rot_matrix and acc_matrix (3,3,num), theta(3,num), and the last
+   * drag(d,num) / torque(3,num) of colloid_compute_interaction */
+  int cdyn;
+  mcfg_colloid_dynamics cd;
+  double *cm, *cmmi, *cvh, *comh, *cfh, *calh, *crot, *cacc, *ctheta, *cdrag, *ctorque;
   /* moving boundaries (Class_Boundary.F90): shear_type, shear_freq, the
    * current shear_v per face, Lees-Edwards shear_length along x of the y+
    * face (the y- face's is its negative), time_current */
@@ -335,6 +343,8 @@ void orc_destroy(orc_state* s) {
   if (!s) return;
   free_arrays(s);
   free(s->cx); free(s->cv); free(s->com); free(s->crad);
+  free(s->cm); free(s->cmmi); free(s->cvh); free(s->comh); free(s->cfh); free(s->calh);
+  free(s->crot); free(s->cacc); free(s->ctheta); free(s->cdrag); free(s->ctorque);
   free(s->lhbx); free(s->lpdx); free(s->pbox);
   free(s);
 }
@@ -1013,11 +1023,300 @@ int orc_colloid_repulsion(orc_state* s, double* force) {
         F = F0 / hn * exp(-h / hn) / (1.0 - exp(-h / hn)) -
             F0 / hn * exp(-5.0) / (1.0 - exp(-5.0));
       }
+      /* R12 / r first, then F times it (colloid_compute_repulsion_cc.F90:
+       * 155-156); F_p(i) += F_ij, F_p(j) -= F_ij
+       * (colloid_compute_interaction.F90), so each colloid's sum runs over
+       * its partners in index order */
       for (int a = 0; a < d; ++a) {
-        force[i * d + a] += F * R12[a] / r;
-        force[j * d + a] -= F * R12[a] / r;
+        const double fij = F * (R12[a] / r);
+        force[i * d + a] = force[i * d + a] + fij;
+        force[j * d + a] = force[j * d + a] - fij;
       }
     }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------
+ * Rigid-body dynamics of the colloids, marching_integrate_VV.F90:455-765
+ * (explicit integrate_colloid_type 1-2) and the initial accelerations of
+ * marching_marching.F90:995-1110.
+ * ---------------------------------------------------------------------- */
+
+/* Adams-Bashforth order of a step (the Colloid routines' "IF (step < itype)
+ * order = step ELSE order = itype") */
+static int ab_order(int64_t step, int itype) { return step < itype ? (int)step : itype; }
+
+/* Adams-Bashforth increment over the history h (level k at h[k * stride]),
+ * in the operation order of colloid_integrate_translate_position.F90,
+ * colloid_integrate_translate_velocity.F90, colloid_integrate_rotate_
+ * velocity.F90 and colloid_compute_rotation_vector.F90 (coefficients
+ * times levels, left to right, times dt, over the divisor) */
+static double ab_incr(int order, const double* h, size_t st, double dt) {
+  switch (order) {
+    case 1:
+      return h[0] * dt;
+    case 2:
+      return (3.0 * h[0] - h[st]) * dt / 2.0;
+    case 3:
+      return (23.0 * h[0] - 16.0 * h[st] + 5.0 * h[2 * st]) * dt / 12.0;
+    case 4:
+      return (55.0 * h[0] - 59.0 * h[st] + 37.0 * h[2 * st] - 9.0 * h[3 * st]) * dt / 24.0;
+    default:
+      return (1901.0 * h[0] - 2774.0 * h[st] + 2616.0 * h[2 * st] - 1274.0 * h[3 * st] +
+              251.0 * h[4 * st]) *
+             dt / 720.0;
+  }
+}
+
+/* "i = itype; DO WHILE (i >= 2): h(:,:,i) = h(:,:,i-1)" of the history of
+ * n values per level */
+static void ab_shift(double* h, size_t n, int itype) {
+  for (int k = itype - 1; k >= 1; --k) memcpy(h + (size_t)k * n, h + (size_t)(k - 1) * n,
+                                               sizeof(double) * n);
+}
+
+/* tool_rotation_matrix.F90: rotation by phi about the unit axis ax,
+ * rm(i,j) at rm[i + 3j] */
+static void rotation_matrix(const double* ax, double phi, double* rm) {
+  const double cp = cos(phi), cp1 = 1.0 - cp, sp = sin(phi);
+  rm[0 + 3 * 0] = ax[0] * ax[0] * cp1 + cp;
+  rm[0 + 3 * 1] = ax[0] * ax[1] * cp1 - ax[2] * sp;
+  rm[0 + 3 * 2] = ax[0] * ax[2] * cp1 + ax[1] * sp;
+  rm[1 + 3 * 0] = ax[1] * ax[0] * cp1 + ax[2] * sp;
+  rm[1 + 3 * 1] = ax[1] * ax[1] * cp1 + cp;
+  rm[1 + 3 * 2] = ax[1] * ax[2] * cp1 - ax[0] * sp;
+  rm[2 + 3 * 0] = ax[2] * ax[0] * cp1 - ax[1] * sp;
+  rm[2 + 3 * 1] = ax[2] * ax[1] * cp1 + ax[0] * sp;
+  rm[2 + 3 * 2] = ax[2] * ax[2] * cp1 + cp;
+}
+
+int orc_set_colloid_dynamics(orc_state* s, const mcfg_colloid_dynamics* cd, const double* mass,
+                             const double* mmi, const double* v_hist, const double* omega_hist,
+                             const double* f_hist, const double* alpha_hist,
+                             const double* acc_matrix, const double* theta) {
+  const int d = s->d, nc = s->cp.num_colloid;
+  if (!cd || cd->integrate_AB < 1 || cd->integrate_AB > 5 || cd->sub_time_step < 1 || !mass ||
+      !mmi || (cd->body_force_type != 0 && cd->body_force_type != 1))
+    return fail(s, "bad colloid dynamics");
+  const int AB = cd->integrate_AB;
+  s->cd = *cd;
+  double** arrs[] = {&s->cm, &s->cmmi, &s->cvh, &s->comh, &s->cfh, &s->calh,
+                     &s->crot, &s->cacc, &s->ctheta, &s->cdrag, &s->ctorque};
+  const size_t sizes[] = {(size_t)nc, (size_t)nc * 3, (size_t)nc * d * AB, (size_t)nc * 3 * AB,
+                          (size_t)nc * d * AB, (size_t)nc * 3 * AB, (size_t)nc * 9,
+                          (size_t)nc * 9, (size_t)nc * 3, (size_t)nc * d, (size_t)nc * 3};
+  for (int q = 0; q < 11; ++q) {
+    free(*arrs[q]);
+    *arrs[q] = (double*)calloc(sizes[q] + 1, sizeof(double));
+  }
+  memcpy(s->cm, mass, sizeof(double) * (size_t)nc);
+  memcpy(s->cmmi, mmi, sizeof(double) * (size_t)nc * 3);
+  if (v_hist) memcpy(s->cvh, v_hist, sizeof(double) * sizes[2]);
+  else memcpy(s->cvh, s->cv, sizeof(double) * (size_t)nc * d);
+  if (omega_hist) memcpy(s->comh, omega_hist, sizeof(double) * sizes[3]);
+  else memcpy(s->comh, s->com, sizeof(double) * (size_t)nc * 3);
+  if (f_hist) memcpy(s->cfh, f_hist, sizeof(double) * sizes[4]);
+  if (alpha_hist) memcpy(s->calh, alpha_hist, sizeof(double) * sizes[5]);
+  for (int c = 0; c < nc; ++c)
+    for (int q = 0; q < 9; ++q) s->crot[c * 9 + q] = (q % 4 == 0) ? 1.0 : 0.0;
+  if (acc_matrix) memcpy(s->cacc, acc_matrix, sizeof(double) * (size_t)nc * 9);
+  else memcpy(s->cacc, s->crot, sizeof(double) * (size_t)nc * 9);
+  if (theta) memcpy(s->ctheta, theta, sizeof(double) * (size_t)nc * 3);
+  /* level 1 of the histories is the colloids' current velocity */
+  memcpy(s->cv, s->cvh, sizeof(double) * (size_t)nc * d);
+  memcpy(s->com, s->comh, sizeof(double) * (size_t)nc * 3);
+  s->cdyn = 1;
+  return 0;
+}
+
+/* colloid_compute_interaction.F90 (repulsion only; no lubrication, no
+ * walls) + colloid_apply_body_force.F90 + colloid_compute_translate_
+ * acceleration.F90, from the fluid's drag and torque */
+static void colloid_translate_accel(orc_state* s, const double* fdrag, const double* ftorque) {
+  const int d = s->d, nc = s->cp.num_colloid, AB = s->cd.integrate_AB;
+  double* rep = (double*)calloc((size_t)nc * d + 1, sizeof(double));
+  orc_colloid_repulsion(s, rep);
+  for (int q = 0; q < nc * d; ++q) s->cdrag[q] = fdrag[q] + rep[q];
+  for (int q = 0; q < nc * 3; ++q) s->ctorque[q] = ftorque[q];
+  free(rep);
+  if (s->cd.body_force_type == 1)
+    for (int a = 0; a < d; ++a)
+      for (int c = 0; c < nc; ++c)
+        s->cdrag[c * d + a] = s->cdrag[c * d + a] + s->cd.body_force[a] * s->cm[c];
+  ab_shift(s->cfh, (size_t)nc * d, AB);
+  for (int a = 0; a < d; ++a)
+    for (int c = 0; c < nc; ++c)
+      s->cfh[c * d + a] = s->cp.translate ? s->cdrag[c * d + a] / s->cm[c] : 0.0;
+}
+
+/* colloid_compute_rotate_acceleration.F90 (spheres in 3D, disks in 2D) */
+static void colloid_rotate_accel(orc_state* s) {
+  const int nc = s->cp.num_colloid, AB = s->cd.integrate_AB;
+  ab_shift(s->calh, (size_t)nc * 3, AB);
+  if (s->cp.rotate) {
+    for (int c = 0; c < nc; ++c) {
+      if (s->d == 2) {
+        s->calh[c * 3 + 2] = s->ctorque[c * 3 + 2] / s->cmmi[c * 3 + 2];
+      } else {
+        for (int a = 0; a < 3; ++a) s->calh[c * 3 + a] = s->ctorque[c * 3 + a] / s->cmmi[c * 3 + a];
+      }
+    }
+  } else {
+    for (int q = 0; q < nc * 3; ++q) s->calh[q] = 0.0;
+  }
+}
+
+/* colloid_adjust_colloid.F90: periodic faces wrap the centre back by whole
+ * box lengths; a solid wall face puts it one radius inside (and stops that
+ * velocity component) */
+static void colloid_adjust(orc_state* s) {
+  const int d = s->d, nc = s->cp.num_colloid;
+  for (int c = 0; c < nc; ++c)
+    for (int a = 0; a < d; ++a) {
+      double* x = &s->cx[c * d + a];
+      const double lo = s->p.min_phys[a], hi = s->p.max_phys[a], L = hi - lo;
+      if (*x < lo) {
+        if (s->p.bcdef[2 * a] == MCFG_BC_PERIODIC) {
+          const int nover = (int)((hi - *x) / L);
+          *x = *x + L * (double)nover;
+        } else if (s->p.bcdef[2 * a] == MCFG_BC_WALL_SOLID) {
+          *x = lo + s->crad[c];
+          s->cvh[c * d + a] = 0.0;
+        }
+      }
+      if (*x >= hi) {
+        if (s->p.bcdef[2 * a + 1] == MCFG_BC_PERIODIC) {
+          const int nover = (int)((*x - lo) / L);
+          *x = *x - L * (double)nover;
+        } else if (s->p.bcdef[2 * a + 1] == MCFG_BC_WALL_SOLID) {
+          *x = hi - s->crad[c] - s->machine_zero;
+          s->cvh[c * d + a] = 0.0;
+        }
+      }
+    }
+}
+
+/* marching_marching.F90:995-1110: after the first right-hand side, the
+ * fluid's drag and torque, repulsion, body force and both accelerations */
+static int colloid_initial_accel(orc_state* s) {
+  const int d = s->d, nc = s->cp.num_colloid;
+  double* dr = (double*)calloc((size_t)nc * d + 1, sizeof(double));
+  double* tq = (double*)calloc((size_t)nc * 3 + 1, sizeof(double));
+  orc_colloid_drag(s, dr, tq);
+  colloid_translate_accel(s, dr, tq);
+  colloid_rotate_accel(s);
+  free(dr);
+  free(tq);
+  return 0;
+}
+
+/* The colloid part of a VV step, marching_integrate_VV.F90:455-765 */
+int orc_colloid_integrate(orc_state* s, int64_t step, double dt) {
+  if (!s->cdyn) return fail(s, "orc_set_colloid_dynamics must come first");
+  const int d = s->d, nc = s->cp.num_colloid, AB = s->cd.integrate_AB;
+  if (nc == 0) return 0;
+  double* dr = (double*)calloc((size_t)nc * d + 1, sizeof(double));
+  double* tq = (double*)calloc((size_t)nc * 3 + 1, sizeof(double));
+  orc_colloid_drag(s, dr, tq); /* particles_collect_colloid_interaction */
+  if (s->cp.translate || s->cp.rotate) {
+    const int nsub = s->cd.sub_time_step;
+    const double dts = dt / (double)nsub;
+    for (int i = 1; i <= nsub; ++i) {
+      const int oa = ab_order(step - 1 + i - s->cd.step_start, AB);
+      /* colloid_integrate_rotate_velocity is called with step-1+i+step_start */
+      const int orr = ab_order(step - 1 + i + s->cd.step_start, AB);
+      if (oa < 1 || orr < 1) {
+        free(dr);
+        free(tq);
+        return fail(s, "colloid integration before the first step");
+      }
+      if (s->cp.rotate) {
+        for (int c = 0; c < nc; ++c) {
+          double ax[3], phi;
+          for (int a = 0; a < 3; ++a) ax[a] = ab_incr(oa, &s->comh[c * 3 + a], (size_t)nc * 3, dts);
+          phi = sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);
+          if (phi < s->machine_zero) {
+            phi = 0.0;
+            ax[0] = 1.0;
+            ax[1] = ax[2] = 0.0;
+          } else {
+            for (int a = 0; a < 3; ++a) ax[a] = ax[a] / phi;
+          }
+          s->ctheta[c * 3 + 2] = s->ctheta[c * 3 + 2] + phi;
+          rotation_matrix(ax, phi, &s->crot[c * 9]);
+          double acc[9];
+          for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+              double t = 0.0;
+              for (int q = 0; q < 3; ++q) t = t + s->crot[c * 9 + a + 3 * q] * s->cacc[c * 9 + q + 3 * b];
+              acc[a + 3 * b] = t;
+            }
+          memcpy(&s->cacc[c * 9], acc, sizeof acc);
+        }
+      }
+      /* particles_compute_colloid_relative_position: boundary particles
+       * relative to the nearest centre image, turned by the rotation */
+      for (int64_t j = 0; j < s->nreal; ++j) {
+        const int c = s->sid[j] - 1;
+        if (s->sid[j] <= 0 || c >= nc) continue;
+        double ximg[3], rx[3] = {0, 0, 0}, vimg[3];
+        colloid_nearest_image(s, &s->x[j * d], c, ximg, rx, vimg);
+        if (s->cp.rotate) {
+          for (int a = 0; a < d; ++a) {
+            double t = 0.0;
+            for (int q = 0; q < d; ++q) t = t + s->crot[c * 9 + a + 3 * q] * rx[q];
+            s->x[j * d + a] = t;
+          }
+        } else {
+          for (int a = 0; a < d; ++a) s->x[j * d + a] = rx[a];
+        }
+      }
+      if (s->cp.rotate) {
+        ab_shift(s->comh, (size_t)nc * 3, AB);
+        for (int q = 0; q < nc * 3; ++q)
+          s->comh[q] = s->comh[q] + ab_incr(orr, &s->calh[q], (size_t)nc * 3, dts);
+      }
+      if (s->cp.translate) {
+        for (int q = 0; q < nc * d; ++q)
+          s->cx[q] = s->cx[q] + ab_incr(oa, &s->cvh[q], (size_t)nc * d, dts);
+        ab_shift(s->cvh, (size_t)nc * d, AB);
+        for (int q = 0; q < nc * d; ++q)
+          s->cvh[q] = s->cvh[q] + ab_incr(oa, &s->cfh[q], (size_t)nc * d, dts);
+      }
+      colloid_translate_accel(s, dr, tq);
+      colloid_adjust(s);
+      colloid_rotate_accel(s);
+      /* particles_compute_colloid_absolute_position */
+      for (int64_t j = 0; j < s->nreal; ++j) {
+        const int c = s->sid[j] - 1;
+        if (s->sid[j] <= 0 || c >= nc) continue;
+        for (int a = 0; a < d; ++a) s->x[j * d + a] = s->x[j * d + a] + s->cx[c * d + a];
+      }
+      memcpy(s->cv, s->cvh, sizeof(double) * (size_t)nc * d);
+      memcpy(s->com, s->comh, sizeof(double) * (size_t)nc * 3);
+    }
+  }
+  free(dr);
+  free(tq);
+  s->have_list = s->have_density = s->have_pressure = 0;
+  return 0;
+}
+
+int orc_get_colloid_state(const orc_state* s, double* x, double* v_hist, double* omega_hist,
+                          double* f_hist, double* alpha_hist, double* drag, double* torque,
+                          double* rot, double* acc, double* theta) {
+  const int d = s->d, nc = s->cp.num_colloid, AB = s->cd.integrate_AB;
+  if (x) memcpy(x, s->cx, sizeof(double) * (size_t)nc * d);
+  if (!s->cdyn) return 0;
+  if (v_hist) memcpy(v_hist, s->cvh, sizeof(double) * (size_t)nc * d * AB);
+  if (omega_hist) memcpy(omega_hist, s->comh, sizeof(double) * (size_t)nc * 3 * AB);
+  if (f_hist) memcpy(f_hist, s->cfh, sizeof(double) * (size_t)nc * d * AB);
+  if (alpha_hist) memcpy(alpha_hist, s->calh, sizeof(double) * (size_t)nc * 3 * AB);
+  if (drag) memcpy(drag, s->cdrag, sizeof(double) * (size_t)nc * d);
+  if (torque) memcpy(torque, s->ctorque, sizeof(double) * (size_t)nc * 3);
+  if (rot) memcpy(rot, s->crot, sizeof(double) * (size_t)nc * 9);
+  if (acc) memcpy(acc, s->cacc, sizeof(double) * (size_t)nc * 9);
+  if (theta) memcpy(theta, s->ctheta, sizeof(double) * (size_t)nc * 3);
   return 0;
 }
 
@@ -1574,7 +1873,10 @@ int orc_init_force(orc_state* s, int64_t step) {
   if (s->walls || s->le) boundary_update(s, s->time_current, s->time_current);
   int rc = orc_adjust_particles(s);
   if (rc) return rc;
-  return rhs(s, step);
+  rc = rhs(s, step);
+  if (rc) return rc;
+  if (s->cdyn && s->cp.num_colloid > 0) return colloid_initial_accel(s);
+  return 0;
 }
 
 /* marching_integrate_VV.F90:303-1620; time_current advanced first
@@ -1588,6 +1890,11 @@ int orc_step_vv(orc_state* s, int64_t step, double dt) {
   orc_integrate_velocity(s, dt, 0.5);
   orc_integrate_position(s, dt);
   if (!s->p.Newtonian) integrate_ct(s, dt, 0.5); /* marching_integrate_VV.F90:413 */
+  if (s->cdyn && s->cp.num_colloid > 0) {
+    /* :455-765 */
+    int rcc = orc_colloid_integrate(s, step, dt);
+    if (rcc) return rcc;
+  }
   if (s->walls || s->le) {
     /* :783-806: boundary update, wall particles x + v dt
      * (particles_integrate_boundary_position.F90) */

@@ -73,6 +73,17 @@ int orc_move_colloids(orc_state* s, const double* x_new, const double* rot, cons
                       const double* omega);
 int orc_colloid_drag(orc_state* s, double* drag, double* torque);
 int orc_colloid_repulsion(orc_state* s, double* force);
+/* rigid-body dynamics of the colloids (marching_integrate_VV.F90:455-765),
+ * arguments as mcfg_set_colloid_dynamics; orc_step_vv then runs the colloid
+ * part of every step and orc_init_force the initial accelerations */
+int orc_set_colloid_dynamics(orc_state* s, const mcfg_colloid_dynamics* cd, const double* mass,
+                             const double* mmi, const double* v_hist, const double* omega_hist,
+                             const double* f_hist, const double* alpha_hist,
+                             const double* acc_matrix, const double* theta);
+int orc_colloid_integrate(orc_state* s, int64_t step, double dt);
+int orc_get_colloid_state(const orc_state* s, double* x, double* v_hist, double* omega_hist,
+                          double* f_hist, double* alpha_hist, double* drag, double* torque,
+                          double* rot, double* acc, double* theta);
 /* counts: [0] reals, [1] ghosts, [2] pairs inside cut-off (last force) */
 int orc_counts(const orc_state* s, int64_t* counts);
 /* per-phase wall seconds accumulated since create:

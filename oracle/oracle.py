@@ -20,7 +20,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent))
 
-from mcf_gb300.params import ColloidParams, SDPDParams  # noqa: E402  (struct layouts only)
+from mcf_gb300.params import ColloidDynamics, ColloidParams, SDPDParams  # noqa: E402  (layouts only)
 
 from . import build as _build  # noqa: E402
 
@@ -75,6 +75,11 @@ def load(rebuild: bool = True) -> C.CDLL:
         "orc_colloid_drag": (C.c_int, [_h, _dp, _dp]),
         "orc_move_colloids": (C.c_int, [_h, _dp, _dp, _dp, _dp]),
         "orc_colloid_repulsion": (C.c_int, [_h, _dp]),
+        "orc_set_colloid_dynamics": (C.c_int, [_h, C.POINTER(ColloidDynamics), _dp, _dp, _dp, _dp,
+                                               _dp, _dp, _dp, _dp]),
+        "orc_colloid_integrate": (C.c_int, [_h, C.c_int64, C.c_double]),
+        "orc_get_colloid_state": (C.c_int, [_h, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                            _dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -121,6 +126,11 @@ class Oracle:
             self.close()
         except Exception:
             pass
+
+    @property
+    def sid(self) -> np.ndarray:
+        """species id of each uploaded particle (host order)"""
+        return self._id[:, 1]
 
     def set_threads(self, n: int):
         self.lib.orc_set_threads(self._h, int(n))
@@ -250,6 +260,31 @@ class Oracle:
         out = np.zeros((self._cp.num_colloid, self.dim))
         self._check("colloid_repulsion", self.lib.orc_colloid_repulsion(self._h,
                                                                          _ptr(out, C.c_double)))
+        return out
+
+    def set_colloid_dynamics(self, cd, mass, mmi, v_hist=None, omega_hist=None, f_hist=None,
+                             alpha_hist=None, acc_matrix=None, theta=None):
+        self._cd = cd
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float64)
+                for a in (mass, mmi, v_hist, omega_hist, f_hist, alpha_hist, acc_matrix, theta)]
+        self._check("set_colloid_dynamics", self.lib.orc_set_colloid_dynamics(
+            self._h, C.byref(cd), *[_ptr(a, C.c_double) for a in arrs]))
+
+    def colloid_integrate(self, step, dt):
+        self._check("colloid_integrate", self.lib.orc_colloid_integrate(self._h, int(step),
+                                                                         float(dt)))
+
+    def colloid_state(self):
+        """x, v, omega, f, alpha histories (level-major), drag, torque,
+        rot_matrix, acc_matrix, theta"""
+        nc, d, ab = self._cp.num_colloid, self.dim, self._cd.integrate_AB
+        out = {"x": np.zeros((nc, d)), "v": np.zeros((ab, nc, d)), "omega": np.zeros((ab, nc, 3)),
+               "f": np.zeros((ab, nc, d)), "alpha": np.zeros((ab, nc, 3)),
+               "drag": np.zeros((nc, d)), "torque": np.zeros((nc, 3)),
+               "rot": np.zeros((nc, 9)), "acc": np.zeros((nc, 9)), "theta": np.zeros((nc, 3))}
+        keys = ["x", "v", "omega", "f", "alpha", "drag", "torque", "rot", "acc", "theta"]
+        self._check("get_colloid_state", self.lib.orc_get_colloid_state(
+            self._h, *[_ptr(out[k], C.c_double) for k in keys]))
         return out
 
     def pair_we(self, step, pidi, pidj, e):
