@@ -87,7 +87,13 @@ def parse():
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32",
                     help="path of the headline value (fp64: the plain FP64 path, for profiling "
                          "its sweeps; the FP64 comparison line is then left out)")
-    ap.add_argument("--accuracy-steps", type=int, default=200)
+    ap.add_argument("--accuracy-steps", type=int, default=5000,
+                    help="VV steps of the FP32-vs-FP64 run on the headline workload (the "
+                         "5000 of its configuration)")
+    ap.add_argument("--accuracy-seeds", type=int, default=1,
+                    help="Philox keys of the FP32-vs-FP64 run (errors: mean and max)")
+    ap.add_argument("--channel-steps", type=int, default=40000,
+                    help="VV steps of the developed-channel FP32-vs-FP64 run")
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     return ap.parse_args()
 
@@ -193,22 +199,37 @@ class ClockSampler:
 
 # ---------------------------------------------------------- CPU baseline
 def cpu_baseline(w, steps: int, threads: int | None = None) -> dict:
+    """The CPU restatement of MCF's step on the host cores, in MCF's own loop
+    mode (symmetry = T: each pair once, half-shell cell pairs, ghost put),
+    parallelised over x-slabs of cells in two colours; beside it the
+    full-stencil loops (symmetry = F, every pair from both sides) and one
+    core with the symmetric loops (one MCF MPI rank's work)."""
     from oracle.oracle import Oracle
 
     threads = threads or os.cpu_count() or 1
-    p = w.params.copy()
-    p.symmetry = 0 if threads > 1 else 1  # full stencil parallelises race-free
-    o = Oracle(p, threads=threads)
-    o.upload(w.x, w.v, w.m, w.id)
-    o.marching_init_force(0)
-    t0 = time.perf_counter()
-    o.run_vv(0, steps, w.dt)
-    dt = time.perf_counter() - t0
+
+    def timed(symmetry):
+        p = w.params.copy()
+        p.symmetry = symmetry
+        o = Oracle(p, threads=threads)
+        o.upload(w.x, w.v, w.m, w.id)
+        o.marching_init_force(0)
+        t0 = time.perf_counter()
+        o.run_vv(0, steps, w.dt)
+        return time.perf_counter() - t0
+
+    dt = timed(1)
     out = {"value": w.n_fluid * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
            "sample": f"{w.name}: {steps} full VV steps of all {w.n} particles "
-                     f"({w.n_fluid} fluid), OpenMP full-stencil loops, {dt:.1f} s",
+                     f"({w.n_fluid} fluid), MCF's symmetric loops (symmetry = T) on "
+                     f"{threads} threads, {dt:.1f} s",
            "seconds_per_step": dt / steps, "cpu_model": cpu_model()}
     if threads > 1:
+        dtf = timed(0)
+        out["full_stencil"] = {"value": w.n_fluid * steps / dtf, "unit": UNIT, "cores": threads,
+                               "seconds_per_step": dtf / steps,
+                               "sample": "the same steps with the full-stencil loops "
+                                         "(symmetry = F, each pair from both sides)"}
         # one core, MCF's symmetric loops: the work of one MCF MPI rank,
         # on a 40^3 sub-box of the same workload (one step, a few seconds)
         from mcf_gb300 import configs
@@ -258,7 +279,7 @@ def run_reference(args, ws, rank):
     def make(n_side):
         w = configs.c3_poiseuille_3d(n_side=n_side)
         p = w.params.copy()
-        p.symmetry = 0  # full-stencil loops: race-free over cells
+        p.symmetry = 1  # MCF's own loop mode: half-shell pairs, each once
         o = Oracle(p, threads=threads)
         o.upload(w.x, w.v, w.m, w.id)
         o.marching_init_force(0)
@@ -289,7 +310,8 @@ def run_reference(args, ws, rank):
         "config": {"workload": w.name + " with y-walls (CPU sample of the 100^3 workload)",
                    "n_fluid": w.n_fluid, "n_wall": w.n - w.n_fluid,
                    "note": "CPU restatement of MCF's FP64 SDPD step (MCF is Fortran+MPI and "
-                           "cannot be built here), OpenMP over all host cores"},
+                           "cannot be built here) with MCF's symmetric loops (symmetry = T), "
+                           "x-slabs of cells in two colours over all host cores"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} timed full VV steps of a {w.n_fluid}-fluid "
                                    f"sub-box of the 1M workload ({w.n} particles)"},
@@ -399,65 +421,114 @@ def adjoint_cost(torch, w, T, K, local, wts):
                       "reverse_over_forward leaves out the forward pass that evaluates J"}
 
 
-def fp32_accuracy(w, steps, local):
-    """FP32-mixed against FP64 after `steps` VV steps from the same state
-    (same Philox keys, so the only difference is FP32 pair arithmetic): bulk
-    mean velocity and the velocity profile u_x(y) in unit slabs at the end,
-    and, averaged over the second half of the run, the wall shear stress
-    (x-force on each wall's particles per area) and the shear stress
-    statistic S_xy."""
+def fp32_accuracy(w, steps, local, seeds=(0,), samples=20):
+    """FP32-mixed against FP64 over `steps` VV steps from the same state,
+    for each seed offset in `seeds` (the Philox key of the Wiener increments
+    is params.seed + offset, the same in both precisions, so the only
+    difference is FP32 pair arithmetic).  Per seed: the bulk mean velocity
+    and the velocity profile u_x(y) in unit slabs at the end; averaged over
+    `samples` snapshots of the second half of the run, the wall shear stress
+    (x-force of the fluid on each wall's particles per wall area) and the
+    shear-stress profile tau_xy(y) (per-particle stresses s_xy summed per
+    unit slab over the slab volume).  Errors are relative to the FP64
+    run's scale; mean and max over the seeds are reported."""
     import numpy as np
 
     from mcf_gb300 import SDPD
     from mcf_gb300.params import PRECISION_FP32_MIXED, PRECISION_FP64
 
-    out = {}
-    res = {}
     sid = w.id[:, 1]
     fl = sid == 0
-    area = (w.params.max_phys[0] - w.params.min_phys[0]) * (w.params.max_phys[2] -
-                                                            w.params.min_phys[2])
-    for name, prec in (("fp32", PRECISION_FP32_MIXED), ("fp64", PRECISION_FP64)):
-        p = w.params.copy()
+    P = w.params
+    d = int(P.num_dim)
+    lx = P.max_phys[0] - P.min_phys[0]
+    lz = (P.max_phys[2] - P.min_phys[2]) if d == 3 else 1.0
+    area = lx * lz
+    nb = int(round(P.max_phys[1] - P.min_phys[1]))
+    wall_sids = sorted(set(int(q) for q in np.unique(sid) if q < 0))
+
+    def slab(x):
+        return np.clip(np.floor(x[:, 1] - P.min_phys[1]).astype(int), 0, nb - 1)
+
+    def run(prec, seed):
+        p = P.copy()
         p.precision = prec
         p.stress_tensor = 1
         p.device = local
+        p.seed = P.seed + seed
         sd = SDPD(p)
         sd.upload(w.x, w.v, w.m, w.id)
         sd.marching_init_force(0)
         half = steps // 2
         sd.run_vv(0, half, w.dt)
-        walls, sxy = [], []
-        every = max(1, (steps - half) // 10)
-        for s in range(half, steps, every):
-            sd.run_vv(s, every, w.dt)
-            _, _, st = sd.statistic_compute_statistic()
-            f = sd.download("f")["f"]
-            walls.append([float((w.m[sid == q] * f[sid == q, 0]).sum() / area) for q in (-3, -4)])
-            sxy.append(0.5 * (st[1] + st[3]))
-        d = sd.download("x", "v")
-        res[name] = (d, np.mean(walls, axis=0), float(np.mean(sxy)))
+        walls, taus = [], []
+        every = max(1, (steps - half) // samples)
+        s0 = half
+        while s0 + every <= steps:
+            sd.run_vv(s0, every, w.dt)
+            s0 += every
+            st = sd.download("x", "f", "s")
+            f, x = st["f"], st["x"]
+            walls.append([float((w.m[sid == q] * f[sid == q, 0]).sum() / area) for q in wall_sids])
+            sxy = 0.5 * (st["s"][:, 1] + st["s"][:, d])
+            taus.append(np.bincount(slab(x[fl]), weights=sxy[fl], minlength=nb) / area)
+        if s0 < steps:
+            sd.run_vv(s0, steps - s0, w.dt)
+        e = sd.download("x", "v")
         del sd
+        prof = np.bincount(slab(e["x"][fl]), weights=e["v"][fl, 0], minlength=nb) / np.maximum(
+            np.bincount(slab(e["x"][fl]), minlength=nb), 1)
+        return {"u": float(e["v"][fl, 0].mean()), "prof": prof,
+                "walls": np.mean(walls, axis=0) if walls else np.zeros(0),
+                "tau": np.mean(taus, axis=0) if taus else np.zeros(nb)}
 
-    def summary(d, walls, sxy):
-        x, v = d["x"], d["v"]
-        ybin = np.floor(x[fl, 1] - w.params.min_phys[1]).astype(int)
-        nb = int(round(w.params.max_phys[1] - w.params.min_phys[1]))
-        ybin = np.clip(ybin, 0, nb - 1)
-        prof = np.bincount(ybin, weights=v[fl, 0], minlength=nb) / np.maximum(
-            np.bincount(ybin, minlength=nb), 1)
-        return float(v[fl, 0].mean()), prof, list(walls), sxy
-
-    u32, p32, w32, s32 = summary(*res["fp32"])
-    u64, p64, w64, s64 = summary(*res["fp64"])
-    out["steps"] = steps
-    out["mean_velocity_rel"] = abs(u32 - u64) / abs(u64)
-    out["velocity_profile_rel"] = float(np.max(np.abs(p32 - p64)) / np.max(np.abs(p64)))
-    out["wall_shear_stress_rel"] = float(max(abs(a - b) / abs(b) for a, b in zip(w32, w64)))
-    out["shear_stress_rel"] = abs(s32 - s64) / abs(s64)
-    out["mean_velocity_fp64"] = u64
-    out["wall_shear_stress_fp64"] = [float(x) for x in w64]
+    errs = {"mean_velocity_rel": [], "velocity_profile_rel": [], "wall_shear_stress_rel": [],
+            "shear_stress_profile_rel": []}
+    ref = {"mean_velocity_fp64": [], "wall_shear_stress_fp64": [], "max_shear_stress_fp64": []}
+    for sd_off in seeds:
+        a, b = run(PRECISION_FP32_MIXED, sd_off), run(PRECISION_FP64, sd_off)
+        errs["mean_velocity_rel"].append(abs(a["u"] - b["u"]) / abs(b["u"]))
+        errs["velocity_profile_rel"].append(
+            float(np.max(np.abs(a["prof"] - b["prof"])) / np.max(np.abs(b["prof"]))))
+        if len(b["walls"]):
+            errs["wall_shear_stress_rel"].append(
+                float(np.max(np.abs(a["walls"] - b["walls"]) / np.abs(b["walls"]))))
+        errs["shear_stress_profile_rel"].append(
+            float(np.max(np.abs(a["tau"] - b["tau"])) / np.max(np.abs(b["tau"]))))
+        ref["mean_velocity_fp64"].append(b["u"])
+        ref["wall_shear_stress_fp64"].append([float(q) for q in b["walls"]])
+        ref["max_shear_stress_fp64"].append(float(np.max(np.abs(b["tau"]))))
+    out = {"steps": steps, "dt": w.dt, "seeds": len(seeds), "samples": samples}
+    for k, vals in errs.items():
+        if vals:
+            out[k] = {"mean": float(np.mean(vals)), "max": float(np.max(vals))}
+    out.update(ref)
     out["reference"] = "the FP64 GPU path (itself within 1e-12 of the CPU oracle per step)"
+    return out
+
+
+def developed_channel(local, steps=40000):
+    """FP32-mixed against FP64 on a developed Poiseuille flow: a 3D channel
+    of 20 x 20 x 20 lattice sites between solid y walls (Morris no-slip, 4
+    wall layers per side), C3's fluid (c = 20, eta = 0.5, kT = 1e-4 with the
+    Wiener increments) driven by g_x = 0.005 (u_max ~ 0.5, Mach 0.025), dt =
+    0.01 (MCF's criteria allow 0.0125), run to t = 400, two viscous times
+    L^2/nu (the slowest transient mode has decayed to e^-10)."""
+    from mcf_gb300 import configs
+
+    w = configs.poiseuille_channel(dim=3, n_side=20, force=0.005)
+    p = w.params
+    p.c = 20.0
+    p.eta = 0.5
+    p.kt = 1e-4
+    p.Brownian = 1
+    w.dt = 0.01
+    p.dt = 0.01
+    out = fp32_accuracy(w, steps, local, seeds=(0,), samples=40)
+    out["workload"] = ("developed Poiseuille channel 20^3 + walls (c 20, eta 0.5, kT 1e-4, "
+                       "g_x 0.005, dt 0.01)")
+    nu = p.eta / 1.0
+    out["u_max_analytic"] = 0.005 * 20.0 ** 2 / (8.0 * nu)
     return out
 
 
@@ -546,7 +617,10 @@ def run_ours(args, ws, rank, local):
                 "fp32_mixed_speedup": value / v64, "roofline": roof64}
         del sd64
         if not args.no_accuracy:
-            err["long_run"] = fp32_accuracy(w, args.accuracy_steps, local)
+            err["long_run"] = fp32_accuracy(w, args.accuracy_steps, local,
+                                            seeds=tuple(range(args.accuracy_seeds)))
+            err["long_run"]["workload"] = w.name + " with y-walls"
+            err["developed_channel"] = developed_channel(local, args.channel_steps)
     # end to end through the C-ABI with host buffers
     e2e = None
     if not args.no_e2e:

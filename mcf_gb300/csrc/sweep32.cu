@@ -263,48 +263,95 @@ __device__ __forceinline__ void nn_pair(ForceAcc<D, NNW, STRESS>& A, const float
     for (int a = 0; a < D; ++a) A.L[a + D * b] += (vj[a] - vi[a]) * r[b] * fac;
 }
 
+// A partner's records, gathered one pair ahead of their use.
+struct PairData {
+  float4 o, v, c;
+  int sl, j;
+};
+
+__device__ __forceinline__ PairData load_pair(int ent, const int* s_start,
+                                              const float4* __restrict__ off,
+                                              const float4* __restrict__ vf,
+                                              const float4* __restrict__ pcf) {
+  PairData d;
+  d.sl = ent >> kLocalBits;
+  d.j = s_start[d.sl * kReuseTPB + threadIdx.x] + (ent & (kMaxCellCount - 1));
+  d.o = off[d.j];
+  d.v = vf[d.j];
+  d.c = pcf[d.j];
+  return d;
+}
+
 // Fluid-fluid pair: no species tests, no boundary terms.
 template <int D, bool NNW, bool STRESS>
-__device__ __forceinline__ void pair_fluid(const Consts& k, ForceAcc<D, NNW, STRESS>& A, int ent,
-                                           const int* s_start, const float4* slot_tab,
-                                           const float4* __restrict__ off,
-                                           const float4* __restrict__ vf,
-                                           const float4* __restrict__ pcf, const float* qq,
-                                           uint32_t step, float inv_sqdt, bool noise) {
-  const int sl = ent >> kLocalBits;
-  const int j = s_start[sl * kReuseTPB + threadIdx.x] + (ent & (kMaxCellCount - 1));
-  const float4 oj = off[j], vj4 = vf[j], cj = pcf[j];
-  const float4 so = slot_tab[sl];
+__device__ __forceinline__ void pair_fluid(const Consts& k, ForceAcc<D, NNW, STRESS>& A,
+                                           const PairData& P, const float4* slot_tab,
+                                           const float* qq, uint32_t step, float inv_sqdt,
+                                           bool noise) {
+  const float4 so = slot_tab[P.sl];
   float r[3];
-  r[0] = (A.oi.x - oj.x) - so.x;
-  r[1] = (A.oi.y - oj.y) - so.y;
-  r[2] = (D == 3) ? (A.oi.z - oj.z) - so.z : 0.f;
+  r[0] = (A.oi.x - P.o.x) - so.x;
+  r[1] = (A.oi.y - P.o.y) - so.y;
+  r[2] = (D == 3) ? (A.oi.z - P.o.z) - so.z : 0.f;
   float d2 = r[0] * r[0] + r[1] * r[1];
   if (D == 3) d2 += r[2] * r[2];
   const float inv_d = rsqrtf(d2);
   const float d = d2 * inv_d;
   const float vi[3] = {A.v4i.x, A.v4i.y, A.v4i.z};
-  const float vj[3] = {vj4.x + so.w, vj4.y, vj4.z};
+  const float vj[3] = {P.v.x + so.w, P.v.y, P.v.z};
   const float gw = kernel_gradw<float>(k, d);
   float vij[3];
 #pragma unroll
   for (int a = 0; a < D; ++a) vij[a] = vi[a] - vj[a];
   float z[6];
-  if (noise) pair_draw<D>(k.rhs_force_type, k.rk, step, A.pidi, __float_as_int(vj4.w), z);
+  if (noise) pair_draw<D>(k.rhs_force_type, k.rk, step, A.pidi, __float_as_int(P.v.w), z);
   float pa[3];
-  pair_force<float, D>(k, r, inv_d, vij, A.ci.x, A.ci.y, cj.x, cj.y, gw, noise, z, inv_sqdt, pa);
+  pair_force<float, D>(k, r, inv_d, vij, A.ci.x, A.ci.y, P.c.x, P.c.y, gw, noise, z, inv_sqdt,
+                       pa);
   if (NNW) {
     float qj[1 + D * D];
 #pragma unroll
-    for (int cc = 0; cc <= D * D; ++cc) qj[cc] = qq[(size_t)cc * k.n + j];
+    for (int cc = 0; cc <= D * D; ++cc) qj[cc] = qq[(size_t)cc * k.n + P.j];
     nn_pair<D, NNW, STRESS>(A, A.qi, qj, r, vi, vj, gw, inv_d, pa);
   }
   float si_s, sj_s;
-  pair_scales<float>(k.rhs_force_type, A.ci.z, cj.z, si_s, sj_s);
+  pair_scales<float>(k.rhs_force_type, A.ci.z, P.c.z, si_s, sj_s);
 #pragma unroll
   for (int a = 0; a < D; ++a) pa[a] *= si_s;
   acc_add<D, NNW, STRESS>(A, pa, r);
 }
+
+// Walks the set bits of the mask words of one particle over the logical
+// candidates [start, end).
+struct BitCursor {
+  const uint32_t* __restrict__ mask;
+  int n, i, end, w0;
+  uint32_t bits;
+  __device__ __forceinline__ BitCursor(const uint32_t* m, int n_, int i_, int start, int end_)
+      : mask(m), n(n_), i(i_), end(end_) {
+    if (start >= end) {
+      w0 = end;
+      bits = 0u;
+      return;
+    }
+    w0 = start & ~31;
+    bits = mask[(size_t)(w0 >> 5) * n + i];
+    if (start > w0) bits &= ~((1u << (start - w0)) - 1u);
+    if (end - w0 < 32) bits &= (1u << (end - w0)) - 1u;
+  }
+  // the next candidate with its bit set, -1 past the end
+  __device__ __forceinline__ int next() {
+    while (bits == 0u) {
+      w0 += 32;
+      if (w0 >= end) return -1;
+      bits = mask[(size_t)(w0 >> 5) * n + i];
+      if (end - w0 < 32) bits &= (1u << (end - w0)) - 1u;
+    }
+    const int p = w0 + __ffs(bits) - 1;
+    bits &= bits - 1u;
+    return p;
+  }
+};
 
 // Any pair with a wall or colloid particle (pp_interaction_fw/_wf/_fc/_cf/
 // _cc.inc): the boundary particle takes its no-slip velocity and the fluid
@@ -503,17 +550,23 @@ __global__ void __launch_bounds__(kReuseTPB)
   const int vc = vcount[i];
   const int nff = vc & 0xffff, ntot = nff + (vc >> 16);
   if (S == 1) {
-    // fluid-fluid segment
-    for (int w0 = 0; w0 < nff; w0 += 32) {
-      uint32_t bits = mask[(size_t)(w0 >> 5) * n + i];
-      if (nff - w0 < 32) bits &= (1u << (nff - w0)) - 1u;
-      while (bits) {
-        const int p = w0 + __ffs(bits) - 1;
-        bits &= bits - 1u;
-        const int ent = vl[(size_t)p * n + i];
-        pair_fluid<D, NNW, STRESS>(k, A, ent, s_start, slot_tab, off, vf, pcf, qq, step,
-                                   inv_sqdt, noise);
+    // fluid-fluid segment: the next pair's records are gathered while the
+    // current pair is computed, the entry after it one step earlier still
+    BitCursor bc(mask, n, i, 0, nff);
+    int p = bc.next();
+    int pn = (p >= 0) ? bc.next() : -1;
+    int ent_n = (pn >= 0) ? (int)vl[(size_t)pn * n + i] : 0;
+    PairData nxt;
+    if (p >= 0) nxt = load_pair(vl[(size_t)p * n + i], s_start, off, vf, pcf);
+    while (p >= 0) {
+      const PairData cur = nxt;
+      p = pn;
+      if (p >= 0) {
+        nxt = load_pair(ent_n, s_start, off, vf, pcf);
+        pn = bc.next();
+        if (pn >= 0) ent_n = vl[(size_t)pn * n + i];
       }
+      pair_fluid<D, NNW, STRESS>(k, A, cur, slot_tab, qq, step, inv_sqdt, noise);
     }
     // wall / colloid segment
     for (int w0 = nff & ~31; w0 < ntot; w0 += 32) {
@@ -533,8 +586,8 @@ __global__ void __launch_bounds__(kReuseTPB)
       if (!((mask[(size_t)(p >> 5) * n + i] >> (p & 31)) & 1u)) continue;
       const int ent = vl[(size_t)cand_row(p, nff, vcap) * n + i];
       if (p < nff)
-        pair_fluid<D, NNW, STRESS>(k, A, ent, s_start, slot_tab, off, vf, pcf, qq, step,
-                                   inv_sqdt, noise);
+        pair_fluid<D, NNW, STRESS>(k, A, load_pair(ent, s_start, off, vf, pcf), slot_tab, qq,
+                                   step, inv_sqdt, noise);
       else
         pair_general<D, NNW, STRESS>(k, A, ent, s_start, slot_tab, off, vf, pcf, wd, x, qq, ca,
                                      step, inv_sqdt, noise);

@@ -810,6 +810,29 @@ static void for_all_pairs(orc_state* s, pair_fn fn, void* ctx) {
       const int k = kst + (int)(c / ((int64_t)nx * ny));
       loop_centre_cell(s, i, j, k, fn, ctx, &npairs);
     }
+  } else if (s->nthreads > 1) {
+    /* MCF's symmetric half-shell loops (symmetry = T) on all threads: each
+     * centre cell writes to particles of cells at x offsets 0 and +1 only
+     * (ppm_neighlist_MkNeighIdx's 2x2x2 block; periodic images are ghost
+     * copies, folded back after the loop), so x-slabs of at least one cell
+     * column, run in two colours (even slabs, then odd), never write the
+     * same particle at the same time.  Each particle's sums keep a fixed
+     * order: deterministic, and equal to the sequential loops to rounding. */
+    const int nx = en[0] - st[0] + 1;
+    int nslab = 2 * s->nthreads;
+    if (nslab > nx) nslab = nx;
+    for (int colour = 0; colour < 2; ++colour) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) num_threads(s->nthreads) reduction(+ : npairs)
+#endif
+      for (int q = colour; q < nslab; q += 2) {
+        const int i0 = st[0] + (int)((int64_t)q * nx / nslab);
+        const int i1 = st[0] + (int)((int64_t)(q + 1) * nx / nslab);
+        for (int k = kst; k <= ken; ++k)
+          for (int j = st[1]; j <= en[1]; ++j)
+            for (int i = i0; i < i1; ++i) loop_centre_cell(s, i, j, k, fn, ctx, &npairs);
+      }
+    }
   } else {
     for (int k = kst; k <= ken; ++k)
       for (int j = st[1]; j <= en[1]; ++j)

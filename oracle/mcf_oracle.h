@@ -35,8 +35,10 @@ orc_state* orc_create(const mcfg_params* p, char* err, int errlen);
 void orc_destroy(orc_state* s);
 const char* orc_last_error(const orc_state* s);
 
-/* threads used by the pair loops: 1 = MCF's sequential symmetric loops;
- * >1 = OpenMP over cells with the full (symmetry=F) stencil */
+/* threads used by the pair loops.  symmetry = T (MCF's half-shell loops):
+ * 1 thread runs them in MCF's sequential order, more threads run x-slabs of
+ * cells in two colours (race-free, deterministic).  symmetry = F (full
+ * stencil): OpenMP over centre cells. */
 int orc_set_threads(orc_state* s, int nthreads);
 
 int orc_upload(orc_state* s, int64_t n, const double* x, const double* v,

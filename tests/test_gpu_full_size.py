@@ -71,7 +71,13 @@ def rhs_close(g, o, step=0, tol=1e-12):
     a = g.download("rho", "f")
     b = o.download("rho", "f")
     assert np.all(np.abs(a["rho"] - b["rho"]) <= 1e-12 * np.abs(b["rho"]))
-    scale = o.force_scale()[:, None] + np.abs(b["f"])
+    # per-particle scale sum_j |a_ij| + |a_i|, with a floor of 1e-9 of its
+    # median: the pressure c^2 (rho - rho_ref) carries an absolute error of
+    # c^2 rho eps whatever its size, so a particle whose partners all sit
+    # within ~1e-7 of rho_ref (a million-particle box has some) has forces
+    # without relative accuracy in either implementation
+    fs = o.force_scale()
+    scale = fs[:, None] + np.abs(b["f"]) + 1e-9 * np.median(fs)
     err = np.abs(a["f"] - b["f"])
     ok = err <= tol * scale
     assert np.all(ok), worst(err, tol * scale, o.sid, a["f"], b["f"])

@@ -22,6 +22,14 @@ Workload: periodic cubes (squares) at dx = 1 with C2's physics (quintic
 rc = 3, c = 10, eta = 1, kT = 1e-3), velocities from Maxwell-Boltzmann,
 dt = 1e-3 to equilibrate (about 10 time units; the start from a lattice
 relaxes slowly through its sound modes) and for sampling.
+
+At C2's own size (64^3 = 262,144 particles) and time step (1e-4, 2000
+steps after the equilibration) the same comparisons run with an ensemble:
+the shear stress of 512 sub-boxes of 8^3 lattice sites (each a nearly
+independent sample, 200 snapshots) gives the stress-fluctuation variance to
+about 1.5%, so FP32-mixed and FP64 (independent streams) must agree within
+5%; equipartition within 1% in both; the velocity autocorrelation of 20,000
+particles within 0.01.
 """
 import numpy as np
 import pytest
@@ -129,6 +137,41 @@ def test_vacf_and_stress_variance_fp32_vs_fp64(gpu_lib):
     # 200 shear-stress samples a few steps correlated: ~15-25% sampling error
     ratio = np.var(s_a) / np.var(s_b)
     assert abs(ratio - 1.0) < 0.35, ratio
+
+
+def test_c2_64cubed_ensemble_statistics_fp32_vs_fp64(gpu_lib):
+    w = fluct_workload(n_side=64)
+    eq = equilibrated(w, 10000).download("x", "v")
+    rng = np.random.default_rng(64)
+    pick = rng.choice(w.n, 20000, replace=False)
+    nsub = 8  # sub-boxes per axis
+    out = []
+    for prec, seed in ((PRECISION_FP64, 11), (PRECISION_FP32_MIXED, 12)):
+        wp = fluct_workload(n_side=64, precision=prec, seed=seed)
+        wp.x, wp.v = eq["x"], eq["v"]
+        wp.dt = 1e-4  # C2's time step
+        sd = equilibrated(wp, 0)
+        ke, subs, vs = [], [], []
+        for s0 in range(0, 2000, 10):
+            sd.run_vv(s0, 10, wp.dt)
+            st = sd.download("x", "v", "s")
+            ke.append(0.5 * float((wp.m[:, None] * st["v"] ** 2).sum()))
+            cell = np.floor(np.mod(st["x"], 64.0) / (64.0 / nsub)).astype(int)
+            key = cell[:, 0] + nsub * (cell[:, 1] + nsub * cell[:, 2])
+            sxy = 0.5 * (st["s"][:, 1] + st["s"][:, 3])
+            subs.append(np.bincount(key, weights=sxy, minlength=nsub ** 3))
+            vs.append(st["v"][pick].copy())
+        out.append((np.array(ke), np.array(subs), np.array(vs), wp))
+    (ke_a, sub_a, v_a, w_a), (ke_b, sub_b, v_b, w_b) = out
+    for ke, wp in ((ke_a, w_a), (ke_b, w_b)):
+        ratio = t_kin(ke, wp) / expected_ratio(3, 3)
+        assert abs(ratio - 1.0) < 0.01, ratio
+    ca, cb = vacf(v_a, 100), vacf(v_b, 100)
+    assert np.max(np.abs(ca - cb)) < 0.01, np.max(np.abs(ca - cb))
+    # variance of the sub-box shear stress about its own mean
+    va = np.var(sub_a - sub_a.mean(0))
+    vb = np.var(sub_b - sub_b.mean(0))
+    assert abs(va / vb - 1.0) < 0.05, va / vb
 
 
 def test_fluctuating_trajectory_matches_oracle(gpu_lib):

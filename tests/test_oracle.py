@@ -325,3 +325,33 @@ def test_colloid_move_is_rigid():
         assert np.allclose(r1, r0 @ R.T, atol=1e-12)
     fl = w.id[:, 1] == 0
     assert np.array_equal(x0[fl], x1[fl])
+
+
+def test_threaded_symmetric_loops_match_sequential():
+    # MCF's half-shell loops (symmetry = T) on several threads (x-slabs of
+    # cells in two colours) give the sequential loops' result to rounding,
+    # and the same bits on every run
+    import numpy as np
+
+    from mcf_gb300 import configs
+    from oracle.oracle import Oracle
+
+    w = configs.c3_poiseuille_3d(n_side=16)
+    rng = np.random.default_rng(3)
+    fl = w.id[:, 1] == 0
+    w.x[fl] += rng.uniform(-0.1, 0.1, (int(fl.sum()), 3))
+    w.v[fl] = rng.normal(0.0, 1e-2, (int(fl.sum()), 3))
+    p = w.params.copy()
+    p.symmetry = 1
+    out = []
+    for th in (1, 4, 4):
+        o = Oracle(p, threads=th)
+        o.upload(w.x, w.v, w.m, w.id)
+        o.marching_init_force(0)
+        o.run_vv(0, 3, w.dt)
+        out.append(o.download("x", "v", "rho", "f"))
+    scale = np.abs(out[0]["f"]).max()
+    assert np.max(np.abs(out[1]["f"] - out[0]["f"])) <= 1e-12 * scale
+    assert np.max(np.abs(out[1]["rho"] - out[0]["rho"])) <= 1e-13
+    for k in ("x", "v", "rho", "f"):
+        assert np.array_equal(out[1][k], out[2][k])
