@@ -39,9 +39,12 @@ extern "C" {
 #define MCFG_ENOTSUP -9    /* option not supported by the library            */
 
 /* ---- enumerations (values are MCF's own) -------------------------------- */
-/* boundary types, PPM ppm_param.h: periodic 1, symmetry 3, wall_sym 7,
- * wall_solid 9, Lees-Edwards 10 */
+/* boundary types, PPM ppm_param.h: periodic 1, freespace 2, symmetry 3,
+ * wall_sym 7, wall_solid 9, Lees-Edwards 10.  A freespace face has no
+ * periodic images and no wall particles: the faces of one subdomain of a
+ * decomposed box, whose halo particles the caller supplies. */
 #define MCFG_BC_PERIODIC 1
+#define MCFG_BC_FREESPACE 2
 #define MCFG_BC_WALL_SOLID 9
 #define MCFG_BC_LE 10
 
@@ -53,10 +56,11 @@ extern "C" {
  * mcf_config/physics_config.mcf. */
 typedef struct mcfg_params {
   int32_t num_dim;            /* 2 or 3                                      */
-  int32_t bcdef[6];           /* per face x-,x+,y-,y+,z-,z+: 1 periodic, 9
-                                 solid wall, 10 Lees-Edwards (y faces only:
-                                 planes sliding along x; x, z periodic with
-                                 min_phys_t 0; no walls or colloids)        */
+  int32_t bcdef[6];           /* per face x-,x+,y-,y+,z-,z+: 1 periodic, 2
+                                 freespace, 9 solid wall, 10 Lees-Edwards (y
+                                 faces only: planes sliding along x; x, z
+                                 periodic with min_phys_t 0; no walls or
+                                 colloids)                                   */
   double min_phys[3];         /* fluid domain                                */
   double max_phys[3];
   double min_phys_t[3];       /* total domain incl. wall layers              */
@@ -210,6 +214,12 @@ int mcfg_build_list(mcfg_handle* h, int32_t* num_cell_dim,
  * rhs_density.F90:95-96 (includes the self term W(0) and the half-shell
  * pair fold-back of particles_map_ghost_put).  Needs mcfg_build_list. */
 int mcfg_compute_density(mcfg_handle* h);
+
+/* Overwrite the densities rho[n] (host order) after mcfg_compute_density,
+ * before mcfg_compute_pressure: the second ghost get of MCF's step
+ * (particles_map_ghost_get.F90 at marching_integrate_VV.F90:1128), for a
+ * subdomain whose halo particles' densities come from their owners. */
+int mcfg_update_density(mcfg_handle* h, const double* rho);
 
 /* Equation of state for all particles, particles_compute_pressure.F90:66-95
  * -> stateEquation_compute_pressure.F90:147-180. */

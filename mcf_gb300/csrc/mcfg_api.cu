@@ -189,9 +189,12 @@ const char* validate_params(const mcfg_params* p) {
   for (int a = 0; a < p->num_dim; ++a) {
     const int lo = p->bcdef[2 * a], hi = p->bcdef[2 * a + 1];
     const bool le_ok = (a == 1 && lo == MCFG_BC_LE && hi == MCFG_BC_LE);
-    if (!le_ok && ((lo != MCFG_BC_PERIODIC && lo != MCFG_BC_WALL_SOLID) ||
-                   (hi != MCFG_BC_PERIODIC && hi != MCFG_BC_WALL_SOLID)))
-      return "bcdef: periodic (1) and solid wall (9) faces, Lees-Edwards (10) on both y faces";
+    auto plain = [](int b) {
+      return b == MCFG_BC_PERIODIC || b == MCFG_BC_FREESPACE || b == MCFG_BC_WALL_SOLID;
+    };
+    if (!le_ok && (!plain(lo) || !plain(hi)))
+      return "bcdef: periodic (1), freespace (2) and solid wall (9) faces, Lees-Edwards (10) "
+             "on both y faces";
     if ((lo == MCFG_BC_PERIODIC) != (hi == MCFG_BC_PERIODIC))
       return "bcdef: a periodic face needs a periodic opposite face";
     if (le && a != 1) {
@@ -836,6 +839,13 @@ static Handle::GraphSlot* graph_for(Handle* h, double dt) {
 
 namespace {
 
+// one value per particle from host order into the sorted slots
+__global__ void k_scalar_from_host(int n, const double* __restrict__ src,
+                                   const int* __restrict__ hidx, double* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[hidx[i]];
+}
+
 __global__ void k_upload_force(int n, int d, const double* __restrict__ hf,
                                const int* __restrict__ hidx, double4_32a* __restrict__ f) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1132,6 +1142,24 @@ int mcfg_compute_density(mcfg_handle* h) {
   TRY(compute_density(h, false));
   TRY(check_device_errors(h));
   h->have_density = true;
+  h->have_pressure = false;
+  return MCFG_OK;
+}
+
+int mcfg_update_density(mcfg_handle* h, const double* rho) {
+  GUARD(h);
+  if (!rho) return set_error(h, MCFG_EINVAL, "mcfg_update_density: NULL rho");
+  if (!h->have_density) return set_error(h, MCFG_ESTATE, "mcfg_compute_density must come first");
+  const int n = (int)h->n;
+  if (n > 0) {
+    if (cuda_check(h, cudaMemcpyAsync(h->up_m, rho, sizeof(double) * (size_t)n,
+                                      cudaMemcpyHostToDevice, h->stream), "density copy"))
+      return MCFG_ECUDA;
+    const int tb = 256, gb = (n + tb - 1) / tb;
+    k_scalar_from_host<<<gb, tb, 0, h->stream>>>(n, h->up_m, h->hidx, h->rho);
+    h->launches++;
+    if (cuda_check(h, cudaGetLastError(), "density update launch")) return MCFG_ECUDA;
+  }
   h->have_pressure = false;
   return MCFG_OK;
 }

@@ -54,6 +54,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "mcfg_build_list": (C.c_int, [_h, _ip, _ip, _ip]),
         "mcfg_compute_density": (C.c_int, [_h]),
         "mcfg_compute_pressure": (C.c_int, [_h]),
+        "mcfg_update_density": (C.c_int, [_h, _dp]),
         "mcfg_compute_interaction": (C.c_int, [_h, C.c_int64]),
         "mcfg_apply_body_force": (C.c_int, [_h]),
         "mcfg_integrate_velocity": (C.c_int, [_h, C.c_double, C.c_double]),
@@ -255,6 +256,13 @@ class SDPD:
 
     def particles_compute_density(self) -> None:
         self._check("particles_compute_density", self.lib.mcfg_compute_density(self._h))
+
+    def update_density(self, rho) -> None:
+        """mcfg_update_density: densities (host order) from the caller, e.g. a
+        subdomain's halo particles' densities from their owners"""
+        r = _as(rho, np.float64, (self.n,))
+        self._check("mcfg_update_density", self.lib.mcfg_update_density(self._h,
+                                                                         _ptr(r, C.c_double)))
 
     def particles_compute_pressure(self) -> None:
         self._check("particles_compute_pressure", self.lib.mcfg_compute_pressure(self._h))

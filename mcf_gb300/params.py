@@ -33,6 +33,7 @@ STATUS_NAMES = {
 }
 
 BC_PERIODIC = 1
+BC_FREESPACE = 2  # no images, no wall particles (a subdomain's cut faces)
 BC_WALL_SOLID = 9
 BC_LE = 10  # Lees-Edwards (y faces, sliding along x)
 PRECISION_FP64 = 0

@@ -1399,6 +1399,17 @@ int orc_compute_density(orc_state* s) {
   return 0;
 }
 
+/* the second ghost get of marching_integrate_VV.F90:1128 for a subdomain:
+ * densities of the real particles from the caller, then the periodic ghost
+ * copies refreshed from them */
+int orc_update_density(orc_state* s, const double* rho) {
+  if (!s->have_density) return fail(s, "orc_update_density: no density");
+  memcpy(s->rho, rho, sizeof(double) * (size_t)s->nreal);
+  ghost_refresh(s);
+  s->have_pressure = 0;
+  return 0;
+}
+
 /* ------------------------------------------------------------------------
  * Pressure: particles_compute_pressure.F90:66-95 ->
  * stateEquation_compute_pressure.F90:147-180 (vector forms).

@@ -48,6 +48,7 @@ int orc_build_list(orc_state* s);
 int orc_export_lists(orc_state* s, int32_t* num_cell_dim, int32_t* cell_start,
                      int32_t* lpdx);
 int orc_compute_density(orc_state* s);
+int orc_update_density(orc_state* s, const double* rho);
 int orc_compute_pressure(orc_state* s);
 int orc_compute_interaction(orc_state* s, int64_t step);
 int orc_apply_body_force(orc_state* s);

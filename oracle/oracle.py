@@ -47,6 +47,7 @@ def load(rebuild: bool = True) -> C.CDLL:
         "orc_export_lists": (C.c_int, [_h, _ip, _ip, _ip]),
         "orc_compute_density": (C.c_int, [_h]),
         "orc_compute_pressure": (C.c_int, [_h]),
+        "orc_update_density": (C.c_int, [_h, _dp]),
         "orc_compute_interaction": (C.c_int, [_h, C.c_int64]),
         "orc_apply_body_force": (C.c_int, [_h]),
         "orc_integrate_velocity": (C.c_int, [_h, C.c_double, C.c_double]),
@@ -179,6 +180,10 @@ class Oracle:
 
     def particles_compute_density(self):
         self._check("density", self.lib.orc_compute_density(self._h))
+
+    def update_density(self, rho):
+        r = np.ascontiguousarray(rho, np.float64).reshape(self.n)
+        self._check("update_density", self.lib.orc_update_density(self._h, _ptr(r, C.c_double)))
 
     def particles_compute_pressure(self):
         self._check("pressure", self.lib.orc_compute_pressure(self._h))

@@ -1,0 +1,137 @@
+"""x-slab domain decomposition (mcf_gb300.decomp) on the CPU.
+
+The decomposed run must follow the undivided box to rounding: the same
+pairs, the same Wiener increments (keyed by the particle ids), summed in
+another order.  The CPU oracle runs every slab:
+  - slabs of one process exchanging in memory (1, 2 and 3 slabs; with one
+    slab the halos are the box's own periodic images);
+  - one slab per process, world_size 2 and 4, gloo point-to-point messages
+    over 127.0.0.1 (migration and both ghost gets cross process borders).
+Bars: positions within 1e-11 of the box, velocities within 1e-9 of the
+velocity scale, densities within 1e-12 relative, accelerations within 1e-9
+of their scale, after the initial right-hand side and 6 steps with the
+random force on, particles migrating between slabs.
+"""
+import os
+import socket
+
+import numpy as np
+import pytest
+
+from mcf_gb300 import configs
+from mcf_gb300.decomp import LocalExchange, SlabDecomposition, TorchExchange
+from oracle.oracle import Oracle
+
+NSTEPS = 6
+
+
+def workload():
+    # 18 x 18 x 18 lattice between y walls, C3's physics with a faster flow
+    # so that particles cross slab faces during the steps
+    w = configs.c3_poiseuille_3d(n_side=18)
+    rng = np.random.default_rng(18)
+    fl = w.id[:, 1] == 0
+    # lattice planes 0.01 below every integer x (slab faces at 6, 9, 12, 18):
+    # particles cross them within the first steps
+    w.x[fl, 0] += 0.49
+    w.x[fl] += rng.uniform(-0.1, 0.1, (int(fl.sum()), 3))
+    w.v[fl] = rng.normal(0.0, 0.3, (int(fl.sum()), 3))
+    w.v[fl, 0] += 1.0
+    p = w.params
+    p.kt = 1e-3
+    p.Brownian = 1
+    w.dt = 2e-3
+    p.dt = w.dt  # the random force's time step in the stage routines
+    return w
+
+
+def undivided(w):
+    o = Oracle(w.params)
+    o.upload(w.x, w.v, w.m, w.id)
+    o.marching_init_force(0)
+    o.run_vv(0, NSTEPS, w.dt)
+    return o.download("x", "v", "rho", "f")
+
+
+def by_pid(parts, n, d):
+    out = {k: np.full((n, d) if k in ("x", "v", "f") else (n,), np.nan)
+           for k in ("x", "v", "f", "rho")}
+    seen = np.zeros(n, int)
+    for part in parts:
+        idx = part["id"][:, 0] - 1
+        seen[idx] += 1
+        for k in out:
+            out[k][idx] = part[k]
+    assert np.all(seen == 1)  # every particle owned by exactly one slab
+    return out
+
+
+def check(w, got, ref):
+    L = 18.0
+    dx = got["x"] - ref["x"]
+    dx -= L * np.round(dx / L)  # a slab may hold a particle in another image
+    assert np.max(np.abs(dx)) <= 1e-11 * L
+    assert np.max(np.abs(got["v"] - ref["v"])) <= 1e-9 * np.abs(ref["v"]).max()
+    assert np.max(np.abs(got["rho"] - ref["rho"]) / ref["rho"]) <= 1e-12
+    assert np.max(np.abs(got["f"] - ref["f"])) <= 1e-9 * np.abs(ref["f"]).max()
+
+
+@pytest.mark.parametrize("nslab", [1, 2, 3])
+def test_slabs_in_one_process_follow_the_undivided_box(nslab):
+    w = workload()
+    ref = undivided(w)
+    dec = SlabDecomposition(w.params, nslab, factory=Oracle, exchange=LocalExchange())
+    dec.upload(w.x, w.v, w.m, w.id)
+    dec.init_force(0)
+    dec.run_vv(0, NSTEPS, w.dt)
+    got = by_pid(dec.owned_state(), w.n, 3)
+    check(w, got, ref)
+    assert dec.migrated > 0  # particles crossed slab faces (or the periodic x face)
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _rank_main(rank, world, port, q):
+    import torch.distributed as dist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        w = workload()
+        dec = SlabDecomposition(w.params, world, factory=Oracle, exchange=TorchExchange(3),
+                                mine=[rank])
+        dec.upload(w.x, w.v, w.m, w.id)
+        dec.init_force(0)
+        dec.run_vv(0, NSTEPS, w.dt)
+        parts = dec.owned_state()
+        gathered = [None] * world if rank == 0 else None
+        dist.gather_object(parts[0], gathered, dst=0)
+        if rank == 0:
+            q.put(gathered)
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world", [2, 4])
+def test_slabs_on_gloo_ranks_follow_the_undivided_box(world):
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    parts = q.get(timeout=300)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    w = workload()
+    check(w, by_pid(parts, w.n, 3), undivided(w))

@@ -1,0 +1,54 @@
+"""x-slab decomposition with GPU handles (mcf_gb300.decomp).
+
+Two and three slabs of one box, each slab its own handle on the one GPU of
+this run, halos exchanged through host copies in one process: the owned
+particles follow the undivided GPU run and the CPU oracle to rounding (the
+bars of the CPU decomposition tests), FP64; the FP32-mixed slabs follow the
+undivided FP32-mixed run within the FP32 trajectory bar.
+"""
+import numpy as np
+import pytest
+
+from mcf_gb300 import SDPD
+from mcf_gb300.decomp import LocalExchange, SlabDecomposition
+from mcf_gb300.params import PRECISION_FP32_MIXED
+from tests.test_decomposition import NSTEPS, by_pid, check, undivided, workload
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_undivided(w):
+    g = SDPD(w.params)
+    g.upload(w.x, w.v, w.m, w.id)
+    g.marching_init_force(0)
+    g.run_vv(0, NSTEPS, w.dt)
+    return g.download("x", "v", "rho", "f")
+
+
+@pytest.mark.parametrize("nslab", [2, 3])
+def test_gpu_slabs_follow_the_undivided_box(gpu_lib, nslab):
+    w = workload()
+    dec = SlabDecomposition(w.params, nslab, factory=SDPD, exchange=LocalExchange())
+    dec.upload(w.x, w.v, w.m, w.id)
+    dec.init_force(0)
+    dec.run_vv(0, NSTEPS, w.dt)
+    got = by_pid(dec.owned_state(), w.n, 3)
+    assert dec.migrated > 0
+    check(w, got, gpu_undivided(w))
+    check(w, got, undivided(w))
+
+
+def test_gpu_slabs_fp32_mixed(gpu_lib):
+    w = workload()
+    w.params.precision = PRECISION_FP32_MIXED
+    dec = SlabDecomposition(w.params, 2, factory=SDPD, exchange=LocalExchange())
+    dec.upload(w.x, w.v, w.m, w.id)
+    dec.init_force(0)
+    dec.run_vv(0, NSTEPS, w.dt)
+    got = by_pid(dec.owned_state(), w.n, 3)
+    ref = gpu_undivided(w)
+    L = 18.0
+    dx = got["x"] - ref["x"]
+    dx -= L * np.round(dx / L)
+    assert np.max(np.abs(dx)) <= 1e-6 * L
+    assert np.max(np.abs(got["v"] - ref["v"])) <= 1e-4 * np.abs(ref["v"]).max()
