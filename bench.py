@@ -84,6 +84,9 @@ def parse():
     ap.add_argument("--no-output", action="store_true")
     ap.add_argument("--no-lees-edwards", action="store_true")
     ap.add_argument("--no-mcf-deck", action="store_true")
+    ap.add_argument("--no-colloids", action="store_true")
+    ap.add_argument("--c4-steps", type=int, default=2000,
+                    help="VV steps of the FP32-vs-FP64 colloid run (C4's 2000)")
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32",
                     help="path of the headline value (fp64: the plain FP64 path, for profiling "
                          "its sweeps; the FP64 comparison line is then left out)")
@@ -374,10 +377,27 @@ def roofline_for(sd, torch, w, prec_idx, peaks, step0, clock_mhz=None):
             issue = {"achieved": ach, "peak": pk, "unit": "warp instructions/s", "frac": ach / pk,
                      "warp_instructions_per_launch": wi * w.n, "sms": sms,
                      "clock_mhz": clock_mhz}
-    return {"kernel_phase": top, "bound": "hbm", "achieved": achieved, "peak": peak,
+    fp64_pipe = None
+    if prec_idx and tf.exists():
+        # the FP64 path is bound by the FP64 pipe: its busy fraction and the
+        # FLOP rate (ncu FLOPs per particle of the same sweep on 64^3 x this
+        # launch's particles / its event time) against 2 DFMA a clock per SM
+        fp = json.loads(tf.read_text()).get("fp64_pipe", {}).get(top)
+        if fp:
+            sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+            clk = clock_mhz or 2070.0
+            ach = fp["flop_per_particle"] * w.n / (avg_ms / 1e3)
+            pk = 4.0 * sms * clk * 1e6
+            fp64_pipe = {"kernel": fp["kernel"], "pipe_active_ncu": fp["pipe_active"],
+                         "flop_frac_ncu": fp["flop_frac"], "achieved": ach / 1e12, "peak": pk / 1e12,
+                         "unit": "TFLOP/s", "frac": ach / pk,
+                         "peak_source": f"nominal: {sms} SMs x 2 DFMA x 2 FLOP x {clk:.0f} MHz"}
+    return {"kernel_phase": top, "bound": "fp64 pipe" if prec_idx else "hbm",
+            "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": (achieved / peak) if peak else None, "traffic": traffic,
             "avg_ms": avg_ms, "algo_bytes_per_launch": algo,
-            "peak_source": peaks.get("source"), "phase_share": share, "issue": issue}
+            "peak_source": peaks.get("source"), "phase_share": share, "issue": issue,
+            "fp64_pipe": fp64_pipe}
 
 
 def adjoint_cost(torch, w, T, K, local, wts):
@@ -532,6 +552,74 @@ def developed_channel(local, steps=40000):
     return out
 
 
+def colloid_suspension(args, local, ws, torch):
+    """C4: 96^3 lattice with 200 rigid spheres (radius 4 dx, DLVO repulsion,
+    g_x = 0.05, kT = 1e-3), the colloids integrated on the device
+    (Adams-Bashforth order 2, mcfg_set_colloid_dynamics).  FP32-mixed with
+    list reuse: particle-steps/s over the timed steps (all particles: solvent
+    and boundary).  Then FP32-mixed against FP64 over args.c4_steps steps
+    from the same state and Philox key: the colloids' velocities V and
+    angular velocities Omega, error relative to each quantity's largest
+    FP64 magnitude."""
+    import math
+
+    import numpy as np
+
+    from mcf_gb300 import SDPD, configs
+    from mcf_gb300.params import PRECISION_FP32_MIXED, PRECISION_FP64, ColloidDynamics
+
+    w, cs = configs.c4_colloids()
+    cd = ColloidDynamics()
+    cd.integrate_AB = 2
+    cd.sub_time_step = 1
+    cd.body_force_type = 1
+    cd.body_force[0] = w.params.body_force[0]
+    m = 4.0 / 3.0 * math.pi * cs.radius ** 3.0
+    mmi = np.repeat((0.4 * m * cs.radius ** 2)[:, None], 3, 1)
+
+    def make(prec, reuse):
+        p = w.params.copy()
+        p.precision = prec
+        p.device = local
+        p.reserved[1] = reuse
+        sd = SDPD(p)
+        sd.upload(w.x, w.v, w.m, w.id)
+        sd.set_colloids(cs.params, cs.x, cs.v, cs.omega, cs.radius)
+        sd.set_colloid_dynamics(cd, m, mmi)
+        sd.marching_init_force(0)
+        return sd
+
+    sd = make(PRECISION_FP32_MIXED, 1)
+    sd.run_vv(0, args.warmup, w.dt)
+    k = max(3, min(args.steps, 100))
+    t, launches = timed_run(sd, torch, k, args.warmup, w.dt, ws)
+    t = max_over_ranks(t, ws)
+    out = {"workload": f"{w.name} (the colloids integrated on the device, AB2), FP32-mixed "
+                       "with list reuse",
+           "n": w.n, "n_boundary": int((w.id[:, 1] > 0).sum()), "n_colloid": int(cs.x.shape[0]),
+           "value": aggregate_throughput(w.n * k, t, ws), "unit": UNIT,
+           "ms_per_step": 1e3 * t / k, "steps": k, "gpu_launches": int(launches)}
+    del sd
+    if args.c4_steps > 0:
+        res = {}
+        for name, prec in (("fp32", PRECISION_FP32_MIXED), ("fp64", PRECISION_FP64)):
+            sd = make(prec, 1)
+            sd.run_vv(0, args.c4_steps, w.dt)
+            res[name] = sd.colloid_state()
+            del sd
+        a, b = res["fp32"], res["fp64"]
+        out["fp32_error_vs_fp64"] = {
+            "steps": args.c4_steps,
+            "velocity_rel": float(np.max(np.abs(a["v"][0] - b["v"][0])) /
+                                  np.max(np.abs(b["v"][0]))),
+            "angular_velocity_rel": float(np.max(np.abs(a["omega"][0] - b["omega"][0])) /
+                                          np.max(np.abs(b["omega"][0]))),
+            "centre_abs": float(np.max(np.abs(a["x"] - b["x"]))),
+            "max_velocity_fp64": float(np.max(np.abs(b["v"][0]))),
+            "max_angular_velocity_fp64": float(np.max(np.abs(b["omega"][0])))}
+    return out
+
+
 def run_ours(args, ws, rank, local):
     import numpy as np
     import torch
@@ -612,7 +700,8 @@ def run_ours(args, ws, rank, local):
         t64, _ = timed_run(sd64, torch, k64, 2, w.dt, ws)
         t64 = max_over_ranks(t64, ws)
         v64 = aggregate_throughput(w.n_fluid * k64, t64, ws)
-        roof64 = roofline_for(sd64, torch, w64, 1, peaks, 2 + k64)
+        roof64 = roofline_for(sd64, torch, w64, 1, peaks, 2 + k64,
+                              clocks.get("sm_mhz") if clocks else None)
         fp64 = {"value": v64, "unit": UNIT, "steps": k64, "ms_per_step": 1e3 * t64 / k64,
                 "fp32_mixed_speedup": value / v64, "roofline": roof64}
         del sd64
@@ -727,6 +816,9 @@ def run_ours(args, ws, rank, local):
     # MCF's own 1M-particle scalability deck (cut-off 4 dx, Batchelor
     # equation of state, Hu-Adams angular force), read through
     # mcf_config.load_mcf_deck from a deck written in MCF's format
+    colloids = None
+    if not args.no_colloids:
+        colloids = colloid_suspension(args, local, ws, torch)
     mcf_deck = None
     if not args.no_mcf_deck:
         from mcf_gb300.configs import write_mcf_scalability_deck
@@ -783,7 +875,7 @@ def run_ours(args, ws, rank, local):
                    "pairs_per_step": info["num_pairs"], "list_reuse": list_reuse},
         "roofline": roof, "fp64": fp64, "fp32_error_vs_fp64": err, "e2e": e2e,
         "adjoint": adjoint, "output_write": output, "lees_edwards": lees_edwards,
-        "mcf_scalability_deck": mcf_deck,
+        "mcf_scalability_deck": mcf_deck, "colloid_suspension": colloids,
         "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
         "pair_interactions_per_s": info["num_pairs"] * args.steps * ws / tmax,
     }

@@ -11,10 +11,11 @@
 // as one bit per candidate, mask[word][n] -- 16 bytes a particle -- instead
 // of writing the step's pairs out as a second 16-bit list (226 bytes a
 // particle on the 100^3 workload, which the force sweep then read back).
-// The force sweep walks the set bits: the fluid-fluid segment with a body
-// that has no species tests (no wall or colloid terms), the other segment
-// with the general body (Morris no-slip walls, colloid no-slip, boundary
-// pressure).  Every pair is still evaluated from both sides (gather, no
+// The force sweep walks the candidates: the fluid-fluid segment in lockstep
+// across the warp (the list rows stay coalesced; a lane whose bit is clear
+// idles that iteration) with a body that has no species tests (no wall or
+// colloid terms), the other segment over its set bits with the general body
+// (Morris no-slip walls, colloid no-slip, boundary pressure).  Every pair is still evaluated from both sides (gather, no
 // scatter, no atomics), sums run in candidate order: deterministic.
 //
 // Reference: particles_compute_density.F90:578-867, particles_compute_
@@ -321,38 +322,6 @@ __device__ __forceinline__ void pair_fluid(const Consts& k, ForceAcc<D, NNW, STR
   acc_add<D, NNW, STRESS>(A, pa, r);
 }
 
-// Walks the set bits of the mask words of one particle over the logical
-// candidates [start, end).
-struct BitCursor {
-  const uint32_t* __restrict__ mask;
-  int n, i, end, w0;
-  uint32_t bits;
-  __device__ __forceinline__ BitCursor(const uint32_t* m, int n_, int i_, int start, int end_)
-      : mask(m), n(n_), i(i_), end(end_) {
-    if (start >= end) {
-      w0 = end;
-      bits = 0u;
-      return;
-    }
-    w0 = start & ~31;
-    bits = mask[(size_t)(w0 >> 5) * n + i];
-    if (start > w0) bits &= ~((1u << (start - w0)) - 1u);
-    if (end - w0 < 32) bits &= (1u << (end - w0)) - 1u;
-  }
-  // the next candidate with its bit set, -1 past the end
-  __device__ __forceinline__ int next() {
-    while (bits == 0u) {
-      w0 += 32;
-      if (w0 >= end) return -1;
-      bits = mask[(size_t)(w0 >> 5) * n + i];
-      if (end - w0 < 32) bits &= (1u << (end - w0)) - 1u;
-    }
-    const int p = w0 + __ffs(bits) - 1;
-    bits &= bits - 1u;
-    return p;
-  }
-};
-
 // Any pair with a wall or colloid particle (pp_interaction_fw/_wf/_fc/_cf/
 // _cc.inc): the boundary particle takes its no-slip velocity and the fluid
 // partner's pressure (Oldroyd-B: density and pressure tensor).
@@ -550,23 +519,29 @@ __global__ void __launch_bounds__(kReuseTPB)
   const int vc = vcount[i];
   const int nff = vc & 0xffff, ntot = nff + (vc >> 16);
   if (S == 1) {
-    // fluid-fluid segment: the next pair's records are gathered while the
-    // current pair is computed, the entry after it one step earlier still
-    BitCursor bc(mask, n, i, 0, nff);
-    int p = bc.next();
-    int pn = (p >= 0) ? bc.next() : -1;
-    int ent_n = (pn >= 0) ? (int)vl[(size_t)pn * n + i] : 0;
+    // fluid-fluid segment in lockstep over the candidates (coalesced list
+    // rows); a lane whose bit is clear idles that iteration
+    uint32_t word = 0;
+    bool has_n = false;
     PairData nxt;
-    if (p >= 0) nxt = load_pair(vl[(size_t)p * n + i], s_start, off, vf, pcf);
-    while (p >= 0) {
+    int ent_n = 0;
+    if (nff > 0) {
+      word = mask[i];
+      has_n = word & 1u;
+      if (has_n) nxt = load_pair(vl[i], s_start, off, vf, pcf);
+      if (nff > 1) ent_n = vl[(size_t)n + i];
+    }
+    for (int p = 0; p < nff; ++p) {
+      const bool has = has_n;
       const PairData cur = nxt;
-      p = pn;
-      if (p >= 0) {
-        nxt = load_pair(ent_n, s_start, off, vf, pcf);
-        pn = bc.next();
-        if (pn >= 0) ent_n = vl[(size_t)pn * n + i];
+      const int q = p + 1;
+      if (q < nff) {
+        if ((q & 31) == 0) word = mask[(size_t)(q >> 5) * n + i];
+        has_n = (word >> (q & 31)) & 1u;
+        if (has_n) nxt = load_pair(ent_n, s_start, off, vf, pcf);
+        if (q + 1 < nff) ent_n = vl[(size_t)(q + 1) * n + i];
       }
-      pair_fluid<D, NNW, STRESS>(k, A, cur, slot_tab, qq, step, inv_sqdt, noise);
+      if (has) pair_fluid<D, NNW, STRESS>(k, A, cur, slot_tab, qq, step, inv_sqdt, noise);
     }
     // wall / colloid segment
     for (int w0 = nff & ~31; w0 < ntot; w0 += 32) {

@@ -1,12 +1,15 @@
 """FP64 GPU path against the oracle at the sizes of the five workloads.
 
 The other parity tests run on 12^3-24^3 boxes; these run the workloads at
-their own sizes through the C-ABI, with the oracle's OpenMP loops (MCF's
-full-stencil loop mode, symmetry = F, over all host cores) as the checker:
+their own sizes through the C-ABI, with the oracle's threaded loops (MCF's
+symmetric loop mode, symmetry = T, x-slabs of cells over all host cores)
+as the checker:
 
   - C2, 64^3 = 262,144 particles, jittered lattice: cell lists bit-exact,
-    one right-hand side at 1e-12 (density relative, acceleration of the
-    per-particle scale sum_j |a_ij|), one with the random force at 1e-5 of
+    one right-hand side at 1e-12 (density relative; acceleration of the
+    per-particle scale sum_j |a_ij| + |a_i|, floored at 1e-6 of its median,
+    since a pressure near zero has no relative accuracy), one with the
+    random force at 1e-5 of
     the scale (FP32 Box-Muller normals, as in the small-box tests), then 10
     kT = 0 steps: positions within 1e-9 of the box, velocities within 1e-7
     of the velocity scale (the bars of the 100-step C1 trajectory);
@@ -71,13 +74,14 @@ def rhs_close(g, o, step=0, tol=1e-12):
     a = g.download("rho", "f")
     b = o.download("rho", "f")
     assert np.all(np.abs(a["rho"] - b["rho"]) <= 1e-12 * np.abs(b["rho"]))
-    # per-particle scale sum_j |a_ij| + |a_i|, with a floor of 1e-9 of its
+    # per-particle scale sum_j |a_ij| + |a_i|, with a floor of 1e-6 of its
     # median: the pressure c^2 (rho - rho_ref) carries an absolute error of
-    # c^2 rho eps whatever its size, so a particle whose partners all sit
-    # within ~1e-7 of rho_ref (a million-particle box has some) has forces
-    # without relative accuracy in either implementation
+    # c^2 rho eps whatever its size, so the pressure force of a particle whose
+    # partners all sit within ~1e-4 of rho_ref (a million-particle box has
+    # some, most of them wall particles with few fluid partners near the
+    # cut-off) has no relative accuracy in either implementation
     fs = o.force_scale()
-    scale = fs[:, None] + np.abs(b["f"]) + 1e-9 * np.median(fs)
+    scale = fs[:, None] + np.abs(b["f"]) + 1e-6 * np.median(fs)
     err = np.abs(a["f"] - b["f"])
     ok = err <= tol * scale
     assert np.all(ok), worst(err, tol * scale, o.sid, a["f"], b["f"])
