@@ -120,13 +120,11 @@ void free_all(Handle* h) {
   h->out_dev = nullptr;
   h->out_host = nullptr;
   h->out_cap = 0;
-  for (void* p : {(void*)h->x_ref, (void*)h->vl, (void*)h->vcount, (void*)h->d_rebuild,
-                  (void*)h->vmask})
+  for (void* p : {(void*)h->x_ref, (void*)h->vl, (void*)h->vcount, (void*)h->d_rebuild})
     if (p) cudaFree(p);
   h->x_ref = nullptr;
   h->vl = nullptr;
-  h->vmask = nullptr;
-  h->masked = false;
+  h->split_list = false;
   h->vcount = h->d_rebuild = nullptr;
   h->vcap = 0;
   h->reuse_valid = false;
@@ -514,9 +512,7 @@ int ensure_capacity(Handle* h, int64_t n64) {
       if ((rc = dalloc(h, &h->x_ref, cap)) || (rc = dalloc(h, &h->vl, cap * (size_t)h->vcap)) ||
           (rc = dalloc(h, &h->vcount, cap)) || (rc = dalloc(h, &h->d_rebuild, 2)))
         return rc;
-      if (h->p.precision != MCFG_PRECISION_FP64 &&
-          (rc = dalloc(h, &h->vmask, cap * (size_t)((h->vcap + 31) / 32))))
-        return rc;
+      h->partitioned = h->p.precision != MCFG_PRECISION_FP64;
       if (cuda_check(h, cudaMemsetAsync(h->d_rebuild, 0, 2 * sizeof(int), h->stream),
                      "memset rebuild"))
         return MCFG_ECUDA;

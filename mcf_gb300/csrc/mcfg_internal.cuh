@@ -220,8 +220,9 @@ struct Handle {
   uint16_t* vl = nullptr;        // [vcap][n] candidates within rc + skin (slot<<11 | local);
                                  // FP32 handles: fluid-fluid pairs from row 0 up, the
                                  // others from row vcap-1 down (sweep32.cu)
-  uint32_t* vmask = nullptr;     // FP32: [vcap/32][n] the step's pairs among the candidates
-  bool masked = false;           // the last density sweep wrote vmask (force_mask follows)
+  bool partitioned = false;      // FP32 lists: fluid-fluid rows up, the others down
+  bool split_list = false;       // the last density sweep wrote a partitioned nl
+                                 // (force_list follows)
   int* vcount = nullptr;         // [n]
   int vcap = 0;
   int* d_rebuild = nullptr;      // [0] rebuild request, [1] rebuilds done
@@ -320,9 +321,9 @@ int verlet_build_gated(Handle* h);
 int compute_density(Handle* h, bool with_pressure, bool reuse = false);
 int compute_pressure(Handle* h);
 int compute_force(Handle* h, int64_t step, int fuse_mode, double dt);
-// FP32-mixed sweeps over the candidate list with a per-step pair mask
-int density_mask(Handle* h, bool with_pressure);
-int force_mask(Handle* h, int64_t step, int fuse_mode, double dt);
+// FP32-mixed sweeps over the partitioned candidate list (sweep32.cu)
+int density_list(Handle* h, bool with_pressure);
+int force_list(Handle* h, int64_t step, int fuse_mode, double dt);
 int apply_body_force(Handle* h);
 int integrate_velocity(Handle* h, double dt, double lambda);
 int integrate_position(Handle* h, double dt);

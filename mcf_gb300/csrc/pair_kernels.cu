@@ -1418,11 +1418,11 @@ int verlet_build_gated(Handle* h) {
   const int g = grid_for(h);
   if (k.d == 3)
     k_verlet_build<3><<<g, kWarpsPerBlock * 32, 0, h->stream>>>(
-        k, h->d_rebuild, h->cell_start, h->off, h->vl, h->vcount, h->vcap, h->vmask != nullptr,
+        k, h->d_rebuild, h->cell_start, h->off, h->vl, h->vcount, h->vcap, h->partitioned ? 1 : 0,
         h->d_err);
   else
     k_verlet_build<2><<<g, kWarpsPerBlock * 32, 0, h->stream>>>(
-        k, h->d_rebuild, h->cell_start, h->off, h->vl, h->vcount, h->vcap, h->vmask != nullptr,
+        k, h->d_rebuild, h->cell_start, h->off, h->vl, h->vcount, h->vcap, h->partitioned ? 1 : 0,
         h->d_err);
   k_rebuild_done<<<1, 1, 0, h->stream>>>(h->d_rebuild);
   h->launches += 2;
@@ -1438,8 +1438,8 @@ int compute_density(Handle* h, bool with_pressure, bool reuse) {
     return MCFG_ECUDA;
   const int g = grid_for(h);
   const bool fp64 = h->p.precision == MCFG_PRECISION_FP64;
-  h->masked = reuse && !fp64;
-  if (h->masked) return density_mask(h, with_pressure);
+  h->split_list = reuse && !fp64;
+  if (h->split_list) return density_list(h, with_pressure);
   if (reuse) {
     const int n = (int)h->n;
     if (n == 0) return MCFG_OK;
@@ -1450,7 +1450,7 @@ int compute_density(Handle* h, bool with_pressure, bool reuse) {
       h->nl, h->ncount, h->nhs, h->neigh_cap, h->rho, h->pr, h->pc, h->pcf, h->vf,              \
       with_pressure ? 1 : 0, h->d_err, h->d_stats, h->d_pairs, NN{h->ct, h->act, h->vgt, h->qq}, \
       CollArgs{h->v, h->rxc, h->rxcf})
-    // FP64 only: the FP32 path runs density_mask (sweep32.cu)
+    // FP64 only: the FP32 path runs density_list (sweep32.cu)
     if (k.d == 3)
       LAUNCH_R(3, true, 1, gr);
     else
@@ -1496,7 +1496,7 @@ int compute_pressure(Handle* h) {
 }
 
 int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
-  if (h->masked) return force_mask(h, step, fuse_mode, dt);
+  if (h->split_list) return force_list(h, step, fuse_mode, dt);
   Consts& k = h->k;
   cudaStream_t s = h->stream;
   const int g = grid_for(h);

@@ -7,16 +7,16 @@
 // the last row down.  vcount packs both counts (fluid-fluid | other << 16).
 //
 // Each step the density sweep re-tests every candidate exactly (the FP32
-// test of the per-step scan, same operation order) and records the outcome
-// as one bit per candidate, mask[word][n] -- 16 bytes a particle -- instead
-// of writing the step's pairs out as a second 16-bit list (226 bytes a
-// particle on the 100^3 workload, which the force sweep then read back).
-// The force sweep walks the candidates: the fluid-fluid segment in lockstep
-// across the warp (the list rows stay coalesced; a lane whose bit is clear
-// idles that iteration) with a body that has no species tests (no wall or
-// colloid terms), the other segment over its set bits with the general body
-// (Morris no-slip walls, colloid no-slip, boundary pressure).  Every pair is still evaluated from both sides (gather, no
-// scatter, no atomics), sums run in candidate order: deterministic.
+// test of the per-step scan, same operation order) and writes the step's
+// pairs as a compact list in the same two segments (nl rows from 0 up and
+// from the last row down, ncount = fluid-fluid | other << 16): coalesced
+// rows and no holes, so the force sweep walks every list row with all lanes
+// busy.  The force sweep takes the fluid-fluid segment with a body that has
+// no species tests (no wall or colloid terms), gathering the next pair's
+// records while it computes the current one, and the other segment with the
+// general body (Morris no-slip walls, colloid no-slip, boundary pressure).
+// Every pair is evaluated from both sides (gather, no scatter, no atomics),
+// sums run in list order: deterministic.
 //
 // Reference: particles_compute_density.F90:578-867, particles_compute_
 // interaction.F90:609-900, pp_interaction*.inc, rhs_force_ff_Newtonian*.F90.
@@ -36,18 +36,19 @@ __device__ __forceinline__ int cand_row(int p, int nff, int vcap) {
 
 // Density over the candidate list, S lanes per particle (S = 4 below
 // kSplitBelow particles, as the force sweep).  Candidate p of particle i is
-// a pair when its FP32 test passes; bit p of the mask records it.
+// a pair when its FP32 test passes; kept pairs go to the compact list, the
+// fluid-fluid ones from row 0 up, the others from row cap-1 down.
 template <int D, int S>
 __global__ void __launch_bounds__(kReuseTPB)
-    k_density_mask(Consts k, const int* __restrict__ cell_start, const int* __restrict__ cell_of,
+    k_density_list(Consts k, const int* __restrict__ cell_start, const int* __restrict__ cell_of,
                    const float4* __restrict__ off, const double4_32a* __restrict__ x,
                    const double4_32a* __restrict__ v, const double* __restrict__ m,
                    const int* __restrict__ pid, const uint16_t* __restrict__ vl,
-                   const int* __restrict__ vcount, int vcap, uint32_t* __restrict__ mask,
-                   double* __restrict__ rho, double* __restrict__ pr, float4* __restrict__ pcf,
-                   float4* __restrict__ vf, int with_pressure, unsigned* __restrict__ err,
-                   int* __restrict__ stats, unsigned long long* __restrict__ pairs, NN nn,
-                   CollArgs ca) {
+                   const int* __restrict__ vcount, int vcap, uint16_t* __restrict__ nl,
+                   int* __restrict__ ncount, int cap, double* __restrict__ rho,
+                   double* __restrict__ pr, float4* __restrict__ pcf, float4* __restrict__ vf,
+                   int with_pressure, unsigned* __restrict__ err, int* __restrict__ stats,
+                   unsigned long long* __restrict__ pairs, NN nn, CollArgs ca) {
   __shared__ int s_start[kMaxStencil * kReuseTPB];
   __shared__ float4 s_slot[kSlotTable];
   const int n = k.n, tid = threadIdx.x;
@@ -55,7 +56,7 @@ __global__ void __launch_bounds__(kReuseTPB)
   const int i = gt / S, lane_s = gt % S;
   fill_slot_offsets<D>(k, s_slot);
   __syncthreads();
-  int kept = 0, si = 0;
+  int kff = 0, ko = 0, si = 0;
   bool acc_i = false;
   float sum = 0.0f, comp = 0.0f;
   if (i < n) {
@@ -72,7 +73,6 @@ __global__ void __launch_bounds__(kReuseTPB)
       // candidates in groups of four: their entries, then their offsets,
       // are loaded before any is used (the sweep waits on these gathers)
       constexpr int kGather = 4;
-      uint32_t word = 0;
       for (int p0 = 0; p0 < ntot; p0 += kGather) {
         int entg[kGather], jg[kGather];
         float4 og[kGather];
@@ -98,47 +98,48 @@ __global__ void __launch_bounds__(kReuseTPB)
             const float tz = (oi.z - so.z) - oj.z;
             t2 += tz * tz;
           }
-          if (t2 < k.rc2f) {
-            word |= 1u << (p & 31);
-            ++kept;
-            if (acc_i) {
-              // W as k_density's second phase rounds it: (o_i - o_j) - slot
-              const float rx = (oi.x - oj.x) - so.x, ry = (oi.y - oj.y) - so.y;
-              float d2 = rx * rx + ry * ry;
-              if (D == 3) {
-                const float rz = (oi.z - oj.z) - so.z;
-                d2 += rz * rz;
-              }
-              float w = kernel_w<float>(k, sqrtf(d2));
-              if (mass) w *= (float)m[jg[u]];
-              const float y = w - comp;
-              const float tt = sum + y;
-              comp = (tt - sum) - y;
-              sum = tt;
-            }
+          if (!(t2 < k.rc2f)) continue;
+          if (kff + ko < cap) {
+            const int row = (p < nff) ? kff : cap - 1 - ko;
+            nl[(size_t)row * n + i] = (uint16_t)entg[u];
           }
-          if ((p & 31) == 31) {
-            mask[(size_t)(p >> 5) * n + i] = word;
-            word = 0;
+          if (p < nff)
+            ++kff;
+          else
+            ++ko;
+          if (!acc_i) continue;
+          // W as k_density's second phase rounds it: (o_i - o_j) - slot
+          const float rx = (oi.x - oj.x) - so.x, ry = (oi.y - oj.y) - so.y;
+          float d2 = rx * rx + ry * ry;
+          if (D == 3) {
+            const float rz = (oi.z - oj.z) - so.z;
+            d2 += rz * rz;
           }
+          float w = kernel_w<float>(k, sqrtf(d2));
+          if (mass) w *= (float)m[jg[u]];
+          const float y = w - comp;
+          const float tt = sum + y;
+          comp = (tt - sum) - y;
+          sum = tt;
         }
       }
-      if (ntot & 31) mask[(size_t)(ntot >> 5) * n + i] = word;
     } else {
-      // lane l tests candidates l, l + S, ...; the group's ballot assembles
-      // the mask word, written by the group's first lane
+      // lane l tests candidates l, l + S, ...; the group's ballots place the
+      // kept pairs in candidate order in their segment
       const int base = (tid & 31) & ~(S - 1);
       const unsigned gmask = ((1u << S) - 1u) << base;
-      uint32_t word = 0;
+      const unsigned below = (1u << lane_s) - 1u;
       for (int p0 = 0; p0 < ntot; p0 += S) {
         const int p = p0 + lane_s;
         bool in = false;
+        int ent = 0, j = 0;
+        float4 oj = make_float4(0.f, 0.f, 0.f, 0.f), so = oj;
         if (p < ntot) {
-          const int ent = vl[(size_t)cand_row(p, nff, vcap) * n + i];
+          ent = vl[(size_t)cand_row(p, nff, vcap) * n + i];
           const int sl = ent >> kLocalBits;
-          const int j = s_start[sl * kReuseTPB + tid] + (ent & (kMaxCellCount - 1));
-          const float4 oj = off[j];
-          const float4 so = slot_tab[sl];
+          j = s_start[sl * kReuseTPB + tid] + (ent & (kMaxCellCount - 1));
+          oj = off[j];
+          so = slot_tab[sl];
           const float tx = (oi.x - so.x) - oj.x, ty = (oi.y - so.y) - oj.y;
           float t2 = tx * tx + ty * ty;
           if (D == 3) {
@@ -146,7 +147,17 @@ __global__ void __launch_bounds__(kReuseTPB)
             t2 += tz * tz;
           }
           in = t2 < k.rc2f;
-          if (in && acc_i) {
+        }
+        const unsigned bf = (__ballot_sync(gmask, in && p < nff) >> base) & ((1u << S) - 1u);
+        const unsigned bo = (__ballot_sync(gmask, in && p >= nff) >> base) & ((1u << S) - 1u);
+        if (in) {
+          const bool front = p < nff;
+          const int pos = front ? kff + __popc(bf & below) : ko + __popc(bo & below);
+          if (kff + ko + __popc(bf | bo) <= cap) {
+            const int row = front ? pos : cap - 1 - pos;
+            nl[(size_t)row * n + i] = (uint16_t)ent;
+          }
+          if (acc_i) {
             const float rx = (oi.x - oj.x) - so.x, ry = (oi.y - oj.y) - so.y;
             float d2 = rx * rx + ry * ry;
             if (D == 3) {
@@ -161,32 +172,29 @@ __global__ void __launch_bounds__(kReuseTPB)
             sum = tt;
           }
         }
-        const unsigned bal = (__ballot_sync(gmask, in) >> base) & ((1u << S) - 1u);
-        word |= bal << (p0 & 31);
-        kept += in ? 1 : 0;
-        if (((p0 + S) & 31) == 0 || p0 + S >= ntot) {
-          if (lane_s == 0) mask[(size_t)(p0 >> 5) * n + i] = word;
-          word = 0;
-        }
+        kff += __popc(bf);
+        ko += __popc(bo);
       }
-      // the lanes' sums and counts, added in lane order
+      // the lanes' sums, added in lane order
       const float part = sum - comp;
       float tot = part;
-      int kt = kept;
-      for (int q = 1; q < S; ++q) {
-        tot += __shfl_sync(gmask, part, base + q);
-        kt += __shfl_sync(gmask, kept, base + q);
-      }
+      for (int q = 1; q < S; ++q) tot += __shfl_sync(gmask, part, base + q);
       sum = tot;
       comp = 0.0f;
-      kept = kt;
     }
   }
   int my_max = 0;
   unsigned long long my_pairs = 0;
   if (i < n && lane_s == 0) {
+    const int kept = kff + ko;
+    if (kept > cap) {
+      atomicOr(err, kErrNeighOverflow);
+      kff = min(kff, cap);
+      ko = min(ko, cap - kff);
+    }
+    ncount[i] = kff | (ko << 16);
     my_max = kept;
-    my_pairs = (unsigned long long)kept;
+    my_pairs = (unsigned long long)(kff + ko);
     const double mi = m[i];
     const double rho_i = (double)(sum - comp);
     double rho_out;
@@ -466,14 +474,15 @@ __device__ __forceinline__ void pair_general(const Consts& k, ForceAcc<D, NNW, S
   acc_add<D, NNW, STRESS>(A, pa, r);
 }
 
-// FP32-mixed force sweep over the set bits of the density sweep's mask,
-// S lanes per particle (lane l takes the candidates p = l mod S); the lanes'
-// sums are added in lane order by the first lane, which runs the epilogue.
+// FP32-mixed force sweep over the density sweep's compact pair list,
+// S lanes per particle (lane l takes the list entries q = l mod S); the
+// lanes' sums are added in lane order by the first lane, which runs the
+// epilogue.
 template <int D, bool NNW, bool STRESS, int S>
 __global__ void __launch_bounds__(kReuseTPB)
-    k_force_mask(Consts k, const int* __restrict__ cell_start, const int* __restrict__ cell_of,
-                 const uint16_t* __restrict__ vl, const int* __restrict__ vcount, int vcap,
-                 const uint32_t* __restrict__ mask, const float4* __restrict__ off,
+    k_force_list(Consts k, const int* __restrict__ cell_start, const int* __restrict__ cell_of,
+                 const uint16_t* __restrict__ nl, const int* __restrict__ ncount, int cap,
+                 const float4* __restrict__ off,
                  const double4_32a* __restrict__ x, const double4_32a* __restrict__ v,
                  const float4* __restrict__ pcf, const float4* __restrict__ vf,
                  const float2* __restrict__ wd, double4_32a* __restrict__ f,
@@ -516,51 +525,33 @@ __global__ void __launch_bounds__(kReuseTPB)
 #pragma unroll
     for (int a = 0; a < 9; ++a) A.sacc[a] = 0.f;
   }
-  const int vc = vcount[i];
-  const int nff = vc & 0xffff, ntot = nff + (vc >> 16);
+  const int nc = ncount[i];
+  const int kff = nc & 0xffff, ntot = kff + (nc >> 16);
   if (S == 1) {
-    // fluid-fluid segment in lockstep over the candidates (coalesced list
-    // rows); a lane whose bit is clear idles that iteration
-    uint32_t word = 0;
-    bool has_n = false;
+    // fluid-fluid segment: the next pair's records are gathered while the
+    // current pair is computed, the entry after it one step earlier still
     PairData nxt;
     int ent_n = 0;
-    if (nff > 0) {
-      word = mask[i];
-      has_n = word & 1u;
-      if (has_n) nxt = load_pair(vl[i], s_start, off, vf, pcf);
-      if (nff > 1) ent_n = vl[(size_t)n + i];
-    }
-    for (int p = 0; p < nff; ++p) {
-      const bool has = has_n;
+    if (kff > 0) nxt = load_pair(nl[i], s_start, off, vf, pcf);
+    if (kff > 1) ent_n = nl[(size_t)n + i];
+    for (int e = 0; e < kff; ++e) {
       const PairData cur = nxt;
-      const int q = p + 1;
-      if (q < nff) {
-        if ((q & 31) == 0) word = mask[(size_t)(q >> 5) * n + i];
-        has_n = (word >> (q & 31)) & 1u;
-        if (has_n) nxt = load_pair(ent_n, s_start, off, vf, pcf);
-        if (q + 1 < nff) ent_n = vl[(size_t)(q + 1) * n + i];
+      if (e + 1 < kff) {
+        nxt = load_pair(ent_n, s_start, off, vf, pcf);
+        if (e + 2 < kff) ent_n = nl[(size_t)(e + 2) * n + i];
       }
-      if (has) pair_fluid<D, NNW, STRESS>(k, A, cur, slot_tab, qq, step, inv_sqdt, noise);
+      pair_fluid<D, NNW, STRESS>(k, A, cur, slot_tab, qq, step, inv_sqdt, noise);
     }
-    // wall / colloid segment
-    for (int w0 = nff & ~31; w0 < ntot; w0 += 32) {
-      uint32_t bits = mask[(size_t)(w0 >> 5) * n + i];
-      if (w0 < nff) bits &= ~((1u << (nff - w0)) - 1u);
-      if (ntot - w0 < 32) bits &= (1u << (ntot - w0)) - 1u;
-      while (bits) {
-        const int p = w0 + __ffs(bits) - 1;
-        bits &= bits - 1u;
-        const int ent = vl[(size_t)(vcap - 1 - (p - nff)) * n + i];
-        pair_general<D, NNW, STRESS>(k, A, ent, s_start, slot_tab, off, vf, pcf, wd, x, qq, ca,
-                                     step, inv_sqdt, noise);
-      }
+    // wall / colloid segment, from the last row down
+    for (int e = kff; e < ntot; ++e) {
+      const int ent = nl[(size_t)(cap - 1 - (e - kff)) * n + i];
+      pair_general<D, NNW, STRESS>(k, A, ent, s_start, slot_tab, off, vf, pcf, wd, x, qq, ca,
+                                   step, inv_sqdt, noise);
     }
   } else {
-    for (int p = lane_s; p < ntot; p += S) {
-      if (!((mask[(size_t)(p >> 5) * n + i] >> (p & 31)) & 1u)) continue;
-      const int ent = vl[(size_t)cand_row(p, nff, vcap) * n + i];
-      if (p < nff)
+    for (int e = lane_s; e < ntot; e += S) {
+      const int ent = nl[(size_t)cand_row(e, kff, cap) * n + i];
+      if (e < kff)
         pair_fluid<D, NNW, STRESS>(k, A, load_pair(ent, s_start, off, vf, pcf), slot_tab, qq,
                                    step, inv_sqdt, noise);
       else
@@ -614,7 +605,7 @@ __global__ void __launch_bounds__(kReuseTPB)
 
 }  // namespace
 
-int density_mask(Handle* h, bool with_pressure) {
+int density_list(Handle* h, bool with_pressure) {
   Consts& k = h->k;
   cudaStream_t s = h->stream;
   const int n = (int)h->n;
@@ -626,10 +617,11 @@ int density_mask(Handle* h, bool with_pressure) {
   const int S = split ? 4 : 1;
   const int g = (int)(((int64_t)n * S + kReuseTPB - 1) / kReuseTPB);
 #define LAUNCH(DD, SS)                                                                          \
-  k_density_mask<DD, SS><<<g, kReuseTPB, 0, s>>>(                                              \
+  k_density_list<DD, SS><<<g, kReuseTPB, 0, s>>>(                                              \
       k, h->cell_start, h->cell_of, h->off, h->x, h->v, h->m, h->pid, h->vl, h->vcount, h->vcap, \
-      h->vmask, h->rho, h->pr, h->pcf, h->vf, with_pressure ? 1 : 0, h->d_err, h->d_stats,     \
-      h->d_pairs, NN{h->ct, h->act, h->vgt, h->qq}, CollArgs{h->v, h->rxc, h->rxcf})
+      h->nl, h->ncount, h->neigh_cap, h->rho, h->pr, h->pcf, h->vf, with_pressure ? 1 : 0,      \
+      h->d_err, h->d_stats, h->d_pairs, NN{h->ct, h->act, h->vgt, h->qq},                       \
+      CollArgs{h->v, h->rxc, h->rxcf})
   if (k.d == 3) {
     if (split) LAUNCH(3, 4); else LAUNCH(3, 1);
   } else {
@@ -640,7 +632,7 @@ int density_mask(Handle* h, bool with_pressure) {
   return cuda_check(h, cudaGetLastError(), "density launch") ? MCFG_ECUDA : MCFG_OK;
 }
 
-int force_mask(Handle* h, int64_t step, int fuse_mode, double dt) {
+int force_list(Handle* h, int64_t step, int fuse_mode, double dt) {
   Consts& k = h->k;
   cudaStream_t s = h->stream;
   const int n = (int)h->n;
@@ -654,8 +646,8 @@ int force_mask(Handle* h, int64_t step, int fuse_mode, double dt) {
     const int S = split ? 4 : 1;
     const int g = (int)(((int64_t)n * S + kReuseTPB - 1) / kReuseTPB);
 #define LAUNCH(DD, NW, ST, SS)                                                                  \
-  k_force_mask<DD, NW, ST, SS><<<g, kReuseTPB, 0, s>>>(                                        \
-      k, h->cell_start, h->cell_of, h->vl, h->vcount, h->vcap, h->vmask, h->off, h->x, h->v,    \
+  k_force_list<DD, NW, ST, SS><<<g, kReuseTPB, 0, s>>>(                                        \
+      k, h->cell_start, h->cell_of, h->nl, h->ncount, h->neigh_cap, h->off, h->x, h->v,         \
       h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step, step_ptr,        \
       inv_sqdt, h->d_err, nn, ca)
 #define PICK_S(DD, NW, ST)         \
