@@ -2,9 +2,13 @@
 
 Two and three slabs of one box, each slab its own handle on the one GPU of
 this run, halos exchanged through host copies in one process: the owned
-particles follow the undivided GPU run and the CPU oracle to rounding (the
-bars of the CPU decomposition tests), FP64; the FP32-mixed slabs follow the
-undivided FP32-mixed run within the FP32 trajectory bar.
+particles follow the undivided GPU run to rounding (the bars of the CPU
+decomposition tests: both draw the same FP32 normals), FP64, and the CPU
+oracle's undivided run at the random-force bars of the parity tests (the
+GPU's FP32 Box-Muller normals differ from the CPU's in the last bits:
+positions 1e-9 of the box, velocities, accelerations 1e-5 of their scale,
+densities 1e-9); the FP32-mixed slabs follow the undivided FP32-mixed run
+within the FP32 trajectory bar.
 """
 import numpy as np
 import pytest
@@ -35,7 +39,7 @@ def test_gpu_slabs_follow_the_undivided_box(gpu_lib, nslab):
     got = by_pid(dec.owned_state(), w.n, 3)
     assert dec.migrated > 0
     check(w, got, gpu_undivided(w))
-    check(w, got, undivided(w))
+    check(w, got, undivided(w), bars=(1e-9, 1e-5, 1e-9, 1e-5))
 
 
 def test_gpu_slabs_fp32_mixed(gpu_lib):
