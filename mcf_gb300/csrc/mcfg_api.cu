@@ -124,7 +124,6 @@ void free_all(Handle* h) {
     if (p) cudaFree(p);
   h->x_ref = nullptr;
   h->vl = nullptr;
-  h->split_list = false;
   h->vcount = h->d_rebuild = nullptr;
   h->vcap = 0;
   h->reuse_valid = false;

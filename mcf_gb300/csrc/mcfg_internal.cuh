@@ -194,7 +194,9 @@ struct Handle {
   float4* off = nullptr;     // FP32 offset to the cell origin, w = cell id
   int* cell_of = nullptr;    // cell per sorted particle (ncell = outside)
   // ---- neighbours ----
-  uint16_t* nl = nullptr;    // [neigh_cap][cap] entries slot<<11|local
+  uint16_t* nl = nullptr;    // [neigh_cap][cap] entries slot<<11|local; FP32 list reuse:
+                             // fluid-fluid pairs from row 0 up, the others from the
+                             // last row down, ncount = fluid-fluid | other << 16
   int* ncount = nullptr;     // [cap]
   int* nhs = nullptr;        // [cap] first entry of the owned (forward) half
   void* jp = nullptr;        // symmetric force partial sums [(NSF+1)*3][cap] (T)
@@ -221,8 +223,6 @@ struct Handle {
                                  // FP32 handles: fluid-fluid pairs from row 0 up, the
                                  // others from row vcap-1 down (sweep32.cu)
   bool partitioned = false;      // FP32 lists: fluid-fluid rows up, the others down
-  bool split_list = false;       // the last density sweep wrote a partitioned nl
-                                 // (force_list follows)
   int* vcount = nullptr;         // [n]
   int vcap = 0;
   int* d_rebuild = nullptr;      // [0] rebuild request, [1] rebuilds done
@@ -323,7 +323,6 @@ int compute_pressure(Handle* h);
 int compute_force(Handle* h, int64_t step, int fuse_mode, double dt);
 // FP32-mixed sweeps over the partitioned candidate list (sweep32.cu)
 int density_list(Handle* h, bool with_pressure);
-int force_list(Handle* h, int64_t step, int fuse_mode, double dt);
 int apply_body_force(Handle* h);
 int integrate_velocity(Handle* h, double dt, double lambda);
 int integrate_position(Handle* h, double dt);

@@ -732,8 +732,8 @@ __device__ __forceinline__ JData load_j(const int* __restrict__ s_start, int ent
 template <int D, bool NNW, int S>
 __global__ void __launch_bounds__(kReuseTPB, 5)
     k_force32(Consts k, const int* __restrict__ cell_start, const int* __restrict__ cell_of,
-              const uint16_t* __restrict__ nl,
-              const int* __restrict__ ncount, const float4* __restrict__ off,
+              const uint16_t* __restrict__ nl, const int* __restrict__ ncount, int cap,
+              const float4* __restrict__ off,
               const double4_32a* __restrict__ x, const double4_32a* __restrict__ v,
               const float4* __restrict__ pcf, const float4* __restrict__ vf,
               const float2* __restrict__ wd, double4_32a* __restrict__ f,
@@ -779,16 +779,20 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
   T sacc[9];
 #pragma unroll
   for (int a = 0; a < 9; ++a) sacc[a] = 0.f;
-  const int cnt = ncount[i];
+  // the list's two segments (fluid-fluid pairs from row 0 up, the others
+  // from row cap-1 down; a per-step list has only the first)
+  const int nc = ncount[i];
+  const int nff = nc & 0xffff, cnt = nff + (nc >> 16);
   JData nxt;
   int ent_n1 = 0;
-  if (lane_s < cnt) nxt = load_j<D>(s_start, nl[(size_t)lane_s * n + i], off, vf, pcf);
-  if (lane_s + S < cnt) ent_n1 = nl[(size_t)(lane_s + S) * n + i];
+  if (lane_s < cnt)
+    nxt = load_j<D>(s_start, nl[(size_t)cand_row(lane_s, nff, cap) * n + i], off, vf, pcf);
+  if (lane_s + S < cnt) ent_n1 = nl[(size_t)cand_row(lane_s + S, nff, cap) * n + i];
   for (int e = lane_s; e < cnt; e += S) {
     const JData cur = nxt;
     if (e + S < cnt) {
       nxt = load_j<D>(s_start, ent_n1, off, vf, pcf);
-      if (e + 2 * S < cnt) ent_n1 = nl[(size_t)(e + 2 * S) * n + i];
+      if (e + 2 * S < cnt) ent_n1 = nl[(size_t)cand_row(e + 2 * S, nff, cap) * n + i];
     }
     const int sj = __float_as_int(cur.o.w);
     if (si != 0 && sj != 0 && !(si > 0 && sj > 0 && si != sj && k.pp_cc)) continue;
@@ -1438,8 +1442,8 @@ int compute_density(Handle* h, bool with_pressure, bool reuse) {
     return MCFG_ECUDA;
   const int g = grid_for(h);
   const bool fp64 = h->p.precision == MCFG_PRECISION_FP64;
-  h->split_list = reuse && !fp64;
-  if (h->split_list) return density_list(h, with_pressure);
+  // FP32 with list reuse: the compact two-segment pair list (sweep32.cu)
+  if (reuse && !fp64) return density_list(h, with_pressure);
   if (reuse) {
     const int n = (int)h->n;
     if (n == 0) return MCFG_OK;
@@ -1496,7 +1500,6 @@ int compute_pressure(Handle* h) {
 }
 
 int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
-  if (h->split_list) return force_list(h, step, fuse_mode, dt);
   Consts& k = h->k;
   cudaStream_t s = h->stream;
   const int g = grid_for(h);
@@ -1558,14 +1561,14 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
   do {                                                                                           \
     if (split)                                                                                   \
       k_force32<DD, NW, 4><<<gp4, kReuseTPB, 0, s>>>(                                            \
-          k, h->cell_start, h->cell_of, h->nl, h->ncount, h->off, h->x, h->v, h->pcf, h->vf,     \
-          h->wd, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step, step_ptr, (float)inv_sqdt,   \
-          h->d_err, nn, ca);                                                                     \
+          k, h->cell_start, h->cell_of, h->nl, h->ncount, h->neigh_cap, h->off, h->x, h->v,      \
+          h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step, step_ptr,     \
+          (float)inv_sqdt, h->d_err, nn, ca);                                                                     \
     else                                                                                         \
       k_force32<DD, NW, 1><<<gp, kReuseTPB, 0, s>>>(                                             \
-          k, h->cell_start, h->cell_of, h->nl, h->ncount, h->off, h->x, h->v, h->pcf, h->vf,     \
-          h->wd, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step, step_ptr, (float)inv_sqdt,   \
-          h->d_err, nn, ca);                                                                     \
+          k, h->cell_start, h->cell_of, h->nl, h->ncount, h->neigh_cap, h->off, h->x, h->v,      \
+          h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step, step_ptr,     \
+          (float)inv_sqdt, h->d_err, nn, ca);                                                                     \
   } while (0)
     if (k.d == 3) {
       if (k.newtonian) LAUNCH_F32(3, false); else LAUNCH_F32(3, true);

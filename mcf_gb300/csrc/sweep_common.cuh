@@ -140,6 +140,13 @@ __device__ __forceinline__ void fill_slot_offsets(const Consts& k, float4* s_slo
   if (e < kSlotTable) s_slot[e] = slot_offset<D>(k, e % kMaxStencil, e / kMaxStencil);
 }
 
+// Physical list row of logical entry p of a list in two segments: entries
+// below nff from row 0 up, the others from row cap-1 down (the FP32
+// candidate and pair lists; an unsplit list has nff = its count).
+__device__ __forceinline__ int cand_row(int p, int nff, int cap) {
+  return p < nff ? p : cap - 1 - (p - nff);
+}
+
 // slot offsets of the Lees-Edwards row state of the home cell
 __device__ __forceinline__ const float4* slot_table(const Consts& k, const float4* s_slot,
                                                    int cell) {
