@@ -32,9 +32,20 @@ rebuilt every step and with the candidate list kept across steps.
 `mcf_scalability_deck` runs the physics of MCF's own 1M-particle
 scalability input (cut-off 4 dx, Batchelor equation of state, Hu-Adams
 angular force) read from an MCF deck by mcf_config.load_mcf_deck.
-`cpu_baseline` is the CPU restatement
-of MCF's path (the oracle; MCF itself cannot be built here) on the host
-cores.  With --impl reference only that CPU path is timed.
+`fp32_error_vs_fp64` runs the workload for --accuracy-steps (5000, the
+whole C3 run) in FP32-mixed and in FP64 from the same state with the same
+Philox keys and states the errors of the mean velocity, the u_x(y) profile,
+the wall shear stress and the shear stress S_xy (over --accuracy-seeds
+seeds), then the same on a developed Poiseuille channel (--channel-steps,
+two viscous times).  `colloid_suspension` is C4: a 96^3 lattice with 200
+rigid spheres integrated on the device (Adams-Bashforth), FP32-mixed
+particle-steps/s and the colloids' velocity and angular-velocity errors
+against FP64 over --c4-steps steps.  `cpu_baseline` is the CPU
+restatement of MCF's path (the oracle; MCF itself cannot be built here) on
+the host cores in MCF's symmetric loop mode (symmetry = T, each pair once;
+x-slabs of cells in two colours over the threads), with the full-stencil
+mode and one core beside it.  With --impl reference only that CPU path is
+timed.
 
 With torchrun (N > 1) every rank runs an independent replica on its own GPU
 ("replicas only": this workload is not decomposed across GPUs); value sums
