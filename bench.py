@@ -452,7 +452,7 @@ def adjoint_cost(torch, w, T, K, local, wts):
                       "reverse_over_forward leaves out the forward pass that evaluates J"}
 
 
-def fp32_accuracy(w, steps, local, seeds=(0,), samples=20):
+def fp32_accuracy(w, steps, local, seeds=(0,), samples=20, floor_seed=None):
     """FP32-mixed against FP64 over `steps` VV steps from the same state,
     for each seed offset in `seeds` (the Philox key of the Wiener increments
     is params.seed + offset, the same in both precisions, so the only
@@ -462,7 +462,12 @@ def fp32_accuracy(w, steps, local, seeds=(0,), samples=20):
     (x-force of the fluid on each wall's particles per wall area) and the
     shear-stress profile tau_xy(y) (per-particle stresses s_xy summed per
     unit slab over the slab volume).  Errors are relative to the FP64
-    run's scale; mean and max over the seeds are reported."""
+    run's scale; mean and max over the seeds are reported.  With floor_seed,
+    the same errors between the FP64 run and an FP64 run with the Philox key
+    offset by floor_seed (another noise realisation) are reported beside them
+    as the statistical floor: once the trajectories have decorrelated, the
+    FP32-vs-FP64 differences of time-averaged quantities are thermal noise
+    unless they exceed that floor."""
     import numpy as np
 
     from mcf_gb300 import SDPD
@@ -513,11 +518,7 @@ def fp32_accuracy(w, steps, local, seeds=(0,), samples=20):
                 "walls": np.mean(walls, axis=0) if walls else np.zeros(0),
                 "tau": np.mean(taus, axis=0) if taus else np.zeros(nb)}
 
-    errs = {"mean_velocity_rel": [], "velocity_profile_rel": [], "wall_shear_stress_rel": [],
-            "shear_stress_profile_rel": []}
-    ref = {"mean_velocity_fp64": [], "wall_shear_stress_fp64": [], "max_shear_stress_fp64": []}
-    for sd_off in seeds:
-        a, b = run(PRECISION_FP32_MIXED, sd_off), run(PRECISION_FP64, sd_off)
+    def compare(a, b, errs):
         errs["mean_velocity_rel"].append(abs(a["u"] - b["u"]) / abs(b["u"]))
         errs["velocity_profile_rel"].append(
             float(np.max(np.abs(a["prof"] - b["prof"])) / np.max(np.abs(b["prof"]))))
@@ -526,6 +527,17 @@ def fp32_accuracy(w, steps, local, seeds=(0,), samples=20):
                 float(np.max(np.abs(a["walls"] - b["walls"]) / np.abs(b["walls"]))))
         errs["shear_stress_profile_rel"].append(
             float(np.max(np.abs(a["tau"] - b["tau"])) / np.max(np.abs(b["tau"]))))
+
+    keys = ("mean_velocity_rel", "velocity_profile_rel", "wall_shear_stress_rel",
+            "shear_stress_profile_rel")
+    errs = {k: [] for k in keys}
+    floor = {k: [] for k in keys}
+    ref = {"mean_velocity_fp64": [], "wall_shear_stress_fp64": [], "max_shear_stress_fp64": []}
+    for sd_off in seeds:
+        a, b = run(PRECISION_FP32_MIXED, sd_off), run(PRECISION_FP64, sd_off)
+        compare(a, b, errs)
+        if floor_seed is not None:
+            compare(run(PRECISION_FP64, sd_off + floor_seed), b, floor)
         ref["mean_velocity_fp64"].append(b["u"])
         ref["wall_shear_stress_fp64"].append([float(q) for q in b["walls"]])
         ref["max_shear_stress_fp64"].append(float(np.max(np.abs(b["tau"]))))
@@ -533,6 +545,12 @@ def fp32_accuracy(w, steps, local, seeds=(0,), samples=20):
     for k, vals in errs.items():
         if vals:
             out[k] = {"mean": float(np.mean(vals)), "max": float(np.max(vals))}
+    if floor_seed is not None:
+        out["fp64_other_seed"] = {k: {"mean": float(np.mean(v)), "max": float(np.max(v))}
+                                  for k, v in floor.items() if v}
+        out["fp64_other_seed"]["what"] = (
+            "the same errors between FP64 runs with different Philox keys: the thermal-noise "
+            "floor of the time averages")
     out.update(ref)
     out["reference"] = "the FP64 GPU path (itself within 1e-12 of the CPU oracle per step)"
     return out
@@ -555,7 +573,7 @@ def developed_channel(local, steps=40000):
     p.Brownian = 1
     w.dt = 0.01
     p.dt = 0.01
-    out = fp32_accuracy(w, steps, local, seeds=(0,), samples=40)
+    out = fp32_accuracy(w, steps, local, seeds=(0,), samples=40, floor_seed=1000)
     out["workload"] = ("developed Poiseuille channel 20^3 + walls (c 20, eta 0.5, kT 1e-4, "
                        "g_x 0.005, dt 0.01)")
     nu = p.eta / 1.0
