@@ -433,6 +433,12 @@ int mcfg_colloid_repulsion(mcfg_handle* h, double* force);
 int mcfg_statistics(mcfg_handle* h, double* k_energy, double* momentum,
                     double* stress);
 
+/* The same sums over the first n_owned particles of the last upload (host
+ * order): a subdomain's own particles, its ghost copies left out -- the
+ * per-rank sums MCF all-reduces at statistic_compute_statistic.F90:348-403. */
+int mcfg_statistics_owned(mcfg_handle* h, int64_t n_owned, double* k_energy,
+                          double* momentum, double* stress);
+
 /* Wait for all work of the handle to finish (error check point). */
 int mcfg_synchronize(mcfg_handle* h);
 

@@ -1682,7 +1682,16 @@ int mcfg_colloid_repulsion(mcfg_handle* h, double* force) {
 int mcfg_statistics(mcfg_handle* h, double* k_energy, double* momentum, double* stress) {
   GUARD(h);
   if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
-  return statistics(h, k_energy, momentum, stress);
+  return statistics(h, k_energy, momentum, stress, h->n);
+}
+
+int mcfg_statistics_owned(mcfg_handle* h, int64_t n_owned, double* k_energy, double* momentum,
+                          double* stress) {
+  GUARD(h);
+  if (!h->have_particles) return set_error(h, MCFG_ESTATE, "no particles uploaded");
+  if (n_owned < 0 || n_owned > h->n)
+    return set_error(h, MCFG_EINVAL, "n_owned must lie in [0, n]");
+  return statistics(h, k_energy, momentum, stress, n_owned);
 }
 
 void* mcfg_get_stream(mcfg_handle* h) { return h ? (void*)h->stream : nullptr; }

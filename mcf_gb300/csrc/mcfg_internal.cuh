@@ -328,7 +328,8 @@ int integrate_velocity(Handle* h, double dt, double lambda);
 int integrate_position(Handle* h, double dt);
 int adjust_particles(Handle* h);
 int kick_drift_wrap(Handle* h, double dt);
-int statistics(Handle* h, double* ke, double* mom, double* stress);
+// FP64 sums over the particles of host index < owned (all of them: owned = n)
+int statistics(Handle* h, double* ke, double* mom, double* stress, int64_t owned);
 // second half kick v += (0.5 a) dt and, Oldroyd-B, ct += (act dt) 0.5 (the
 // unfused tail of a VV step, bit-identical to the fused force epilogue)
 int kick_ct_half(Handle* h, double dt);

@@ -312,7 +312,7 @@ static void host_e16_8(double x, std::string& line) {
 int write_statistic_line(Handle* h, const char* path, int64_t step, double time) {
   const int d = h->p.num_dim;
   double ke = 0.0, mom[3] = {0.0, 0.0, 0.0}, st[9] = {0.0};
-  const int rc = statistics(h, &ke, mom, st);
+  const int rc = statistics(h, &ke, mom, st, h->n);
   if (rc != MCFG_OK) return rc;
   std::string line;
   if (step >= -99999999 && step <= 999999999) {

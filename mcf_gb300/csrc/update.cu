@@ -155,12 +155,14 @@ constexpr int kRedVals = 13;  // ke, mom[3], stress[9]
 template <int D>
 __global__ void k_stats_partial(Consts k, const double4_32a* __restrict__ v,
                                 const double* __restrict__ m, const int* __restrict__ sid,
-                                const double* __restrict__ st, double* __restrict__ part) {
+                                const double* __restrict__ st, const int* __restrict__ hidx,
+                                int64_t owned, double* __restrict__ part) {
   __shared__ double sm[kRedVals][kRedThreads];
   double acc[kRedVals];
 #pragma unroll
   for (int q = 0; q < kRedVals; ++q) acc[q] = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k.n; i += gridDim.x * blockDim.x) {
+    if (hidx[i] >= owned) continue;  // a subdomain's ghost copy
     const int s = sid[i];
     if (s == 0) {
       const double4_32a vv = v[i];
@@ -512,7 +514,7 @@ int apply_body_force(Handle* h) {
   return cuda_check(h, cudaGetLastError(), "body force launch") ? MCFG_ECUDA : MCFG_OK;
 }
 
-int statistics(Handle* h, double* ke, double* mom, double* stress) {
+int statistics(Handle* h, double* ke, double* mom, double* stress, int64_t owned) {
   const int n = (int)h->n;
   int nb = (n + kRedThreads - 1) / kRedThreads;
   if (nb > 1024) nb = 1024;
@@ -520,9 +522,11 @@ int statistics(Handle* h, double* ke, double* mom, double* stress) {
   double* part = h->red;
   double* out = h->red + (size_t)1024 * kRedVals;
   if (h->k.d == 3)
-    k_stats_partial<3><<<nb, kRedThreads, 0, h->stream>>>(h->k, h->v, h->m, h->sid, h->st, part);
+    k_stats_partial<3><<<nb, kRedThreads, 0, h->stream>>>(h->k, h->v, h->m, h->sid, h->st,
+                                                          h->hidx, owned, part);
   else
-    k_stats_partial<2><<<nb, kRedThreads, 0, h->stream>>>(h->k, h->v, h->m, h->sid, h->st, part);
+    k_stats_partial<2><<<nb, kRedThreads, 0, h->stream>>>(h->k, h->v, h->m, h->sid, h->st,
+                                                          h->hidx, owned, part);
   k_stats_final<<<1, 32, 0, h->stream>>>(part, nb, out);
   h->launches += 2;
   double res[kRedVals];

@@ -27,6 +27,10 @@ forces and needs two ghost gets a step and no ghost put:
      (mcfg_update_density), in the order of ghost get 1;
   6. pressure, pair force, body force, half kick.
 
+Statistics (kinetic energy, momentum, stress) are summed per subdomain over
+its own particles (mcfg_statistics_owned) and all-reduced over the
+subdomains, as MCF sums per rank and calls MPI_ALLREDUCE.
+
 Owned particles' densities and forces are sums over the same partners as
 in the undivided box (to summation order); the Wiener increments are keyed
 by the particle ids, so the decomposed run follows the undivided one to
@@ -57,6 +61,10 @@ class LocalExchange:
         n = len(outbox)
         return [{"left": outbox[(r - 1) % n]["right"], "right": outbox[(r + 1) % n]["left"]}
                 for r in range(n)]
+
+    def allreduce(self, vec):
+        """sum over all subdomains: they are all in this process already"""
+        return np.asarray(vec, np.float64)
 
 
 class TorchExchange:
@@ -109,6 +117,15 @@ class TorchExchange:
         from_left = self._send_recv(box["right"], right, left)
         from_right = self._send_recv(box["left"], left, right)
         return [{"left": from_left, "right": from_right}]
+
+    def allreduce(self, vec):
+        """sum of the ranks' FP64 vectors (MCF's MPI_ALLREDUCE of the
+        statistic sums, statistic_compute_statistic.F90:348-403)"""
+        import torch
+
+        t = torch.from_numpy(np.array(vec, np.float64))
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return t.numpy()
 
 
 class Subdomain:
@@ -282,6 +299,18 @@ class SlabDecomposition:
     def run_vv(self, step0, nsteps, dt):
         for k in range(1, nsteps + 1):
             self.step_vv(step0 + k, dt)
+
+    def statistics(self):
+        """kinetic energy, momentum[3] and stress[9] of the whole box
+        (statistic_compute_statistic.F90:230-303): every subdomain sums its
+        own particles (its ghosts left out), then the sums are all-reduced
+        over the subdomains (:348-403)."""
+        loc = np.zeros(13)
+        for s in self.subs:
+            ke, mom, st = s.h.statistic_compute_statistic(n_owned=s.n_own)
+            loc += np.concatenate([[ke], mom, st])
+        tot = self.exchange.allreduce(loc)
+        return float(tot[0]), tot[1:4].copy(), tot[4:13].copy()
 
     # -- results -----------------------------------------------------------------
     def owned_state(self, fields=("x", "v", "rho", "f")):

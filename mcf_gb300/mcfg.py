@@ -68,6 +68,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
                                        _dp, _dp, _dp, _dp]),
         "mcfg_download": (C.c_int, [_h, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
         "mcfg_statistics": (C.c_int, [_h, _dp, _dp, _dp]),
+        "mcfg_statistics_owned": (C.c_int, [_h, C.c_int64, _dp, _dp, _dp]),
         "mcfg_synchronize": (C.c_int, [_h]),
         "mcfg_upload_force": (C.c_int, [_h, _dp]),
         "mcfg_get_stream": (C.c_void_p, [_h]),
@@ -325,13 +326,19 @@ class SDPD:
             _ptr(out.get("ct"), C.c_double)))
         return (J.value, g, out) if state_grads else (J.value, g)
 
-    def statistic_compute_statistic(self):
+    def statistic_compute_statistic(self, n_owned=None):
+        """kinetic energy, momentum[3], stress[9]; with n_owned, over the first
+        n_owned particles of the last upload only (a subdomain's own)"""
         ke = C.c_double()
         mom = np.zeros(3)
         st = np.zeros(9)
-        self._check("statistic_compute_statistic",
-                    self.lib.mcfg_statistics(self._h, C.byref(ke), _ptr(mom, C.c_double),
-                                             _ptr(st, C.c_double)))
+        if n_owned is None:
+            rc = self.lib.mcfg_statistics(self._h, C.byref(ke), _ptr(mom, C.c_double),
+                                          _ptr(st, C.c_double))
+        else:
+            rc = self.lib.mcfg_statistics_owned(self._h, int(n_owned), C.byref(ke),
+                                                _ptr(mom, C.c_double), _ptr(st, C.c_double))
+        self._check("statistic_compute_statistic", rc)
         return ke.value, mom, st
 
     # -- colloids (Class_Colloid) -------------------------------------------

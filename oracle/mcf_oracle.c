@@ -1980,11 +1980,15 @@ int orc_download(orc_state* s, double* x, double* v, double* rho, double* p,
   return 0;
 }
 
-/* statistic_compute_statistic.F90:230-303 */
-int orc_statistics(orc_state* s, double* k_energy, double* momentum, double* stress) {
+/* statistic_compute_statistic.F90:230-303 over the first n_owned reals (a
+ * rank's own particles: the sums MCF all-reduces over the ranks at
+ * statistic_compute_statistic.F90:348-403) */
+int orc_statistics_owned(orc_state* s, int64_t n_owned, double* k_energy, double* momentum,
+                         double* stress) {
   const int d = s->d, d2 = d * d;
   double ke = 0.0, mom[3] = {0, 0, 0}, st[9] = {0};
-  for (int64_t j = 0; j < s->nreal; ++j) {
+  const int64_t nown = n_owned < s->nreal ? n_owned : s->nreal;
+  for (int64_t j = 0; j < nown; ++j) {
     if (s->sid[j] == 0) {
       double v2 = 0.0;
       for (int a = 0; a < d; ++a) v2 = v2 + s->v[j * d + a] * s->v[j * d + a];
@@ -2000,6 +2004,11 @@ int orc_statistics(orc_state* s, double* k_energy, double* momentum, double* str
   if (stress)
     for (int a = 0; a < 9; ++a) stress[a] = a < d2 ? st[a] : 0.0;
   return 0;
+}
+
+/* statistic_compute_statistic.F90:230-303 */
+int orc_statistics(orc_state* s, double* k_energy, double* momentum, double* stress) {
+  return orc_statistics_owned(s, s->nreal, k_energy, momentum, stress);
 }
 
 int orc_force_scale(const orc_state* s, double* out) {

@@ -66,6 +66,9 @@ int orc_download(orc_state* s, double* x, double* v, double* rho, double* p,
                  double* f, double* ct, double* s_out);
 int orc_statistics(orc_state* s, double* k_energy, double* momentum,
                    double* stress);
+/* the same sums over the first n_owned particles (host order) */
+int orc_statistics_owned(orc_state* s, int64_t n_owned, double* k_energy, double* momentum,
+                         double* stress);
 
 /* per real particle: sum over its pairs of |pair acceleration| (the scale
  * of the force parity tolerance); valid after orc_compute_interaction */

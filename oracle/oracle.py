@@ -59,6 +59,7 @@ def load(rebuild: bool = True) -> C.CDLL:
         "orc_time": (C.c_double, [_h]),
         "orc_download": (C.c_int, [_h, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
         "orc_statistics": (C.c_int, [_h, _dp, _dp, _dp]),
+        "orc_statistics_owned": (C.c_int, [_h, C.c_int64, _dp, _dp, _dp]),
         "orc_counts": (C.c_int, [_h, C.POINTER(C.c_int64)]),
         "orc_force_scale": (C.c_int, [_h, _dp]),
         "orc_timers": (C.c_int, [_h, _dp]),
@@ -220,13 +221,19 @@ class Oracle:
     def time(self) -> float:
         return float(self.lib.orc_time(self._h))
 
-    def statistic_compute_statistic(self):
+    def statistic_compute_statistic(self, n_owned=None):
+        """kinetic energy, momentum[3], stress[9]; with n_owned, over the first
+        n_owned particles only (a subdomain's own, its ghosts left out)"""
         ke = C.c_double()
         mom = np.zeros(3)
         st = np.zeros(9)
-        self._check("statistics", self.lib.orc_statistics(self._h, C.byref(ke),
-                                                          _ptr(mom, C.c_double),
-                                                          _ptr(st, C.c_double)))
+        if n_owned is None:
+            rc = self.lib.orc_statistics(self._h, C.byref(ke), _ptr(mom, C.c_double),
+                                         _ptr(st, C.c_double))
+        else:
+            rc = self.lib.orc_statistics_owned(self._h, int(n_owned), C.byref(ke),
+                                               _ptr(mom, C.c_double), _ptr(st, C.c_double))
+        self._check("statistics", rc)
         return ke.value, mom, st
 
     def force_scale(self) -> np.ndarray:

@@ -10,7 +10,9 @@ another order.  The CPU oracle runs every slab:
 Bars: positions within 1e-11 of the box, velocities within 1e-9 of the
 velocity scale, densities within 1e-12 relative, accelerations within 1e-9
 of their scale, after the initial right-hand side and 6 steps with the
-random force on, particles migrating between slabs.
+random force on, particles migrating between slabs.  The box's statistics
+(kinetic energy, momentum, stress), summed per slab over its own particles
+and all-reduced over the slabs, within 1e-9 of the undivided box's.
 """
 import os
 import socket
@@ -40,17 +42,28 @@ def workload():
     p = w.params
     p.kt = 1e-3
     p.Brownian = 1
+    p.stress_tensor = 1  # the statistics' stress sum
     w.dt = 2e-3
     p.dt = w.dt  # the random force's time step in the stage routines
     return w
 
 
-def undivided(w):
+def undivided(w, stats=False):
     o = Oracle(w.params)
     o.upload(w.x, w.v, w.m, w.id)
     o.marching_init_force(0)
     o.run_vv(0, NSTEPS, w.dt)
-    return o.download("x", "v", "rho", "f")
+    out = o.download("x", "v", "rho", "f")
+    return (out, o.statistic_compute_statistic()) if stats else out
+
+
+def stats_close(got, ref, tol=1e-9):
+    """kinetic energy relative; momentum and stress within tol of their scale"""
+    assert abs(got[0] - ref[0]) <= tol * abs(ref[0])
+    for q in (1, 2):
+        scale = np.abs(ref[q]).max()
+        assert scale > 0
+        assert np.max(np.abs(got[q] - ref[q])) <= tol * scale
 
 
 def by_pid(parts, n, d):
@@ -82,7 +95,7 @@ def check(w, got, ref, bars=(1e-11, 1e-9, 1e-12, 1e-9)):
 @pytest.mark.parametrize("nslab", [1, 2, 3])
 def test_slabs_in_one_process_follow_the_undivided_box(nslab):
     w = workload()
-    ref = undivided(w)
+    ref, ref_stats = undivided(w, stats=True)
     dec = SlabDecomposition(w.params, nslab, factory=Oracle, exchange=LocalExchange())
     dec.upload(w.x, w.v, w.m, w.id)
     dec.init_force(0)
@@ -90,6 +103,7 @@ def test_slabs_in_one_process_follow_the_undivided_box(nslab):
     got = by_pid(dec.owned_state(), w.n, 3)
     check(w, got, ref)
     assert dec.migrated > 0  # particles crossed slab faces (or the periodic x face)
+    stats_close(dec.statistics(), ref_stats)
 
 
 def _free_port():
@@ -114,8 +128,9 @@ def _rank_main(rank, world, port, q):
         dec.init_force(0)
         dec.run_vv(0, NSTEPS, w.dt)
         parts = dec.owned_state()
+        stats = dec.statistics()  # all-reduced over the ranks
         gathered = [None] * world if rank == 0 else None
-        dist.gather_object(parts[0], gathered, dst=0)
+        dist.gather_object((parts[0], stats), gathered, dst=0)
         if rank == 0:
             q.put(gathered)
     finally:
@@ -132,9 +147,12 @@ def test_slabs_on_gloo_ranks_follow_the_undivided_box(world):
     procs = [ctx.Process(target=_rank_main, args=(r, world, port, q)) for r in range(world)]
     for p in procs:
         p.start()
-    parts = q.get(timeout=300)
+    gathered = q.get(timeout=300)
     for p in procs:
         p.join(timeout=120)
         assert p.exitcode == 0
     w = workload()
-    check(w, by_pid(parts, w.n, 3), undivided(w))
+    ref, ref_stats = undivided(w, stats=True)
+    check(w, by_pid([g[0] for g in gathered], w.n, 3), ref)
+    for _, stats in gathered:  # every rank holds the box's sums
+        stats_close(stats, ref_stats)

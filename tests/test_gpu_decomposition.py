@@ -16,7 +16,8 @@ import pytest
 from mcf_gb300 import SDPD
 from mcf_gb300.decomp import LocalExchange, SlabDecomposition
 from mcf_gb300.params import PRECISION_FP32_MIXED
-from tests.test_decomposition import NSTEPS, by_pid, check, undivided, workload
+from tests.test_decomposition import (NSTEPS, by_pid, check, stats_close, undivided,
+                                      workload)
 
 pytestmark = pytest.mark.gpu
 
@@ -40,6 +41,12 @@ def test_gpu_slabs_follow_the_undivided_box(gpu_lib, nslab):
     assert dec.migrated > 0
     check(w, got, gpu_undivided(w))
     check(w, got, undivided(w), bars=(1e-9, 1e-5, 1e-9, 1e-5))
+    # the box's statistics from the slabs' own particles, all-reduced
+    g = SDPD(w.params)
+    g.upload(w.x, w.v, w.m, w.id)
+    g.marching_init_force(0)
+    g.run_vv(0, NSTEPS, w.dt)
+    stats_close(dec.statistics(), g.statistic_compute_statistic())
 
 
 def test_gpu_slabs_fp32_mixed(gpu_lib):
