@@ -275,19 +275,20 @@ __global__ void k_rebuild_done(int* __restrict__ flag) {
   flag[0] = 0;
 }
 
-// Density over the candidate list, one thread per particle: the step's
-// exact pair test (FP64 path: the FP64 separation of MCF; FP32 path: the
-// FP32 test of k_density's scan, same operation order), the step's neighbour
-// list for the force sweep, the W sum and the epilogue of k_density.
-template <int D, bool FP64, int S>
+// FP64 density over the candidate list, one thread per particle: the step's
+// exact pair test with MCF's FP64 separation, the step's neighbour list for
+// the force sweeps (nhs: the first entry of the forward half the symmetric
+// sweep owns), the W sum and the epilogue of k_density.  The FP32 path runs
+// k_density_list (sweep32.cu).
+template <int D>
 __global__ void __launch_bounds__(kReuseTPB)
     k_density_reuse(Consts k, const int* __restrict__ cell_start, const int* __restrict__ cell_of,
-                    const float4* __restrict__ off, const double4_32a* __restrict__ x,
-                    const double4_32a* __restrict__ v, const double* __restrict__ m,
-                    const int* __restrict__ sid, const int* __restrict__ pid,
-                    const uint16_t* __restrict__ vl, const int* __restrict__ vcount,
-                    uint16_t* __restrict__ nl, int* __restrict__ ncount, int* __restrict__ nhs,
-                    int cap, double* __restrict__ rho, double* __restrict__ pr,
+                    const double4_32a* __restrict__ x, const double4_32a* __restrict__ v,
+                    const double* __restrict__ m, const int* __restrict__ sid,
+                    const int* __restrict__ pid, const uint16_t* __restrict__ vl,
+                    const int* __restrict__ vcount, uint16_t* __restrict__ nl,
+                    int* __restrict__ ncount, int* __restrict__ nhs, int cap,
+                    double* __restrict__ rho, double* __restrict__ pr,
                     double4_32a* __restrict__ pc, float4* __restrict__ pcf,
                     float4* __restrict__ vf, int with_pressure, unsigned* __restrict__ err,
                     int* __restrict__ stats, unsigned long long* __restrict__ pairs, NN nn,
@@ -295,166 +296,38 @@ __global__ void __launch_bounds__(kReuseTPB)
   constexpr int CENTER = (D == 3) ? 13 : 4;
   __shared__ int s_start[kMaxStencil * kReuseTPB];
   __shared__ int s_shift[kMaxStencil * kReuseTPB];
-  __shared__ float4 s_slot[kSlotTable];
   const int n = k.n, tid = threadIdx.x;
-  // S lanes per particle in the FP32 path for small systems (as k_force32):
-  // lane l tests candidates l, l + S, ...; the step's list keeps candidate
-  // order (positions from the group's ballot) and the W sums are added in
-  // lane order
-  const int gt = blockIdx.x * kReuseTPB + tid;
-  const int i = gt / S, lane_s = gt % S;
+  const int i = blockIdx.x * kReuseTPB + tid;
   int my_max = 0;
   unsigned long long my_pairs = 0;
-  fill_slot_offsets<D>(k, s_slot);
-  __syncthreads();
-  int kept = 0, hs = -1, si = 0;
-  bool acc_i = false;
-  double rho_i = 0.0;
   if (i < n) {
     const int celli = cell_of[i];
     build_lane_table<D, kReuseTPB>(k, celli, cell_start, s_start, s_shift);
-    const float4* slot_tab = slot_table(k, s_slot, celli);
     const int li = i - s_start[CENTER * kReuseTPB + tid];
-    si = sid[i];
-    acc_i = dyn_rho(k, si);
+    const int si = sid[i];
+    const bool acc_i = dyn_rho(k, si);
     const int cnt = vcount[i];
-    if (FP64) {
-      const double4_32a xi4 = x[i];
-      const double xi[3] = {xi4.x, xi4.y, xi4.z};
-      double sum = 0.0;
-      for (int e = 0; e < cnt; ++e) {
-        const int ent = vl[(size_t)e * n + i];
-        const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
-        const int j = s_start[sl * kReuseTPB + tid] + q;
-        const double4_32a xj4 = x[j];
-        const double xj[3] = {xj4.x, xj4.y, xj4.z};
-        double r[3];
-        const double d2 = exact_sep<D>(k, xi, xj, s_shift[sl * kReuseTPB + tid], r);
-        if (d2 >= k.rc2) continue;
-        if (hs < 0 && (sl > CENTER || (sl == CENTER && q > li))) hs = kept;
-        if (kept < cap) nl[(size_t)kept * n + i] = (uint16_t)ent;
-        ++kept;
-        if (acc_i) {
-          const double w = kernel_w<double>(k, sqrt(d2));
-          sum += (k.rhs_density_type == 1) ? w * m[j] : w;
-        }
+    const double4_32a xi4 = x[i];
+    const double xi[3] = {xi4.x, xi4.y, xi4.z};
+    double sum = 0.0;
+    int kept = 0, hs = -1;
+    for (int e = 0; e < cnt; ++e) {
+      const int ent = vl[(size_t)e * n + i];
+      const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
+      const int j = s_start[sl * kReuseTPB + tid] + q;
+      const double4_32a xj4 = x[j];
+      const double xj[3] = {xj4.x, xj4.y, xj4.z};
+      double r[3];
+      const double d2 = exact_sep<D>(k, xi, xj, s_shift[sl * kReuseTPB + tid], r);
+      if (d2 >= k.rc2) continue;
+      if (hs < 0 && (sl > CENTER || (sl == CENTER && q > li))) hs = kept;
+      if (kept < cap) nl[(size_t)kept * n + i] = (uint16_t)ent;
+      ++kept;
+      if (acc_i) {
+        const double w = kernel_w<double>(k, sqrt(d2));
+        sum += (k.rhs_density_type == 1) ? w * m[j] : w;
       }
-      rho_i = sum;
-    } else if (S > 1) {
-      const float4 oi = off[i];
-      const bool mass = k.rhs_density_type == 1;
-      float sum = 0.0f, comp = 0.0f;
-      const int base = (tid & 31) & ~(S - 1);
-      const unsigned gmask = ((1u << S) - 1u) << base;
-      for (int e0 = 0; e0 < cnt; e0 += S) {
-        const int e = e0 + lane_s;
-        bool in = false, fwd = false;
-        int ent = 0;
-        float rx = 0.f, ry = 0.f, rz = 0.f;
-        int j = 0;
-        if (e < cnt) {
-          ent = vl[(size_t)e * n + i];
-          const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
-          j = s_start[sl * kReuseTPB + tid] + q;
-          const float4 oj = off[j];
-          const float4 so = slot_tab[sl];
-          const float sx = so.x, sy = so.y, sz = (D == 3) ? so.z : 0.0f;
-          // the pair test as k_density's scan rounds it: (o_i - slot) - o_j
-          const float tx = (oi.x - sx) - oj.x, ty = (oi.y - sy) - oj.y;
-          float t2 = tx * tx + ty * ty;
-          if (D == 3) {
-            const float tz = (oi.z - sz) - oj.z;
-            t2 += tz * tz;
-          }
-          in = t2 < k.rc2f;
-          fwd = in && (sl > CENTER || (sl == CENTER && q > li));
-          rx = (oi.x - oj.x) - sx;
-          ry = (oi.y - oj.y) - sy;
-          rz = (D == 3) ? (oi.z - oj.z) - sz : 0.f;
-        }
-        const unsigned bal = __ballot_sync(gmask, in) >> base;
-        const unsigned fb = __ballot_sync(gmask, fwd) >> base;
-        if (hs < 0 && fb) hs = kept + __popc(bal & ((1u << (__ffs(fb) - 1)) - 1u));
-        if (in) {
-          const int pos = kept + __popc(bal & ((1u << lane_s) - 1u));
-          if (pos < cap) nl[(size_t)pos * n + i] = (uint16_t)ent;
-          if (acc_i) {
-            // W as k_density's second phase rounds it: (o_i - o_j) - slot
-            float d2 = rx * rx + ry * ry;
-            if (D == 3) d2 += rz * rz;
-            float w = kernel_w<float>(k, sqrtf(d2));
-            if (mass) w *= (float)m[j];
-            const float y = w - comp;
-            const float tt = sum + y;
-            comp = (tt - sum) - y;
-            sum = tt;
-          }
-        }
-        kept += __popc(bal);
-      }
-      const float part = sum - comp;
-      float tot = part;
-      for (int q = 1; q < S; ++q) tot += __shfl_sync(gmask, part, base + q);
-      rho_i = (double)tot;
-    } else {
-      const float4 oi = off[i];
-      const bool mass = k.rhs_density_type == 1;
-      float sum = 0.0f, comp = 0.0f;
-      // candidates in groups of kGather: their entries, then their offsets,
-      // are loaded before any is used (the sweep waits on these gathers)
-      constexpr int kGather = 4;
-      for (int e0 = 0; e0 < cnt; e0 += kGather) {
-        int entg[kGather], jg[kGather];
-        float4 og[kGather];
-#pragma unroll
-        for (int u = 0; u < kGather; ++u)
-          entg[u] = (e0 + u < cnt) ? (int)vl[(size_t)(e0 + u) * n + i] : 0;
-#pragma unroll
-        for (int u = 0; u < kGather; ++u) {
-          jg[u] = s_start[(entg[u] >> kLocalBits) * kReuseTPB + tid] +
-                  (entg[u] & (kMaxCellCount - 1));
-          og[u] = (e0 + u < cnt) ? off[jg[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-#pragma unroll
-        for (int u = 0; u < kGather; ++u) {
-          if (e0 + u >= cnt) break;
-          const int ent = entg[u];
-          const int sl = ent >> kLocalBits, q = ent & (kMaxCellCount - 1);
-          const int j = jg[u];
-          const float4 oj = og[u];
-          const float4 so = slot_tab[sl];
-          const float sx = so.x, sy = so.y, sz = (D == 3) ? so.z : 0.0f;
-          // the pair test as k_density's scan rounds it: (o_i - slot) - o_j
-          const float tx = (oi.x - sx) - oj.x, ty = (oi.y - sy) - oj.y;
-          float t2 = tx * tx + ty * ty;
-          if (D == 3) {
-            const float tz = (oi.z - sz) - oj.z;
-            t2 += tz * tz;
-          }
-          if (!(t2 < k.rc2f)) continue;
-          if (hs < 0 && (sl > CENTER || (sl == CENTER && q > li))) hs = kept;
-          if (kept < cap) nl[(size_t)kept * n + i] = (uint16_t)ent;
-          ++kept;
-          if (!acc_i) continue;
-          // W as k_density's second phase rounds it: (o_i - o_j) - slot
-          const float rx = (oi.x - oj.x) - sx, ry = (oi.y - oj.y) - sy;
-          float d2 = rx * rx + ry * ry;
-          if (D == 3) {
-            const float rz = (oi.z - oj.z) - sz;
-            d2 += rz * rz;
-          }
-          float w = kernel_w<float>(k, sqrtf(d2));
-          if (mass) w *= (float)m[j];
-          const float y = w - comp;
-          const float tt = sum + y;
-          comp = (tt - sum) - y;
-          sum = tt;
-        }
-      }
-      rho_i = (double)sum;
     }
-  }
-  if (i < n && lane_s == 0) {
     if (kept > cap) atomicOr(err, kErrNeighOverflow);
     my_max = kept;
     kept = min(kept, cap);
@@ -464,7 +337,7 @@ __global__ void __launch_bounds__(kReuseTPB)
     const double mi = m[i];
     double rho_out;
     if (acc_i) {
-      rho_out = ((k.rhs_density_type == 1) ? k.w0 * mi : k.w0) + rho_i;
+      rho_out = ((k.rhs_density_type == 1) ? k.w0 * mi : k.w0) + sum;
     } else {
       rho_out = (k.rhs_density_type == 1) ? k.init_density : k.init_density / mi;
     }
@@ -473,7 +346,7 @@ __global__ void __launch_bounds__(kReuseTPB)
     if (with_pressure) {
       const double4_32a vi4 =
           (si > 0 && k.ncoll > 0) ? colloid_particle_update<D>(k, i, si, x[i], ca) : v[i];
-      write_particle_records<FP64>(k, i, rho_out, mi, pid[i], vi4, pr, pc, pcf, vf, nn);
+      write_particle_records<true>(k, i, rho_out, mi, pid[i], vi4, pr, pc, pcf, vf, nn);
     }
   }
 #pragma unroll
@@ -1448,17 +1321,16 @@ int compute_density(Handle* h, bool with_pressure, bool reuse) {
     const int n = (int)h->n;
     if (n == 0) return MCFG_OK;
     const int gr = (n + kReuseTPB - 1) / kReuseTPB;
-#define LAUNCH_R(DD, PP, SS, G)                                                                 \
-  k_density_reuse<DD, PP, SS><<<G, kReuseTPB, 0, s>>>(                                          \
-      k, h->cell_start, h->cell_of, h->off, h->x, h->v, h->m, h->sid, h->pid, h->vl, h->vcount, \
-      h->nl, h->ncount, h->nhs, h->neigh_cap, h->rho, h->pr, h->pc, h->pcf, h->vf,              \
+#define LAUNCH_R(DD)                                                                            \
+  k_density_reuse<DD><<<gr, kReuseTPB, 0, s>>>(                                                 \
+      k, h->cell_start, h->cell_of, h->x, h->v, h->m, h->sid, h->pid, h->vl, h->vcount, h->nl,  \
+      h->ncount, h->nhs, h->neigh_cap, h->rho, h->pr, h->pc, h->pcf, h->vf,                     \
       with_pressure ? 1 : 0, h->d_err, h->d_stats, h->d_pairs, NN{h->ct, h->act, h->vgt, h->qq}, \
       CollArgs{h->v, h->rxc, h->rxcf})
-    // FP64 only: the FP32 path runs density_list (sweep32.cu)
     if (k.d == 3)
-      LAUNCH_R(3, true, 1, gr);
+      LAUNCH_R(3);
     else
-      LAUNCH_R(2, true, 1, gr);
+      LAUNCH_R(2);
 #undef LAUNCH_R
     h->launches++;
     return cuda_check(h, cudaGetLastError(), "density launch") ? MCFG_ECUDA : MCFG_OK;
