@@ -261,7 +261,11 @@ int mcfg_run_vv(mcfg_handle* h, int64_t step0, int32_t nsteps, double dt);
  * runs on a second stream, overlapping the density and force sweeps (the
  * positions are final once the step's list phase is done).  The forces stay
  * on the device between steps (MCF does not change them between steps;
- * mcfg_download returns them on output steps). */
+ * mcfg_download returns them on output steps).  With neighbour-list reuse
+ * and page-locked x, v (pinned, or mcfg_host_register), the call replays a
+ * CUDA graph captured for these arrays (the copies, the step, the copies
+ * back): the same bits as per-step launches, fewer launch gaps.  The arrays
+ * must stay registered while the handle steps with them. */
 int mcfg_step_vv_host(mcfg_handle* h, int64_t step, double dt, double* x, double* v);
 
 /* Page-lock a caller's host array (cudaHostRegister) so that the copies of

@@ -46,21 +46,39 @@ void resolve_phases(Handle* h) {
   }
 }
 
-int check_device_errors(Handle* h) {
-  unsigned e = 0;
-  int st[4] = {0, 0, 0, 0};
-  unsigned long long pairs = 0;
-  if (cuda_check(h, cudaMemcpyAsync(&e, h->d_err, sizeof e, cudaMemcpyDeviceToHost, h->stream),
-                 "error flag copy"))
+#define TRY_STATUS(expr) \
+  do {                    \
+    int _rc = (expr);     \
+    if (_rc) return _rc;  \
+  } while (0)
+
+// the device status words into h->h_status (pinned), on the handle's stream
+static int status_copy_async(Handle* h) {
+  if (!h->h_status &&
+      cuda_check(h, cudaHostAlloc((void**)&h->h_status, sizeof(Handle::HostStatus),
+                                  cudaHostAllocDefault),
+                 "status buffer"))
     return MCFG_ECUDA;
-  if (cuda_check(h, cudaMemcpyAsync(st, h->d_stats, sizeof st, cudaMemcpyDeviceToHost, h->stream),
-                 "stats copy"))
-    return MCFG_ECUDA;
-  if (cuda_check(h, cudaMemcpyAsync(&pairs, h->d_pairs, sizeof pairs, cudaMemcpyDeviceToHost,
+  Handle::HostStatus* hs = h->h_status;
+  if (cuda_check(h, cudaMemcpyAsync(&hs->err, h->d_err, sizeof hs->err, cudaMemcpyDeviceToHost,
                                     h->stream),
+                 "error flag copy") ||
+      cuda_check(h, cudaMemcpyAsync(hs->stats, h->d_stats, sizeof hs->stats,
+                                    cudaMemcpyDeviceToHost, h->stream),
+                 "stats copy") ||
+      cuda_check(h, cudaMemcpyAsync(&hs->pairs, h->d_pairs, sizeof hs->pairs,
+                                    cudaMemcpyDeviceToHost, h->stream),
                  "pairs copy"))
     return MCFG_ECUDA;
-  if (cuda_check(h, cudaStreamSynchronize(h->stream), "synchronize")) return MCFG_ECUDA;
+  return MCFG_OK;
+}
+
+// the status words copied by status_copy_async, after the stream's sync
+static int status_evaluate(Handle* h) {
+  const unsigned e = h->h_status->err;
+  int st[4];
+  for (int q = 0; q < 4; ++q) st[q] = h->h_status->stats[q];
+  const unsigned long long pairs = h->h_status->pairs;
   resolve_phases(h);
   h->max_neigh = st[1];
   h->num_pairs = (int64_t)pairs;
@@ -80,6 +98,12 @@ int check_device_errors(Handle* h) {
     if (e & kErrNonFinite) return set_error(h, MCFG_EPHYS, "non-finite acceleration");
   }
   return MCFG_OK;
+}
+
+int check_device_errors(Handle* h) {
+  TRY_STATUS(status_copy_async(h));
+  if (cuda_check(h, cudaStreamSynchronize(h->stream), "synchronize")) return MCFG_ECUDA;
+  return status_evaluate(h);
 }
 
 }  // namespace mcfg
@@ -761,6 +785,10 @@ void destroy_graphs(Handle* h) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g = Handle::GraphSlot{};
   }
+  for (auto& g : h->hgraphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = Handle::HostGraph{};
+  }
 }
 
 // run_vv may replay captured steps: list reuse (the rebuild is decided on the
@@ -827,6 +855,124 @@ static Handle::GraphSlot* graph_for(Handle* h, double dt) {
   slot->dt = dt;
   slot->v = v0;
   slot->launches = captured + 2;
+  return slot;
+}
+
+// page-locked host memory (pinned, or registered with mcfg_host_register):
+// what a captured memcpy node may read and write
+static bool page_locked(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// the staging regions of mcfg_step_vv_host in up_x: x out | v out | x in
+static double* stage_x_in(Handle* h) { return h->up_x + (size_t)h->n * 6; }
+static double* stage_v_out(Handle* h) { return h->up_x + (size_t)h->n * 3; }
+
+// one host step's device work after its inputs are enqueued: the state
+// update, the step (positions back on the copy stream from its list phase),
+// the velocities back
+static int host_step_body(Handle* h, int64_t step, double dt, double* x, double* v) {
+  const int n = (int)h->n, d = h->p.num_dim;
+  const size_t bytes = sizeof(double) * (size_t)n * d;
+  const int tb = 256, gb = (n + tb - 1) / tb;
+  cudaStream_t s = h->stream;
+  k_update_state<<<gb, tb, 0, s>>>(h->k, n, h->slot_of, stage_x_in(h), h->up_v, nullptr, h->x,
+                                   h->v, h->f);
+  h->launches++;
+  if (cuda_check(h, cudaGetLastError(), "update state kernel")) return MCFG_ECUDA;
+  h->have_list = h->have_density = h->have_pressure = false;
+  h->dt = dt;
+  h->io_x_out = x;
+  const int rc = vv_step(h, step, dt);
+  h->io_x_out = nullptr;
+  if (rc != MCFG_OK) return rc;
+  k_download<<<gb, tb, 0, s>>>(n, d, h->hidx, h->v, stage_v_out(h));
+  h->launches++;
+  if (cuda_check(h, cudaMemcpyAsync(v, stage_v_out(h), bytes, cudaMemcpyDeviceToHost, s),
+                 "v out"))
+    return MCFG_ECUDA;
+  return MCFG_OK;
+}
+
+// the captured host step for these arrays and the current velocity buffer,
+// or null (not eligible, or the capture failed: plain launches then)
+static Handle::HostGraph* host_graph_for(Handle* h, double dt, double* x, double* v) {
+  if (!graph_eligible(h) || h->hgraph_off || !page_locked(x) || !page_locked(v)) return nullptr;
+  for (auto& g : h->hgraphs)
+    if (g.exec && g.gen == h->graph_gen && g.dt == dt && g.v == (const void*)h->v && g.hx == x &&
+        g.hv == v)
+      return &g;
+  if (!h->d_step && cudaMalloc(&h->d_step, sizeof(int64_t)) != cudaSuccess) {
+    cudaGetLastError();
+    h->hgraph_off = true;
+    return nullptr;
+  }
+  // a slot that no longer matches, else the one of the other velocity buffer
+  Handle::HostGraph* slot = nullptr;
+  for (auto& g : h->hgraphs)
+    if (!g.exec || g.gen != h->graph_gen || g.dt != dt || g.hx != x || g.hv != v) {
+      slot = &g;
+      break;
+    }
+  if (!slot) slot = (h->hgraphs[0].v != (const void*)h->v) ? &h->hgraphs[0] : &h->hgraphs[1];
+  if (slot->exec) cudaGraphExecDestroy(slot->exec);
+  *slot = Handle::HostGraph{};
+  // the capture runs no step: the host-side state it changes is put back
+  double4_32a* const v0 = h->v;
+  double4_32a* const v20 = h->v2;
+  const int64_t launches0 = h->launches;
+  const double t0 = h->time_current;
+  const bool unwrapped0 = h->unwrapped, hl = h->have_list, hd = h->have_density,
+             hp = h->have_pressure, hf = h->have_force;
+  const double dt0 = h->dt;
+  const size_t bytes = sizeof(double) * (size_t)h->n * h->p.num_dim;
+  cudaStream_t s = h->stream;
+  cudaGraph_t graph = nullptr;
+  bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  if (ok) {
+    h->graph_capturing = true;
+    ok = cudaMemcpyAsync(stage_x_in(h), x, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+         cudaMemcpyAsync(h->up_v, v, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+         host_step_body(h, 0, dt, x, v) == MCFG_OK;
+    // the copy stream's positions joined back into the captured stream
+    const bool joined = cudaEventRecord(h->ev_join, h->copy_stream) == cudaSuccess &&
+                        cudaStreamWaitEvent(s, h->ev_join, 0) == cudaSuccess;
+    h->graph_capturing = false;
+    const bool ended = cudaStreamEndCapture(s, &graph) == cudaSuccess;
+    ok = ok && joined && ended && graph != nullptr &&
+         cudaGraphInstantiate(&slot->exec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+  }
+  const int64_t captured = h->launches - launches0;
+  h->launches = launches0;
+  h->v = v0;
+  h->v2 = v20;
+  h->time_current = t0;
+  h->unwrapped = unwrapped0;
+  h->have_list = hl;
+  h->have_density = hd;
+  h->have_pressure = hp;
+  h->have_force = hf;
+  h->dt = dt0;
+  if (!ok) {
+    cudaGetLastError();
+    if (slot->exec) cudaGraphExecDestroy(slot->exec);
+    *slot = Handle::HostGraph{};
+    h->hgraph_off = true;
+    h->err.clear();
+    return nullptr;
+  }
+  slot->gen = h->graph_gen;
+  slot->dt = dt;
+  slot->v = v0;
+  slot->hx = x;
+  slot->hv = v;
+  slot->launches = captured;
   return slot;
 }
 
@@ -925,6 +1071,8 @@ int mcfg_destroy(mcfg_handle* h) {
     cudaStreamDestroy(h->copy_stream);
   }
   if (h->ev_x) cudaEventDestroy(h->ev_x);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->h_status) cudaFreeHost(h->h_status);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return MCFG_OK;
@@ -1274,39 +1422,43 @@ int mcfg_step_vv_host(mcfg_handle* h, int64_t step, double dt, double* x, double
   if (!h->copy_stream &&
       (cuda_check(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking),
                   "copy stream") ||
-       cuda_check(h, cudaEventCreateWithFlags(&h->ev_x, cudaEventDisableTiming), "copy event")))
+       cuda_check(h, cudaEventCreateWithFlags(&h->ev_x, cudaEventDisableTiming), "copy event") ||
+       cuda_check(h, cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming),
+                  "join event")))
     return MCFG_ECUDA;
   cudaStream_t s = h->stream;
   const size_t bytes = sizeof(double) * (size_t)n * d;
-  // the step's inputs: x, v into their particles' current slots
-  if (cuda_check(h, cudaMemcpyAsync(h->up_x + (size_t)n * 6, x, bytes, cudaMemcpyHostToDevice, s),
-                 "x in") ||
-      cuda_check(h, cudaMemcpyAsync(h->up_v, v, bytes, cudaMemcpyHostToDevice, s), "v in"))
-    return MCFG_ECUDA;
-  const int tb = 256, gb = (n + tb - 1) / tb;
-  k_update_state<<<gb, tb, 0, s>>>(h->k, n, h->slot_of, h->up_x + (size_t)n * 6, h->up_v, nullptr,
-                                   h->x, h->v, h->f);
-  h->launches++;
-  if (cuda_check(h, cudaGetLastError(), "update state kernel")) return MCFG_ECUDA;
-  h->have_list = h->have_density = h->have_pressure = false;
-  h->dt = dt;
-  // the step; its list phase starts the positions' copy back (copy stream)
-  h->io_x_out = x;
-  const int rc = vv_step(h, step, dt);
-  h->io_x_out = nullptr;
-  if (rc != MCFG_OK) {
-    cudaStreamSynchronize(h->copy_stream);
-    return rc;
+  Handle::HostGraph* g = host_graph_for(h, dt, x, v);
+  if (g) {
+    // the captured step (list reuse, arrays page-locked): the Philox step
+    // from the device counter; the host-side state the step changes
+    k_step_set<<<1, 1, 0, s>>>(h->d_step, step);
+    if (cuda_check(h, cudaGraphLaunch(g->exec, s), "host step graph")) return MCFG_ECUDA;
+    h->launches += g->launches + 1;
+    h->time_current = h->time_current + dt;
+    std::swap(h->v, h->v2);
+    h->unwrapped = true;
+    h->dt = dt;
+    h->have_list = false;
+    h->have_density = h->have_pressure = h->have_force = true;
+  } else {
+    // the step's inputs: x, v into their particles' current slots
+    if (cuda_check(h, cudaMemcpyAsync(stage_x_in(h), x, bytes, cudaMemcpyHostToDevice, s),
+                   "x in") ||
+        cuda_check(h, cudaMemcpyAsync(h->up_v, v, bytes, cudaMemcpyHostToDevice, s), "v in"))
+      return MCFG_ECUDA;
+    const int rc = host_step_body(h, step, dt, x, v);
+    if (rc != MCFG_OK) {
+      cudaStreamSynchronize(h->copy_stream);
+      return rc;
+    }
   }
-  // the step's velocities after the second kick
-  double* stage_v = h->up_x + (size_t)n * 3;
-  k_download<<<gb, tb, 0, s>>>(n, d, h->hidx, h->v, stage_v);
-  h->launches++;
-  if (cuda_check(h, cudaMemcpyAsync(v, stage_v, bytes, cudaMemcpyDeviceToHost, s), "v out") ||
+  // the status words behind the velocities, then one synchronisation
+  if (status_copy_async(h) != MCFG_OK ||
       cuda_check(h, cudaStreamSynchronize(s), "step sync") ||
       cuda_check(h, cudaStreamSynchronize(h->copy_stream), "x out sync"))
     return MCFG_ECUDA;
-  return check_device_errors(h);
+  return status_evaluate(h);
 }
 
 int mcfg_run_vv(mcfg_handle* h, int64_t step0, int32_t nsteps, double dt) {

@@ -123,7 +123,16 @@ struct Handle {
   // array it fills (null outside that call)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t ev_x = nullptr;
+  cudaEvent_t ev_join = nullptr;  // the copy stream joined back (captured host step)
   double* io_x_out = nullptr;
+  // device status words (error flags, list statistics, pair count) copied
+  // to pinned memory behind a host step, read after its one synchronisation
+  struct HostStatus {
+    unsigned err;
+    int stats[4];
+    unsigned long long pairs;
+  };
+  HostStatus* h_status = nullptr;
   std::string err;
   bool have_particles = false, have_list = false, have_density = false,
        have_pressure = false, have_force = false;
@@ -246,6 +255,20 @@ struct Handle {
     const void* v = nullptr;
     int64_t launches = 0;
   } graphs[2];
+  // mcfg_step_vv_host with page-locked host arrays replays a captured step:
+  // inputs over, the step (positions back on the copy stream), velocities
+  // back; one graph per velocity buffer (the fused kick swaps v and v2) and
+  // pair of host arrays, baked into the memcpy nodes
+  struct HostGraph {
+    cudaGraphExec_t exec = nullptr;
+    uint64_t gen = 0;
+    double dt = 0.0;
+    const void* v = nullptr;
+    const double* hx = nullptr;
+    const double* hv = nullptr;
+    int64_t launches = 0;
+  } hgraphs[2];
+  bool hgraph_off = false;  // a host-step capture failed: plain launches from then on
   // ---- particle-file text (output.cu), grow-only, null until the first write ----
   char* out_dev = nullptr;
   char* out_host = nullptr;  // pinned

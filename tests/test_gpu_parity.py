@@ -592,32 +592,47 @@ def test_step_vv_host_equals_update_step_download(gpu_lib):
 
 
 def test_host_registered_arrays_step_alike(gpu_lib):
-    # MCF's ordinary host arrays page-locked with mcfg_host_register: the
-    # same steps as with plain arrays, bit for bit; unregistering leaves
-    # them usable
-    w = jittered_3d(n_side=14)
-    w.params.reserved[1] = 1
-    outs = []
-    for reg in (False, True):
-        g = SDPD(w.params)
-        g.upload(w.x, w.v, w.m, w.id)
-        g.marching_init_force(0)
-        st = g.download("x", "v")
-        x = np.ascontiguousarray(st["x"])
-        v = np.ascontiguousarray(st["v"])
-        if reg:
-            g.host_register(x)
-            g.host_register(v)
-        for s in range(1, 6):
-            g.step_vv_host(s, w.dt, x, v)
-        if reg:
-            g.host_unregister(x)
-            g.host_unregister(v)
-        outs.append((x.copy(), v.copy()))
-    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    # MCF's ordinary host arrays page-locked with mcfg_host_register: with
+    # list reuse the host step then replays a captured graph (inputs over,
+    # the step, positions and velocities back); plain arrays take per-step
+    # launches.  The same steps bit for bit, FP64 and FP32-mixed, across
+    # device-side rebuilds; unregistering leaves the arrays usable
+    # particles past skin/2 (0.495 in the 12^3 box) within a few steps
+    fast = jittered_3d(n_side=12)
+    fast.v = np.random.default_rng(9).normal(0, 2.0, fast.v.shape)
+    cases = [(jittered_3d(n_side=14), None, 0), (make_golden.workload("walls_small"), None, 1),
+             (fast, 1e-2, 1)]
+    for w, dt, prec in cases:
+        dt = dt or w.dt
+        outs = []
+        for reg in (False, True):
+            p = w.params.copy()
+            p.reserved[1] = 1
+            p.precision = PRECISION_FP32_MIXED if prec else 0
+            g = SDPD(p)
+            g.upload(w.x, w.v, w.m, w.id)
+            g.marching_init_force(0)
+            st = g.download("x", "v")
+            x = np.ascontiguousarray(st["x"])
+            v = np.ascontiguousarray(st["v"])
+            if reg:
+                g.host_register(x)
+                g.host_register(v)
+            for s in range(1, 16):
+                g.step_vv_host(s, dt, x, v)
+            if reg:
+                g.host_unregister(x)
+                g.host_unregister(v)
+            outs.append((x.copy(), v.copy(), g.download("f")["f"], g.info()))
+        for q in range(3):
+            assert np.array_equal(outs[0][q], outs[1][q]), q
+        assert outs[0][3]["list_rebuilds"] == outs[1][3]["list_rebuilds"]
+        assert outs[0][3]["time_current"] == outs[1][3]["time_current"]
+        if w is fast:
+            assert outs[1][3]["list_rebuilds"] > 1  # rebuilds inside the replays
     with pytest.raises(Exception):
         g.host_unregister(x)  # no longer registered
-    g.step_vv_host(6, w.dt, x, v)  # the failed call leaves the handle usable
+    g.step_vv_host(16, dt, x, v)  # the failed call leaves the handle usable
 
 
 def test_run_vv_graph_replay_equals_step_vv(gpu_lib):
