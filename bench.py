@@ -281,7 +281,9 @@ def cpu_model() -> str:
 
 def run_reference(args, ws, rank):
     """Reference arm: the CPU path on all host cores.  A step is one full VV
-    step of a sub-box of the same workload, sized from a one-step
+    step of a slice of the same workload: the full 100 sites along x (the
+    threads take x-slabs of cells in two colours, so a narrower box would
+    leave cores idle) and fewer along y and z, sized from a one-step
     calibration so that warm-up plus timed steps take about two minutes."""
     from mcf_gb300 import configs
     from oracle.oracle import Oracle
@@ -290,8 +292,8 @@ def run_reference(args, ws, rank):
         return
     threads = os.cpu_count() or 1
 
-    def make(n_side):
-        w = configs.c3_poiseuille_3d(n_side=n_side)
+    def make(n_yz):
+        w = configs.c3_poiseuille_3d(n_side=args.n_side, n_yz=n_yz)
         p = w.params.copy()
         p.symmetry = 1  # MCF's own loop mode: half-shell pairs, each once
         o = Oracle(p, threads=threads)
@@ -299,16 +301,16 @@ def run_reference(args, ws, rank):
         o.marching_init_force(0)
         return w, o
 
-    n_side = min(args.n_side, 40)
-    w, o = make(n_side)
+    n_yz = min(args.n_side, 24)
+    w, o = make(n_yz)
     t0 = time.perf_counter()
     o.run_vv(0, 1, w.dt)
     t1 = time.perf_counter() - t0
     budget = 120.0
     nsteps = args.warmup + args.steps
-    scale = (budget / max(nsteps * t1, 1e-9)) ** (1.0 / 3.0)
-    n_new = int(max(12, min(args.n_side, n_side * scale)))
-    if n_new != n_side:
+    scale = (budget / max(nsteps * t1, 1e-9)) ** 0.5
+    n_new = int(max(12, min(args.n_side, n_yz * scale)))
+    if n_new != n_yz:
         w, o = make(n_new)
         o.run_vv(0, 1, w.dt)
     o.run_vv(1, args.warmup, w.dt)
@@ -321,7 +323,7 @@ def run_reference(args, ws, rank):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": w.name + " with y-walls (CPU sample of the 100^3 workload)",
+        "config": {"workload": w.name + " with y-walls (CPU slice of the 100^3 workload)",
                    "n_fluid": w.n_fluid, "n_wall": w.n - w.n_fluid,
                    "note": "CPU restatement of MCF's FP64 SDPD step (MCF is Fortran+MPI and "
                            "cannot be built here) with MCF's symmetric loops (symmetry = T), "

@@ -142,11 +142,12 @@ def c2_fluctuating_3d(n_side: int = 64, precision: int = PRECISION_FP64,
 
 
 def c3_poiseuille_3d(n_side: int = 100, precision: int = PRECISION_FP64, walls: bool = True,
-                     seed: int = BASE_SEED + 3) -> Workload:
+                     seed: int = BASE_SEED + 3, n_yz: int | None = None) -> Workload:
     """3D 100^3, dx=1, rc=3, c=20, eta=0.5, g_x=0.1, kT=1e-4, dt=5e-5,
     5000 steps.  Poiseuille in y with solid walls in y (4 layers of
     constant-density wall particles per side, Morris no-slip) or, with
-    walls=False, MCF's periodic reverse-Poiseuille force."""
+    walls=False, MCF's periodic reverse-Poiseuille force.  n_yz: a box of
+    n_side sites along x and n_yz along y and z (a slice of the workload)."""
     L = float(n_side)
     if walls:
         nl = wall_layers(3.0, 1.0)
@@ -159,7 +160,14 @@ def c3_poiseuille_3d(n_side: int = 100, precision: int = PRECISION_FP64, walls: 
         p = make_params(**_box(3, 0.0, L), cut_off=3.0, c=20.0, eta=0.5, kt=1e-4, Brownian=1,
                         body_force_type=2, body_force=[0.1, 0.0, 0.0], dt=5e-5,
                         precision=precision, seed=seed)
-    return _finish(f"C3 3D {n_side}^3 Poiseuille", p, [1.0] * 3, 0.0, 0.0, seed, 5e-5, 5000)
+    name = f"C3 3D {n_side}^3 Poiseuille"
+    if n_yz is not None and n_yz != n_side:
+        for a in (1, 2):
+            off = p.min_phys[a] - p.min_phys_t[a]
+            p.max_phys[a] = float(n_yz)
+            p.max_phys_t[a] = float(n_yz) + off
+        name = f"C3 3D {n_side}x{n_yz}x{n_yz} Poiseuille"
+    return _finish(name, p, [1.0] * 3, 0.0, 0.0, seed, 5e-5, 5000)
 
 
 def c5_oldroyd_b_2d(n_side: int = 128, precision: int = PRECISION_FP64, seed: int = BASE_SEED + 5,
