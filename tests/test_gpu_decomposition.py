@@ -63,3 +63,30 @@ def test_gpu_slabs_fp32_mixed(gpu_lib):
     dx -= L * np.round(dx / L)
     assert np.max(np.abs(dx)) <= 1e-6 * L
     assert np.max(np.abs(got["v"] - ref["v"])) <= 1e-4 * np.abs(ref["v"]).max()
+
+
+def test_statistics_owned_contract(gpu_lib):
+    # all particles: mcfg_statistics' sums; none: zeros; out of range: refused
+    from mcf_gb300.mcfg import MCFGError
+
+    w = workload()
+    g = SDPD(w.params)
+    g.upload(w.x, w.v, w.m, w.id)
+    g.marching_init_force(0)
+    g.run_vv(0, 2, w.dt)
+    ke, mom, st = g.statistic_compute_statistic()
+    ke_o, mom_o, st_o = g.statistic_compute_statistic(n_owned=w.n)
+    assert ke_o == ke and np.array_equal(mom_o, mom) and np.array_equal(st_o, st)
+    ke0, mom0, st0 = g.statistic_compute_statistic(n_owned=0)
+    assert ke0 == 0.0 and not np.any(mom0) and not np.any(st0)
+    # the first half in host order against the same sums on the host
+    half = w.n // 2
+    keh, momh, _ = g.statistic_compute_statistic(n_owned=half)
+    d = g.download("v")["v"][:half]
+    fl = w.id[:half, 1] == 0
+    ref_ke = 0.5 * float(np.sum(w.m[:half][fl] * np.sum(d[fl] ** 2, axis=1)))
+    assert abs(keh - ref_ke) <= 1e-12 * ref_ke
+    assert np.allclose(momh, (w.m[:half][fl, None] * d[fl]).sum(0), rtol=1e-12, atol=1e-15)
+    for bad in (-1, w.n + 1):
+        with pytest.raises(MCFGError):
+            g.statistic_compute_statistic(n_owned=bad)
