@@ -620,7 +620,6 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
   // one thread per particle, whatever its cell: per-thread neighbour-cell
   // tables keep every lane busy (2D cells hold ~9 particles)
   __shared__ int s_start[kMaxStencil * kReuseTPB];
-  __shared__ int s_shift[kMaxStencil * kReuseTPB];
   const int n = k.n;
   const bool noise = k.noise != 0;
   const bool walls = k.wall_axis != -1;
@@ -631,7 +630,7 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
   const int i = gt / S, lane_s = gt % S;
   if (i >= n) return;  // the S lanes of a particle leave together
   const int celli = cell_of[i];
-  build_lane_table<D, kReuseTPB>(k, celli, cell_start, s_start, s_shift);
+  build_lane_table<D, kReuseTPB, false>(k, celli, cell_start, s_start, nullptr);
   const float4* slot_tab = slot_table(k, s_slot, celli);
   const float4 oi = off[i];
   const int si = __float_as_int(oi.w);
