@@ -1441,6 +1441,7 @@ int mcfg_step_vv_host(mcfg_handle* h, int64_t step, double dt, double* x, double
     h->dt = dt;
     h->have_list = false;
     h->have_density = h->have_pressure = h->have_force = true;
+    if (h->cdyn) h->coll_host_stale = true;  // the replayed step moved the colloids
   } else {
     // the step's inputs: x, v into their particles' current slots
     if (cuda_check(h, cudaMemcpyAsync(stage_x_in(h), x, bytes, cudaMemcpyHostToDevice, s),
@@ -1484,6 +1485,8 @@ int mcfg_run_vv(mcfg_handle* h, int64_t step0, int32_t nsteps, double dt) {
       h->time_current = h->time_current + dt;
       h->time_current = h->time_current + dt;
     }
+    // the replayed steps moved the colloids on the device
+    if (h->cdyn) h->coll_host_stale = true;
   }
   return check_device_errors(h);
 }

@@ -139,6 +139,62 @@ def test_colloid_dynamics_reuse_graph_and_fp32(gpu_lib):
     assert ev < 1e-4 and ew < 1e-3, (ev, ew)
 
 
+def test_colloid_state_between_graph_replays(gpu_lib):
+    # run, read the colloids, run again, read again: every read after graph
+    # replays (run_vv's two-step graph, the host-array step's graph) returns
+    # the device's current state, as per-step launches do
+    w, cs, cd, m, mmi = case(ab=2, nsub=1)
+    dt = w.dt * 20
+    p = w.params.copy()
+    p.Brownian = 0
+    p.kt = 0.0
+    p.reserved[1] = 1
+    p.precision = PRECISION_FP32_MIXED
+    ref = SDPD(p)
+    start(ref, w, cs, cd, m, mmi)
+    ref_states = []
+    for s in range(1, 21):
+        ref.marching_integrate_VV(s, dt)
+        if s in (8, 20):
+            ref_states.append(ref.colloid_state())
+    g = SDPD(p)
+    start(g, w, cs, cd, m, mmi)
+    g.run_vv(0, 8, dt)
+    a8 = g.colloid_state()
+    g.run_vv(8, 12, dt)
+    a20 = g.colloid_state()
+    for got, want in ((a8, ref_states[0]), (a20, ref_states[1])):
+        for k in ("x", "v", "omega"):
+            assert np.array_equal(got[k], want[k]), k
+    # the host-array step: registered arrays replay its graph, plain arrays
+    # take per-step launches; the reads between the steps agree
+    runs = []
+    for reg in (False, True):
+        h = SDPD(p)
+        start(h, w, cs, cd, m, mmi)
+        st = h.download("x", "v")
+        x, v = np.ascontiguousarray(st["x"]), np.ascontiguousarray(st["v"])
+        if reg:
+            h.host_register(x)
+            h.host_register(v)
+        try:
+            for s in range(1, 9):
+                h.step_vv_host(s, dt, x, v)
+            b8 = h.colloid_state()
+            for s in range(9, 21):
+                h.step_vv_host(s, dt, x, v)
+            b20 = h.colloid_state()
+        finally:
+            if reg:
+                h.host_unregister(x)
+                h.host_unregister(v)
+        runs.append((b8, b20))
+    for got, want in zip(runs[1], runs[0]):
+        for k in ("x", "v", "omega"):
+            assert np.array_equal(got[k], want[k]), k
+    assert not np.array_equal(runs[1][0]["x"], runs[1][1]["x"])  # the colloids moved
+
+
 def test_move_colloids_refused_while_integrating_on_device(gpu_lib):
     from mcf_gb300.mcfg import MCFGError
 
