@@ -1,4 +1,4 @@
-"""Fluctuating SDPD judged statistically (kT > 0, Philox Wiener increments).
+"""Fluctuating SDPD checked statistically (kT > 0, Philox Wiener increments).
 
 Equipartition.  The kinetic temperature <m v_a^2> is compared with what the
 reference's random force implies:
