@@ -49,7 +49,9 @@ timed.
 
 With torchrun (N > 1) every rank runs an independent replica on its own GPU
 ("replicas only": this workload is not decomposed across GPUs); value sums
-the ranks' particle-steps over the slowest rank's time.
+the ranks' particle-steps over the slowest rank's time.  The single-GPU
+studies (accuracy, C4, adjoint, Lees-Edwards, MCF deck, output file) run at
+N = 1 only; the N-GPU line keeps the headline, FP64 and e2e.
 """
 from __future__ import annotations
 
@@ -662,6 +664,13 @@ def run_ours(args, ws, rank, local):
     from mcf_gb300.params import PRECISION_FP32_MIXED, PRECISION_FP64
 
     torch.cuda.set_device(local)
+    # with several ranks every replica would repeat the single-GPU studies
+    # (minutes each, all GPUs held): the N-GPU line keeps the headline, the
+    # FP64 line and e2e; the studies run at N = 1
+    single_gpu_studies = ws == 1
+    if not single_gpu_studies:
+        args.no_accuracy = args.no_lees_edwards = args.no_colloids = True
+        args.no_mcf_deck = args.no_adjoint = args.no_output = True
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
@@ -914,6 +923,8 @@ def run_ours(args, ws, rank, local):
         "adjoint": adjoint, "output_write": output, "lees_edwards": lees_edwards,
         "mcf_scalability_deck": mcf_deck, "colloid_suspension": colloids,
         "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
+        "single_gpu_studies": "in this line" if single_gpu_studies else
+                              "run at N = 1 only (accuracy, C4, adjoint, Lees-Edwards, deck, output)",
         "pair_interactions_per_s": info["num_pairs"] * args.steps * ws / tmax,
     }
     print(json.dumps(line), flush=True)
