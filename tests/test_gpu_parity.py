@@ -635,6 +635,45 @@ def test_host_registered_arrays_step_alike(gpu_lib):
     g.step_vv_host(16, dt, x, v)  # the failed call leaves the handle usable
 
 
+def test_host_step_graph_follows_a_new_particle_set(gpu_lib):
+    # the captured host step bakes buffers and host arrays: a new upload
+    # (another n, other registered arrays) must recapture, and the handle
+    # then steps exactly as a fresh one does
+    def registered_run(g, w, steps):
+        st = g.download("x", "v")
+        x, v = np.ascontiguousarray(st["x"]), np.ascontiguousarray(st["v"])
+        g.host_register(x)
+        g.host_register(v)
+        try:
+            for s in range(1, steps + 1):
+                g.step_vv_host(s, w.dt, x, v)
+        finally:
+            g.host_unregister(x)
+            g.host_unregister(v)
+        return x, v
+
+    w1, w2 = jittered_3d(n_side=12), jittered_3d(n_side=14)
+    p = w1.params.copy()
+    p.reserved[1] = 1
+    p.precision = PRECISION_FP32_MIXED
+    p2 = w2.params.copy()
+    p2.reserved[1] = 1
+    p2.precision = PRECISION_FP32_MIXED
+    g = SDPD(p2)  # sized for the larger set, used for both
+    g.upload(w1.x, w1.v, w1.m, w1.id)
+    g.marching_init_force(0)
+    registered_run(g, w1, 6)
+    g.upload(w2.x, w2.v, w2.m, w2.id)
+    g.marching_init_force(0)
+    xa, va = registered_run(g, w2, 6)
+    fresh = SDPD(p2)
+    fresh.upload(w2.x, w2.v, w2.m, w2.id)
+    fresh.marching_init_force(0)
+    xb, vb = registered_run(fresh, w2, 6)
+    assert xa.shape == xb.shape == (w2.n, 3)
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+
+
 def test_run_vv_graph_replay_equals_step_vv(gpu_lib):
     # with list reuse mcfg_run_vv replays a captured pair of steps (the
     # Philox step from the device counter), mcfg_step_vv launches every
