@@ -624,6 +624,72 @@ int kdw(Handle* h, double dt) {
   return kick_drift_wrap(h, dt);
 }
 
+}  // namespace mcfg
+
+namespace {
+
+// opens the rebuild body of a captured step when the kick-drift kernel has
+// raised the rebuild flag
+__global__ void k_set_rebuild_cond(cudaGraphConditionalHandle c, const int* __restrict__ flag) {
+  cudaGraphSetConditional(c, flag[0] != 0 ? 1u : 0u);
+}
+
+}  // namespace
+
+namespace mcfg {
+
+// Inside a stream capture: the gated rebuild as the body of a conditional
+// node after the kernel that sets its condition.  Any refusal by the
+// runtime returns MCFG_ENOTSUP (the caller recaptures without it).
+static int rebuild_conditional(Handle* h) {
+  if (!h->cond_stream &&
+      cudaStreamCreateWithFlags(&h->cond_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return MCFG_ENOTSUP;
+  cudaStream_t s = h->stream;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t graph = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusActive || graph == nullptr)
+    return MCFG_ENOTSUP;
+  cudaGraphConditionalHandle cond;
+  if (cudaGraphConditionalHandleCreate(&cond, graph, 0, cudaGraphCondAssignDefault) !=
+      cudaSuccess)
+    return MCFG_ENOTSUP;
+  k_set_rebuild_cond<<<1, 1, 0, s>>>(cond, h->d_rebuild);
+  h->launches++;
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, &deps, nullptr, &ndeps) != cudaSuccess)
+    return MCFG_ENOTSUP;
+  cudaGraphNodeParams np{};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = cond;
+  np.conditional.type = cudaGraphCondTypeIf;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &np) != cudaSuccess)
+    return MCFG_ENOTSUP;
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  // the rebuild kernels, launched on the handle's stream, go into the body
+  if (cudaStreamBeginCaptureToGraph(h->cond_stream, body, nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return MCFG_ENOTSUP;
+  h->stream = h->cond_stream;
+  int rc = wrap_gated(h);
+  if (rc == MCFG_OK) rc = gated_cell_list(h);
+  if (rc == MCFG_OK) rc = verlet_build_gated(h);
+  h->stream = s;
+  cudaGraph_t ended = nullptr;
+  const bool body_ok = cudaStreamEndCapture(h->cond_stream, &ended) == cudaSuccess;
+  if (rc != MCFG_OK) return rc;
+  if (!body_ok ||
+      cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1,
+                                          cudaStreamSetCaptureDependencies) != cudaSuccess)
+    return MCFG_ENOTSUP;
+  return MCFG_OK;
+}
+
 // the right-hand side in list-reuse mode: the rebuild kernels return at once
 // unless a particle has moved more than skin/2 (or no candidate list matches
 // the particles yet), then the density over the candidate list and the force
@@ -633,9 +699,13 @@ int rhs_reuse(Handle* h, int64_t step, int fuse_mode, double dt) {
     if (!h->reuse_valid &&
         cuda_check(h, cudaMemsetAsync(h->d_rebuild, 0xff, sizeof(int), h->stream), "rebuild flag"))
       return MCFG_ECUDA;
-    TRY(wrap_gated(h));
-    TRY(gated_cell_list(h));
-    TRY(verlet_build_gated(h));
+    if (h->graph_capturing && !h->cond_off) {
+      TRY(rebuild_conditional(h));
+    } else {
+      TRY(wrap_gated(h));
+      TRY(gated_cell_list(h));
+      TRY(verlet_build_gated(h));
+    }
     h->reuse_valid = true;
   }
   h->have_list = false;  // stage entry points rebuild MCF's list themselves
@@ -821,34 +891,52 @@ static Handle::GraphSlot* graph_for(Handle* h, double dt) {
     }
   if (slot->exec) cudaGraphExecDestroy(slot->exec);
   *slot = Handle::GraphSlot{};
-  const void* v0 = h->v;
+  double4_32a* const v0 = h->v;
+  double4_32a* const v20 = h->v2;
   const int64_t launches0 = h->launches;
   const double t0 = h->time_current;
-  cudaGraph_t graph = nullptr;
-  bool ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-  if (ok) {
-    h->graph_capturing = true;
-    for (int q = 0; q < 2 && ok; ++q) {
-      ok = (!h->cdyn || colloid_section(h, 0, dt) == MCFG_OK) &&
-           kick_drift_reuse(h, dt) == MCFG_OK && rhs_reuse(h, 0, kForceBodyKick, dt) == MCFG_OK;
-      k_step_advance<<<1, 1, 0, h->stream>>>(h->d_step);
+  bool ok = false;
+  int64_t captured = 0;
+  // with the rebuild in a conditional node first; if the runtime refuses
+  // that, once more with the gated kernels in the graph itself
+  for (int attempt = 0; attempt < 2 && !ok; ++attempt) {
+    if (attempt == 1) {
+      if (h->cond_off) break;
+      h->cond_off = true;
     }
-    h->graph_capturing = false;
-    const bool ended = cudaStreamEndCapture(h->stream, &graph) == cudaSuccess;
-    ok = ok && ended && graph != nullptr &&
-         cudaGraphInstantiate(&slot->exec, graph, 0) == cudaSuccess;
-    if (graph) cudaGraphDestroy(graph);
+    cudaGraph_t graph = nullptr;
+    ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      h->graph_capturing = true;
+      for (int q = 0; q < 2 && ok; ++q) {
+        ok = (!h->cdyn || colloid_section(h, 0, dt) == MCFG_OK) &&
+             kick_drift_reuse(h, dt) == MCFG_OK &&
+             rhs_reuse(h, 0, kForceBodyKick, dt) == MCFG_OK;
+        k_step_advance<<<1, 1, 0, h->stream>>>(h->d_step);
+      }
+      h->graph_capturing = false;
+      const bool ended = cudaStreamEndCapture(h->stream, &graph) == cudaSuccess;
+      ok = ok && ended && graph != nullptr &&
+           cudaGraphInstantiate(&slot->exec, graph, 0) == cudaSuccess;
+      if (graph) cudaGraphDestroy(graph);
+    }
+    h->time_current = t0;  // the capture ran no step
+    captured = h->launches - launches0;
+    h->launches = launches0;
+    if (!ok || h->v != v0) {
+      // nothing ran: the buffers the captured kicks swapped go back
+      ok = false;
+      cudaGetLastError();
+      if (slot->exec) cudaGraphExecDestroy(slot->exec);
+      *slot = Handle::GraphSlot{};
+      h->v = v0;
+      h->v2 = v20;
+      h->err.clear();
+    }
   }
-  h->time_current = t0;  // capture ran no step
-  const int64_t captured = h->launches - launches0;
-  h->launches = launches0;
-  if (!ok || h->v != v0) {
-    // fall back to plain launches for this handle; the capture ran nothing
-    cudaGetLastError();
-    if (slot->exec) cudaGraphExecDestroy(slot->exec);
-    *slot = Handle::GraphSlot{};
+  if (!ok) {
+    // plain launches for this handle from now on
     h->graph_off = true;
-    h->err.clear();
     return nullptr;
   }
   slot->gen = h->graph_gen;
@@ -932,21 +1020,35 @@ static Handle::HostGraph* host_graph_for(Handle* h, double dt, double* x, double
   const double dt0 = h->dt;
   const size_t bytes = sizeof(double) * (size_t)h->n * h->p.num_dim;
   cudaStream_t s = h->stream;
-  cudaGraph_t graph = nullptr;
-  bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-  if (ok) {
-    h->graph_capturing = true;
-    ok = cudaMemcpyAsync(stage_x_in(h), x, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-         cudaMemcpyAsync(h->up_v, v, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-         host_step_body(h, 0, dt, x, v) == MCFG_OK;
-    // the copy stream's positions joined back into the captured stream
-    const bool joined = cudaEventRecord(h->ev_join, h->copy_stream) == cudaSuccess &&
-                        cudaStreamWaitEvent(s, h->ev_join, 0) == cudaSuccess;
-    h->graph_capturing = false;
-    const bool ended = cudaStreamEndCapture(s, &graph) == cudaSuccess;
-    ok = ok && joined && ended && graph != nullptr &&
-         cudaGraphInstantiate(&slot->exec, graph, 0) == cudaSuccess;
-    if (graph) cudaGraphDestroy(graph);
+  bool ok = false;
+  for (int attempt = 0; attempt < 2 && !ok; ++attempt) {
+    if (attempt == 1) {
+      // once more with the gated rebuild kernels in the graph itself
+      if (h->cond_off) break;
+      h->cond_off = true;
+      cudaGetLastError();
+      if (slot->exec) cudaGraphExecDestroy(slot->exec);
+      slot->exec = nullptr;
+      h->launches = launches0;
+      h->v = v0;
+      h->v2 = v20;
+    }
+    cudaGraph_t graph = nullptr;
+    ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      h->graph_capturing = true;
+      ok = cudaMemcpyAsync(stage_x_in(h), x, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+           cudaMemcpyAsync(h->up_v, v, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+           host_step_body(h, 0, dt, x, v) == MCFG_OK;
+      // the copy stream's positions joined back into the captured stream
+      const bool joined = cudaEventRecord(h->ev_join, h->copy_stream) == cudaSuccess &&
+                          cudaStreamWaitEvent(s, h->ev_join, 0) == cudaSuccess;
+      h->graph_capturing = false;
+      const bool ended = cudaStreamEndCapture(s, &graph) == cudaSuccess;
+      ok = ok && joined && ended && graph != nullptr &&
+           cudaGraphInstantiate(&slot->exec, graph, 0) == cudaSuccess;
+      if (graph) cudaGraphDestroy(graph);
+    }
   }
   const int64_t captured = h->launches - launches0;
   h->launches = launches0;
@@ -1072,6 +1174,7 @@ int mcfg_destroy(mcfg_handle* h) {
   }
   if (h->ev_x) cudaEventDestroy(h->ev_x);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->cond_stream) cudaStreamDestroy(h->cond_stream);
   if (h->h_status) cudaFreeHost(h->h_status);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;

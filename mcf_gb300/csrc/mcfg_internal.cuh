@@ -269,6 +269,14 @@ struct Handle {
     int64_t launches = 0;
   } hgraphs[2];
   bool hgraph_off = false;  // a host-step capture failed: plain launches from then on
+  // In a captured step the gated rebuild (wrap, MCF's cell list, candidate
+  // list) sits in the body of a conditional node that a one-thread kernel
+  // opens when the kick-drift kernel raised the rebuild flag, so the steps
+  // without a rebuild launch none of its kernels.  The body is captured on
+  // cond_stream.  cond_off: the runtime refused it once; the gated kernels
+  // then sit in the graph itself.
+  cudaStream_t cond_stream = nullptr;
+  bool cond_off = false;
   // ---- particle-file text (output.cu), grow-only, null until the first write ----
   char* out_dev = nullptr;
   char* out_host = nullptr;  // pinned
