@@ -25,7 +25,14 @@ as the checker:
     1e-11 of the box, velocities and angular velocities within 1e-9 of their
     scale, particle positions and velocities at the trajectory bars;
   - C5, 128^2 Oldroyd-B: 10 kT = 0 steps, positions, velocities and the
-    conformation tensor at the bars of the small Oldroyd-B test.
+    conformation tensor at the bars of the small Oldroyd-B test;
+  - the FP32-mixed path at C3's and C4's sizes at the bars of the small
+    FP32-mixed tests (density 2e-6 relative, acceleration 1e-4 of the
+    per-particle scale, the random force with the same Philox draws; the
+    colloids' boundary particles, drag and torque 1e-3), and with list
+    reuse (the candidate list, the compact pair list, the sweep over it)
+    5 kT = 0 steps: positions within 1e-9 of the box, velocities within
+    the acceleration bar accumulated over the steps.
 """
 import os
 
@@ -33,6 +40,7 @@ import numpy as np
 import pytest
 
 from mcf_gb300 import SDPD, configs
+from mcf_gb300.params import PRECISION_FP32_MIXED
 from oracle.oracle import Oracle
 
 pytestmark = pytest.mark.gpu
@@ -204,3 +212,79 @@ def test_c5_128squared_oldroyd_b_10_steps(gpu_lib):
     a, b = trajectory_close(g, o, 10, w.dt, 128.0, tol_x=1e-12, tol_v=1e-10, extra=("ct",))
     assert np.max(np.abs(a["ct"] - b["ct"])) <= 1e-12
     assert np.max(np.abs(b["ct"] - ct0)) > 1e-8  # the tensor has moved
+
+
+def fp32_rhs_close(g, o, step=0, tol_boundary=1e-4):
+    """the FP32-mixed path's bars: density 2e-6 relative, acceleration 1e-4
+    of the per-particle scale (floored at 1e-6 of its median, as above);
+    colloid boundary particles at tol_boundary"""
+    g.marching_init_force(step)
+    o.marching_init_force(step)
+    a = g.download("rho", "f")
+    b = o.download("rho", "f")
+    assert np.max(np.abs(a["rho"] - b["rho"]) / b["rho"]) < 2e-6
+    fs = o.force_scale()
+    tol = np.where(o.sid > 0, tol_boundary, 1e-4)[:, None]
+    scale = tol * (fs[:, None] + 1e-6 * np.median(fs))
+    err = np.abs(a["f"] - b["f"])
+    assert np.all(err <= scale), worst(err, scale, o.sid, a["f"], b["f"])
+
+
+def c3_case():
+    w = configs.c3_poiseuille_3d()
+    rng = np.random.default_rng(100)
+    fl = w.id[:, 1] == 0
+    w.x[fl] += rng.uniform(-0.05, 0.05, (int(fl.sum()), 3))
+    w.v[fl] = rng.normal(0.0, 1e-3, (int(fl.sum()), 3))
+    return w
+
+
+def test_c3_100cubed_fp32_mixed_rhs(gpu_lib):
+    w = c3_case()
+    g, o = pair(w, Brownian=0, kt=0.0, precision=PRECISION_FP32_MIXED)
+    fp32_rhs_close(g, o)
+    g, o = pair(w, precision=PRECISION_FP32_MIXED)  # kT = 1e-4, Hu-Adams noise
+    fp32_rhs_close(g, o, step=7)
+
+
+def test_c3_100cubed_fp32_mixed_list_reuse_5_steps(gpu_lib):
+    # the headline path: candidate list, compact pair list, force sweep over it
+    w = c3_case()
+    p = w.params.copy()
+    p.Brownian, p.kt, p.precision = 0, 0.0, PRECISION_FP32_MIXED
+    p.reserved[1] = 1
+    g = SDPD(p)
+    g.upload(w.x, w.v, w.m, w.id)
+    o = Oracle(p, threads=THREADS)
+    o.upload(w.x, w.v, w.m, w.id)
+    g.marching_init_force(0)
+    o.marching_init_force(0)
+    g.run_vv(0, 5, w.dt)
+    o.run_vv(0, 5, w.dt)
+    a = g.download("x", "v")
+    b = o.download("x", "v")
+    assert np.max(np.abs(a["x"] - b["x"])) <= 1e-9 * 100.0
+    # the acceleration bar (1e-4 of the largest per-particle scale)
+    # accumulated over the 5 steps
+    assert np.max(np.abs(a["v"] - b["v"])) <= 1e-4 * o.force_scale().max() * 5 * w.dt
+    assert g.info()["num_pairs"] > 100 * w.n
+
+
+def test_c4_96cubed_200_colloids_fp32_mixed_rhs(gpu_lib):
+    w, cs = configs.c4_colloids(v_scale=0.05, omega_scale=0.02)
+    rng = np.random.default_rng(96)
+    fl = w.id[:, 1] == 0
+    w.x[fl] += rng.uniform(-0.05, 0.05, (int(fl.sum()), 3))
+    w.v[fl] = rng.normal(0.0, 1e-3, (int(fl.sum()), 3))
+    g, o = pair(w, Brownian=0, kt=0.0, precision=PRECISION_FP32_MIXED)
+    for h in (g, o):
+        h.set_colloids(cs.params, cs.x, cs.v, cs.omega, cs.radius)
+    # the boundary particles carry the FP32 no-slip term (their offsets to
+    # the centre and the clamped distance ratio in FP32): 1e-3 of their
+    # scale, and so drag and torque
+    fp32_rhs_close(g, o, tol_boundary=1e-3)
+    da, ta = g.colloid_drag()
+    db, tb = o.colloid_drag()
+    scale = np.abs(db).max() + np.abs(tb).max()
+    assert np.max(np.abs(da - db)) <= 1e-3 * scale
+    assert np.max(np.abs(ta - tb)) <= 1e-3 * scale
