@@ -32,7 +32,9 @@ as the checker:
     colloids' boundary particles, drag and torque 1e-3), and with list
     reuse (the candidate list, the compact pair list, the sweep over it)
     5 kT = 0 steps: positions within 1e-9 of the box, velocities within
-    the acceleration bar accumulated over the steps.
+    the acceleration bar accumulated over the steps; C2's right-hand side
+    with the random force; C5's conformation tensor after 10 steps within
+    1e-3 of its change.
 """
 import os
 
@@ -288,3 +290,29 @@ def test_c4_96cubed_200_colloids_fp32_mixed_rhs(gpu_lib):
     scale = np.abs(db).max() + np.abs(tb).max()
     assert np.max(np.abs(da - db)) <= 1e-3 * scale
     assert np.max(np.abs(ta - tb)) <= 1e-3 * scale
+
+
+def test_c2_64cubed_fp32_mixed_rhs_with_random_force(gpu_lib):
+    w = c2_case()
+    g, o = pair(w, precision=PRECISION_FP32_MIXED)  # kT = 1e-3, Hu-Adams noise
+    fp32_rhs_close(g, o, step=11)
+
+
+def test_c5_128squared_oldroyd_b_fp32_mixed_10_steps(gpu_lib):
+    # the conformation tensor stays FP64; its change over the steps within
+    # 1e-3 of the FP64 oracle's (the small Oldroyd-B FP32 bar)
+    w = configs.c5_oldroyd_b_2d()
+    rng = np.random.default_rng(128)
+    w.x = w.x + rng.uniform(-0.05, 0.05, w.x.shape)
+    g, o = pair(w, Brownian=0, kt=0.0, precision=PRECISION_FP32_MIXED)
+    ct0 = np.tile(np.array([1.0, 0.0, 0.0, 1.0]), (w.n, 1))
+    for h in (g, o):
+        h.upload(w.x, w.v, w.m, w.id, ct0)
+        h.marching_init_force(0)
+        h.run_vv(0, 10, w.dt)
+    a = g.download("ct", "x")
+    b = o.download("ct", "x")
+    dev = np.abs(b["ct"] - ct0)
+    assert dev.max() > 1e-8
+    assert np.max(np.abs(a["ct"] - b["ct"])) <= 1e-3 * dev.max() + 1e-9
+    assert np.max(np.abs(a["x"] - b["x"])) <= 1e-9 * 128.0
