@@ -410,12 +410,35 @@ def roofline_for(sd, torch, w, prec_idx, peaks, step0, clock_mhz=None):
                          "flop_frac_ncu": fp["flop_frac"], "achieved": ach / 1e12, "peak": pk / 1e12,
                          "unit": "TFLOP/s", "frac": ach / pk,
                          "peak_source": f"nominal: {sms} SMs x 2 DFMA x 2 FLOP x {clk:.0f} MHz"}
+    fp32_flops = None
+    if not prec_idx and tf.exists():
+        # FP32 (non-tensor) FLOP rate of the FP32 sweep: ncu's FADD + FMUL +
+        # 2 FFMA per particle of the same sweep on 64^3 x this launch's
+        # particles / its event time, against 128 FP32 lanes x 2 FLOP per
+        # clock per SM; beside it the pair-body model of the algorithmic
+        # FLOPs (~80 a pair side for the Hu-Adams force, ~25 for the
+        # density, without the noise's integer work)
+        fl = json.loads(tf.read_text()).get("fp32_flop_per_particle", {}).get(top)
+        if fl:
+            sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+            clk = clock_mhz or 2070.0
+            ach = fl * w.n / (avg_ms / 1e3)
+            pk = 256.0 * sms * clk * 1e6
+            per_pair = {"force": 80, "density": 25}.get(top)
+            info = sd.info()
+            pairs = info["num_pairs"] / max(w.n, 1)
+            fp32_flops = {"achieved": ach / 1e12, "peak": pk / 1e12, "unit": "TFLOP/s",
+                          "frac": ach / pk, "flop_per_particle_ncu": fl,
+                          "algorithmic_flop_per_particle":
+                              (per_pair * pairs) if per_pair else None,
+                          "peak_source": f"nominal: {sms} SMs x 128 FP32 lanes x 2 FLOP x "
+                                         f"{clk:.0f} MHz"}
     return {"kernel_phase": top, "bound": "fp64 pipe" if prec_idx else "hbm",
             "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": (achieved / peak) if peak else None, "traffic": traffic,
             "avg_ms": avg_ms, "algo_bytes_per_launch": algo,
             "peak_source": peaks.get("source"), "phase_share": share, "issue": issue,
-            "fp64_pipe": fp64_pipe}
+            "fp64_pipe": fp64_pipe, "fp32_flops": fp32_flops}
 
 
 def adjoint_cost(torch, w, T, K, local, wts):
