@@ -602,7 +602,10 @@ __device__ __forceinline__ JData load_j(const int* __restrict__ s_start, int ent
 // particle leaves most of the GPU idle and each thread's serial pair loop
 // sets the time): lane l takes list entries l, l + S, ...; the lanes' sums
 // are added in lane order by the first lane, which runs the epilogue.
-template <int D, bool NNW, int S>
+// STRESS: the per-particle stress s_i += r_ij (x) a_ij / 2 is accumulated
+// (a compile-time switch: its nine sums would otherwise stay live across
+// the pair loop of every run).
+template <int D, bool NNW, int S, bool STRESS>
 __global__ void __launch_bounds__(kReuseTPB, 5)
     k_force32(Consts k, const int* __restrict__ cell_start, const int* __restrict__ cell_of,
               const uint16_t* __restrict__ nl, const int* __restrict__ ncount, int cap,
@@ -830,7 +833,7 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
       comp[a] = (tt - acc[a]) - y;
       acc[a] = tt;
     }
-    if (k.stress) {
+    if (STRESS) {
 #pragma unroll
       for (int b = 0; b < D; ++b)
 #pragma unroll
@@ -859,7 +862,7 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
         L[cc] = tot;
       }
     }
-    if (k.stress) {
+    if (STRESS) {
 #pragma unroll
       for (int a = 0; a < 9; ++a) {
         T tot = sacc[a];
@@ -869,7 +872,7 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
     }
     if (lane_s != 0) return;
   }
-  if (k.stress) {
+  if (STRESS) {
 #pragma unroll
     for (int a = 0; a < D * D; ++a) st[(size_t)a * n + i] = (double)sacc[a];
   }
@@ -1444,24 +1447,30 @@ int compute_force(Handle* h, int64_t step, int fuse_mode, double dt) {
     }
 #undef LAUNCH_F64
   } else {
-#define LAUNCH_F32(DD, NW)                                                                      \
+#define LAUNCH_F32(DD, NW, ST)                                                                  \
   do {                                                                                           \
     if (split)                                                                                   \
-      k_force32<DD, NW, 4><<<gp4, kReuseTPB, 0, s>>>(                                            \
+      k_force32<DD, NW, 4, ST><<<gp4, kReuseTPB, 0, s>>>(                                        \
           k, h->cell_start, h->cell_of, h->nl, h->ncount, h->neigh_cap, h->off, h->x, h->v,      \
           h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step, step_ptr,     \
-          (float)inv_sqdt, h->d_err, nn, ca);                                                                     \
+          (float)inv_sqdt, h->d_err, nn, ca);                                                    \
     else                                                                                         \
-      k_force32<DD, NW, 1><<<gp, kReuseTPB, 0, s>>>(                                             \
+      k_force32<DD, NW, 1, ST><<<gp, kReuseTPB, 0, s>>>(                                         \
           k, h->cell_start, h->cell_of, h->nl, h->ncount, h->neigh_cap, h->off, h->x, h->v,      \
           h->pcf, h->vf, h->wd, h->f, h->st, fuse_mode, dt, h->v2, (uint32_t)step, step_ptr,     \
-          (float)inv_sqdt, h->d_err, nn, ca);                                                                     \
+          (float)inv_sqdt, h->d_err, nn, ca);                                                    \
+  } while (0)
+#define PICK_F32_ST(DD, NW)                   \
+  do {                                        \
+    if (k.stress) LAUNCH_F32(DD, NW, true);   \
+    else LAUNCH_F32(DD, NW, false);           \
   } while (0)
     if (k.d == 3) {
-      if (k.newtonian) LAUNCH_F32(3, false); else LAUNCH_F32(3, true);
+      if (k.newtonian) PICK_F32_ST(3, false); else PICK_F32_ST(3, true);
     } else {
-      if (k.newtonian) LAUNCH_F32(2, false); else LAUNCH_F32(2, true);
+      if (k.newtonian) PICK_F32_ST(2, false); else PICK_F32_ST(2, true);
     }
+#undef PICK_F32_ST
 #undef LAUNCH_F32
   }
   h->launches++;
