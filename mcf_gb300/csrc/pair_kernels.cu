@@ -635,26 +635,11 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
   const int celli = cell_of[i];
   build_lane_table<D, kReuseTPB, false>(k, celli, cell_start, s_start, nullptr);
   const float4* slot_tab = slot_table(k, s_slot, celli);
-  // the particle's own records (offset, velocity, pair coefficients) sit
-  // in shared memory and are re-read every pair by loads the compiler does
-  // not hoist: 12 fewer live registers across the pair loop, which the
-  // scheduler spends on the pair arithmetic (1.5% faster at the same 96
-  // registers, same bits)
-  __shared__ float4 s_own[3 * kReuseTPB];
-  s_own[threadIdx.x] = off[i];
-  s_own[kReuseTPB + threadIdx.x] = vf[i];
-  s_own[2 * kReuseTPB + threadIdx.x] = pcf[i];
-  asm volatile("" ::: "memory");  // the stores above come before the loads below
-  const int si = __float_as_int(s_own[threadIdx.x].w);
-  const int pidi = __float_as_int(s_own[kReuseTPB + threadIdx.x].w);
-  const unsigned own_base = (unsigned)__cvta_generic_to_shared(&s_own[threadIdx.x]);
-  auto own = [own_base](int q) {
-    float4 r;
-    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
-                 : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
-                 : "r"(own_base + (unsigned)(q * kReuseTPB * 16)));
-    return r;
-  };
+  const float4 oi = off[i];
+  const int si = __float_as_int(oi.w);
+  const float4 v4i = vf[i];
+  const int pidi = __float_as_int(v4i.w);
+  const float4 ci = pcf[i];
   const float2 wdi = (walls && k.wall_axis >= 0) ? wd[i] : make_float2(0.f, 0.f);
   constexpr bool nnw = NNW;  // Oldroyd-B terms compiled only when used
   const float* qq = (const float*)nn.qq;
@@ -686,7 +671,6 @@ __global__ void __launch_bounds__(kReuseTPB, 5)
     }
     const int sj = __float_as_int(cur.o.w);
     if (si != 0 && sj != 0 && !(si > 0 && sj > 0 && si != sj && k.pp_cc)) continue;
-    const float4 oi = own(0), v4i = own(1), ci = own(2);
     const int sl = cur.sl;
     T r[3];
     const float4 so = slot_tab[sl];
