@@ -156,3 +156,22 @@ def test_slabs_on_gloo_ranks_follow_the_undivided_box(world):
     check(w, by_pid([g[0] for g in gathered], w.n, 3), ref)
     for _, stats in gathered:  # every rank holds the box's sums
         stats_close(stats, ref_stats)
+
+
+def test_a_slab_without_particles():
+    # a void across one of four slabs: that slab owns nothing (it still
+    # receives halo particles and returns no densities of its own); the
+    # others follow the undivided box as before
+    w = workload()
+    keep = ~((w.x[:, 0] >= 9.0) & (w.x[:, 0] < 13.5))  # slab 2 of 4 spans [9, 13.5)
+    w.x, w.v, w.m, w.id = w.x[keep], w.v[keep], w.m[keep], w.id[keep].copy()
+    w.id[:, 0] = np.arange(1, w.n + 1, dtype=np.int32)
+    w.v[w.id[:, 1] == 0, 0] -= 1.0  # no mean drift into the void during the steps
+    ref = undivided(w)
+    dec = SlabDecomposition(w.params, 4, factory=Oracle, exchange=LocalExchange())
+    dec.upload(w.x, w.v, w.m, w.id)
+    assert dec.subs[2].n_own == 0
+    dec.init_force(0)
+    dec.run_vv(0, NSTEPS, w.dt)
+    got = by_pid(dec.owned_state(), w.n, 3)
+    check(w, got, ref)

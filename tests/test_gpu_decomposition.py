@@ -90,3 +90,20 @@ def test_statistics_owned_contract(gpu_lib):
     for bad in (-1, w.n + 1):
         with pytest.raises(MCFGError):
             g.statistic_compute_statistic(n_owned=bad)
+
+
+def test_gpu_slab_without_particles(gpu_lib):
+    # a void across one of four slabs: that handle holds halo particles
+    # only (or none), the decomposed run still follows the undivided one
+    w = workload()
+    keep = ~((w.x[:, 0] >= 9.0) & (w.x[:, 0] < 13.5))
+    w.x, w.v, w.m, w.id = w.x[keep], w.v[keep], w.m[keep], w.id[keep].copy()
+    w.id[:, 0] = np.arange(1, w.n + 1, dtype=np.int32)
+    w.v[w.id[:, 1] == 0, 0] -= 1.0
+    dec = SlabDecomposition(w.params, 4, factory=SDPD, exchange=LocalExchange())
+    dec.upload(w.x, w.v, w.m, w.id)
+    assert dec.subs[2].n_own == 0
+    dec.init_force(0)
+    dec.run_vv(0, NSTEPS, w.dt)
+    got = by_pid(dec.owned_state(), w.n, 3)
+    check(w, got, gpu_undivided(w))
