@@ -604,9 +604,10 @@ __device__ __forceinline__ JData load_j(const int* __restrict__ s_start, int ent
 // are added in lane order by the first lane, which runs the epilogue.
 // STRESS: the per-particle stress s_i += r_ij (x) a_ij / 2 is accumulated
 // (a compile-time switch: its nine sums would otherwise stay live across
-// the pair loop of every run).
+// the pair loop of every run).  The 3D Oldroyd-B instances take 4 blocks
+// per SM: at 5 (96 registers) they spill the polymer terms.
 template <int D, bool NNW, int S, bool STRESS>
-__global__ void __launch_bounds__(kReuseTPB, 5)
+__global__ void __launch_bounds__(kReuseTPB, (NNW && D == 3) ? 4 : 5)
     k_force32(Consts k, const int* __restrict__ cell_start, const int* __restrict__ cell_of,
               const uint16_t* __restrict__ nl, const int* __restrict__ ncount, int cap,
               const float4* __restrict__ off,
