@@ -676,9 +676,12 @@ static int rebuild_conditional(Handle* h) {
                                     cudaStreamCaptureModeThreadLocal) != cudaSuccess)
     return MCFG_ENOTSUP;
   h->stream = h->cond_stream;
+  // the body runs on rebuild steps only: a replay's launch count leaves it out
+  const int64_t launches0 = h->launches;
   int rc = wrap_gated(h);
   if (rc == MCFG_OK) rc = gated_cell_list(h);
   if (rc == MCFG_OK) rc = verlet_build_gated(h);
+  h->launches = launches0;
   h->stream = s;
   cudaGraph_t ended = nullptr;
   const bool body_ok = cudaStreamEndCapture(h->cond_stream, &ended) == cudaSuccess;
