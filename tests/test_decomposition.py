@@ -175,3 +175,24 @@ def test_a_slab_without_particles():
     dec.run_vv(0, NSTEPS, w.dt)
     got = by_pid(dec.owned_state(), w.n, 3)
     check(w, got, ref)
+
+
+def test_decomposition_refuses_what_it_does_not_cover():
+    from mcf_gb300.params import BC_WALL_SOLID
+
+    w = workload()
+    p = w.params.copy()
+    p.bcdef[0] = p.bcdef[1] = BC_WALL_SOLID
+    with pytest.raises(ValueError, match="periodic along x"):
+        SlabDecomposition(p, 2, factory=Oracle)
+    with pytest.raises(ValueError, match="narrower than the halo"):
+        SlabDecomposition(w.params, 7, factory=Oracle)  # 18/7 < 3.0003
+    p = w.params.copy()
+    p.Newtonian = 0
+    with pytest.raises(ValueError, match="Newtonian"):
+        SlabDecomposition(p, 2, factory=Oracle)
+    dec = SlabDecomposition(w.params, 2, factory=Oracle, exchange=LocalExchange())
+    dec.upload(w.x, w.v, w.m, w.id)
+    dec.init_force(0)
+    with pytest.raises(ValueError, match="params.dt"):
+        dec.step_vv(1, 2.0 * w.params.dt)
